@@ -1,0 +1,364 @@
+"""Benchmark of the GB300 FDTD engine (prints one JSON line on rank 0).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+                    [--workload plain3d|plain2d]
+
+Metric: Gcell-updates/s, one cell-update = one cell of the PML-extended grid advanced one full
+time step (velocity + pressure + memory variables). A bench step is one pass of the time loop
+over ``steps_per_bench_step`` time steps of the workload:
+* plain2d: the 2D forward workload (944 x 688 extended cells, 4000 time steps = one full solve);
+  its 60 MB working set fits in L2, so L2 is flushed (a 256 MB write) before every bench step.
+* plain3d: the 3D forward workload (512^3 + PML 32 + transition 32 -> 656^3 extended cells,
+  nT = 3000), bench step = 100 time steps; its ~30 GB working set is far larger than L2.
+
+``value`` is device-timed (CUDA events on the engine's stream) with the medium and wavefield
+resident in HBM. ``e2e`` is the same metric through the public C ABI with host buffers: each e2e
+step uploads that step's inputs from pinned host memory (plain2d: every map and the source
+signals, i.e. a full ``fw_set_fields``; plain3d: the source-signal columns of the step's 100
+time steps) and reads the step's sensor traces back to host memory.
+
+Multi-GPU (torchrun): every rank runs an independent replica of the workload (the engine does
+not shard a single solve); ``value`` = cell-updates of all ranks / max rank time ("weak").
+``--impl reference`` times the reference path's CPU implementation: the reference ships no
+CPU engine and its GPU executables are x86-64 binaries that cannot run on the aarch64 GB300
+host, so the FP64 oracle restatement of the same time loop runs on the host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "Gcell-updates/s"
+L2_BYTES = 126 * 1024 * 1024
+
+
+# --------------------------------------------------------------------------------- utilities
+def dist_info():
+    return (int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)),
+            int(os.environ.get("LOCAL_RANK", 0)))
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    QUERY = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 7:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = max(mx, float(parts[1]))
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[3:7]):
+                if flag.lower() in ("active", "1"):
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx or None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def traffic_from_profiles(workload: str):
+    """DRAM bytes per cell-update recorded from an ncu capture, if a summary is committed."""
+    path = ROOT / "profiles" / f"traffic_{workload}.txt"
+    if not path.exists():
+        return None
+    for ln in path.read_text().splitlines():
+        if ln.startswith("dram_bytes_per_cell_update:"):
+            return float(ln.split(":", 1)[1])
+    return None
+
+
+# --------------------------------------------------------------------------------- workloads
+def make_workload(name: str, rank: int):
+    """Return (inputs-or-builder, steps_per_bench_step, description dict)."""
+    if name == "plain2d":
+        from fullwave25_gb300.workloads import plain_2d_inputs
+
+        inp = plain_2d_inputs(seed=rank)
+        desc = {"workload": "plain 2D forward, 768x512 + PML 40 + transition 40 (944x688), "
+                            "nt 4000, 8 random ellipses, 2 relaxation mechanisms",
+                "grid": list(inp.shape), "nt": inp.nt, "steps_per_bench_step": inp.nt,
+                "l2": "flushed (256 MB write) before every bench step; working set 60 MB"}
+        return inp, inp.nt, desc
+    if name == "plain3d":
+        from fullwave25_gb300.workloads3d import plain_3d_device_inputs
+
+        dinp = plain_3d_device_inputs(seed=rank)
+        desc = {"workload": "plain 3D forward, 512^3 + PML 32 + transition 32 (656^3), nt 3000, "
+                            "layered fat/muscle/liver with perturbed interfaces and 0.5% scatterers,"
+                            " 64-element plane-wave source, 256x256 sensor plane",
+                "grid": list(dinp.shape), "nt": dinp.nt, "steps_per_bench_step": 100,
+                "l2": "inputs larger than L2 (working set ~30 GB)"}
+        return dinp, 100, desc
+    raise ValueError(f"unknown workload {name}")
+
+
+# --------------------------------------------------------------------------------- CPU baseline
+def time_oracle(workload: str, budget_s: float):
+    """FP64 oracle on a bounded sample: the workload's grid for as many steps as fit in budget."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from fdtd_oracle import Oracle
+
+    if workload == "plain2d":
+        from fullwave25_gb300.workloads import plain_2d_inputs
+
+        inp = plain_2d_inputs()
+        label = "plain 2D grid 944x688"
+    else:
+        from fullwave25_gb300.workloads3d import plain_3d_host_sample
+
+        inp = plain_3d_host_sample()
+        label = f"plain 3D medium, {inp.shape[0]}x{inp.shape[1]}x{inp.shape[2]} sub-block"
+    o = Oracle(inp)
+    o.step()  # warm-up
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and steps < inp.nt - 1:
+        o.step()
+        steps += 1
+    el = time.perf_counter() - t0
+    cells = int(np.prod(inp.shape))
+    return {"value": cells * steps / el / 1e9, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"FP64 NumPy oracle, {label}, {steps} time steps in {el:.1f} s "
+                      f"(single-threaded NumPy)"}
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return
+    per_step_budget = float(os.environ.get("FWGB_REF_SAMPLE_S", "8"))
+    vals = []
+    for i in range(args.warmup + args.steps):
+        r = time_oracle(args.workload, per_step_budget)
+        if i >= args.warmup:
+            vals.append(r["value"])
+    v = statistics.mean(vals)
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": args.workload, "engine": "FP64 NumPy oracle restatement "
+                       "(reference engine is a closed x86-64 CUDA executable; no CPU engine)"},
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
+                             "sample": r["sample"]},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# --------------------------------------------------------------------------------- GPU arm
+def run_gpu(args):
+    import torch
+
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.workloads import algorithmic_bytes_per_cell
+
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    inputs, chunk, desc = make_workload(args.workload, rank)
+    engine = Engine(inputs) if args.workload == "plain2d" else inputs.make_engine()
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    nt = inputs.nt
+    cells = int(np.prod(inputs.shape))
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    do_flush = args.workload == "plain2d"
+
+    def bench_step(i):
+        # plain2d: one full solve; plain3d: `chunk` steps continuing a solve
+        if args.workload == "plain2d":
+            engine.reset(sptr)
+            engine.advance(nt, sptr)
+        else:
+            if engine.current_step + chunk > nt:
+                engine.reset(sptr)
+            engine.advance(chunk, sptr)
+
+    def barrier():
+        torch.cuda.synchronize(dev)
+        if world > 1:
+            torch.distributed.barrier()
+
+    for i in range(args.warmup):
+        bench_step(i)
+    barrier()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    with ClockSampler(local) as clocks:
+        barrier()
+        t0 = time.perf_counter()
+        for i in range(args.steps):
+            if do_flush:
+                flush.fill_(float(i))
+            starts[i].record(stream)
+            bench_step(i)
+            ends[i].record(stream)
+        barrier()
+        wall = time.perf_counter() - t0
+    dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
+    t_rank = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        torch.distributed.all_reduce(t_rank, op=torch.distributed.ReduceOp.MAX)
+    dev_ms_max = float(t_rank.item())
+    units_per_rank = cells * chunk * args.steps
+    value = units_per_rank * world / (dev_ms_max / 1e3) / 1e9
+    ms_per_step = dev_ms_max / args.steps
+
+    # roofline: one time step (velocity + pressure kernels) over the whole grid
+    step_s = (dev_ms / 1e3) / (chunk * args.steps)
+    alg_bytes = algorithmic_bytes_per_cell(len(inputs.shape)) * cells
+    achieved = alg_bytes / step_s / 1e9
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (
+        ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    tr = traffic_from_profiles(args.workload)
+
+    # e2e through the C ABI with host buffers
+    e2e = run_e2e(args, engine, inputs, chunk, sptr, dev, world)
+    clk = clocks.summary()
+    if rank != 0:
+        engine.close()
+        return
+    cpu = time_oracle(args.workload, float(os.environ.get("FWGB_CPU_SAMPLE_S", "15"))) if (
+        world == 1 and not args.no_cpu_baseline) else None
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {**desc, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+                   "wall_s_timed": wall},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak,
+                     "traffic": (tr * cells if tr is not None else None),
+                     "kernel": "time step = velocity + pressure kernels",
+                     "algorithmic_bytes_per_cell_update":
+                         algorithmic_bytes_per_cell(len(inputs.shape)),
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
+                     else "fallback 6800 GB/s"},
+        "cpu_baseline": cpu,
+        "e2e": e2e,
+        "gpu_launches": int(engine.launches_per_step * chunk * args.steps),
+        "clocks": clk,
+    }
+    print(json.dumps(line), flush=True)
+    engine.close()
+
+
+def run_e2e(args, engine, inputs, chunk, sptr, dev, world):
+    import torch
+
+    from fullwave25_gb300.engine import Engine
+
+    n_e2e = max(1, min(args.steps, 5))
+    if args.workload == "plain2d":
+        # pinned host copies of every input array
+        pinned = {}
+
+        def pin(a):
+            t = torch.empty(a.shape, dtype=torch.float32 if a.dtype != np.int32 else torch.int32,
+                            pin_memory=True)
+            t.numpy()[...] = a
+            pinned[id(t)] = t
+            return t.numpy()
+
+        import copy
+
+        host = copy.copy(inputs)
+        host.maps = {k: pin(v) for k, v in inputs.maps.items()}
+        host.dcmap = pin(inputs.dcmap)
+        host.icmat = pin(inputs.icmat)
+        out = torch.empty((inputs.n_out, inputs.outc.shape[0]), dtype=torch.float32,
+                          pin_memory=True).numpy()
+        h2d = sum(v.nbytes for v in host.maps.values()) + host.dcmap.nbytes + host.icmat.nbytes
+        d2h = out.nbytes
+        import ctypes as C
+
+        from fullwave25_gb300.engine import _FP
+
+        torch.cuda.synchronize(dev)
+        t0 = time.perf_counter()
+        for _ in range(n_e2e):
+            engine.set_fields(host)
+            engine._call("fw_run", C.c_void_p(sptr), out.ctypes.data_as(_FP), 0)
+        torch.cuda.synchronize(dev)
+        el = time.perf_counter() - t0
+        cells = int(np.prod(inputs.shape))
+        return {"value": cells * inputs.nt * n_e2e * world / el / 1e9, "unit": METRIC,
+                "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                "steps": n_e2e, "api": "fw_set_fields(host) + fw_run(host traces)"}
+    return inputs.run_e2e(engine, chunk, n_e2e, sptr, dev, world)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--workload", default=os.environ.get("FWGB_WORKLOAD", "plain2d"),
+                    choices=["plain2d", "plain3d"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        print("warning: fewer than 3 warm-up steps requested; using 3", file=sys.stderr)
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,614 @@
+// Host side of the FDTD engine: the C ABI declared in include/fwgb.h.
+//
+// One handle owns the device memory of one simulation: padded state and map arrays, the tap
+// table, per-tile source/air/sensor lists and the trace buffer. Time steps are issued as two
+// kernels per step (velocity, then pressure + tile epilogue); blocks of steps are captured once
+// into a CUDA graph and replayed, so the per-step host cost is one graph launch per block.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "../../include/fwgb.h"
+#include "engine_common.cuh"
+#include "kernels_direct.cuh"
+
+using namespace fwgb;
+
+namespace {
+
+thread_local std::string g_create_error = "no error";
+
+struct Tiling {
+  int t[3];   // tile extent along x, y, z (z unused in 2D)
+  int n[3];   // tiles along x, y, z
+  int count() const { return n[0] * n[1] * n[2]; }
+};
+
+}  // namespace
+
+struct fw_handle {
+  fw_desc d{};
+  int ndim = 0;
+  int64_t nx = 0, ny = 0, nz = 1, pitch = 0;  // pitch = padded length of the last axis
+  int64_t ncells_padded = 0;
+  std::string err = "no error";
+  // device memory
+  float* state = nullptr;      // n_state padded arrays
+  float* maps = nullptr;       // n_maps padded arrays
+  int32_t* dcmap = nullptr;
+  float* taps = nullptr;
+  float* icmat_t = nullptr;    // [nt_ic][ncoords]
+  float* traces = nullptr;     // [n_out][ncoordsout]
+  int* step = nullptr;
+  void* lists = nullptr;       // one allocation for all per-tile lists
+  size_t bytes = 0;
+  bool has_beta = false, fields_set = false;
+  int n_out = 0;
+  int32_t host_step = 0;
+  Tiling tiling{};
+  StepArgs args{};
+  cudaStream_t capture_stream = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  int graph_steps = 0;
+};
+
+namespace {
+
+int fail(fw_handle* h, int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (h) h->err = buf; else g_create_error = buf;
+  return code;
+}
+
+#define FW_CUDA(h, call)                                                                   \
+  do {                                                                                     \
+    cudaError_t e_ = (call);                                                               \
+    if (e_ != cudaSuccess)                                                                 \
+      return fail(h, e_ == cudaErrorMemoryAllocation ? FW_ERR_OOM : FW_ERR_CUDA,           \
+                  "%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+  } while (0)
+
+int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
+
+int n_state(int ndim) { return 1 + ndim + 4 * ndim; }
+// maps: rdt_rho, dt_k, beta2dt, inv_ku, inv_kx, au1 bu1 au2 bu2 ax1 bx1 ax2 bx2
+constexpr int kMaps = 13;
+
+Tiling make_tiling(const fw_handle* h) {
+  Tiling t{};
+  if (h->ndim == 2) {
+    t.t[0] = kD2TX; t.t[1] = kD2TY; t.t[2] = 1;
+  } else {
+    t.t[0] = kD3TX; t.t[1] = kD3TY; t.t[2] = kD3TZ;
+  }
+  const int64_t ext[3] = {h->nx, h->ny, h->nz};
+  for (int a = 0; a < 3; ++a) {
+    if (a == 2 && h->ndim == 2) { t.n[a] = 1; continue; }
+    const int64_t body = ext[a] - 2 * kGhost;
+    t.n[a] = (int)((body + t.t[a] - 1) / t.t[a]);
+  }
+  return t;
+}
+
+// Tile (block of the pressure kernel) that owns cell (i, j, k). Ghost cells belong to the tile
+// of the nearest body cell, so that sources or sensors placed there are still served.
+int tile_of(const fw_handle* h, int64_t i, int64_t j, int64_t k) {
+  const Tiling& t = h->tiling;
+  auto idx = [&](int64_t v, int64_t n, int a) {
+    v = std::min(std::max(v, (int64_t)kGhost), n - kGhost - 1) - kGhost;
+    return (int)(v / t.t[a]);
+  };
+  const int tx = idx(i, h->nx, 0), ty = idx(j, h->ny, 1);
+  const int tz = h->ndim == 3 ? idx(k, h->nz, 2) : 0;
+  return (tx * t.n[1] + ty) * t.n[2] + tz;
+}
+
+int64_t padded_index(const fw_handle* h, int64_t i, int64_t j, int64_t k) {
+  return h->ndim == 2 ? i * h->pitch + j : (i * h->ny + j) * h->pitch + k;
+}
+
+__global__ void transform_maps(float* rho_to_rdt, float* k_to_dtk, float* beta_to_2dt,
+                               float* inv_ku, float* inv_kx, int64_t n, float dt) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const float r = rho_to_rdt[c];
+    rho_to_rdt[c] = r != 0.f ? dt / r : 0.f;
+    k_to_dtk[c] = dt * k_to_dtk[c];
+    beta_to_2dt[c] = 2.f * dt * beta_to_2dt[c];
+    const float ku = inv_ku[c], kx = inv_kx[c];
+    inv_ku[c] = ku != 0.f ? 1.f / ku : 0.f;
+    inv_kx[c] = kx != 0.f ? 1.f / kx : 0.f;
+  }
+}
+
+__global__ void transpose_icmat(const float* src, float* dst, int ncoords, int nt_ic) {
+  // src [ncoords][nt_ic] -> dst [nt_ic][ncoords]
+  __shared__ float tile[32][33];
+  const int n0 = blockIdx.x * 32, k0 = blockIdx.y * 32;
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int k = k0 + r, n = n0 + threadIdx.x;
+    if (k < ncoords && n < nt_ic) tile[r][threadIdx.x] = src[(size_t)k * nt_ic + n];
+  }
+  __syncthreads();
+  for (int r = threadIdx.y; r < 32; r += blockDim.y) {
+    const int n = n0 + r, k = k0 + threadIdx.x;
+    if (k < ncoords && n < nt_ic) dst[(size_t)n * ncoords + k] = tile[threadIdx.x][r];
+  }
+}
+
+__global__ void any_nonzero(const float* a, int64_t n, int* flag) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x)
+    if (a[c] != 0.f) { *flag = 1; return; }
+}
+
+__global__ void gather_dense(const float* src, float* dst, int64_t rows, int64_t len,
+                             int64_t pitch) {
+  const int64_t total = rows * len;
+  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x)
+    dst[e] = src[(e / len) * pitch + e % len];
+}
+
+float* state_field(fw_handle* h, int idx) { return h->state + (size_t)idx * h->ncells_padded; }
+float* map_field(fw_handle* h, int idx) { return h->maps + (size_t)idx * h->ncells_padded; }
+
+// Copy a dense C-order grid array (host or device) into a padded device array.
+int upload_grid(fw_handle* h, void* dst, const void* src, size_t elem, bool on_device,
+                cudaStream_t s) {
+  const int64_t last = h->ndim == 2 ? h->ny : h->nz;
+  const int64_t rows = h->ndim == 2 ? h->nx : h->nx * h->ny;
+  FW_CUDA(h, cudaMemcpy2DAsync(dst, h->pitch * elem, src, last * elem, last * elem, rows,
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s));
+  return FW_OK;
+}
+
+void launch_step(fw_handle* h, cudaStream_t s) {
+  const Tiling& t = h->tiling;
+  if (h->ndim == 2) {
+    dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
+    vel2d_direct<<<grid, block, 0, s>>>(h->args);
+    if (h->has_beta) prs2d_direct<true><<<grid, block, 0, s>>>(h->args);
+    else prs2d_direct<false><<<grid, block, 0, s>>>(h->args);
+  } else {
+    dim3 grid(t.n[2], t.n[1], t.n[0]), block(kD3TZ, kD3TY, kD3TX);
+    vel3d_direct<<<grid, block, 0, s>>>(h->args);
+    if (h->has_beta) prs3d_direct<true><<<grid, block, 0, s>>>(h->args);
+    else prs3d_direct<false><<<grid, block, 0, s>>>(h->args);
+  }
+}
+
+int build_graph(fw_handle* h, int steps) {
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  FW_CUDA(h, cudaStreamBeginCapture(h->capture_stream, cudaStreamCaptureModeThreadLocal));
+  for (int n = 0; n < steps; ++n) launch_step(h, h->capture_stream);
+  cudaError_t e = cudaStreamEndCapture(h->capture_stream, &graph);
+  if (e != cudaSuccess) return fail(h, FW_ERR_CUDA, "graph capture failed: %s", cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&h->graph, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(h, FW_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
+  h->graph_steps = steps;
+  return FW_OK;
+}
+
+int check_desc(const fw_desc* d) {
+  if (!d) return fail(nullptr, FW_ERR_ARGUMENT, "desc is NULL");
+  if (d->ndim != 2 && d->ndim != 3) return fail(nullptr, FW_ERR_ARGUMENT, "ndim must be 2 or 3, got %d", d->ndim);
+  const int nz = d->ndim == 3 ? d->nz : 1;
+  if (d->nx <= 2 * kGhost || d->ny <= 2 * kGhost || (d->ndim == 3 && nz <= 2 * kGhost))
+    return fail(nullptr, FW_ERR_ARGUMENT, "every axis needs more than %d cells (got %d x %d x %d)",
+                2 * kGhost, d->nx, d->ny, nz);
+  if (d->nt < 0 || d->nt_ic < 0 || d->mod_t < 1 || d->ncoords < 0 || d->ncoordsout < 0 ||
+      d->ncoordszero < 0 || d->ndmap < 1)
+    return fail(nullptr, FW_ERR_ARGUMENT, "negative count or modT/ndmap < 1");
+  if (!(d->dt > 0.f) || !(d->dx > 0.f) || !(d->dy > 0.f) || (d->ndim == 3 && !(d->dz > 0.f)))
+    return fail(nullptr, FW_ERR_ARGUMENT, "grid spacing and time step must be positive");
+  if (d->isotropic != 1)
+    return fail(nullptr, FW_ERR_UNSUPPORTED, "only the isotropic relaxation engine is implemented");
+  if (d->n_relax != 2)
+    return fail(nullptr, FW_ERR_UNSUPPORTED, "only n_relax = 2 is implemented (got %d)", d->n_relax);
+  return FW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fw_abi_version(void) { return FWGB_ABI_VERSION; }
+
+int fw_create(const fw_desc* desc, fw_handle** out) {
+  if (!out) return fail(nullptr, FW_ERR_ARGUMENT, "out is NULL");
+  *out = nullptr;
+  int st = check_desc(desc);
+  if (st) return st;
+  fw_handle* h = new (std::nothrow) fw_handle();
+  if (!h) return fail(nullptr, FW_ERR_OOM, "host allocation failed");
+  h->d = *desc;
+  h->ndim = desc->ndim;
+  h->nx = desc->nx;
+  h->ny = desc->ny;
+  h->nz = desc->ndim == 3 ? desc->nz : 1;
+  h->pitch = round_up(h->ndim == 2 ? h->ny : h->nz, 32);
+  h->ncells_padded = h->ndim == 2 ? h->nx * h->pitch : h->nx * h->ny * h->pitch;
+  h->n_out = (desc->nt + desc->mod_t - 1) / desc->mod_t;
+  h->tiling = make_tiling(h);
+  auto alloc = [&](void** p, size_t bytes) -> int {
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+      cudaGetLastError();
+      return fail(nullptr, e == cudaErrorMemoryAllocation ? FW_ERR_OOM : FW_ERR_CUDA,
+                  "cudaMalloc(%zu bytes) failed: %s", bytes, cudaGetErrorString(e));
+    }
+    h->bytes += bytes;
+    return FW_OK;
+  };
+  const size_t cells = (size_t)h->ncells_padded;
+  if ((st = alloc((void**)&h->state, cells * n_state(h->ndim) * sizeof(float))) ||
+      (st = alloc((void**)&h->maps, cells * kMaps * sizeof(float))) ||
+      (st = alloc((void**)&h->dcmap, cells * sizeof(int32_t))) ||
+      (st = alloc((void**)&h->taps, (size_t)desc->ndmap * kTapStride * sizeof(float))) ||
+      (st = alloc((void**)&h->icmat_t, (size_t)desc->ncoords * desc->nt_ic * sizeof(float))) ||
+      (st = alloc((void**)&h->traces, (size_t)h->n_out * desc->ncoordsout * sizeof(float))) ||
+      (st = alloc((void**)&h->step, sizeof(int) * 4))) {
+    fw_destroy(h);
+    return st;
+  }
+  if (cudaStreamCreateWithFlags(&h->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    fw_destroy(h);
+    return fail(nullptr, FW_ERR_CUDA, "stream creation failed");
+  }
+  // zero everything once: ghost cells, padding and memory variables start at zero
+  if (cudaMemset(h->state, 0, cells * n_state(h->ndim) * sizeof(float)) != cudaSuccess ||
+      cudaMemset(h->maps, 0, cells * kMaps * sizeof(float)) != cudaSuccess ||
+      cudaMemset(h->dcmap, 0, cells * sizeof(int32_t)) != cudaSuccess ||
+      cudaMemset(h->step, 0, sizeof(int) * 4) != cudaSuccess) {
+    fw_destroy(h);
+    return fail(nullptr, FW_ERR_CUDA, "initial cudaMemset failed");
+  }
+  // argument block
+  StepArgs& A = h->args;
+  A.g.nx = (int)h->nx; A.g.ny = (int)h->ny; A.g.nz = (int)h->nz;
+  A.g.sx = h->ndim == 2 ? h->pitch : h->ny * h->pitch;
+  A.g.sy = h->ndim == 2 ? 1 : h->pitch;
+  A.g.inv_h[0] = 1.f / desc->dx;
+  A.g.inv_h[1] = 1.f / desc->dy;
+  A.g.inv_h[2] = h->ndim == 3 ? 1.f / desc->dz : 0.f;
+  int s = 0;
+  A.f.p = state_field(h, s++);
+  for (int a = 0; a < 3; ++a) A.f.v[a] = a < h->ndim ? state_field(h, s++) : nullptr;
+  for (int a = 0; a < 3; ++a)
+    for (int nu = 0; nu < 2; ++nu) A.f.psi[a][nu] = a < h->ndim ? state_field(h, s++) : nullptr;
+  for (int a = 0; a < 3; ++a)
+    for (int nu = 0; nu < 2; ++nu) A.f.phi[a][nu] = a < h->ndim ? state_field(h, s++) : nullptr;
+  A.m.rdt_rho = map_field(h, 0);
+  A.m.dt_k = map_field(h, 1);
+  A.m.beta2dt = map_field(h, 2);
+  A.m.inv_ku = map_field(h, 3);
+  A.m.inv_kx = map_field(h, 4);
+  A.m.au[0] = map_field(h, 5); A.m.bu[0] = map_field(h, 6);
+  A.m.au[1] = map_field(h, 7); A.m.bu[1] = map_field(h, 8);
+  A.m.ax[0] = map_field(h, 9); A.m.bx[0] = map_field(h, 10);
+  A.m.ax[1] = map_field(h, 11); A.m.bx[1] = map_field(h, 12);
+  A.m.dcmap = h->dcmap;
+  A.m.taps = h->taps;
+  A.l.icmat_t = h->icmat_t;
+  A.l.traces = h->traces;
+  A.l.ncoords = desc->ncoords;
+  A.l.ncoordsout = desc->ncoordsout;
+  A.l.nt_ic = desc->nt_ic;
+  A.l.mod_t = desc->mod_t;
+  A.step = h->step;
+  *out = h;
+  return FW_OK;
+}
+
+int fw_set_fields(fw_handle* h, const fw_fields* f) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  if (!f) return fail(h, FW_ERR_ARGUMENT, "fields is NULL");
+  const fw_desc& d = h->d;
+  const float* need[] = {f->d, f->dmap, f->c, f->rho, f->K, f->beta, f->kappax, f->kappau,
+                         f->apmlu1, f->bpmlu1, f->apmlx1, f->bpmlx1, f->apmlu2, f->bpmlu2,
+                         f->apmlx2, f->bpmlx2};
+  for (const float* p : need)
+    if (!p) return fail(h, FW_ERR_ARGUMENT, "a required map or table pointer is NULL");
+  if (!f->dcmap) return fail(h, FW_ERR_ARGUMENT, "dcmap is NULL");
+  if ((d.ncoords && (!f->icc || (d.nt_ic && !f->icmat))) || (d.ncoordsout && !f->outc) ||
+      (d.ncoordszero && !f->icczero))
+    return fail(h, FW_ERR_ARGUMENT, "coordinate or icmat pointer is NULL");
+  const bool dev = f->on_device != 0;
+  cudaStream_t s = h->capture_stream;
+  // captured graphs hold the old list pointers and kernel choice: rebuild them on next use
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+    h->graph_steps = 0;
+  }
+  const size_t dense = (size_t)h->nx * h->ny * h->nz;
+  const int nd = h->ndim;
+
+  // -- coordinates (validated on the host) and per-tile lists ---------------------------------
+  auto fetch_i32 = [&](const int32_t* src, size_t n, std::vector<int32_t>& out) -> int {
+    out.resize(n);
+    if (!n) return FW_OK;
+    FW_CUDA(h, cudaMemcpy(out.data(), src, n * sizeof(int32_t),
+                          dev ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+    return FW_OK;
+  };
+  std::vector<int32_t> icc, outc, zero, dcm;
+  int st;
+  if ((st = fetch_i32(f->icc, (size_t)d.ncoords * nd, icc)) ||
+      (st = fetch_i32(f->outc, (size_t)d.ncoordsout * nd, outc)) ||
+      (st = fetch_i32(f->icczero, (size_t)d.ncoordszero * nd, zero)) ||
+      (st = fetch_i32(f->dcmap, dense, dcm)))
+    return st;
+  for (size_t c = 0; c < dense; ++c)
+    if (dcm[c] < 0 || dcm[c] >= d.ndmap)
+      return fail(h, FW_ERR_ARGUMENT, "dcmap[%zu] = %d outside [0, %d)", c, dcm[c], d.ndmap);
+  const int64_t ext[3] = {h->nx, h->ny, h->nz};
+  auto cell_of = [&](const std::vector<int32_t>& v, size_t e, int64_t* cell, int* tile) -> bool {
+    int64_t q[3] = {0, 0, 0};
+    for (int a = 0; a < nd; ++a) {
+      q[a] = v[e * nd + a];
+      if (q[a] < 0 || q[a] >= ext[a]) return false;
+    }
+    *cell = padded_index(h, q[0], q[1], q[2]);
+    *tile = tile_of(h, q[0], q[1], q[2]);
+    return true;
+  };
+  const int ntiles = h->tiling.count();
+  struct Entry { int tile; int64_t cell; int32_t k; };
+  auto build = [&](const std::vector<int32_t>& v, int n, const char* name, bool dedupe_last,
+                   std::vector<Entry>& out) -> int {
+    out.clear();
+    out.reserve(n);
+    for (int e = 0; e < n; ++e) {
+      Entry en{0, 0, e};
+      if (!cell_of(v, (size_t)e, &en.cell, &en.tile))
+        return fail(h, FW_ERR_ARGUMENT, "%s[%d] lies outside the %d-D grid", name, e, nd);
+      out.push_back(en);
+    }
+    if (dedupe_last) {  // a cell listed twice is driven by its last entry
+      std::vector<Entry> tmp = out;
+      std::stable_sort(tmp.begin(), tmp.end(), [](const Entry& a, const Entry& b) { return a.cell < b.cell; });
+      out.clear();
+      for (size_t e = 0; e < tmp.size(); ++e)
+        if (e + 1 == tmp.size() || tmp[e + 1].cell != tmp[e].cell) out.push_back(tmp[e]);
+    }
+    std::stable_sort(out.begin(), out.end(), [](const Entry& a, const Entry& b) {
+      return a.tile != b.tile ? a.tile < b.tile : a.k < b.k;
+    });
+    return FW_OK;
+  };
+  std::vector<Entry> es, ez, eo;
+  if ((st = build(icc, d.ncoords, "icc", true, es)) ||
+      (st = build(zero, d.ncoordszero, "icczero", true, ez)) ||
+      (st = build(outc, d.ncoordsout, "outc", false, eo)))
+    return st;
+  // layout: src_ptr, zero_ptr, rec_ptr (int32, ntiles+1 each), src_k, rec_k (int32),
+  //         then src_cell, zero_cell, rec_cell (int64, 8-byte aligned)
+  const size_t n_i32 = 3 * (size_t)(ntiles + 1) + es.size() + eo.size();
+  const size_t off64 = round_up((int64_t)(n_i32 * 4), 16);
+  const size_t n_i64 = es.size() + ez.size() + eo.size();
+  std::vector<unsigned char> blob(off64 + n_i64 * 8 + 16, 0);
+  int32_t* i32 = reinterpret_cast<int32_t*>(blob.data());
+  int64_t* i64 = reinterpret_cast<int64_t*>(blob.data() + off64);
+  auto fill_ptr = [&](const std::vector<Entry>& v, int32_t* ptr) {
+    std::fill(ptr, ptr + ntiles + 1, 0);
+    for (const Entry& e : v) ptr[e.tile + 1]++;
+    for (int t = 0; t < ntiles; ++t) ptr[t + 1] += ptr[t];
+  };
+  int32_t* src_ptr = i32;
+  int32_t* zero_ptr = src_ptr + ntiles + 1;
+  int32_t* rec_ptr = zero_ptr + ntiles + 1;
+  int32_t* src_k = rec_ptr + ntiles + 1;
+  int32_t* rec_k = src_k + es.size();
+  fill_ptr(es, src_ptr);
+  fill_ptr(ez, zero_ptr);
+  fill_ptr(eo, rec_ptr);
+  int64_t* src_cell = i64;
+  int64_t* zero_cell = src_cell + es.size();
+  int64_t* rec_cell = zero_cell + ez.size();
+  for (size_t e = 0; e < es.size(); ++e) { src_k[e] = es[e].k; src_cell[e] = es[e].cell; }
+  for (size_t e = 0; e < ez.size(); ++e) zero_cell[e] = ez[e].cell;
+  for (size_t e = 0; e < eo.size(); ++e) { rec_k[e] = eo[e].k; rec_cell[e] = eo[e].cell; }
+  if (h->lists) { cudaFree(h->lists); h->lists = nullptr; }
+  FW_CUDA(h, cudaMalloc(&h->lists, blob.size()));
+  FW_CUDA(h, cudaMemcpy(h->lists, blob.data(), blob.size(), cudaMemcpyHostToDevice));
+  unsigned char* L = static_cast<unsigned char*>(h->lists);
+  const size_t o_src_k = (size_t)(src_k - i32) * 4, o_rec_k = (size_t)(rec_k - i32) * 4;
+  h->args.l.src_ptr = reinterpret_cast<int32_t*>(L);
+  h->args.l.zero_ptr = reinterpret_cast<int32_t*>(L) + ntiles + 1;
+  h->args.l.rec_ptr = reinterpret_cast<int32_t*>(L) + 2 * (ntiles + 1);
+  h->args.l.src_k = reinterpret_cast<int32_t*>(L + o_src_k);
+  h->args.l.rec_k = reinterpret_cast<int32_t*>(L + o_rec_k);
+  h->args.l.src_cell = reinterpret_cast<int64_t*>(L + off64);
+  h->args.l.zero_cell = reinterpret_cast<int64_t*>(L + off64) + es.size();
+  h->args.l.rec_cell = reinterpret_cast<int64_t*>(L + off64) + es.size() + ez.size();
+
+  // -- maps -------------------------------------------------------------------------------------
+  struct { const float* src; int idx; } mapsrc[] = {
+      {f->rho, 0}, {f->K, 1}, {f->beta, 2}, {f->kappau, 3}, {f->kappax, 4},
+      {f->apmlu1, 5}, {f->bpmlu1, 6}, {f->apmlu2, 7}, {f->bpmlu2, 8},
+      {f->apmlx1, 9}, {f->bpmlx1, 10}, {f->apmlx2, 11}, {f->bpmlx2, 12}};
+  for (auto& m : mapsrc)
+    if ((st = upload_grid(h, map_field(h, m.idx), m.src, sizeof(float), dev, s))) return st;
+  if ((st = upload_grid(h, h->dcmap, dcm.data(), sizeof(int32_t), false, s))) return st;
+  transform_maps<<<1024, 256, 0, s>>>(map_field(h, 0), map_field(h, 1), map_field(h, 2),
+                                      map_field(h, 3), map_field(h, 4), h->ncells_padded, d.dt);
+  FW_CUDA(h, cudaGetLastError());
+  // beta: use the nonlinear kernel only when some cell has beta != 0
+  any_nonzero<<<1024, 256, 0, s>>>(map_field(h, 2), h->ncells_padded, h->step + 2);
+  FW_CUDA(h, cudaGetLastError());
+  int flag = 0;
+  FW_CUDA(h, cudaMemcpyAsync(&flag, h->step + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FW_CUDA(h, cudaStreamSynchronize(s));
+  h->has_beta = flag != 0;
+  h->args.m.beta2dt = h->has_beta ? map_field(h, 2) : nullptr;
+
+  // -- tap table [ndmap][12] ----------------------------------------------------------------------
+  std::vector<float> dmap((size_t)18 * d.ndmap), taps((size_t)d.ndmap * kTapStride, 0.f);
+  FW_CUDA(h, cudaMemcpy(dmap.data(), f->dmap, dmap.size() * sizeof(float),
+                        dev ? cudaMemcpyDeviceToHost : cudaMemcpyHostToHost));
+  for (int e = 0; e < d.ndmap; ++e) {
+    for (int m = 1; m <= 8; ++m) taps[(size_t)e * kTapStride + m - 1] = dmap[((size_t)m * 2 + 0) * d.ndmap + e];
+    taps[(size_t)e * kTapStride + 8] = dmap[((size_t)1 * 2 + 1) * d.ndmap + e];
+  }
+  FW_CUDA(h, cudaMemcpy(h->taps, taps.data(), taps.size() * sizeof(float), cudaMemcpyHostToDevice));
+
+  // -- source signals -------------------------------------------------------------------------
+  h->fields_set = true;
+  if (d.ncoords && d.nt_ic) {
+    if ((st = fw_set_source_signal(h, f->icmat, f->on_device))) { h->fields_set = false; return st; }
+  }
+  st = fw_reset(h, s);
+  if (st) return st;
+  FW_CUDA(h, cudaStreamSynchronize(s));
+  return FW_OK;
+}
+
+int fw_set_source_signal(fw_handle* h, const float* icmat, int32_t on_device) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  const fw_desc& d = h->d;
+  if (!d.ncoords || !d.nt_ic) return FW_OK;
+  if (!icmat) return fail(h, FW_ERR_ARGUMENT, "icmat is NULL");
+  const size_t n = (size_t)d.ncoords * d.nt_ic;
+  float* staging = nullptr;
+  FW_CUDA(h, cudaMalloc(&staging, n * sizeof(float)));
+  cudaStream_t s = h->capture_stream;
+  cudaError_t e = cudaMemcpyAsync(staging, icmat, n * sizeof(float),
+                                  on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) {
+    dim3 grid((d.nt_ic + 31) / 32, (d.ncoords + 31) / 32), block(32, 8);
+    transpose_icmat<<<grid, block, 0, s>>>(staging, h->icmat_t, d.ncoords, d.nt_ic);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  cudaFree(staging);
+  if (e != cudaSuccess) return fail(h, FW_ERR_CUDA, "source upload failed: %s", cudaGetErrorString(e));
+  return FW_OK;
+}
+
+int fw_reset(fw_handle* h, void* stream) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  FW_CUDA(h, cudaMemsetAsync(h->state, 0, (size_t)h->ncells_padded * n_state(h->ndim) * sizeof(float), s));
+  FW_CUDA(h, cudaMemsetAsync(h->traces, 0, (size_t)h->n_out * h->d.ncoordsout * sizeof(float) + 0, s));
+  FW_CUDA(h, cudaMemsetAsync(h->step, 0, sizeof(int), s));
+  h->host_step = 0;
+  return FW_OK;
+}
+
+int fw_advance(fw_handle* h, void* stream, int32_t n_steps) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called before stepping");
+  if (n_steps < 0 || (int64_t)h->host_step + n_steps > h->d.nt)
+    return fail(h, FW_ERR_ARGUMENT, "cannot advance %d steps from step %d (nt = %d)", n_steps,
+                h->host_step, h->d.nt);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  constexpr int kGraphSteps = 64;
+  int left = n_steps;
+  if (left >= kGraphSteps) {
+    if (h->graph_steps != kGraphSteps) {
+      int st = build_graph(h, kGraphSteps);
+      if (st) return st;
+    }
+    while (left >= kGraphSteps) {
+      FW_CUDA(h, cudaGraphLaunch(h->graph, s));
+      left -= kGraphSteps;
+    }
+  }
+  for (; left > 0; --left) launch_step(h, s);
+  FW_CUDA(h, cudaGetLastError());
+  h->host_step += n_steps;
+  return FW_OK;
+}
+
+int fw_run(fw_handle* h, void* stream, float* out, int32_t out_on_device) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  int st;
+  if ((st = fw_reset(h, stream)) || (st = fw_advance(h, stream, h->d.nt))) return st;
+  if (out) return fw_read_traces(h, stream, 0, h->n_out, out, out_on_device);
+  return FW_OK;
+}
+
+int fw_read_traces(fw_handle* h, void* stream, int32_t row0, int32_t n_rows, float* dst,
+                   int32_t on_device) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  if (row0 < 0 || n_rows < 0 || row0 + n_rows > h->n_out)
+    return fail(h, FW_ERR_ARGUMENT, "trace rows [%d, %d) outside [0, %d)", row0, row0 + n_rows, h->n_out);
+  if (!dst && n_rows) return fail(h, FW_ERR_ARGUMENT, "dst is NULL");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t n = (size_t)n_rows * h->d.ncoordsout;
+  if (n) FW_CUDA(h, cudaMemcpyAsync(dst, h->traces + (size_t)row0 * h->d.ncoordsout, n * sizeof(float),
+                                    on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+  if (!on_device) FW_CUDA(h, cudaStreamSynchronize(s));
+  return FW_OK;
+}
+
+int fw_trace_buffer(fw_handle* h, float** dev_ptr) {
+  if (!h || !dev_ptr) return fail(h, FW_ERR_ARGUMENT, "NULL argument");
+  *dev_ptr = h->traces;
+  return FW_OK;
+}
+
+int fw_get_field(fw_handle* h, void* stream, int32_t field, float* dst, int32_t on_device) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  if (field < 0 || field > h->ndim || !dst) return fail(h, FW_ERR_ARGUMENT, "bad field %d or NULL dst", field);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const float* src = field == 0 ? h->args.f.p : h->args.f.v[field - 1];
+  const int64_t last = h->ndim == 2 ? h->ny : h->nz;
+  const int64_t rows = h->ndim == 2 ? h->nx : h->nx * h->ny;
+  FW_CUDA(h, cudaMemcpy2DAsync(dst, last * sizeof(float), src, h->pitch * sizeof(float),
+                               last * sizeof(float), rows,
+                               on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
+  if (!on_device) FW_CUDA(h, cudaStreamSynchronize(s));
+  return FW_OK;
+}
+
+int fw_current_step(const fw_handle* h, int32_t* step) {
+  if (!h || !step) return FW_ERR_ARGUMENT;
+  *step = h->host_step;
+  return FW_OK;
+}
+
+int fw_device_bytes(const fw_handle* h, uint64_t* bytes) {
+  if (!h || !bytes) return FW_ERR_ARGUMENT;
+  *bytes = h->bytes;
+  return FW_OK;
+}
+
+int fw_launches_per_step(const fw_handle* h, int32_t* n) {
+  if (!h || !n) return FW_ERR_ARGUMENT;
+  *n = 2;
+  return FW_OK;
+}
+
+int fw_destroy(fw_handle* h) {
+  if (!h) return FW_OK;
+  if (h->graph) cudaGraphExecDestroy(h->graph);
+  if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
+  void* ptrs[] = {h->state, h->maps, h->dcmap, h->taps, h->icmat_t, h->traces, h->step, h->lists};
+  for (void* p : ptrs)
+    if (p) cudaFree(p);
+  delete h;
+  return FW_OK;
+}
+
+const char* fw_last_error(const fw_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+}  // extern "C"

@@ -1,0 +1,103 @@
+// Shared definitions of the FDTD engine: device-side parameter blocks and small helpers.
+//
+// Memory layout in HBM (one handle = one simulation):
+//   every field and map is a separate float32 (dcmap: int32) array in C order with the last
+//   axis padded to a multiple of 32 elements (128 bytes), so that every row of the contiguous
+//   axis starts on a 128-byte boundary; padding and the 8-cell ghost layer hold zeros and are
+//   never updated. Cell (i, j[, k]) lives at ((i * ny + j) * pitch + k) in 3D and
+//   (i * pitch + j) in 2D.
+//   state  (read + written every step): p, v[ndim], psi[ndim][2] (pressure-gradient memory
+//          variables), phi[ndim][2] (velocity-divergence memory variables)
+//   maps   (read every step):  dt/rho, dt*K, 1/kappau, 1/kappax, a/b for u1 u2 x1 x2, dcmap,
+//          and 2*dt*beta only when beta is not identically zero
+//   taps   [ndmap][12] float32: axial taps c1..c8, off-axis tap, 3 zeros
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace fwgb {
+
+constexpr int kGhost = 8;          // taps per side = ghost cells per side
+constexpr int kTapStride = 12;     // floats per tap set
+
+struct Lists {
+  // Per-tile compressed lists (tile = the block of kernel B that owns the cell).
+  const int32_t* src_ptr;   // [n_tiles + 1]
+  const int64_t* src_cell;  // padded linear index
+  const int32_t* src_k;     // source index (row of icmat)
+  const int32_t* zero_ptr;
+  const int64_t* zero_cell;
+  const int32_t* rec_ptr;
+  const int64_t* rec_cell;
+  const int32_t* rec_k;     // sensor index (column of the traces)
+  const float* icmat_t;     // [nt_ic][ncoords]
+  float* traces;            // [n_out][ncoordsout]
+  int32_t ncoords, ncoordsout, nt_ic, mod_t;
+};
+
+struct Grid {
+  int32_t nx, ny, nz;        // nz = 1 in 2D
+  int64_t sx, sy;            // strides (elements) of axis x and y; the last axis has stride 1
+  float inv_h[3];            // 1/dx, 1/dy, 1/dz
+};
+
+struct Fields {
+  float* p;
+  float* v[3];
+  float* psi[3][2];
+  float* phi[3][2];
+};
+
+struct Maps {
+  const float* rdt_rho;      // dt / rho
+  const float* dt_k;         // dt * K
+  const float* beta2dt;      // 2 dt beta, or nullptr when beta == 0 everywhere
+  const float* inv_ku;       // 1 / kappau
+  const float* inv_kx;       // 1 / kappax
+  const float* au[2];
+  const float* bu[2];
+  const float* ax[2];
+  const float* bx[2];
+  const int32_t* dcmap;
+  const float* taps;         // [ndmap][12]
+};
+
+struct StepArgs {
+  Grid g;
+  Fields f;
+  Maps m;
+  Lists l;
+  int* step;                 // device step counter: velocity kernel of step n sets it to n+1
+};
+
+__device__ __forceinline__ void load_taps(const float* taps, int dc, float (&c)[8], float& co) {
+  const float4* t = reinterpret_cast<const float4*>(taps + (size_t)dc * kTapStride);
+  float4 a = __ldg(t), b = __ldg(t + 1), e = __ldg(t + 2);
+  c[0] = a.x; c[1] = a.y; c[2] = a.z; c[3] = a.w;
+  c[4] = b.x; c[5] = b.y; c[6] = b.z; c[7] = b.w;
+  co = e.x;
+}
+
+// Source injection, air zeroing and sensor recording for the cells owned by this block's tile.
+// Called by every thread of kernel B after its pressure writes; `tid`/`nthr` span the block.
+__device__ __forceinline__ void tile_epilogue(const StepArgs& A, float* p, int tile, int tid,
+                                              int nthr) {
+  const Lists& L = A.l;
+  const int n = *A.step - 1;
+  __syncthreads();
+  if (n < L.nt_ic) {
+    const float* col = L.icmat_t + (size_t)n * L.ncoords;
+    for (int e = L.src_ptr[tile] + tid; e < L.src_ptr[tile + 1]; e += nthr)
+      p[L.src_cell[e]] = col[L.src_k[e]];
+  }
+  __syncthreads();
+  for (int e = L.zero_ptr[tile] + tid; e < L.zero_ptr[tile + 1]; e += nthr) p[L.zero_cell[e]] = 0.f;
+  __syncthreads();
+  if (n % L.mod_t == 0) {
+    float* row = L.traces + (size_t)(n / L.mod_t) * L.ncoordsout;
+    for (int e = L.rec_ptr[tile] + tid; e < L.rec_ptr[tile + 1]; e += nthr)
+      row[L.rec_k[e]] = p[L.rec_cell[e]];
+  }
+}
+
+}  // namespace fwgb

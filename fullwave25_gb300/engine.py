@@ -1,0 +1,255 @@
+"""ctypes binding of the C ABI in ``include/fwgb.h`` (``libfwgb.so``).
+
+This is the only module that talks to the native library. There is no CPU fallback: if the
+library is missing or no CUDA device is present, :func:`load_library` / :class:`Engine` raise.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+import numpy as np
+
+from .inputs import ISOTROPIC_MAPS, EngineInputs
+
+LIB_PATH = Path(__file__).resolve().parent / "libfwgb.so"
+
+FW_STATUS = {0: "FW_OK", 1: "FW_ERR_ARGUMENT", 2: "FW_ERR_CUDA", 3: "FW_ERR_STATE",
+             4: "FW_ERR_OOM", 5: "FW_ERR_DEVICE", 6: "FW_ERR_UNSUPPORTED"}
+
+# every symbol include/fwgb.h declares
+EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_source_signal", "fw_run",
+            "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
+            "fw_current_step", "fw_device_bytes", "fw_launches_per_step", "fw_destroy",
+            "fw_last_error")
+
+
+class FwDesc(C.Structure):
+    _fields_ = [("ndim", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("nt", C.c_int32), ("nt_ic", C.c_int32), ("mod_t", C.c_int32),
+                ("dx", C.c_float), ("dy", C.c_float), ("dz", C.c_float), ("dt", C.c_float),
+                ("c0", C.c_float), ("ncoords", C.c_int32), ("ncoordsout", C.c_int32),
+                ("ncoordszero", C.c_int32), ("ndmap", C.c_int32), ("isotropic", C.c_int32),
+                ("n_relax", C.c_int32)]
+
+
+_FP = C.POINTER(C.c_float)
+_IP = C.POINTER(C.c_int32)
+
+
+class FwFields(C.Structure):
+    _fields_ = [("d", _FP), ("dmap", _FP), ("dcmap", _IP), ("c", _FP), ("rho", _FP), ("K", _FP),
+                ("beta", _FP), ("kappax", _FP), ("kappau", _FP),
+                ("apmlu1", _FP), ("bpmlu1", _FP), ("apmlx1", _FP), ("bpmlx1", _FP),
+                ("apmlu2", _FP), ("bpmlu2", _FP), ("apmlx2", _FP), ("bpmlx2", _FP),
+                ("icc", _IP), ("outc", _IP), ("icczero", _IP), ("icmat", _FP),
+                ("on_device", C.c_int32)]
+
+
+class EngineError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, call: str, status: int, message: str) -> None:
+        super().__init__(f"{call} -> {FW_STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def load_library(path: Path | None = None) -> C.CDLL:
+    """Load ``libfwgb.so`` and declare its signatures; raises if it is not built."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise FileNotFoundError(
+            f"{p} is missing: build the CUDA engine first (python -m fullwave25_gb300.build)")
+    lib = C.CDLL(str(p))
+    vp = C.c_void_p
+    H = C.c_void_p
+    sig = {
+        "fw_abi_version": (C.c_int, []),
+        "fw_create": (C.c_int, [C.POINTER(FwDesc), C.POINTER(H)]),
+        "fw_set_fields": (C.c_int, [H, C.POINTER(FwFields)]),
+        "fw_set_source_signal": (C.c_int, [H, _FP, C.c_int32]),
+        "fw_run": (C.c_int, [H, vp, _FP, C.c_int32]),
+        "fw_reset": (C.c_int, [H, vp]),
+        "fw_advance": (C.c_int, [H, vp, C.c_int32]),
+        "fw_read_traces": (C.c_int, [H, vp, C.c_int32, C.c_int32, _FP, C.c_int32]),
+        "fw_trace_buffer": (C.c_int, [H, C.POINTER(_FP)]),
+        "fw_get_field": (C.c_int, [H, vp, C.c_int32, _FP, C.c_int32]),
+        "fw_current_step": (C.c_int, [H, _IP]),
+        "fw_device_bytes": (C.c_int, [H, C.POINTER(C.c_uint64)]),
+        "fw_launches_per_step": (C.c_int, [H, _IP]),
+        "fw_destroy": (C.c_int, [H]),
+        "fw_last_error": (C.c_char_p, [H]),
+    }
+    for name, (res, args) in sig.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+def _fp(a):
+    return a.ctypes.data_as(_FP) if a is not None else None
+
+
+def _ip(a):
+    return a.ctypes.data_as(_IP) if a is not None else None
+
+
+def _c_f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _c_i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def desc_from_inputs(inp: EngineInputs) -> FwDesc:
+    nz = inp.shape[2] if inp.ndim == 3 else 1
+    dz = inp.spacing[2] if inp.ndim == 3 else 0.0
+    return FwDesc(ndim=inp.ndim, nx=inp.shape[0], ny=inp.shape[1], nz=nz, nt=inp.nt,
+                  nt_ic=inp.nt_ic, mod_t=inp.mod_t, dx=inp.spacing[0], dy=inp.spacing[1], dz=dz,
+                  dt=inp.dt, c0=inp.c0, ncoords=inp.icc.shape[0], ncoordsout=inp.outc.shape[0],
+                  ncoordszero=inp.icczero.shape[0], ndmap=inp.dmap.shape[2], isotropic=1,
+                  n_relax=2)
+
+
+class Engine:
+    """One simulation on the current CUDA device, driven through the C ABI."""
+
+    def __init__(self, inputs: EngineInputs, *, validate: bool = True) -> None:
+        if validate:
+            inputs.validate()
+        self.lib = load_library()
+        self.inputs = inputs
+        self.desc = desc_from_inputs(inputs)
+        self._h = C.c_void_p()
+        self._check("fw_create", self.lib.fw_create(C.byref(self.desc), C.byref(self._h)), None)
+        try:
+            self.set_fields(inputs)
+        except Exception:
+            self.close()
+            raise
+
+    # -- plumbing -----------------------------------------------------------------------------
+    def _check(self, call: str, status: int, handle) -> None:
+        if status != 0:
+            msg = self.lib.fw_last_error(handle)
+            raise EngineError(call, status, msg.decode() if msg else "")
+
+    def _call(self, name: str, *args) -> None:
+        self._check(name, getattr(self.lib, name)(self._h, *args), self._h)
+
+    @property
+    def handle(self) -> C.c_void_p:
+        return self._h
+
+    def set_fields(self, inp: EngineInputs) -> None:
+        keep = {}  # holds the contiguous copies alive during the call
+
+        def f(name, arr, conv):
+            keep[name] = conv(arr)
+            return keep[name]
+
+        m = inp.maps
+        fields = FwFields(
+            d=_fp(f("d", inp.d, _c_f32)), dmap=_fp(f("dmap", inp.dmap, _c_f32)),
+            dcmap=_ip(f("dcmap", inp.dcmap, _c_i32)), on_device=0,
+            icc=_ip(f("icc", inp.icc, _c_i32)), outc=_ip(f("outc", inp.outc, _c_i32)),
+            icczero=_ip(f("icczero", inp.icczero, _c_i32)),
+            icmat=_fp(f("icmat", inp.icmat, _c_f32)),
+            **{k: _fp(f(k, m[k], _c_f32)) for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)},
+        )
+        self._call("fw_set_fields", C.byref(fields))
+
+    def set_source_signal(self, icmat: np.ndarray) -> None:
+        a = _c_f32(icmat)
+        if a.shape != self.inputs.icmat.shape:
+            raise ValueError(f"icmat must be {self.inputs.icmat.shape}, got {a.shape}")
+        self._call("fw_set_source_signal", _fp(a), 0)
+
+    # -- stepping -----------------------------------------------------------------------------
+    @property
+    def n_out(self) -> int:
+        return self.inputs.n_out
+
+    def run(self, stream: int | None = None) -> np.ndarray:
+        """Full solve; returns the float32 traces ``[n_out, ncoordsout]`` (genout layout)."""
+        out = np.empty((self.n_out, self.inputs.outc.shape[0]), dtype=np.float32)
+        self._call("fw_run", C.c_void_p(stream or 0), _fp(out), 0)
+        return out
+
+    def run_into(self, dev_ptr: int, stream: int | None = None) -> None:
+        """Full solve writing the traces into device memory at ``dev_ptr`` (asynchronous)."""
+        self._call("fw_run", C.c_void_p(stream or 0), C.cast(C.c_void_p(dev_ptr), _FP), 1)
+
+    def reset(self, stream: int | None = None) -> None:
+        self._call("fw_reset", C.c_void_p(stream or 0))
+
+    def advance(self, n_steps: int, stream: int | None = None) -> None:
+        self._call("fw_advance", C.c_void_p(stream or 0), int(n_steps))
+
+    def read_traces(self, row0: int = 0, n_rows: int | None = None,
+                    stream: int | None = None) -> np.ndarray:
+        n_rows = self.n_out - row0 if n_rows is None else n_rows
+        out = np.empty((n_rows, self.inputs.outc.shape[0]), dtype=np.float32)
+        self._call("fw_read_traces", C.c_void_p(stream or 0), int(row0), int(n_rows), _fp(out), 0)
+        return out
+
+    def read_traces_into(self, row0: int, n_rows: int, dev_ptr: int,
+                         stream: int | None = None) -> None:
+        self._call("fw_read_traces", C.c_void_p(stream or 0), int(row0), int(n_rows),
+                   C.cast(C.c_void_p(dev_ptr), _FP), 1)
+
+    def trace_buffer(self) -> int:
+        p = _FP()
+        self._call("fw_trace_buffer", C.byref(p))
+        return C.cast(p, C.c_void_p).value
+
+    def get_field(self, field: int = 0, stream: int | None = None) -> np.ndarray:
+        out = np.empty(self.inputs.shape, dtype=np.float32)
+        self._call("fw_get_field", C.c_void_p(stream or 0), int(field), _fp(out), 0)
+        return out
+
+    @property
+    def current_step(self) -> int:
+        v = C.c_int32()
+        self._call("fw_current_step", C.byref(v))
+        return v.value
+
+    @property
+    def device_bytes(self) -> int:
+        v = C.c_uint64()
+        self._call("fw_device_bytes", C.byref(v))
+        return v.value
+
+    @property
+    def launches_per_step(self) -> int:
+        v = C.c_int32()
+        self._call("fw_launches_per_step", C.byref(v))
+        return v.value
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            self.lib.fw_destroy(self._h)
+            self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -1,0 +1,144 @@
+/*
+ * fwgb.h — C ABI of the GB300 (sm_103a) FDTD engine for Fullwave 2.5 simulations.
+ *
+ * This library replaces the reference's engine boundary: the closed executable that
+ * fullwave/solver/launcher.py:196-215 runs in a simulation directory, which reads the `.dat`
+ * input set written by fullwave/solver/input_file_writer.py:105-179 and writes `genout.dat`
+ * (float32, time-major [n_out, ncoordsout]) that launcher.py:243-251 loads. Here the same
+ * arrays are passed in memory and the traces come back in the same layout.
+ *
+ * Conventions: every entry point returns an int status (FW_OK = 0); no C++ exception, abort or
+ * device trap crosses this boundary. On failure, fw_last_error() describes the cause. A handle
+ * is used from one host thread at a time; separate handles may run concurrently on separate
+ * CUDA streams. Streams are passed as `void*` (a cudaStream_t; NULL = legacy default stream).
+ */
+#ifndef FWGB_H
+#define FWGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FWGB_ABI_VERSION 1
+
+#if defined(__GNUC__)
+#define FWGB_API __attribute__((visibility("default")))
+#else
+#define FWGB_API
+#endif
+
+enum fw_status {
+    FW_OK = 0,
+    FW_ERR_ARGUMENT = 1,    /* a size, pointer or index is invalid */
+    FW_ERR_CUDA = 2,        /* a CUDA runtime call failed */
+    FW_ERR_STATE = 3,       /* call out of order (e.g. run before fields are set) */
+    FW_ERR_OOM = 4,         /* device allocation failed */
+    FW_ERR_DEVICE = 5,      /* a kernel reported an error through the device status word */
+    FW_ERR_UNSUPPORTED = 6  /* valid input the engine does not implement */
+};
+
+/* Scalars of the engine's file contract: nX nY nZ nT nTic modT dX dY dZ dT c0 ncoords
+ * ncoordsout ncoordszero ndmap (input_file_writer.py:763-803), plus the engine variant.
+ * For 2D, nz = 1 and dz is ignored. The x axis (nx) is the slowest-varying index of every map,
+ * the last axis the fastest (C order, input_file_writer.py:870-881). */
+typedef struct fw_desc {
+    int32_t ndim;           /* 2 or 3 */
+    int32_t nx, ny, nz;
+    int32_t nt;             /* time steps */
+    int32_t nt_ic;          /* columns of icmat: source drives steps n < nt_ic */
+    int32_t mod_t;          /* record every mod_t steps (n % mod_t == 0) */
+    float dx, dy, dz, dt, c0;
+    int32_t ncoords;        /* source cells */
+    int32_t ncoordsout;     /* sensor cells */
+    int32_t ncoordszero;    /* air (zero-pressure) cells */
+    int32_t ndmap;          /* tap sets in dmap */
+    int32_t isotropic;      /* must be 1: the isotropic relaxation build */
+    int32_t n_relax;        /* must be 2 relaxation mechanisms */
+} fw_desc;
+
+/* Arrays of the file contract. Maps are float32 [nx*ny*nz] C order; dcmap int32 of the same
+ * shape holding 0-based tap-set indices; d float32[9*2]; dmap float32[9*2*ndmap] laid out
+ * [9][2][ndmap]; icc/outc/icczero int32 [n][ndim] row-major (x, y[, z]); icmat float32
+ * [ncoords][nt_ic]. `c` and `d` are accepted for contract completeness and validated but the
+ * time loop reads the per-cell tap sets (dmap, dcmap), K and rho. Pointers are host memory
+ * unless on_device = 1 (then device pointers on the handle's device). */
+typedef struct fw_fields {
+    const float *d, *dmap;
+    const int32_t *dcmap;
+    const float *c, *rho, *K, *beta;
+    const float *kappax, *kappau;
+    const float *apmlu1, *bpmlu1, *apmlx1, *bpmlx1;
+    const float *apmlu2, *bpmlu2, *apmlx2, *bpmlx2;
+    const int32_t *icc, *outc, *icczero;
+    const float *icmat;
+    int32_t on_device;
+} fw_fields;
+
+typedef struct fw_handle fw_handle;
+
+/* Library ABI version (FWGB_ABI_VERSION). */
+FWGB_API int fw_abi_version(void);
+
+/* Create an engine for one simulation geometry on the current CUDA device.
+ * Replaces: the executable's start-up that reads nX..ndmap (launcher.py:196-215). */
+FWGB_API int fw_create(const fw_desc *desc, fw_handle **out);
+
+/* Copy the medium, coefficient tables, source/sensor/air coordinates and source signals into
+ * engine-owned device memory, and reset the wavefield.
+ * Replaces: the executable reading d dmap dcmap c rho K beta kappa* apml* bpml* icc outc icmat
+ * icczero (InputFileWriter._save_variables_into_dat_file, input_file_writer.py:563-645). */
+FWGB_API int fw_set_fields(fw_handle *h, const fw_fields *f);
+
+/* Replace only the source signals (a new transmit event on the same medium), float32
+ * [ncoords][nt_ic]. Replaces: the is_static_map re-run that rewrites icmat.dat only
+ * (input_file_writer.py:145-169). */
+FWGB_API int fw_set_source_signal(fw_handle *h, const float *icmat, int32_t on_device);
+
+/* Full solve: reset the wavefield, run nt steps on `stream`, and copy the traces
+ * [n_out][ncoordsout] (n_out = ceil(nt / mod_t)) to `out` (host memory unless
+ * out_on_device = 1). Synchronises `stream` before returning when out is host memory.
+ * Replaces: the executable's time loop and genout.dat (launcher.py:207-251). */
+FWGB_API int fw_run(fw_handle *h, void *stream, float *out, int32_t out_on_device);
+
+/* Zero the wavefield, memory variables, traces and step counter (asynchronous on stream). */
+FWGB_API int fw_reset(fw_handle *h, void *stream);
+
+/* Advance n_steps time steps from the current step (asynchronous on stream). The traces of
+ * recorded steps accumulate in the engine's device trace buffer. */
+FWGB_API int fw_advance(fw_handle *h, void *stream, int32_t n_steps);
+
+/* Copy trace rows [row0, row0 + n_rows) to `dst` (host unless on_device = 1); asynchronous on
+ * stream for device dst, synchronous for host dst. */
+FWGB_API int fw_read_traces(fw_handle *h, void *stream, int32_t row0, int32_t n_rows, float *dst,
+                   int32_t on_device);
+
+/* Device pointer of the trace buffer [n_out][ncoordsout] (valid until fw_destroy). */
+FWGB_API int fw_trace_buffer(fw_handle *h, float **dev_ptr);
+
+/* Copy a wavefield component to dst as a dense C-order [nx][ny][nz] float32 array.
+ * field: 0 = p, 1..3 = velocity along x, y, z (staggered +1/2 on that axis). */
+FWGB_API int fw_get_field(fw_handle *h, void *stream, int32_t field, float *dst, int32_t on_device);
+
+/* Steps taken since the last reset (host-side count of issued steps). */
+FWGB_API int fw_current_step(const fw_handle *h, int32_t *step);
+
+/* Device bytes held by the handle. */
+FWGB_API int fw_device_bytes(const fw_handle *h, uint64_t *bytes);
+
+/* Kernel launches issued per time step (for launch accounting). */
+FWGB_API int fw_launches_per_step(const fw_handle *h, int32_t *n);
+
+/* Release all device memory of the handle. */
+FWGB_API int fw_destroy(fw_handle *h);
+
+/* Description of the last failure on this handle (or of the last failed fw_create when
+ * h == NULL). Never NULL. */
+FWGB_API const char *fw_last_error(const fw_handle *h);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FWGB_H */

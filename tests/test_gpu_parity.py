@@ -1,0 +1,142 @@
+"""GPU engine vs the FP64 oracle through the C ABI (``-m gpu``).
+
+Tolerance: sensor traces of the FP32 engine within 1e-4 relative L2 of the FP64 oracle
+(``||engine - oracle|| / ||oracle||``), the bar the benchmark configurations set.
+Size-independent properties at the full plain-2D workload size (944 x 688 extended, 4000 steps):
+bitwise determinism, bitwise time-shift invariance, linearity to 1e-5, finite output.
+"""
+
+import tempfile
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from fdtd_oracle import rel_l2, run_oracle
+from golden_io import CASE_NAMES, HERE, load_case_inputs, write_case_dir
+
+pytestmark = pytest.mark.gpu
+TOL = 1e-4
+TRACES = np.load(HERE / "oracle_traces.npz")
+
+
+@pytest.mark.parametrize("name", CASE_NAMES)
+def test_launcher_dropin_matches_oracle(engine_lib, cuda, name):
+    from fullwave25_gb300 import Launcher
+
+    with tempfile.TemporaryDirectory() as td:
+        sim = write_case_dir(name, Path(td) / name)
+        inp = load_case_inputs(name)
+        launcher = Launcher(is_3d=inp.ndim == 3, cuda_device_id=0)
+        flat = launcher.run(sim)
+        assert flat.dtype == np.float32 and flat.ndim == 1
+        assert (sim / "genout.dat").exists()
+        got = flat.reshape(-1, inp.outc.shape[0])
+        ref = TRACES[name]
+        assert got.shape == ref.shape
+        err = rel_l2(got, ref)
+        assert err < TOL, f"{name}: rel-L2 {err:.3e}"
+        assert launcher.run(sim, load_results=False) == sim / "genout.dat"
+
+
+def test_launcher_reports_failure_as_simulation_error(engine_lib, cuda):
+    from fullwave25_gb300 import Launcher, SimulationError
+
+    with tempfile.TemporaryDirectory() as td:
+        with pytest.raises(SimulationError):
+            Launcher().run(Path(td))
+        assert (Path(td) / "fw2_execution.log").exists()
+
+
+def test_engine_rejects_out_of_grid_sensor_without_fault(engine_lib, cuda):
+    from fullwave25_gb300.engine import Engine, EngineError
+
+    inp = load_case_inputs("2d_small")
+    inp.outc = inp.outc.copy()
+    inp.outc[1, 1] = 10_000
+    with pytest.raises(EngineError, match="FW_ERR_ARGUMENT"):
+        Engine(inp, validate=False)
+    # the context is still usable
+    good = load_case_inputs("2d_small")
+    with Engine(good) as eng:
+        assert rel_l2(eng.run(), TRACES["2d_small"]) < TOL
+
+
+def test_chunked_advance_equals_full_run(engine_lib, cuda):
+    from fullwave25_gb300.engine import Engine
+
+    inp = load_case_inputs("3d_small")
+    with Engine(inp) as eng:
+        full = eng.run()
+        eng.reset()
+        for n in (1, 64, 17, 38):
+            eng.advance(n)
+        assert eng.current_step == inp.nt
+        chunked = eng.read_traces()
+    np.testing.assert_array_equal(full, chunked)
+
+
+def test_new_source_signal_reuses_medium(engine_lib, cuda):
+    from fullwave25_gb300.engine import Engine
+
+    inp = load_case_inputs("2d_small")
+    with Engine(inp) as eng:
+        eng.run()
+        new = (np.roll(inp.icmat, 5, axis=1) * -0.5).astype(np.float32)
+        eng.set_source_signal(new)
+        got = eng.run()
+    inp.icmat = new
+    assert rel_l2(got, run_oracle(inp)) < TOL
+
+
+def test_solver_api_small_problem(engine_lib, cuda):
+    from fullwave25_gb300 import Solver
+    from fullwave25_gb300.workloads import plain_2d_problem
+
+    grid, medium, source, sensor, _ = plain_2d_problem(shape=(96, 80), nt=300, seed=3)
+    solver = Solver(Path(tempfile.gettempdir()), grid, medium, source, sensor,
+                    pml_layer_thickness_px=12, n_transition_layer=12)
+    out = solver.run()
+    assert out.shape == (sensor.n_sensors, 300)
+    inputs, _ = solver.build_engine_inputs()
+    ref = run_oracle(inputs).T
+    assert rel_l2(out, ref) < TOL
+
+
+def test_plain_2d_reduced_matches_oracle(engine_lib, cuda):
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.workloads import plain_2d_inputs
+
+    inp = plain_2d_inputs(shape=(192, 160), nt=500, n_pml=20, n_transition=20)
+    with Engine(inp) as eng:
+        got = eng.run()
+    err = rel_l2(got, run_oracle(inp))
+    assert err < TOL, f"rel-L2 {err:.3e}"
+
+
+@pytest.fixture(scope="module")
+def plain_2d_full():
+    from fullwave25_gb300.workloads import plain_2d_inputs
+
+    return plain_2d_inputs()
+
+
+def test_full_size_determinism_linearity_shift(engine_lib, cuda, plain_2d_full):
+    from fullwave25_gb300.engine import Engine
+
+    inp = plain_2d_full
+    with Engine(inp) as eng:
+        a = eng.run()
+        b = eng.run()
+        np.testing.assert_array_equal(a, b)
+        assert np.isfinite(a).all() and np.abs(a).max() > 0
+        eng.set_source_signal((inp.icmat * np.float32(2.0)).astype(np.float32))
+        c = eng.run()
+        assert rel_l2(c, 2.0 * a) < 1e-5
+        shift = 11
+        sh = np.zeros_like(inp.icmat)
+        sh[:, shift:] = inp.icmat[:, :-shift]
+        eng.set_source_signal(sh)
+        d = eng.run()
+    np.testing.assert_array_equal(d[shift:], a[:-shift])
+    assert not d[:shift].any()
