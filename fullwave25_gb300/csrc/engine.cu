@@ -503,6 +503,21 @@ int fw_set_source_signal(fw_handle* h, const float* icmat, int32_t on_device) {
   return FW_OK;
 }
 
+int fw_set_source_columns(fw_handle* h, void* stream, const float* cols, int32_t n0,
+                          int32_t ncols, int32_t on_device) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  const fw_desc& d = h->d;
+  if (n0 < 0 || ncols < 0 || (int64_t)n0 + ncols > d.nt_ic)
+    return fail(h, FW_ERR_ARGUMENT, "source columns [%d, %d) outside [0, %d)", n0, n0 + ncols, d.nt_ic);
+  if (!d.ncoords || !ncols) return FW_OK;
+  if (!cols) return fail(h, FW_ERR_ARGUMENT, "cols is NULL");
+  FW_CUDA(h, cudaMemcpyAsync(h->icmat_t + (size_t)n0 * d.ncoords, cols,
+                             (size_t)ncols * d.ncoords * sizeof(float),
+                             on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                             static_cast<cudaStream_t>(stream)));
+  return FW_OK;
+}
+
 int fw_reset(fw_handle* h, void* stream) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   cudaStream_t s = static_cast<cudaStream_t>(stream);

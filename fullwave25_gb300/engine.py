@@ -19,7 +19,8 @@ FW_STATUS = {0: "FW_OK", 1: "FW_ERR_ARGUMENT", 2: "FW_ERR_CUDA", 3: "FW_ERR_STAT
              4: "FW_ERR_OOM", 5: "FW_ERR_DEVICE", 6: "FW_ERR_UNSUPPORTED"}
 
 # every symbol include/fwgb.h declares
-EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_source_signal", "fw_run",
+EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_source_signal",
+            "fw_set_source_columns", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
             "fw_current_step", "fw_device_bytes", "fw_launches_per_step", "fw_destroy",
             "fw_last_error")
@@ -75,6 +76,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_create": (C.c_int, [C.POINTER(FwDesc), C.POINTER(H)]),
         "fw_set_fields": (C.c_int, [H, C.POINTER(FwFields)]),
         "fw_set_source_signal": (C.c_int, [H, _FP, C.c_int32]),
+        "fw_set_source_columns": (C.c_int, [H, vp, _FP, C.c_int32, C.c_int32, C.c_int32]),
         "fw_run": (C.c_int, [H, vp, _FP, C.c_int32]),
         "fw_reset": (C.c_int, [H, vp]),
         "fw_advance": (C.c_int, [H, vp, C.c_int32]),
@@ -112,11 +114,12 @@ def _c_i32(a):
     return np.ascontiguousarray(a, dtype=np.int32)
 
 
-def desc_from_inputs(inp: EngineInputs) -> FwDesc:
+def desc_from_inputs(inp) -> FwDesc:
     nz = inp.shape[2] if inp.ndim == 3 else 1
     dz = inp.spacing[2] if inp.ndim == 3 else 0.0
     return FwDesc(ndim=inp.ndim, nx=inp.shape[0], ny=inp.shape[1], nz=nz, nt=inp.nt,
-                  nt_ic=inp.nt_ic, mod_t=inp.mod_t, dx=inp.spacing[0], dy=inp.spacing[1], dz=dz,
+                  nt_ic=int(inp.icmat.shape[1]), mod_t=inp.mod_t, dx=inp.spacing[0],
+                  dy=inp.spacing[1], dz=dz,
                   dt=inp.dt, c0=inp.c0, ncoords=inp.icc.shape[0], ncoordsout=inp.outc.shape[0],
                   ncoordszero=inp.icczero.shape[0], ndmap=inp.dmap.shape[2], isotropic=1,
                   n_relax=2)
@@ -125,8 +128,8 @@ def desc_from_inputs(inp: EngineInputs) -> FwDesc:
 class Engine:
     """One simulation on the current CUDA device, driven through the C ABI."""
 
-    def __init__(self, inputs: EngineInputs, *, validate: bool = True) -> None:
-        if validate:
+    def __init__(self, inputs, *, validate: bool = True) -> None:
+        if validate and isinstance(inputs, EngineInputs):
             inputs.validate()
         self.lib = load_library()
         self.inputs = inputs
@@ -152,7 +155,9 @@ class Engine:
     def handle(self) -> C.c_void_p:
         return self._h
 
-    def set_fields(self, inp: EngineInputs) -> None:
+    def set_fields(self, inp) -> None:
+        if not isinstance(inp, EngineInputs):
+            return self._set_device_fields(inp)
         keep = {}  # holds the contiguous copies alive during the call
 
         def f(name, arr, conv):
@@ -169,6 +174,38 @@ class Engine:
             **{k: _fp(f(k, m[k], _c_f32)) for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)},
         )
         self._call("fw_set_fields", C.byref(fields))
+
+    def _set_device_fields(self, inp) -> None:
+        """Fields given as CUDA tensors (``workloads3d.DeviceInputs``): no host round trip."""
+        import torch  # noqa: PLC0415
+
+        dev = inp.maps["rho"].device
+        keep = {"d": torch.as_tensor(np.ascontiguousarray(inp.d, np.float32), device=dev),
+                "dmap": torch.as_tensor(np.ascontiguousarray(inp.dmap, np.float32), device=dev)}
+        fptr = lambda t: C.cast(C.c_void_p(t.data_ptr()), _FP) if t.numel() else None  # noqa: E731
+        iptr = lambda t: C.cast(C.c_void_p(t.data_ptr()), _IP) if t.numel() else None  # noqa: E731
+        m = inp.maps
+        for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS):
+            assert m[k].dtype == torch.float32 and m[k].is_contiguous() and m[k].is_cuda, k
+        fields = FwFields(
+            d=fptr(keep["d"]), dmap=fptr(keep["dmap"]), dcmap=iptr(inp.dcmap),
+            icc=iptr(inp.icc), outc=iptr(inp.outc), icczero=iptr(inp.icczero),
+            icmat=fptr(inp.icmat), on_device=1,
+            **{k: fptr(m[k]) for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)})
+        torch.cuda.synchronize(dev)
+        self._call("fw_set_fields", C.byref(fields))
+
+    def set_source_columns(self, cols: np.ndarray, n0: int, stream: int | None = None) -> None:
+        """Upload source samples of steps ``[n0, n0 + len(cols))`` (time-major, host)."""
+        a = np.ascontiguousarray(cols, dtype=np.float32)
+        self._call("fw_set_source_columns", C.c_void_p(stream or 0), _fp(a), int(n0),
+                   int(a.shape[0]), 0)
+
+    def read_traces_to(self, dst: np.ndarray, row0: int, stream: int | None = None) -> None:
+        """Copy trace rows ``[row0, row0 + len(dst))`` into the host array ``dst``."""
+        assert dst.dtype == np.float32 and dst.flags.c_contiguous
+        self._call("fw_read_traces", C.c_void_p(stream or 0), int(row0), int(dst.shape[0]),
+                   _fp(dst), 0)
 
     def set_source_signal(self, icmat: np.ndarray) -> None:
         a = _c_f32(icmat)

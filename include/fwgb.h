@@ -96,6 +96,12 @@ FWGB_API int fw_set_fields(fw_handle *h, const fw_fields *f);
  * (input_file_writer.py:145-169). */
 FWGB_API int fw_set_source_signal(fw_handle *h, const float *icmat, int32_t on_device);
 
+/* Overwrite the source samples of steps [n0, n0 + ncols) with `cols`, float32 time-major
+ * [ncols][ncoords] (row = one time step), asynchronously on `stream`; for streaming transmit
+ * signals step block by step block. */
+FWGB_API int fw_set_source_columns(fw_handle *h, void *stream, const float *cols, int32_t n0,
+                                   int32_t ncols, int32_t on_device);
+
 /* Full solve: reset the wavefield, run nt steps on `stream`, and copy the traces
  * [n_out][ncoordsout] (n_out = ceil(nt / mod_t)) to `out` (host memory unless
  * out_on_device = 1). Synchronises `stream` before returning when out is host memory.
