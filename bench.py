@@ -144,9 +144,10 @@ def make_workload(name: str, rank: int):
 
 # --------------------------------------------------------------------------------- CPU baseline
 def time_oracle(workload: str, budget_s: float):
-    """FP64 oracle on a bounded sample: the workload's grid for as many steps as fit in budget."""
+    """FP64 C oracle (OpenMP, all host cores) on a bounded sample of the workload: the 2D grid,
+    or a 96^3 block of the 3D medium, for as many time steps as fit in ``budget_s``."""
     sys.path.insert(0, str(ROOT / "oracle"))
-    from fdtd_oracle import Oracle
+    from fdtd_oracle_c import OracleC
 
     if workload == "plain2d":
         from fullwave25_gb300.workloads import plain_2d_inputs
@@ -158,17 +159,19 @@ def time_oracle(workload: str, budget_s: float):
 
         inp = plain_3d_host_sample()
         label = f"plain 3D medium, {inp.shape[0]}x{inp.shape[1]}x{inp.shape[2]} sub-block"
-    o = Oracle(inp)
-    o.step()  # warm-up
+    o = OracleC(inp)
+    o.run(1)  # warm-up
     steps, t0 = 0, time.perf_counter()
-    while time.perf_counter() - t0 < budget_s and steps < inp.nt - 1:
-        o.step()
-        steps += 1
+    while time.perf_counter() - t0 < budget_s and steps + 10 < inp.nt:
+        o.run(10)
+        steps += 10
     el = time.perf_counter() - t0
+    o.close()
     cells = int(np.prod(inp.shape))
-    return {"value": cells * steps / el / 1e9, "unit": METRIC, "cores": 1, "kind": "port",
-            "sample": f"FP64 NumPy oracle, {label}, {steps} time steps in {el:.1f} s "
-                      f"(single-threaded NumPy)"}
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    return {"value": cells * steps / el / 1e9, "unit": METRIC, "cores": cores, "kind": "port",
+            "sample": f"FP64 C oracle (OpenMP, {cores} threads), {label}, {steps} time steps in "
+                      f"{el:.1f} s"}
 
 
 def run_reference(args):
@@ -185,9 +188,9 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "engine": "FP64 NumPy oracle restatement "
+            "config": {"workload": args.workload, "engine": "FP64 C oracle restatement "
                        "(reference engine is a closed x86-64 CUDA executable; no CPU engine)"},
-            "cpu_baseline": {"value": v, "unit": METRIC, "cores": 1, "kind": "port",
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": r["cores"], "kind": "port",
                              "sample": r["sample"]},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line), flush=True)

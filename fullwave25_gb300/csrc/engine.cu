@@ -4,9 +4,11 @@
 // table, per-tile source/air/sensor lists and the trace buffer. Time steps are issued as two
 // kernels per step (velocity, then pressure + tile epilogue); blocks of steps are captured once
 // into a CUDA graph and replayed, so the per-step host cost is one graph launch per block.
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdlib>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -17,12 +19,17 @@
 #include "../../include/fwgb.h"
 #include "engine_common.cuh"
 #include "kernels_direct.cuh"
+#include "kernels_march3d.cuh"
 
 using namespace fwgb;
 
 namespace {
 
 thread_local std::string g_create_error = "no error";
+
+constexpr int kMarchXC = 64;  // x planes per block of the 3D plane-march kernels
+
+enum Variant { kDirect = 0, kMarch = 1 };
 
 struct Tiling {
   int t[3];   // tile extent along x, y, z (z unused in 2D)
@@ -56,6 +63,8 @@ struct fw_handle {
   cudaStream_t capture_stream = nullptr;
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
+  int variant = kDirect;
+  MarchMaps tmaps{};
 };
 
 namespace {
@@ -88,6 +97,8 @@ Tiling make_tiling(const fw_handle* h) {
   Tiling t{};
   if (h->ndim == 2) {
     t.t[0] = kD2TX; t.t[1] = kD2TY; t.t[2] = 1;
+  } else if (h->variant == kMarch) {
+    t.t[0] = kMarchXC; t.t[1] = kMTY; t.t[2] = kMTZ;
   } else {
     t.t[0] = kD3TX; t.t[1] = kD3TY; t.t[2] = kD3TZ;
   }
@@ -152,14 +163,6 @@ __global__ void any_nonzero(const float* a, int64_t n, int* flag) {
     if (a[c] != 0.f) { *flag = 1; return; }
 }
 
-__global__ void gather_dense(const float* src, float* dst, int64_t rows, int64_t len,
-                             int64_t pitch) {
-  const int64_t total = rows * len;
-  for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x)
-    dst[e] = src[(e / len) * pitch + e % len];
-}
-
 float* state_field(fw_handle* h, int idx) { return h->state + (size_t)idx * h->ncells_padded; }
 float* map_field(fw_handle* h, int idx) { return h->maps + (size_t)idx * h->ncells_padded; }
 
@@ -175,6 +178,15 @@ int upload_grid(fw_handle* h, void* dst, const void* src, size_t elem, bool on_d
 
 void launch_step(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
+  if (h->ndim == 3 && h->variant == kMarch) {
+    dim3 grid(t.n[2], t.n[1], t.n[0]), block(kMTZ, kMTY);
+    vel3d_march<kMarchXC><<<grid, block, 0, s>>>(h->args, h->tmaps.p);
+    if (h->has_beta)
+      prs3d_march<kMarchXC, true><<<grid, block, 0, s>>>(h->args, h->tmaps.vx, h->tmaps.vy, h->tmaps.vz);
+    else
+      prs3d_march<kMarchXC, false><<<grid, block, 0, s>>>(h->args, h->tmaps.vx, h->tmaps.vy, h->tmaps.vz);
+    return;
+  }
   if (h->ndim == 2) {
     dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
     vel2d_direct<<<grid, block, 0, s>>>(h->args);
@@ -202,6 +214,43 @@ int build_graph(fw_handle* h, int steps) {
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return fail(h, FW_ERR_CUDA, "graph instantiate failed: %s", cudaGetErrorString(e));
   h->graph_steps = steps;
+  return FW_OK;
+}
+
+using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                   const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                   const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+// 3D float32 tensor map over one padded field: dims (pitch, ny, nx), box (bz, by, 1).
+int encode_field_map(fw_handle* h, CUtensorMap* map, float* base, uint32_t bz, uint32_t by) {
+  static EncodeTiledFn encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
+                                                     cudaEnableDefault, &q);
+    if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
+      return fail(h, FW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+    encode = reinterpret_cast<EncodeTiledFn>(fn);
+  }
+  const cuuint64_t dims[3] = {(cuuint64_t)h->pitch, (cuuint64_t)h->ny, (cuuint64_t)h->nx};
+  const cuuint64_t strides[2] = {(cuuint64_t)h->pitch * 4, (cuuint64_t)(h->pitch * h->ny) * 4};
+  const cuuint32_t box[3] = {bz, by, 1};
+  const cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                      CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return fail(h, FW_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return FW_OK;
+}
+
+// Device status word (step buffer slot 1): non-zero if a kernel gave up on a bounded wait.
+int check_device_status(fw_handle* h, cudaStream_t s) {
+  int st = 0;
+  FW_CUDA(h, cudaMemcpyAsync(&st, h->step + 1, sizeof(int), cudaMemcpyDeviceToHost, s));
+  FW_CUDA(h, cudaStreamSynchronize(s));
+  if (st) return fail(h, FW_ERR_DEVICE, "a kernel reported device status 0x%x (bounded wait timed out)", st);
   return FW_OK;
 }
 
@@ -245,6 +294,10 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   h->pitch = round_up(h->ndim == 2 ? h->ny : h->nz, 32);
   h->ncells_padded = h->ndim == 2 ? h->nx * h->pitch : h->nx * h->ny * h->pitch;
   h->n_out = (desc->nt + desc->mod_t - 1) / desc->mod_t;
+  {
+    const char* v = std::getenv("FWGB_VARIANT");
+    h->variant = (h->ndim == 3 && !(v && std::strcmp(v, "direct") == 0)) ? kMarch : kDirect;
+  }
   h->tiling = make_tiling(h);
   auto alloc = [&](void** p, size_t bytes) -> int {
     if (bytes == 0) bytes = 16;
@@ -313,6 +366,16 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   A.l.nt_ic = desc->nt_ic;
   A.l.mod_t = desc->mod_t;
   A.step = h->step;
+  if (h->variant == kMarch) {
+    if ((st = encode_field_map(h, &h->tmaps.p, A.f.p, kPW, kPH)) ||
+        (st = encode_field_map(h, &h->tmaps.vx, A.f.v[0], kXW, kXH)) ||
+        (st = encode_field_map(h, &h->tmaps.vy, A.f.v[1], kYW, kYH)) ||
+        (st = encode_field_map(h, &h->tmaps.vz, A.f.v[2], kZW, kZH))) {
+      g_create_error = h->err;
+      fw_destroy(h);
+      return st;
+    }
+  }
   *out = h;
   return FW_OK;
 }
@@ -523,7 +586,7 @@ int fw_reset(fw_handle* h, void* stream) {
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   FW_CUDA(h, cudaMemsetAsync(h->state, 0, (size_t)h->ncells_padded * n_state(h->ndim) * sizeof(float), s));
   FW_CUDA(h, cudaMemsetAsync(h->traces, 0, (size_t)h->n_out * h->d.ncoordsout * sizeof(float) + 0, s));
-  FW_CUDA(h, cudaMemsetAsync(h->step, 0, sizeof(int), s));
+  FW_CUDA(h, cudaMemsetAsync(h->step, 0, 2 * sizeof(int), s));
   h->host_step = 0;
   return FW_OK;
 }
@@ -558,7 +621,7 @@ int fw_run(fw_handle* h, void* stream, float* out, int32_t out_on_device) {
   int st;
   if ((st = fw_reset(h, stream)) || (st = fw_advance(h, stream, h->d.nt))) return st;
   if (out) return fw_read_traces(h, stream, 0, h->n_out, out, out_on_device);
-  return FW_OK;
+  return check_device_status(h, static_cast<cudaStream_t>(stream));
 }
 
 int fw_read_traces(fw_handle* h, void* stream, int32_t row0, int32_t n_rows, float* dst,
@@ -571,7 +634,10 @@ int fw_read_traces(fw_handle* h, void* stream, int32_t row0, int32_t n_rows, flo
   const size_t n = (size_t)n_rows * h->d.ncoordsout;
   if (n) FW_CUDA(h, cudaMemcpyAsync(dst, h->traces + (size_t)row0 * h->d.ncoordsout, n * sizeof(float),
                                     on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
-  if (!on_device) FW_CUDA(h, cudaStreamSynchronize(s));
+  if (!on_device) {
+    FW_CUDA(h, cudaStreamSynchronize(s));
+    return check_device_status(h, s);
+  }
   return FW_OK;
 }
 
@@ -604,6 +670,12 @@ int fw_current_step(const fw_handle* h, int32_t* step) {
 int fw_device_bytes(const fw_handle* h, uint64_t* bytes) {
   if (!h || !bytes) return FW_ERR_ARGUMENT;
   *bytes = h->bytes;
+  return FW_OK;
+}
+
+int fw_kernel_variant(const fw_handle* h, int32_t* variant) {
+  if (!h || !variant) return FW_ERR_ARGUMENT;
+  *variant = h->variant;
   return FW_OK;
 }
 

@@ -1,0 +1,231 @@
+// 3D step kernels that march along the slowest axis (x, depth).
+//
+// Block = 32 (z, one warp) x 8 (y) threads; each thread owns one (y, z) column and walks
+// XC consecutive x planes. Per plane:
+//   * the x-derivative taps come from a 16-entry register queue of that column (one new
+//     coalesced load per plane, prefetched one plane ahead);
+//   * the y/z taps and all off-axis taps come from shared-memory copies of planes x-1, x, x+1
+//     (with the y/z halos they need), brought in by TMA into a 4-slot ring: while plane x is
+//     computed, plane x+2 is in flight. Each slot has one mbarrier; waits are bounded.
+//   * the point-wise state and maps of the cell are read and written once, coalesced.
+// The arithmetic (operation order and fused multiply-adds) is the same as the direct kernels.
+#pragma once
+#include "engine_common.cuh"
+#include "tma.cuh"
+
+namespace fwgb {
+
+constexpr int kMTZ = 32, kMTY = 8, kMThreads = kMTZ * kMTY, kRing = 4;
+// velocity kernel: p planes with y and z halos of 8
+constexpr int kPW = kMTZ + 16, kPH = kMTY + 16;
+constexpr int kPSlot = kPW * kPH;                     // 1152 floats = 4608 B
+// pressure kernel: vx (halo 1 in y, z window [-4, 36)), vy (halo 8 in y), vz (halo 8 in z)
+constexpr int kXW = kMTZ + 8, kXH = kMTY + 2;         // 40 x 10
+constexpr int kYW = kMTZ + 8, kYH = kMTY + 16;        // 40 x 24
+constexpr int kZW = kMTZ + 16, kZH = kMTY + 2;        // 48 x 10
+constexpr int kXSlot = 416, kYSlot = kYW * kYH, kZSlot = kZW * kZH;  // vx slot padded to 128 B
+static_assert(kXSlot >= kXW * kXH && (kXSlot * 4) % 128 == 0, "vx slot");
+static_assert((kYSlot * 4) % 128 == 0 && (kZSlot * 4) % 128 == 0 && (kPSlot * 4) % 128 == 0, "slots");
+
+struct MarchMaps {
+  CUtensorMap p, vx, vy, vz;
+};
+
+template <int XC>
+__global__ void __launch_bounds__(kMThreads, 3)
+vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
+  __shared__ alignas(128) float ring[kRing][kPSlot];
+  __shared__ alignas(8) uint64_t bar[kRing];
+  const Grid& g = A.g;
+  int* status = A.step + 1;
+  const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * kMTZ + tz;
+  const int z0 = kGhost + blockIdx.x * kMTZ, y0 = kGhost + blockIdx.y * kMTY;
+  const int xb = kGhost + blockIdx.z * XC;
+  const int xe = min(xb + XC, g.nx - kGhost);
+  const int k = z0 + tz, j = y0 + ty;
+  const bool active = k < g.nz - kGhost && j < g.ny - kGhost;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && blockIdx.z == 0 && tid == 0) *A.step += 1;
+  if (tid == 0) {
+    for (int s = 0; s < kRing; ++s) mbar_init(&bar[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  constexpr uint32_t kBytes = kPSlot * 4;
+  if (tid == 0) {
+    for (int s = 0; s < 3; ++s) {  // planes xb-1, xb, xb+1
+      mbar_arrive_expect_tx(&bar[s], kBytes);
+      tma_load_3d(ring[s], &tm_p, &bar[s], z0 - 8, y0 - 8, xb - 1 + s);
+    }
+  }
+  const int64_t sx = g.sx;
+  const int64_t col = (int64_t)j * g.sy + k;
+  const float* __restrict__ p = A.f.p;
+  float q[16];  // q[t] = p[x - 7 + t]
+#pragma unroll
+  for (int t = 0; t < 16; ++t) q[t] = active ? __ldg(p + (int64_t)(xb - 7 + t) * sx + col) : 0.f;
+  const int si = (ty + 8) * kPW + (tz + 8);
+  for (int x = xb; x < xe; ++x) {
+    const int it = x - xb;
+    __syncthreads();  // the slot of plane x-2 is no longer read
+    if (tid == 0 && x + 1 < xe) {
+      const int s = (it + 3) % kRing;
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&bar[s], kBytes);
+      tma_load_3d(ring[s], &tm_p, &bar[s], z0 - 8, y0 - 8, x + 2);
+    }
+    if (it == 0) {
+      mbar_wait_bounded(&bar[0], 0, status);
+      mbar_wait_bounded(&bar[1], 0, status);
+    }
+    mbar_wait_bounded(&bar[(it + 2) % kRing], ((it + 2) / kRing) & 1, status);
+    const float* Pm = ring[it % kRing];
+    const float* P0 = ring[(it + 1) % kRing];
+    const float* P1 = ring[(it + 2) % kRing];
+    const float qn = (active && x + 9 < g.nx) ? __ldg(p + (int64_t)(x + 9) * sx + col) : 0.f;
+    if (active) {
+      const int64_t c = (int64_t)x * sx + col;
+      float cm[8], co;
+      load_taps(A.m.taps, __ldg(A.m.dcmap + c), cm, co);
+      float gx = 0.f, gy = 0.f, gz = 0.f;
+#pragma unroll
+      for (int m = 1; m <= 8; ++m) {
+        gx = fmaf(cm[m - 1], q[7 + m] - q[8 - m], gx);
+        gy = fmaf(cm[m - 1], P0[si + m * kPW] - P0[si - (m - 1) * kPW], gy);
+        gz = fmaf(cm[m - 1], P0[si + m] - P0[si - (m - 1)], gz);
+      }
+      gx = fmaf(co, ((P1[si + kPW] - P0[si + kPW]) + (P1[si - kPW] - P0[si - kPW])) +
+                        ((P1[si + 1] - P0[si + 1]) + (P1[si - 1] - P0[si - 1])), gx);
+      gy = fmaf(co, ((P1[si + kPW] - P1[si]) + (Pm[si + kPW] - Pm[si])) +
+                        ((P0[si + kPW + 1] - P0[si + 1]) + (P0[si + kPW - 1] - P0[si - 1])), gy);
+      gz = fmaf(co, ((P1[si + 1] - P1[si]) + (Pm[si + 1] - Pm[si])) +
+                        ((P0[si + kPW + 1] - P0[si + kPW]) + (P0[si - kPW + 1] - P0[si - kPW])), gz);
+      gx *= g.inv_h[0];
+      gy *= g.inv_h[1];
+      gz *= g.inv_h[2];
+      const float iku = __ldg(A.m.inv_ku + c), rr = __ldg(A.m.rdt_rho + c);
+      const float a1 = __ldg(A.m.au[0] + c), b1 = __ldg(A.m.bu[0] + c);
+      const float a2 = __ldg(A.m.au[1] + c), b2 = __ldg(A.m.bu[1] + c);
+      const float gg[3] = {gx, gy, gz};
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float s1 = fmaf(b1, A.f.psi[a][0][c], a1 * gg[a]);
+        const float s2 = fmaf(b2, A.f.psi[a][1][c], a2 * gg[a]);
+        A.f.psi[a][0][c] = s1;
+        A.f.psi[a][1][c] = s2;
+        A.f.v[a][c] -= rr * (fmaf(gg[a], iku, s1) + s2);
+      }
+    }
+#pragma unroll
+    for (int t = 0; t < 15; ++t) q[t] = q[t + 1];
+    q[15] = qn;
+  }
+}
+
+template <int XC, bool kBeta>
+__global__ void __launch_bounds__(kMThreads, 3)
+prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
+            const __grid_constant__ CUtensorMap tm_vy, const __grid_constant__ CUtensorMap tm_vz) {
+  __shared__ alignas(128) float rx[kRing][kXSlot];
+  __shared__ alignas(128) float ry[kRing][kYSlot];
+  __shared__ alignas(128) float rz[kRing][kZSlot];
+  __shared__ alignas(8) uint64_t bar[kRing];
+  const Grid& g = A.g;
+  int* status = A.step + 1;
+  const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * kMTZ + tz;
+  const int z0 = kGhost + blockIdx.x * kMTZ, y0 = kGhost + blockIdx.y * kMTY;
+  const int xb = kGhost + blockIdx.z * XC;
+  const int xe = min(xb + XC, g.nx - kGhost);
+  const int k = z0 + tz, j = y0 + ty;
+  const bool active = k < g.nz - kGhost && j < g.ny - kGhost;
+  if (tid == 0) {
+    for (int s = 0; s < kRing; ++s) mbar_init(&bar[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  constexpr uint32_t kBytes = (kXW * kXH + kYSlot + kZSlot) * 4;
+  auto issue = [&](int s, int x) {
+    mbar_arrive_expect_tx(&bar[s], kBytes);
+    tma_load_3d(rx[s], &tm_vx, &bar[s], z0 - 4, y0 - 1, x);
+    tma_load_3d(ry[s], &tm_vy, &bar[s], z0 - 4, y0 - 8, x);
+    tma_load_3d(rz[s], &tm_vz, &bar[s], z0 - 8, y0 - 1, x);
+  };
+  if (tid == 0)
+    for (int s = 0; s < 3; ++s) issue(s, xb - 1 + s);
+  const int64_t sx = g.sx;
+  const int64_t col = (int64_t)j * g.sy + k;
+  const float* __restrict__ vx = A.f.v[0];
+  float* p = A.f.p;
+  float r[16];  // r[t] = vx[x - 8 + t]
+#pragma unroll
+  for (int t = 0; t < 16; ++t) r[t] = active ? __ldg(vx + (int64_t)(xb - 8 + t) * sx + col) : 0.f;
+  const int xi = (ty + 1) * kXW + (tz + 4);
+  const int yi = (ty + 8) * kYW + (tz + 4);
+  const int zi = (ty + 1) * kZW + (tz + 8);
+  for (int x = xb; x < xe; ++x) {
+    const int it = x - xb;
+    __syncthreads();
+    if (tid == 0 && x + 1 < xe) {
+      fence_proxy_async_smem();
+      issue((it + 3) % kRing, x + 2);
+    }
+    if (it == 0) {
+      mbar_wait_bounded(&bar[0], 0, status);
+      mbar_wait_bounded(&bar[1], 0, status);
+    }
+    mbar_wait_bounded(&bar[(it + 2) % kRing], ((it + 2) / kRing) & 1, status);
+    const float* Xm = rx[it % kRing];
+    const float* X0 = rx[(it + 1) % kRing];
+    const float* Ym = ry[it % kRing];
+    const float* Y0 = ry[(it + 1) % kRing];
+    const float* Y1 = ry[(it + 2) % kRing];
+    const float* Zm = rz[it % kRing];
+    const float* Z0 = rz[(it + 1) % kRing];
+    const float* Z1 = rz[(it + 2) % kRing];
+    const float rn = active ? __ldg(vx + (int64_t)(x + 8) * sx + col) : 0.f;
+    if (active) {
+      const int64_t c = (int64_t)x * sx + col;
+      float cm[8], co;
+      load_taps(A.m.taps, __ldg(A.m.dcmap + c), cm, co);
+      float dx = 0.f, dy = 0.f, dz = 0.f;
+#pragma unroll
+      for (int m = 1; m <= 8; ++m) {
+        dx = fmaf(cm[m - 1], r[7 + m] - r[8 - m], dx);
+        dy = fmaf(cm[m - 1], Y0[yi + (m - 1) * kYW] - Y0[yi - m * kYW], dy);
+        dz = fmaf(cm[m - 1], Z0[zi + (m - 1)] - Z0[zi - m], dz);
+      }
+      dx = fmaf(co, ((X0[xi + kXW] - Xm[xi + kXW]) + (X0[xi - kXW] - Xm[xi - kXW])) +
+                        ((X0[xi + 1] - Xm[xi + 1]) + (X0[xi - 1] - Xm[xi - 1])), dx);
+      dy = fmaf(co, ((Y1[yi] - Y1[yi - kYW]) + (Ym[yi] - Ym[yi - kYW])) +
+                        ((Y0[yi + 1] - Y0[yi + 1 - kYW]) + (Y0[yi - 1] - Y0[yi - 1 - kYW])), dy);
+      dz = fmaf(co, ((Z1[zi] - Z1[zi - 1]) + (Zm[zi] - Zm[zi - 1])) +
+                        ((Z0[zi + kZW] - Z0[zi + kZW - 1]) + (Z0[zi - kZW] - Z0[zi - kZW - 1])), dz);
+      dx *= g.inv_h[0];
+      dy *= g.inv_h[1];
+      dz *= g.inv_h[2];
+      const float ikx = __ldg(A.m.inv_kx + c);
+      const float a1 = __ldg(A.m.ax[0] + c), b1 = __ldg(A.m.bx[0] + c);
+      const float a2 = __ldg(A.m.ax[1] + c), b2 = __ldg(A.m.bx[1] + c);
+      const float dd[3] = {dx, dy, dz};
+      float div = 0.f;
+#pragma unroll
+      for (int a = 0; a < 3; ++a) {
+        const float f1 = fmaf(b1, A.f.phi[a][0][c], a1 * dd[a]);
+        const float f2 = fmaf(b2, A.f.phi[a][1][c], a2 * dd[a]);
+        A.f.phi[a][0][c] = f1;
+        A.f.phi[a][1][c] = f2;
+        div += fmaf(dd[a], ikx, f1) + f2;
+      }
+      const float pc = p[c];
+      float coef = __ldg(A.m.dt_k + c);
+      if (kBeta) coef = fmaf(__ldg(A.m.beta2dt + c), pc, coef);
+      p[c] = fmaf(-coef, div, pc);
+    }
+#pragma unroll
+    for (int t = 0; t < 15; ++t) r[t] = r[t + 1];
+    r[15] = rn;
+  }
+  tile_epilogue(A, p, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x, tid,
+                kMThreads);
+}
+
+}  // namespace fwgb

@@ -22,7 +22,8 @@ FW_STATUS = {0: "FW_OK", 1: "FW_ERR_ARGUMENT", 2: "FW_ERR_CUDA", 3: "FW_ERR_STAT
 EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_source_signal",
             "fw_set_source_columns", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
-            "fw_current_step", "fw_device_bytes", "fw_launches_per_step", "fw_destroy",
+            "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_launches_per_step",
+            "fw_destroy",
             "fw_last_error")
 
 
@@ -85,6 +86,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_get_field": (C.c_int, [H, vp, C.c_int32, _FP, C.c_int32]),
         "fw_current_step": (C.c_int, [H, _IP]),
         "fw_device_bytes": (C.c_int, [H, C.POINTER(C.c_uint64)]),
+        "fw_kernel_variant": (C.c_int, [H, _IP]),
         "fw_launches_per_step": (C.c_int, [H, _IP]),
         "fw_destroy": (C.c_int, [H]),
         "fw_last_error": (C.c_char_p, [H]),
@@ -267,6 +269,12 @@ class Engine:
         v = C.c_uint64()
         self._call("fw_device_bytes", C.byref(v))
         return v.value
+
+    @property
+    def kernel_variant(self) -> str:
+        v = C.c_int32()
+        self._call("fw_kernel_variant", C.byref(v))
+        return {0: "direct", 1: "march"}[v.value]
 
     @property
     def launches_per_step(self) -> int:

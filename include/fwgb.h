@@ -133,6 +133,11 @@ FWGB_API int fw_current_step(const fw_handle *h, int32_t *step);
 /* Device bytes held by the handle. */
 FWGB_API int fw_device_bytes(const fw_handle *h, uint64_t *bytes);
 
+/* Kernel family in use: 0 = direct-addressed kernels, 1 = 3D plane-march kernels (TMA-staged
+ * halo planes). 3D handles use 1 unless the environment variable FWGB_VARIANT=direct was set
+ * when the handle was created. */
+FWGB_API int fw_kernel_variant(const fw_handle *h, int32_t *variant);
+
 /* Kernel launches issued per time step (for launch accounting). */
 FWGB_API int fw_launches_per_step(const fw_handle *h, int32_t *n);
 

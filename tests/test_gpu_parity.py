@@ -140,3 +140,56 @@ def test_full_size_determinism_linearity_shift(engine_lib, cuda, plain_2d_full):
         d = eng.run()
     np.testing.assert_array_equal(d[shift:], a[:-shift])
     assert not d[:shift].any()
+
+
+def _engine_with_variant(inp, variant):
+    import os
+
+    from fullwave25_gb300.engine import Engine
+
+    old = os.environ.get("FWGB_VARIANT")
+    os.environ["FWGB_VARIANT"] = variant
+    try:
+        return Engine(inp, validate=False)
+    finally:
+        if old is None:
+            del os.environ["FWGB_VARIANT"]
+        else:
+            os.environ["FWGB_VARIANT"] = old
+
+
+@pytest.fixture(scope="module")
+def plain_3d_small(cuda):
+    from fullwave25_gb300.workloads3d import plain_3d_device_inputs, to_host_inputs
+
+    d = plain_3d_device_inputs(shape=(48, 40, 72), nt=240, n_pml=8, n_transition=8,
+                               sensor_plane=24, element_height=8)
+    return d, to_host_inputs(d)
+
+
+def test_march_kernels_equal_direct_kernels_bitwise(engine_lib, cuda, plain_3d_small):
+    d, host = plain_3d_small
+    with _engine_with_variant(host, "march") as em, _engine_with_variant(host, "direct") as ed:
+        assert em.kernel_variant == "march" and ed.kernel_variant == "direct"
+        a, b = em.run(), ed.run()
+    assert np.abs(a).max() > 0
+    np.testing.assert_array_equal(a, b)
+
+
+def test_plain_3d_reduced_matches_oracle(engine_lib, cuda, plain_3d_small):
+    from fdtd_oracle_c import run_oracle_c
+
+    d, host = plain_3d_small
+    with d.make_engine() as eng:
+        assert eng.kernel_variant == "march"
+        got = eng.run()
+    err = rel_l2(got, run_oracle_c(host))
+    assert err < TOL, f"rel-L2 {err:.3e}"
+
+
+def test_device_and_host_inputs_give_same_traces(engine_lib, cuda, plain_3d_small):
+    from fullwave25_gb300.engine import Engine
+
+    d, host = plain_3d_small
+    with d.make_engine() as a, Engine(host) as b:
+        np.testing.assert_array_equal(a.run(), b.run())
