@@ -78,6 +78,82 @@ __device__ __forceinline__ void load_taps(const float* taps, int dc, float (&c)[
   co = e.x;
 }
 
+// Point-wise operands of one cell for the velocity update, loaded together (all loads issued
+// before any use) and written back together. NDIM velocity components.
+template <int NDIM>
+struct CellVelT {
+  int dc;
+  float iku, rr, a1, b1, a2, b2;
+  float v[NDIM], s1[NDIM], s2[NDIM];
+  __device__ __forceinline__ void load(const StepArgs& A, int64_t c) {
+    dc = __ldg(A.m.dcmap + c);
+    iku = __ldg(A.m.inv_ku + c);
+    rr = __ldg(A.m.rdt_rho + c);
+    a1 = __ldg(A.m.au[0] + c);
+    b1 = __ldg(A.m.bu[0] + c);
+    a2 = __ldg(A.m.au[1] + c);
+    b2 = __ldg(A.m.bu[1] + c);
+#pragma unroll
+    for (int a = 0; a < NDIM; ++a) {
+      v[a] = A.f.v[a][c];
+      s1[a] = A.f.psi[a][0][c];
+      s2[a] = A.f.psi[a][1][c];
+    }
+  }
+  // psi_nu <- b_nu psi_nu + a_nu g ;  v <- v - dt/rho (g / kappau + psi_1 + psi_2)
+  __device__ __forceinline__ void update_store(const StepArgs& A, int64_t c, const float* g) {
+#pragma unroll
+    for (int a = 0; a < NDIM; ++a) {
+      const float n1 = fmaf(b1, s1[a], a1 * g[a]);
+      const float n2 = fmaf(b2, s2[a], a2 * g[a]);
+      A.f.psi[a][0][c] = n1;
+      A.f.psi[a][1][c] = n2;
+      A.f.v[a][c] = fmaf(-rr, fmaf(g[a], iku, n1) + n2, v[a]);
+    }
+  }
+};
+
+template <int NDIM, bool kBeta>
+struct CellPrsT {
+  int dc;
+  float ikx, dtk, b2dt, a1, b1, a2, b2, pc;
+  float f1[NDIM], f2[NDIM];
+  __device__ __forceinline__ void load(const StepArgs& A, int64_t c) {
+    dc = __ldg(A.m.dcmap + c);
+    ikx = __ldg(A.m.inv_kx + c);
+    dtk = __ldg(A.m.dt_k + c);
+    b2dt = kBeta ? __ldg(A.m.beta2dt + c) : 0.f;
+    a1 = __ldg(A.m.ax[0] + c);
+    b1 = __ldg(A.m.bx[0] + c);
+    a2 = __ldg(A.m.ax[1] + c);
+    b2 = __ldg(A.m.bx[1] + c);
+    pc = A.f.p[c];
+#pragma unroll
+    for (int a = 0; a < NDIM; ++a) {
+      f1[a] = A.f.phi[a][0][c];
+      f2[a] = A.f.phi[a][1][c];
+    }
+  }
+  // phi_nu <- b_nu phi_nu + a_nu d ;  p <- p - dt (K + 2 beta p) sum (d / kappax + phi_1 + phi_2)
+  __device__ __forceinline__ void update_store(const StepArgs& A, int64_t c, const float* d) {
+    float div = 0.f;
+#pragma unroll
+    for (int a = 0; a < NDIM; ++a) {
+      const float n1 = fmaf(b1, f1[a], a1 * d[a]);
+      const float n2 = fmaf(b2, f2[a], a2 * d[a]);
+      A.f.phi[a][0][c] = n1;
+      A.f.phi[a][1][c] = n2;
+      div += fmaf(d[a], ikx, n1) + n2;
+    }
+    const float coef = kBeta ? fmaf(b2dt, pc, dtk) : dtk;
+    A.f.p[c] = fmaf(-coef, div, pc);
+  }
+};
+
+using CellVel = CellVelT<3>;
+template <bool kBeta>
+using CellPrs = CellPrsT<3, kBeta>;
+
 // Source injection, air zeroing and sensor recording for the cells owned by this block's tile.
 // Called by every thread of kernel B after its pressure writes; `tid`/`nthr` span the block.
 __device__ __forceinline__ void tile_epilogue(const StepArgs& A, float* p, int tile, int tid,

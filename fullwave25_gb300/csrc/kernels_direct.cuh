@@ -23,8 +23,10 @@ __global__ void __launch_bounds__(256) vel2d_direct(const StepArgs A) {
   const int64_t sx = g.sx;
   const int64_t c = i * sx + j;
   const float* __restrict__ p = A.f.p;
+  CellVelT<2> cv;
+  cv.load(A, c);
   float cm[8], co;
-  load_taps(A.m.taps, __ldg(A.m.dcmap + c), cm, co);
+  load_taps(A.m.taps, cv.dc, cm, co);
   float gx = 0.f, gy = 0.f;
 #pragma unroll
   for (int m = 1; m <= 8; ++m) {
@@ -33,20 +35,8 @@ __global__ void __launch_bounds__(256) vel2d_direct(const StepArgs A) {
   }
   gx = fmaf(co, (__ldg(p + c + sx + 1) - __ldg(p + c + 1)) + (__ldg(p + c + sx - 1) - __ldg(p + c - 1)), gx);
   gy = fmaf(co, (__ldg(p + c + 1 + sx) - __ldg(p + c + sx)) + (__ldg(p + c + 1 - sx) - __ldg(p + c - sx)), gy);
-  gx *= g.inv_h[0];
-  gy *= g.inv_h[1];
-  const float iku = __ldg(A.m.inv_ku + c), rr = __ldg(A.m.rdt_rho + c);
-  const float a1 = __ldg(A.m.au[0] + c), b1 = __ldg(A.m.bu[0] + c);
-  const float a2 = __ldg(A.m.au[1] + c), b2 = __ldg(A.m.bu[1] + c);
-  float s1 = fmaf(b1, A.f.psi[0][0][c], a1 * gx), s2 = fmaf(b2, A.f.psi[0][1][c], a2 * gx);
-  A.f.psi[0][0][c] = s1;
-  A.f.psi[0][1][c] = s2;
-  A.f.v[0][c] -= rr * (fmaf(gx, iku, s1) + s2);
-  s1 = fmaf(b1, A.f.psi[1][0][c], a1 * gy);
-  s2 = fmaf(b2, A.f.psi[1][1][c], a2 * gy);
-  A.f.psi[1][0][c] = s1;
-  A.f.psi[1][1][c] = s2;
-  A.f.v[1][c] -= rr * (fmaf(gy, iku, s1) + s2);
+  const float gg[2] = {gx * g.inv_h[0], gy * g.inv_h[1]};
+  cv.update_store(A, c, gg);
 }
 
 template <bool kBeta>
@@ -60,8 +50,10 @@ __global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
     const int64_t c = i * sx + j;
     const float* __restrict__ vx = A.f.v[0];
     const float* __restrict__ vy = A.f.v[1];
+    CellPrsT<2, kBeta> cp;
+    cp.load(A, c);
     float cm[8], co;
-    load_taps(A.m.taps, __ldg(A.m.dcmap + c), cm, co);
+    load_taps(A.m.taps, cp.dc, cm, co);
     float dx = 0.f, dy = 0.f;
 #pragma unroll
     for (int m = 1; m <= 8; ++m) {
@@ -70,22 +62,8 @@ __global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
     }
     dx = fmaf(co, (__ldg(vx + c + 1) - __ldg(vx + c - sx + 1)) + (__ldg(vx + c - 1) - __ldg(vx + c - sx - 1)), dx);
     dy = fmaf(co, (__ldg(vy + c + sx) - __ldg(vy + c + sx - 1)) + (__ldg(vy + c - sx) - __ldg(vy + c - sx - 1)), dy);
-    dx *= g.inv_h[0];
-    dy *= g.inv_h[1];
-    const float ikx = __ldg(A.m.inv_kx + c);
-    const float a1 = __ldg(A.m.ax[0] + c), b1 = __ldg(A.m.bx[0] + c);
-    const float a2 = __ldg(A.m.ax[1] + c), b2 = __ldg(A.m.bx[1] + c);
-    const float fx1 = fmaf(b1, A.f.phi[0][0][c], a1 * dx), fx2 = fmaf(b2, A.f.phi[0][1][c], a2 * dx);
-    const float fy1 = fmaf(b1, A.f.phi[1][0][c], a1 * dy), fy2 = fmaf(b2, A.f.phi[1][1][c], a2 * dy);
-    A.f.phi[0][0][c] = fx1;
-    A.f.phi[0][1][c] = fx2;
-    A.f.phi[1][0][c] = fy1;
-    A.f.phi[1][1][c] = fy2;
-    const float div = (fmaf(dx, ikx, fx1) + fx2) + (fmaf(dy, ikx, fy1) + fy2);
-    const float pc = p[c];
-    float coef = __ldg(A.m.dt_k + c);
-    if (kBeta) coef = fmaf(__ldg(A.m.beta2dt + c), pc, coef);
-    p[c] = fmaf(-coef, div, pc);
+    const float dd[2] = {dx * g.inv_h[0], dy * g.inv_h[1]};
+    cp.update_store(A, c, dd);
   }
   tile_epilogue(A, p, blockIdx.y * gridDim.x + blockIdx.x, threadIdx.y * blockDim.x + threadIdx.x,
                 blockDim.x * blockDim.y);
@@ -104,8 +82,10 @@ __global__ void __launch_bounds__(256) vel3d_direct(const StepArgs A) {
   const int64_t sx = g.sx, sy = g.sy;
   const int64_t c = i * sx + j * sy + k;
   const float* __restrict__ p = A.f.p;
+  CellVel cv;
+  cv.load(A, c);
   float cm[8], co;
-  load_taps(A.m.taps, __ldg(A.m.dcmap + c), cm, co);
+  load_taps(A.m.taps, cv.dc, cm, co);
   float gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
   for (int m = 1; m <= 8; ++m) {
@@ -117,21 +97,8 @@ __global__ void __launch_bounds__(256) vel3d_direct(const StepArgs A) {
   gx = fmaf(co, ((P(sx + sy) - P(sy)) + (P(sx - sy) - P(-sy))) + ((P(sx + 1) - P(1)) + (P(sx - 1) - P(-1))), gx);
   gy = fmaf(co, ((P(sy + sx) - P(sx)) + (P(sy - sx) - P(-sx))) + ((P(sy + 1) - P(1)) + (P(sy - 1) - P(-1))), gy);
   gz = fmaf(co, ((P(1 + sx) - P(sx)) + (P(1 - sx) - P(-sx))) + ((P(1 + sy) - P(sy)) + (P(1 - sy) - P(-sy))), gz);
-  gx *= g.inv_h[0];
-  gy *= g.inv_h[1];
-  gz *= g.inv_h[2];
-  const float iku = __ldg(A.m.inv_ku + c), rr = __ldg(A.m.rdt_rho + c);
-  const float a1 = __ldg(A.m.au[0] + c), b1 = __ldg(A.m.bu[0] + c);
-  const float a2 = __ldg(A.m.au[1] + c), b2 = __ldg(A.m.bu[1] + c);
-  const float gg[3] = {gx, gy, gz};
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    const float s1 = fmaf(b1, A.f.psi[a][0][c], a1 * gg[a]);
-    const float s2 = fmaf(b2, A.f.psi[a][1][c], a2 * gg[a]);
-    A.f.psi[a][0][c] = s1;
-    A.f.psi[a][1][c] = s2;
-    A.f.v[a][c] -= rr * (fmaf(gg[a], iku, s1) + s2);
-  }
+  const float gg[3] = {gx * g.inv_h[0], gy * g.inv_h[1], gz * g.inv_h[2]};
+  cv.update_store(A, c, gg);
 }
 
 template <bool kBeta>
@@ -147,8 +114,10 @@ __global__ void __launch_bounds__(256) prs3d_direct(const StepArgs A) {
     const float* __restrict__ vx = A.f.v[0];
     const float* __restrict__ vy = A.f.v[1];
     const float* __restrict__ vz = A.f.v[2];
+    CellPrs<kBeta> cp;
+    cp.load(A, c);
     float cm[8], co;
-    load_taps(A.m.taps, __ldg(A.m.dcmap + c), cm, co);
+    load_taps(A.m.taps, cp.dc, cm, co);
     float dx = 0.f, dy = 0.f, dz = 0.f;
 #pragma unroll
     for (int m = 1; m <= 8; ++m) {
@@ -162,26 +131,8 @@ __global__ void __launch_bounds__(256) prs3d_direct(const StepArgs A) {
     dx = fmaf(co, ((X(sy) - X(sy - sx)) + (X(-sy) - X(-sy - sx))) + ((X(1) - X(1 - sx)) + (X(-1) - X(-1 - sx))), dx);
     dy = fmaf(co, ((Y(sx) - Y(sx - sy)) + (Y(-sx) - Y(-sx - sy))) + ((Y(1) - Y(1 - sy)) + (Y(-1) - Y(-1 - sy))), dy);
     dz = fmaf(co, ((Z(sx) - Z(sx - 1)) + (Z(-sx) - Z(-sx - 1))) + ((Z(sy) - Z(sy - 1)) + (Z(-sy) - Z(-sy - 1))), dz);
-    dx *= g.inv_h[0];
-    dy *= g.inv_h[1];
-    dz *= g.inv_h[2];
-    const float ikx = __ldg(A.m.inv_kx + c);
-    const float a1 = __ldg(A.m.ax[0] + c), b1 = __ldg(A.m.bx[0] + c);
-    const float a2 = __ldg(A.m.ax[1] + c), b2 = __ldg(A.m.bx[1] + c);
-    const float dd[3] = {dx, dy, dz};
-    float div = 0.f;
-#pragma unroll
-    for (int a = 0; a < 3; ++a) {
-      const float f1 = fmaf(b1, A.f.phi[a][0][c], a1 * dd[a]);
-      const float f2 = fmaf(b2, A.f.phi[a][1][c], a2 * dd[a]);
-      A.f.phi[a][0][c] = f1;
-      A.f.phi[a][1][c] = f2;
-      div += fmaf(dd[a], ikx, f1) + f2;
-    }
-    const float pc = p[c];
-    float coef = __ldg(A.m.dt_k + c);
-    if (kBeta) coef = fmaf(__ldg(A.m.beta2dt + c), pc, coef);
-    p[c] = fmaf(-coef, div, pc);
+    const float dd[3] = {dx * g.inv_h[0], dy * g.inv_h[1], dz * g.inv_h[2]};
+    cp.update_store(A, c, dd);
   }
   tile_epilogue(A, p, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x,
                 (threadIdx.z * blockDim.y + threadIdx.y) * blockDim.x + threadIdx.x,

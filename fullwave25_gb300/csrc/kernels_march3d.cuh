@@ -66,6 +66,12 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
   const int si = (ty + 8) * kPW + (tz + 8);
   for (int x = xb; x < xe; ++x) {
     const int it = x - xb;
+    const int64_t c = (int64_t)x * sx + col;
+    // point-wise operands of this plane: issued before the block barrier and the TMA wait so
+    // their HBM latency overlaps them
+    CellVel cv;
+    if (active) cv.load(A, c);
+    const float qn = (active && x + 9 < g.nx) ? __ldg(p + (int64_t)(x + 9) * sx + col) : 0.f;
     __syncthreads();  // the slot of plane x-2 is no longer read
     if (tid == 0 && x + 1 < xe) {
       const int s = (it + 3) % kRing;
@@ -81,11 +87,9 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
     const float* Pm = ring[it % kRing];
     const float* P0 = ring[(it + 1) % kRing];
     const float* P1 = ring[(it + 2) % kRing];
-    const float qn = (active && x + 9 < g.nx) ? __ldg(p + (int64_t)(x + 9) * sx + col) : 0.f;
     if (active) {
-      const int64_t c = (int64_t)x * sx + col;
       float cm[8], co;
-      load_taps(A.m.taps, __ldg(A.m.dcmap + c), cm, co);
+      load_taps(A.m.taps, cv.dc, cm, co);
       float gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
       for (int m = 1; m <= 8; ++m) {
@@ -99,21 +103,8 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
                         ((P0[si + kPW + 1] - P0[si + 1]) + (P0[si + kPW - 1] - P0[si - 1])), gy);
       gz = fmaf(co, ((P1[si + 1] - P1[si]) + (Pm[si + 1] - Pm[si])) +
                         ((P0[si + kPW + 1] - P0[si + kPW]) + (P0[si - kPW + 1] - P0[si - kPW])), gz);
-      gx *= g.inv_h[0];
-      gy *= g.inv_h[1];
-      gz *= g.inv_h[2];
-      const float iku = __ldg(A.m.inv_ku + c), rr = __ldg(A.m.rdt_rho + c);
-      const float a1 = __ldg(A.m.au[0] + c), b1 = __ldg(A.m.bu[0] + c);
-      const float a2 = __ldg(A.m.au[1] + c), b2 = __ldg(A.m.bu[1] + c);
-      const float gg[3] = {gx, gy, gz};
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float s1 = fmaf(b1, A.f.psi[a][0][c], a1 * gg[a]);
-        const float s2 = fmaf(b2, A.f.psi[a][1][c], a2 * gg[a]);
-        A.f.psi[a][0][c] = s1;
-        A.f.psi[a][1][c] = s2;
-        A.f.v[a][c] -= rr * (fmaf(gg[a], iku, s1) + s2);
-      }
+      const float gg[3] = {gx * g.inv_h[0], gy * g.inv_h[1], gz * g.inv_h[2]};
+      cv.update_store(A, c, gg);
     }
 #pragma unroll
     for (int t = 0; t < 15; ++t) q[t] = q[t + 1];
@@ -163,6 +154,10 @@ prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
   const int zi = (ty + 1) * kZW + (tz + 8);
   for (int x = xb; x < xe; ++x) {
     const int it = x - xb;
+    const int64_t c = (int64_t)x * sx + col;
+    CellPrs<kBeta> cp;
+    if (active) cp.load(A, c);
+    const float rn = active ? __ldg(vx + (int64_t)(x + 8) * sx + col) : 0.f;
     __syncthreads();
     if (tid == 0 && x + 1 < xe) {
       fence_proxy_async_smem();
@@ -181,11 +176,9 @@ prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
     const float* Zm = rz[it % kRing];
     const float* Z0 = rz[(it + 1) % kRing];
     const float* Z1 = rz[(it + 2) % kRing];
-    const float rn = active ? __ldg(vx + (int64_t)(x + 8) * sx + col) : 0.f;
     if (active) {
-      const int64_t c = (int64_t)x * sx + col;
       float cm[8], co;
-      load_taps(A.m.taps, __ldg(A.m.dcmap + c), cm, co);
+      load_taps(A.m.taps, cp.dc, cm, co);
       float dx = 0.f, dy = 0.f, dz = 0.f;
 #pragma unroll
       for (int m = 1; m <= 8; ++m) {
@@ -199,26 +192,8 @@ prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
                         ((Y0[yi + 1] - Y0[yi + 1 - kYW]) + (Y0[yi - 1] - Y0[yi - 1 - kYW])), dy);
       dz = fmaf(co, ((Z1[zi] - Z1[zi - 1]) + (Zm[zi] - Zm[zi - 1])) +
                         ((Z0[zi + kZW] - Z0[zi + kZW - 1]) + (Z0[zi - kZW] - Z0[zi - kZW - 1])), dz);
-      dx *= g.inv_h[0];
-      dy *= g.inv_h[1];
-      dz *= g.inv_h[2];
-      const float ikx = __ldg(A.m.inv_kx + c);
-      const float a1 = __ldg(A.m.ax[0] + c), b1 = __ldg(A.m.bx[0] + c);
-      const float a2 = __ldg(A.m.ax[1] + c), b2 = __ldg(A.m.bx[1] + c);
-      const float dd[3] = {dx, dy, dz};
-      float div = 0.f;
-#pragma unroll
-      for (int a = 0; a < 3; ++a) {
-        const float f1 = fmaf(b1, A.f.phi[a][0][c], a1 * dd[a]);
-        const float f2 = fmaf(b2, A.f.phi[a][1][c], a2 * dd[a]);
-        A.f.phi[a][0][c] = f1;
-        A.f.phi[a][1][c] = f2;
-        div += fmaf(dd[a], ikx, f1) + f2;
-      }
-      const float pc = p[c];
-      float coef = __ldg(A.m.dt_k + c);
-      if (kBeta) coef = fmaf(__ldg(A.m.beta2dt + c), pc, coef);
-      p[c] = fmaf(-coef, div, pc);
+      const float dd[3] = {dx * g.inv_h[0], dy * g.inv_h[1], dz * g.inv_h[2]};
+      cp.update_store(A, c, dd);
     }
 #pragma unroll
     for (int t = 0; t < 15; ++t) r[t] = r[t + 1];
