@@ -16,7 +16,7 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 LIB = PKG / "libfwgb.so"
-SOURCES = [PKG / "csrc" / "engine.cu"]
+SOURCES = [PKG / "csrc" / "engine.cu", PKG / "csrc" / "noalloc.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 

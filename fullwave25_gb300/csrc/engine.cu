@@ -27,6 +27,13 @@ namespace {
 
 thread_local std::string g_create_error = "no error";
 
+}  // namespace
+
+// Handle-less error text shared with the other translation units of the library.
+void fwgb_set_global_error(const char* msg) { g_create_error = msg; }
+
+namespace {
+
 constexpr int kMarchXC = 64;  // x planes per block of the 3D plane-march kernels
 
 enum Variant { kDirect = 0, kMarch = 1 };

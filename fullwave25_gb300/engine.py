@@ -23,8 +23,7 @@ EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_source_signa
             "fw_set_source_columns", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
             "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_launches_per_step",
-            "fw_destroy",
-            "fw_last_error")
+            "fw_destroy", "fw_run_noalloc", "fw_last_error")
 
 
 class FwDesc(C.Structure):
@@ -89,6 +88,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_kernel_variant": (C.c_int, [H, _IP]),
         "fw_launches_per_step": (C.c_int, [H, _IP]),
         "fw_destroy": (C.c_int, [H]),
+        "fw_run_noalloc": (C.c_int, [C.POINTER(FwDesc), C.POINTER(FwFields), vp, _FP]),
         "fw_last_error": (C.c_char_p, [H]),
     }
     for name, (res, args) in sig.items():

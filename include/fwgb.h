@@ -144,6 +144,26 @@ FWGB_API int fw_launches_per_step(const fw_handle *h, int32_t *n);
 /* Release all device memory of the handle. */
 FWGB_API int fw_destroy(fw_handle *h);
 
+/* Bytes of the file-scope device array that fw_run_noalloc keeps its wavefield in (32 MiB):
+ * 2D grids up to 762,600 cells (11 float32 fields per cell). */
+#define FWGB_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+
+/* Full 2D forward solve that allocates nothing. This entry point has no counterpart in the
+ * reference; it exists for callers that cannot call cudaMalloc while they run: applications whose
+ * device memory comes only from their own pool, processes that must not grow their device
+ * footprint after start-up, or code that only holds device buffers handed to it. Inputs
+ * (`f`, with on_device = 1: device pointers, source coordinates distinct) and the output traces
+ * (device memory, [n_out][ncoordsout]) are the caller's; the wavefield and memory variables live in
+ * one file-scope device array of FWGB_NOALLOC_SCRATCH_BYTES that every GPU which loads this library
+ * holds until the process exits. Grids that need more than that are rejected with
+ * FW_ERR_ARGUMENT; 3D grids with FW_ERR_UNSUPPORTED. Each call zeroes the part of the array it
+ * uses; the array keeps the last call's contents afterwards. All calls share the one array, so
+ * calls that overlap on the GPU (other streams, other host threads) race: serialise them. The first
+ * call on a device looks the array's device address up (cudaGetSymbolAddress) with that device
+ * current; make that first call before any stream capture. Asynchronous on `stream`; errors are
+ * reported by fw_last_error(NULL). Same results as fw_create + fw_set_fields + fw_run. */
+FWGB_API int fw_run_noalloc(const fw_desc *desc, const fw_fields *f, void *stream, float *traces);
+
 /* Description of the last failure on this handle (or of the last failed fw_create when
  * h == NULL). Never NULL. */
 FWGB_API const char *fw_last_error(const fw_handle *h);
