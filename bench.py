@@ -118,8 +118,10 @@ def traffic_from_profiles(workload: str):
 
 
 # --------------------------------------------------------------------------------- workloads
-def make_workload(name: str, rank: int):
-    """Return (inputs-or-builder, steps_per_bench_step, description dict)."""
+def make_workload(name: str, rank: int, grid: int = 0):
+    """Return (inputs-or-builder, steps_per_bench_step, description dict).
+
+    ``grid`` > 0 replaces the 3D workload's 512^3 cells by grid^3 (small profiling cases)."""
     if name == "plain2d":
         from fullwave25_gb300.workloads import plain_2d_inputs
 
@@ -132,8 +134,10 @@ def make_workload(name: str, rank: int):
     if name == "plain3d":
         from fullwave25_gb300.workloads3d import plain_3d_device_inputs
 
-        dinp = plain_3d_device_inputs(seed=rank)
-        desc = {"workload": "plain 3D forward, 512^3 + PML 32 + transition 32 (656^3), nt 3000, "
+        edge = grid or 512
+        dinp = plain_3d_device_inputs(seed=rank, shape=(edge, edge, edge))
+        desc = {"workload": f"plain 3D forward, {edge}^3 + PML 32 + transition 32 "
+                            f"({edge + 144}^3), nt 3000, "
                             "layered fat/muscle/liver with perturbed interfaces and 0.5% scatterers,"
                             " 64-element plane-wave source, 256x256 sensor plane",
                 "grid": list(dinp.shape), "nt": dinp.nt, "steps_per_bench_step": 100,
@@ -210,7 +214,7 @@ def run_gpu(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    inputs, chunk, desc = make_workload(args.workload, rank)
+    inputs, chunk, desc = make_workload(args.workload, rank, args.grid)
     engine = Engine(inputs) if args.workload == "plain2d" else inputs.make_engine()
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
@@ -344,6 +348,79 @@ def run_e2e(args, engine, inputs, chunk, sptr, dev, world):
     return inputs.run_e2e(engine, chunk, n_e2e, sptr, dev, world)
 
 
+def run_batch(args):
+    """Batched 2D workload: the group engine vs the same simulations one by one."""
+    import torch
+
+    from fullwave25_gb300.engine import EngineGroup
+    from fullwave25_gb300.workloads_batch import batch_instance
+
+    rank, world, local = dist_info()
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    ids = [rank * args.batch + i for i in range(args.batch)]
+    t0 = time.perf_counter()
+    insts = [batch_instance(i) for i in ids]
+    build_s = time.perf_counter() - t0
+    engines = [d.make_engine() for d in insts]
+    stream = torch.cuda.current_stream(dev)
+    sptr = stream.cuda_stream
+    units = sum(int(np.prod(d.shape)) * d.nt for d in insts)
+    grp = EngineGroup(engines)
+    for _ in range(args.warmup):
+        grp.run(sptr)
+    torch.cuda.synchronize(dev)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    with ClockSampler(local) as clocks:
+        for i in range(args.steps):
+            ev[2 * i].record(stream)
+            grp.run(sptr)
+            ev[2 * i + 1].record(stream)
+        torch.cuda.synchronize(dev)
+    group_ms = sum(ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(args.steps)) / args.steps
+    # the same simulations one by one (each a full solve on the same device-resident inputs)
+    lat = []
+    for e in engines:
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        e.reset(sptr)
+        e.advance(e.inputs.nt, sptr)
+        b.record(stream)
+        torch.cuda.synchronize(dev)
+        lat.append(a.elapsed_time(b))
+    serial_ms = sum(lat)
+    from fullwave25_gb300.workloads import algorithmic_bytes_per_cell
+
+    achieved = units * algorithmic_bytes_per_cell(2) / (group_ms / 1e3) / 1e9
+    peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (
+        ROOT / "MEASURED_PEAKS.json").exists() else {}
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    line = {"metric": METRIC, "value": units / (group_ms / 1e3) / 1e9, "unit": METRIC,
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": group_ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"batched 2D forward, {len(insts)} simulations of uneven "
+                                   "size (512-2048 x 512-1536 + PML 40 + transition 40), "
+                                   "nt 3000-8000, 128-element transmits",
+                       "bench_step": "one group run = every simulation to its own nt",
+                       "device_build_s": build_s},
+            "sims_per_s": {"batched": len(insts) / (group_ms / 1e3),
+                           "one_by_one": len(insts) / (serial_ms / 1e3),
+                           "batched_over_one_by_one": serial_ms / group_ms},
+            "one_by_one_latency_ms": {"p50": float(np.percentile(lat, 50)),
+                                      "p99": float(np.percentile(lat, 99)),
+                                      "max": float(max(lat))},
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                         "frac": achieved / peak, "traffic": None},
+            "gpu_launches": 2 * max(d.nt for d in insts) * args.steps,
+            "clocks": clocks.summary()}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    grp.close()
+    for e in engines:
+        e.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -351,14 +428,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=os.environ.get("FWGB_WORKLOAD", "plain2d"),
-                    choices=["plain2d", "plain3d"])
+                    choices=["plain2d", "plain3d", "batch2d"])
+    ap.add_argument("--batch", type=int, default=64, help="simulations per rank (batch2d)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--grid", type=int, default=0,
+                    help="3D workload edge in cells (default 512; smaller for profiling)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps requested; using 3", file=sys.stderr)
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch2d":
+        run_batch(args)
     else:
         run_gpu(args)
 

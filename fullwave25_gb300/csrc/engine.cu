@@ -12,6 +12,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
 #include <new>
 #include <string>
 #include <vector>
@@ -704,5 +705,198 @@ int fw_destroy(fw_handle* h) {
 }
 
 const char* fw_last_error(const fw_handle* h) { return h ? h->err.c_str() : g_create_error.c_str(); }
+
+}  // extern "C"
+
+// ------------------------------------------------------------------------------------- groups
+struct fw_group {
+  std::vector<fw_handle*> members;  // sorted by steps left, descending (tiles in the same order)
+  StepArgs* d_args = nullptr;       // one argument block per member (its own step counter)
+  int4* d_tiles = nullptr;          // {member, tile_y, tile_x, tile index within the member}
+  size_t args_cap = 0, tiles_cap = 0;
+  std::vector<int> tiles_upto;      // tiles of the first k members (k = 0..n)
+  bool beta = false;
+  cudaStream_t capture_stream = nullptr;
+  std::map<int, cudaGraphExec_t> graphs;  // active tile count -> graph of kGroupGraphSteps steps
+};
+
+namespace {
+
+constexpr int kGroupGraphSteps = 64;
+
+void group_launch_step(fw_group* g, int n_tiles, cudaStream_t s) {
+  const dim3 block(kD2TY, kD2TX);
+  vel2d_group<<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
+  if (g->beta) prs2d_group<true><<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
+  else prs2d_group<false><<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
+}
+
+int group_graph(fw_group* g, int n_tiles, cudaGraphExec_t* out) {
+  auto it = g->graphs.find(n_tiles);
+  if (it != g->graphs.end()) {
+    *out = it->second;
+    return FW_OK;
+  }
+  cudaGraph_t graph = nullptr;
+  FW_CUDA(nullptr, cudaStreamBeginCapture(g->capture_stream, cudaStreamCaptureModeThreadLocal));
+  for (int n = 0; n < kGroupGraphSteps; ++n) group_launch_step(g, n_tiles, g->capture_stream);
+  FW_CUDA(nullptr, cudaStreamEndCapture(g->capture_stream, &graph));
+  cudaGraphExec_t exec = nullptr;
+  cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(nullptr, FW_ERR_CUDA, "group graph: %s", cudaGetErrorString(e));
+  g->graphs[n_tiles] = exec;
+  *out = exec;
+  return FW_OK;
+}
+
+// (Re)build the member order, argument blocks and tile work list of a group. Members are
+// ordered by steps left (descending) so that, as members finish, the active tiles stay a prefix.
+int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
+  for (int i = 0; i < n; ++i) {
+    const fw_handle* h = handles[i];
+    if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle %d is NULL", i);
+    if (h->ndim != 2 || h->variant != kDirect)
+      return fail(nullptr, FW_ERR_UNSUPPORTED, "group members must be 2D simulations (member %d)", i);
+    if (!h->fields_set) return fail(nullptr, FW_ERR_STATE, "member %d has no fields set", i);
+  }
+  std::vector<fw_handle*> m(handles, handles + n);
+  std::stable_sort(m.begin(), m.end(), [](const fw_handle* a, const fw_handle* b) {
+    return a->d.nt - a->host_step > b->d.nt - b->host_step;
+  });
+  std::vector<StepArgs> args(n);
+  std::vector<int4> tiles;
+  g->members = m;
+  g->tiles_upto.assign(1, 0);
+  g->beta = false;
+  for (int r = 0; r < n; ++r) g->beta = g->beta || m[r]->has_beta;
+  for (int r = 0; r < n; ++r) {
+    fw_handle* h = m[r];
+    args[r] = h->args;
+    // members without beta read their (all-zero) beta buffer when the group uses the beta kernel
+    args[r].m.beta2dt = map_field(h, 2);
+    const Tiling& t = h->tiling;
+    for (int tx = 0; tx < t.n[0]; ++tx)
+      for (int ty = 0; ty < t.n[1]; ++ty) tiles.push_back(make_int4(r, ty, tx, tx * t.n[1] + ty));
+    g->tiles_upto.push_back((int)tiles.size());
+  }
+  if ((size_t)n > g->args_cap || tiles.size() > g->tiles_cap) {
+    for (auto& kv : g->graphs) cudaGraphExecDestroy(kv.second);
+    g->graphs.clear();
+    if (g->d_args) cudaFree(g->d_args);
+    if (g->d_tiles) cudaFree(g->d_tiles);
+    g->d_args = nullptr;
+    g->d_tiles = nullptr;
+    g->args_cap = std::max<size_t>(n, 2 * g->args_cap);
+    g->tiles_cap = std::max<size_t>(tiles.size(), 2 * g->tiles_cap);
+    if (cudaMalloc(&g->d_args, sizeof(StepArgs) * g->args_cap) != cudaSuccess ||
+        cudaMalloc(&g->d_tiles, sizeof(int4) * g->tiles_cap) != cudaSuccess) {
+      g->args_cap = g->tiles_cap = 0;
+      return fail(nullptr, FW_ERR_OOM, "group device allocation failed");
+    }
+  }
+  // graphs read the work list through stable pointers, so they stay valid across rebuilds
+  FW_CUDA(nullptr, cudaMemcpyAsync(g->d_args, args.data(), sizeof(StepArgs) * n,
+                                   cudaMemcpyHostToDevice, g->capture_stream));
+  FW_CUDA(nullptr, cudaMemcpyAsync(g->d_tiles, tiles.data(), sizeof(int4) * tiles.size(),
+                                   cudaMemcpyHostToDevice, g->capture_stream));
+  FW_CUDA(nullptr, cudaStreamSynchronize(g->capture_stream));
+  return FW_OK;
+}
+
+// Advance every member by up to n_steps, each stopping at its own nt.
+int group_advance(fw_group* g, cudaStream_t s, int n_steps) {
+  const int n = (int)g->members.size();
+  int done = 0;
+  while (done < n_steps) {
+    // members still running: a prefix of the order (sorted by steps left)
+    int k = 0;
+    int seg = n_steps - done;
+    for (int r = 0; r < n; ++r) {
+      const int left = g->members[r]->d.nt - g->members[r]->host_step;
+      if (left <= 0) break;
+      k = r + 1;
+      seg = std::min(seg, left);
+    }
+    if (k == 0) break;
+    const int n_tiles = g->tiles_upto[k];
+    int left = seg;
+    if (left >= kGroupGraphSteps) {
+      cudaGraphExec_t exec = nullptr;
+      int st = group_graph(g, n_tiles, &exec);
+      if (st) return st;
+      for (; left >= kGroupGraphSteps; left -= kGroupGraphSteps) FW_CUDA(nullptr, cudaGraphLaunch(exec, s));
+    }
+    for (; left > 0; --left) group_launch_step(g, n_tiles, s);
+    FW_CUDA(nullptr, cudaGetLastError());
+    for (int r = 0; r < k; ++r) g->members[r]->host_step += seg;
+    done += seg;
+  }
+  return FW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fw_group_create(fw_handle* const* handles, int32_t n, fw_group** out) {
+  if (!out || !handles || n <= 0) return fail(nullptr, FW_ERR_ARGUMENT, "need n > 0 handles and out");
+  *out = nullptr;
+  fw_group* g = new (std::nothrow) fw_group();
+  if (!g) return fail(nullptr, FW_ERR_OOM, "host allocation failed");
+  if (cudaStreamCreateWithFlags(&g->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete g;
+    return fail(nullptr, FW_ERR_CUDA, "stream creation failed");
+  }
+  int st = group_set(g, handles, n);
+  if (st) {
+    fw_group_destroy(g);
+    return st;
+  }
+  *out = g;
+  return FW_OK;
+}
+
+int fw_group_set_members(fw_group* g, fw_handle* const* handles, int32_t n) {
+  if (!g || (n > 0 && !handles) || n < 0) return fail(nullptr, FW_ERR_ARGUMENT, "bad group arguments");
+  if (n == 0) {
+    g->members.clear();
+    g->tiles_upto.assign(1, 0);
+    return FW_OK;
+  }
+  return group_set(g, handles, n);
+}
+
+int fw_group_advance(fw_group* g, void* stream, int32_t n_steps) {
+  if (!g || n_steps < 0) return fail(nullptr, FW_ERR_ARGUMENT, "bad group arguments");
+  // the work list order depends on steps left: refresh it before stepping
+  std::vector<fw_handle*> m = g->members;
+  if (!m.empty()) {
+    int st = group_set(g, m.data(), (int)m.size());
+    if (st) return st;
+  }
+  return group_advance(g, static_cast<cudaStream_t>(stream), n_steps);
+}
+
+int fw_group_run(fw_group* g, void* stream) {
+  if (!g) return fail(nullptr, FW_ERR_ARGUMENT, "group is NULL");
+  int max_nt = 0;
+  for (fw_handle* h : g->members) {
+    int st = fw_reset(h, stream);
+    if (st) return fail(nullptr, st, "member reset failed: %s", h->err.c_str());
+    max_nt = std::max(max_nt, (int)h->d.nt);
+  }
+  return fw_group_advance(g, stream, max_nt);
+}
+
+int fw_group_destroy(fw_group* g) {
+  if (!g) return FW_OK;
+  for (auto& kv : g->graphs) cudaGraphExecDestroy(kv.second);
+  if (g->capture_stream) cudaStreamDestroy(g->capture_stream);
+  if (g->d_args) cudaFree(g->d_args);
+  if (g->d_tiles) cudaFree(g->d_tiles);
+  delete g;
+  return FW_OK;
+}
 
 }  // extern "C"

@@ -14,11 +14,12 @@ constexpr int kD2TY = 32, kD2TX = 8;             // 2D tile: 32 cells along y, 8
 constexpr int kD3TZ = 32, kD3TY = 4, kD3TX = 2;  // 3D tile
 
 // ---------------------------------------------------------------------------------------- 2D
-__global__ void __launch_bounds__(256) vel2d_direct(const StepArgs A) {
+// Bodies take the tile (ty along y, tx along x) explicitly so that the single-simulation kernels
+// (tile = block index) and the group kernels (tile from a work list) share them.
+__device__ __forceinline__ void vel2d_body(const StepArgs& A, int tile_y, int tile_x) {
   const Grid& g = A.g;
-  const int j = kGhost + blockIdx.x * kD2TY + threadIdx.x;
-  const int i = kGhost + blockIdx.y * kD2TX + threadIdx.y;
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *A.step += 1;
+  const int j = kGhost + tile_y * kD2TY + threadIdx.x;
+  const int i = kGhost + tile_x * kD2TX + threadIdx.y;
   if (i >= g.nx - kGhost || j >= g.ny - kGhost) return;
   const int64_t sx = g.sx;
   const int64_t c = i * sx + j;
@@ -40,10 +41,10 @@ __global__ void __launch_bounds__(256) vel2d_direct(const StepArgs A) {
 }
 
 template <bool kBeta>
-__global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
+__device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int tile_x, int tile) {
   const Grid& g = A.g;
-  const int j = kGhost + blockIdx.x * kD2TY + threadIdx.x;
-  const int i = kGhost + blockIdx.y * kD2TX + threadIdx.y;
+  const int j = kGhost + tile_y * kD2TY + threadIdx.x;
+  const int i = kGhost + tile_x * kD2TX + threadIdx.y;
   float* p = A.f.p;
   if (i < g.nx - kGhost && j < g.ny - kGhost) {
     const int64_t sx = g.sx;
@@ -65,8 +66,36 @@ __global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
     const float dd[2] = {dx * g.inv_h[0], dy * g.inv_h[1]};
     cp.update_store(A, c, dd);
   }
-  tile_epilogue(A, p, blockIdx.y * gridDim.x + blockIdx.x, threadIdx.y * blockDim.x + threadIdx.x,
-                blockDim.x * blockDim.y);
+  tile_epilogue(A, p, tile, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
+}
+
+__global__ void __launch_bounds__(256) vel2d_direct(const StepArgs A) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *A.step += 1;
+  vel2d_body(A, blockIdx.x, blockIdx.y);
+}
+
+template <bool kBeta>
+__global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
+  prs2d_body<kBeta>(A, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x);
+}
+
+// Group (batched) kernels: block b works on tiles[b] = {simulation, tile_y, tile_x, tile index
+// within that simulation}; `sims` holds one argument block per simulation, each with its own step
+// counter, advanced by the block that owns the simulation's tile 0. One launch per phase advances
+// every listed simulation by one step; simulations may be at different steps.
+__global__ void __launch_bounds__(256) vel2d_group(const StepArgs* __restrict__ sims,
+                                                   const int4* __restrict__ tiles) {
+  const int4 t = tiles[blockIdx.x];
+  const StepArgs& A = sims[t.x];
+  if (t.w == 0 && threadIdx.x == 0 && threadIdx.y == 0) *A.step += 1;
+  vel2d_body(A, t.y, t.z);
+}
+
+template <bool kBeta>
+__global__ void __launch_bounds__(256) prs2d_group(const StepArgs* __restrict__ sims,
+                                                   const int4* __restrict__ tiles) {
+  const int4 t = tiles[blockIdx.x];
+  prs2d_body<kBeta>(sims[t.x], t.y, t.z, t.w);
 }
 
 // ---------------------------------------------------------------------------------------- 3D

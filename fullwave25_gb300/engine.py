@@ -23,7 +23,9 @@ EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_source_signa
             "fw_set_source_columns", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
             "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_launches_per_step",
-            "fw_destroy", "fw_run_noalloc", "fw_last_error")
+            "fw_destroy", "fw_group_create", "fw_group_run", "fw_group_set_members",
+            "fw_group_advance", "fw_group_destroy",
+            "fw_run_noalloc", "fw_last_error")
 
 
 class FwDesc(C.Structure):
@@ -88,6 +90,11 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_kernel_variant": (C.c_int, [H, _IP]),
         "fw_launches_per_step": (C.c_int, [H, _IP]),
         "fw_destroy": (C.c_int, [H]),
+        "fw_group_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
+        "fw_group_run": (C.c_int, [C.c_void_p, vp]),
+        "fw_group_set_members": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32]),
+        "fw_group_advance": (C.c_int, [C.c_void_p, vp, C.c_int32]),
+        "fw_group_destroy": (C.c_int, [C.c_void_p]),
         "fw_run_noalloc": (C.c_int, [C.POINTER(FwDesc), C.POINTER(FwFields), vp, _FP]),
         "fw_last_error": (C.c_char_p, [H]),
     }
@@ -286,6 +293,56 @@ class Engine:
         if getattr(self, "_h", None) and self._h.value:
             self.lib.fw_destroy(self._h)
             self._h = C.c_void_p()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class EngineGroup:
+    """Many 2D simulations stepped together (``fw_group_*``): one launch per phase per step."""
+
+    def __init__(self, engines):
+        self.engines = list(engines)
+        self.lib = load_library()
+        arr = (C.c_void_p * len(self.engines))(*[e.handle.value for e in self.engines])
+        self._g = C.c_void_p()
+        st = self.lib.fw_group_create(arr, len(self.engines), C.byref(self._g))
+        if st:
+            raise EngineError("fw_group_create", st, self.lib.fw_last_error(None).decode())
+
+    def run(self, stream: int | None = None) -> None:
+        st = self.lib.fw_group_run(self._g, C.c_void_p(stream or 0))
+        if st:
+            raise EngineError("fw_group_run", st, self.lib.fw_last_error(None).decode())
+
+    def set_members(self, engines) -> None:
+        self.engines = list(engines)
+        arr = (C.c_void_p * max(1, len(self.engines)))(*[e.handle.value for e in self.engines])
+        st = self.lib.fw_group_set_members(self._g, arr, len(self.engines))
+        if st:
+            raise EngineError("fw_group_set_members", st, self.lib.fw_last_error(None).decode())
+
+    def advance(self, n_steps: int, stream: int | None = None) -> None:
+        st = self.lib.fw_group_advance(self._g, C.c_void_p(stream or 0), int(n_steps))
+        if st:
+            raise EngineError("fw_group_advance", st, self.lib.fw_last_error(None).decode())
+
+    def traces(self) -> list:
+        return [e.read_traces() for e in self.engines]
+
+    def close(self) -> None:
+        if getattr(self, "_g", None) and self._g.value:
+            self.lib.fw_group_destroy(self._g)
+            self._g = C.c_void_p()
 
     def __enter__(self):
         return self

@@ -144,6 +144,32 @@ FWGB_API int fw_launches_per_step(const fw_handle *h, int32_t *n);
 /* Release all device memory of the handle. */
 FWGB_API int fw_destroy(fw_handle *h);
 
+/* A group runs many independent 2D simulations together: every time step is one velocity
+ * launch and one pressure launch over a device work list of (simulation, tile) pairs, so small
+ * simulations share the GPU instead of each leaving it mostly idle; blocks of 64 steps are
+ * captured into CUDA graphs. Members keep their own memory, sources, sensors and nt (a member
+ * stops stepping at its nt; its tiles leave the work list). No counterpart in the reference,
+ * which runs one executable per simulation (fullwave/solver/launcher.py:196-215). */
+typedef struct fw_group fw_group;
+
+/* Build a group over 2D handles whose fields are set (the handles must outlive the group). */
+FWGB_API int fw_group_create(fw_handle *const *handles, int32_t n, fw_group **out);
+
+/* Reset every member and run each for its own nt steps (asynchronous on stream); afterwards
+ * read each member's traces with fw_read_traces. Errors: fw_last_error(NULL). */
+FWGB_API int fw_group_run(fw_group *g, void *stream);
+
+/* Replace the member list (members may be at different steps; continuous batching admits new
+ * simulations and retires finished ones between calls to fw_group_advance). */
+FWGB_API int fw_group_set_members(fw_group *g, fw_handle *const *handles, int32_t n);
+
+/* Advance every member by up to n_steps time steps, each stopping at its own nt
+ * (asynchronous on stream). */
+FWGB_API int fw_group_advance(fw_group *g, void *stream, int32_t n_steps);
+
+/* Release the group (not its members). */
+FWGB_API int fw_group_destroy(fw_group *g);
+
 /* Bytes of the file-scope device array that fw_run_noalloc keeps its wavefield in (32 MiB):
  * 2D grids up to 762,600 cells (11 float32 fields per cell). */
 #define FWGB_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
