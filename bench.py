@@ -167,15 +167,33 @@ def time_oracle(workload: str, budget_s: float):
     o.run(1)  # warm-up
     steps, t0 = 0, time.perf_counter()
     while time.perf_counter() - t0 < budget_s and steps + 10 < inp.nt:
-        o.run(10)
+        traces = o.run(10)
         steps += 10
     el = time.perf_counter() - t0
     o.close()
     cells = int(np.prod(inp.shape))
     cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
-    return {"value": cells * steps / el / 1e9, "unit": METRIC, "cores": cores, "kind": "port",
-            "sample": f"FP64 C oracle (OpenMP, {cores} threads), {label}, {steps} time steps in "
-                      f"{el:.1f} s"}
+    out = {"value": cells * steps / el / 1e9, "unit": METRIC, "cores": cores, "kind": "port",
+           "sample": f"FP64 C oracle (OpenMP, {cores} threads), {label}, {steps} time steps in "
+                     f"{el:.1f} s"}
+    # kept for the parity statement (not part of the JSON line)
+    time_oracle.last = (inp, traces, steps + 1, label)
+    return out
+
+
+def parity_vs_oracle():
+    """rel-L2 of the GPU engine's traces against the FP64 oracle on the CPU-baseline sample."""
+    from fullwave25_gb300.engine import Engine
+
+    inp, ref, n_steps, label = time_oracle.last
+    rows = (n_steps + inp.mod_t - 1) // inp.mod_t
+    with Engine(inp) as eng:
+        eng.advance(n_steps)
+        got = eng.read_traces(0, rows)
+    ref = ref[:rows]
+    err = float(np.linalg.norm(got - ref) / max(np.linalg.norm(ref), 1e-300))
+    return {"rel_l2_vs_fp64_oracle": err, "tolerance": 1e-4,
+            "sample": f"{label}, first {n_steps} time steps, {inp.outc.shape[0]} sensors"}
 
 
 def run_reference(args):
@@ -255,13 +273,11 @@ def run_gpu(args):
         barrier()
         wall = time.perf_counter() - t0
     dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
-    t_rank = torch.tensor([dev_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        torch.distributed.all_reduce(t_rank, op=torch.distributed.ReduceOp.MAX)
-    dev_ms_max = float(t_rank.item())
-    units_per_rank = cells * chunk * args.steps
-    value = units_per_rank * world / (dev_ms_max / 1e3) / 1e9
-    ms_per_step = dev_ms_max / args.steps
+    from fullwave25_gb300.replicas import aggregate_throughput
+
+    _, t_max, units_per_s = aggregate_throughput(cells * chunk * args.steps, dev_ms / 1e3)
+    value = units_per_s / 1e9
+    ms_per_step = t_max * 1e3 / args.steps
 
     # roofline: one time step (velocity + pressure kernels) over the whole grid
     step_s = (dev_ms / 1e3) / (chunk * args.steps)
@@ -280,6 +296,7 @@ def run_gpu(args):
         return
     cpu = time_oracle(args.workload, float(os.environ.get("FWGB_CPU_SAMPLE_S", "15"))) if (
         world == 1 and not args.no_cpu_baseline) else None
+    parity = parity_vs_oracle() if cpu is not None else None
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -295,6 +312,7 @@ def run_gpu(args):
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
                      else "fallback 6800 GB/s"},
         "cpu_baseline": cpu,
+        "parity": parity,
         "e2e": e2e,
         "gpu_launches": int(engine.launches_per_step * chunk * args.steps),
         "clocks": clk,
@@ -358,7 +376,13 @@ def run_batch(args):
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    ids = [rank * args.batch + i for i in range(args.batch)]
+    from fullwave25_gb300.replicas import rank_instances
+
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    ids = rank_instances(rank, world, args.batch)
     t0 = time.perf_counter()
     insts = [batch_instance(i) for i in ids]
     build_s = time.perf_counter() - t0
@@ -421,14 +445,119 @@ def run_batch(args):
         e.close()
 
 
+def run_serve(args):
+    """Serving stream: Poisson arrivals of forward solves, continuous batching vs FIFO."""
+    import torch
+
+    from fullwave25_gb300.server import (Request, engine_bytes, poisson_arrivals,
+                                         serve_continuous, serve_fifo)
+    from fullwave25_gb300.workloads_batch import batch_instance
+
+    torch.cuda.set_device(0)
+    arrivals = poisson_arrivals(args.rate, args.duration, seed=0)
+    scale = args.scale
+
+    def make(i, t):
+        return Request(rid=i, arrival=float(t), build=lambda i=i: batch_instance(i, scale=scale))
+
+    reqs = [make(i, t) for i, t in enumerate(arrivals)]
+    for r in reqs:  # memory need from the instance geometry (built once to measure)
+        d = r.build()
+        r.bytes_needed = engine_bytes(d.shape, d.nt, d.outc.shape[0])
+        del d
+    torch.cuda.synchronize()
+    # warm-up: one small continuous run so that graphs and kernels are loaded
+    serve_continuous(reqs[:3], budget_bytes=args.budget_gb << 30)
+    with ClockSampler(0) as clocks:
+        cont = serve_continuous(reqs, budget_bytes=args.budget_gb << 30, chunk_steps=256)
+    cont_lat = [r.latency for r in reqs]
+    fifo = serve_fifo(reqs)
+    line = {"metric": "simulations/s (serving stream)", "value": cont["sims_per_s"],
+            "unit": "sims/s", "n_gpus": 1, "steps": 1, "warmup": 1,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"Poisson {args.rate} req/s for {args.duration} s of 2D forward "
+                                   f"solves (batched-workload instances at scale {scale}), "
+                                   f"device budget {args.budget_gb} GB, blocks of 256 steps",
+                       "requests": len(reqs)},
+            "continuous": cont, "fifo_one_at_a_time": fifo,
+            "sims_per_s_ratio": cont["sims_per_s"] / fifo["sims_per_s"],
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+    del cont_lat
+
+
+def run_adjoint(args):
+    """Adjoint gradient: 1024^2 grid, nt 6000, 512-sensor row, checkpoints every 200 steps."""
+    import torch
+    from scipy.ndimage import gaussian_filter
+
+    from fullwave25_gb300.adjoint import AdjointProblem
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.workloads import ellipse_medium_2d
+
+    torch.cuda.set_device(0)
+    dev = torch.device("cuda", 0)
+    n = args.grid or 1024
+    nt = 6000 if n == 1024 else int(6000 * n / 1024)
+    dx = 1540 / 3e6 / 12
+    c, rho, a0, gam = ellipse_medium_2d((n, n), dx, seed=0)
+    sig = 2e-3 / dx
+    blur = lambda a: gaussian_filter(a, sig, mode="nearest")  # noqa: E731
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=dev)  # noqa: E731
+    true = (t(c), t(rho), t(a0), t(gam))
+    start = (t(blur(c)), t(blur(rho)), t(blur(a0)), t(gam))
+    prob = AdjointProblem((n, n), nt=nt, n_pml=40, n_transition=40, c_ref=start[0], device=dev,
+                          sensor_step=max(1, n // 512), sensor_row=5)
+    with Engine(prob.build(*true), validate=False) as e:
+        observed = torch.as_tensor(e.run(), device=dev)
+
+    def evaluate():
+        cc, rr, aa = [x.clone().requires_grad_(True) for x in start[:3]]
+        J = prob.misfit(cc, rr, aa, start[3], observed, checkpoint_every=200)
+        J.backward()
+        return float(J), cc.grad, rr.grad, aa.grad
+
+    for _ in range(args.warmup):
+        evaluate()
+    torch.cuda.synchronize(dev)
+    t0 = time.perf_counter()
+    with ClockSampler(0) as clocks:
+        for _ in range(args.steps):
+            J, gc, gr, ga = evaluate()
+        torch.cuda.synchronize(dev)
+    el = (time.perf_counter() - t0) / args.steps
+    ext = prob.build(*start).shape
+    cells = int(np.prod(ext))
+    line = {"metric": "gradient evaluations/s (adjoint)", "value": 1.0 / el, "unit": "grad/s",
+            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 wavefields, f64 gradient accumulation", "data": "synthetic",
+            "config": {"workload": f"adjoint gradient, {n}x{n} + PML 40 + transition 40 "
+                                   f"({ext[0]}x{ext[1]}), nt {nt}, {observed.shape[1]}-sensor "
+                                   "row, true medium vs Gaussian-blurred (sigma 2 mm) start, "
+                                   "gradient w.r.t. c, rho, alpha0, checkpoints every 200 steps",
+                       "misfit": J,
+                       "time_steps_per_evaluation": "3 nt (forward, recompute, adjoint)"},
+            "equivalent_Gcell_updates_per_s": 3 * nt * cells / el / 1e9,
+            "grad_norms": {"c": float(gc.norm()), "rho": float(gr.norm()),
+                           "alpha0": float(ga.norm())},
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
-    ap.add_argument("--workload", default=os.environ.get("FWGB_WORKLOAD", "plain2d"),
-                    choices=["plain2d", "plain3d", "batch2d"])
+    ap.add_argument("--workload", default=os.environ.get("FWGB_WORKLOAD", "plain3d"),
+                    choices=["plain2d", "plain3d", "batch2d", "serve2d", "adjoint2d"])
+    ap.add_argument("--rate", type=float, default=20.0, help="serve2d: arrivals per second")
+    ap.add_argument("--duration", type=float, default=10.0, help="serve2d: stream length [s]")
+    ap.add_argument("--scale", type=float, default=0.5, help="serve2d: instance size scale")
+    ap.add_argument("--budget-gb", type=int, default=150, help="serve2d: device memory budget")
     ap.add_argument("--batch", type=int, default=64, help="simulations per rank (batch2d)")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=0,
@@ -441,6 +570,10 @@ def main():
         run_reference(args)
     elif args.workload == "batch2d":
         run_batch(args)
+    elif args.workload == "serve2d":
+        run_serve(args)
+    elif args.workload == "adjoint2d":
+        run_adjoint(args)
     else:
         run_gpu(args)
 

@@ -1,0 +1,201 @@
+"""Gradients of the sensor-trace misfit with respect to sound speed, density and alpha0 (2D).
+
+Layers:
+1. :func:`map_gradients` runs the engine's checkpointed forward pass and its discrete adjoint
+   (``fw_adjoint_forward`` / ``fw_adjoint_backward``): the misfit ``J = 1/2 sum (traces -
+   observed)^2`` reduced in FP64 on the GPU, and the FP64 time-summed gradient of ``J`` with
+   respect to every coefficient map the time loop multiplies by, chained to the raw input maps
+   (rho, K, kappau, kappax, apml*, bpml*).
+2. :class:`FdtdMisfit` is a ``torch.autograd.Function`` over those raw maps.
+3. :class:`AdjointProblem` builds the raw maps from physical ``c``, ``rho``, ``alpha0`` (and a fixed
+   ``gamma``) on the original grid with differentiable torch operations (PML padding and ramps
+   as in :mod:`fullwave25_gb300.pml`), so ``J.backward()`` yields dJ/dc, dJ/drho, dJ/dalpha0.
+
+The per-cell tap set (``dcmap``, the integer sound speed) is held fixed at the starting medium:
+it is piecewise constant in c and contributes no gradient almost everywhere. Relaxation
+strengths are linear in alpha0 at fixed gamma (``d_nu = alpha0 * d_nu(1, gamma)``, exact for the
+stand-in lookup table), so alpha0 has a gradient; the relaxation rates depend on gamma only.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from . import coefficients
+from .engine import ADJOINT_MAPS, Engine
+from .grid import Grid
+from .medium import relaxation_param_keys
+from .relaxation import default_table
+from .workloads3d import DeviceInputs, extend_edge, pml_relaxation_maps_t
+
+RAW_MAPS = ("rho", "K", "kappau", "kappax", "apmlu1", "bpmlu1", "apmlu2", "bpmlu2",
+            "apmlx1", "bpmlx1", "apmlx2", "bpmlx2")
+
+
+def _torch():
+    import torch  # noqa: PLC0415
+
+    return torch
+
+
+def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=None):
+    """Misfit and raw-map gradients for ``engine`` (its current fields) against ``observed``.
+
+    ``observed``: CUDA float32 tensor ``[n_out, ncoordsout]``. Returns ``(J, traces, grads)`` with
+    ``grads[name]`` a float64 CUDA tensor of the grid shape for every name in ``RAW_MAPS``.
+    """
+    torch = _torch()
+    inp = engine.inputs
+    dev = observed.device
+    engine.adjoint_forward(checkpoint_every, stream)
+    traces = torch.empty_like(observed)
+    engine.read_traces_into(0, inp.n_out, traces.data_ptr(), stream)
+    torch.cuda.synchronize(dev)
+    residual = (traces - observed).contiguous()
+    J = 0.5 * float(torch.sum(residual.double() ** 2))
+    g = torch.zeros((len(ADJOINT_MAPS),) + tuple(inp.shape), dtype=torch.float64, device=dev)
+    engine.adjoint_backward(residual.data_ptr(), g.data_ptr(), stream)
+    torch.cuda.synchronize(dev)
+    gm = dict(zip(ADJOINT_MAPS, g))
+    m = {k: inp.maps[k].double() for k in ("rho", "K", "kappau", "kappax")}
+    dt = float(np.float32(inp.dt))
+    grads = {
+        "rho": gm["rdt_rho"] * (-dt / m["rho"] ** 2),
+        "K": gm["dt_k"] * dt,
+        "kappau": gm["inv_ku"] * (-1.0 / m["kappau"] ** 2),
+        "kappax": gm["inv_kx"] * (-1.0 / m["kappax"] ** 2),
+    }
+    for nu in (1, 2):
+        for ax in ("u", "x"):
+            grads[f"apml{ax}{nu}"] = gm[f"a{ax}{nu}"]
+            grads[f"bpml{ax}{nu}"] = gm[f"b{ax}{nu}"]
+    return J, traces, grads
+
+
+class FdtdMisfit:
+    """``torch.autograd.Function``: J(raw maps) with the engine's adjoint as backward."""
+
+    @staticmethod
+    def apply(template: DeviceInputs, observed, checkpoint_every: int, *maps):
+        torch = _torch()
+
+        class _Fn(torch.autograd.Function):
+            @staticmethod
+            def forward(ctx, *tensors):
+                inp = DeviceInputs(**{**template.__dict__, "maps": {
+                    **template.maps,
+                    **{k: t.detach().to(torch.float32).contiguous()
+                       for k, t in zip(RAW_MAPS, tensors)}}})
+                with Engine(inp, validate=False) as eng:
+                    J, traces, grads = map_gradients(eng, observed, checkpoint_every)
+                ctx.grads = [grads[k] for k in RAW_MAPS]
+                ctx.dtypes = [t.dtype for t in tensors]
+                ctx.traces = traces
+                return torch.tensor(J, dtype=torch.float64, device=observed.device)
+
+            @staticmethod
+            def backward(ctx, gJ):
+                return tuple((gJ * g).to(dt) for g, dt in zip(ctx.grads, ctx.dtypes))
+
+        return _Fn.apply(*maps)
+
+
+class AdjointProblem:
+    """2D medium -> engine inputs, differentiable in c, rho and alpha0 (gamma held fixed)."""
+
+    def __init__(self, shape, *, nt: int, f0: float = 3e6, ppw: int = 12, cfl: float = 0.2,
+                 n_pml: int = 40, n_transition: int = 40, c_ref=None, device=None,
+                 sensor_step: int = 1, source_row: int = 0, sensor_row: int = 5,
+                 p0: float = 1e6, table=None):
+        torch = _torch()
+        self.device = device or torch.device("cuda", torch.cuda.current_device())
+        self.shape = tuple(shape)
+        self.grid = Grid.from_cells(self.shape, f0=f0, nt=nt, ppw=ppw, cfl=cfl)
+        self.nb = n_pml + n_transition + coefficients.N_TAPS
+        self.n_pml, self.n_transition = n_pml, n_transition
+        self.table = table or default_table()
+        self.c_ref = c_ref   # starting medium: fixes dcmap/dmap
+        self.source_row, self.sensor_row = source_row, sensor_row
+        self.sensor_step = sensor_step
+        self.p0 = p0
+
+    def _relaxation(self, a0, gam):
+        """Parameters linear in alpha0: d = alpha0 * d(1, gamma); rates from the gamma bin."""
+        torch = _torch()
+        t = self.table
+        top = len(t.alpha_list) - 1
+        pl = torch.as_tensor(t.power_list.round(10), device=gam.device)
+        g = torch.clamp(gam, float(t.power_list.min()), float(t.power_list.max().round(4)))
+        ig = torch.clamp(torch.searchsorted(pl, g.contiguous()), 0, len(pl) - 1)
+        unit = torch.as_tensor(t.table[top] / max(float(t.alpha_list[top]), 1e-30),
+                               device=gam.device)
+        rates = torch.as_tensor(t.table[top], device=gam.device)
+        keys = relaxation_param_keys(2)
+        out = {}
+        for i, k in enumerate(keys):
+            if k.startswith("kappa"):
+                out[k] = torch.ones_like(a0)
+            elif k.startswith("d_"):
+                out[k] = a0 * unit[ig, i]
+            else:
+                out[k] = rates[ig, i]
+        return out
+
+    def build(self, c, rho, a0, gam) -> DeviceInputs:
+        """Engine inputs (maps keep the autograd graph of c, rho, a0)."""
+        torch = _torch()
+        nb = self.nb
+        p = self._relaxation(a0, gam)
+        for op in ("x1", "x2"):  # mechanism sort by time constant (fullwave/medium.py:121-209)
+            t1 = p[f"d_{op}_nu1"] / p[f"kappa_{op}"] + p[f"alpha_{op}_nu1"]
+            t2 = p[f"d_{op}_nu2"] / p[f"kappa_{op}"] + p[f"alpha_{op}_nu2"]
+            sw = (t2 < t1).detach()
+            for var in ("d", "alpha"):
+                a, b = p[f"{var}_{op}_nu1"], p[f"{var}_{op}_nu2"]
+                p[f"{var}_{op}_nu1"], p[f"{var}_{op}_nu2"] = torch.where(sw, b, a), torch.where(sw, a, b)
+        p = {k: extend_edge(v, nb) for k, v in p.items()}
+        fw2 = pml_relaxation_maps_t({k: v.clone() for k, v in p.items()}, n_pml=self.n_pml,
+                                    n_transition=self.n_transition, dt=self.grid.dt,
+                                    c0=self.grid.c0, dx=self.grid.dx)
+        ce, re = extend_edge(c, nb), extend_edge(rho, nb)
+        maps = {"rho": re, "K": ce * ce * re, "kappau": fw2["kappa_u"], "kappax": fw2["kappa_x"]}
+        for nu in (1, 2):
+            for ax in ("u", "x"):
+                maps[f"apml{ax}{nu}"] = fw2[f"a_pml_{ax}{nu}"]
+                maps[f"bpml{ax}{nu}"] = fw2[f"b_pml_{ax}{nu}"]
+        cref = extend_edge(self.c_ref if self.c_ref is not None else c.detach(), nb).detach()
+        cmin, cmax = float(cref.min()), float(cref.max())
+        dmap = coefficients.d_map(np.array([cmin, cmax]), self.grid.dt, self.grid.dx, is_3d=False)
+        dcmap = (torch.round(cref + 1e-9) - round(cmin + 1e-9)).to(torch.int32).contiguous()
+        nx, ny = self.shape
+        sig = _pulse(self.grid, self.p0)
+        cols = np.arange(ny)
+        icc = np.stack([np.full(ny, self.source_row), cols], axis=1) + nb
+        scols = cols[::self.sensor_step]
+        outc = np.stack([np.full(scols.size, self.sensor_row), scols], axis=1) + nb
+        dev = c.device
+        i32 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.int32), device=dev)  # noqa: E731
+        fmaps = {k: v.detach().to(torch.float32).contiguous() for k, v in maps.items()}
+        fmaps["c"] = ce.detach().to(torch.float32).contiguous()
+        fmaps["beta"] = torch.zeros_like(fmaps["rho"])
+        d = DeviceInputs(shape=(nx + 2 * nb, ny + 2 * nb), nt=self.grid.nt,
+                         spacing=(self.grid.dx, self.grid.dy), dt=self.grid.dt, c0=self.grid.c0,
+                         mod_t=1, d=coefficients.d_matrix(self.grid.cfl, is_3d=False), dmap=dmap,
+                         dcmap=dcmap, maps=fmaps, icc=i32(icc),
+                         icmat=torch.as_tensor(np.tile(sig, (ny, 1)), device=dev),
+                         outc=i32(outc), icczero=i32(np.zeros((0, 2))))
+        d.diff_maps = maps
+        return d
+
+    def misfit(self, c, rho, a0, gam, observed, checkpoint_every: int = 200):
+        """J as a differentiable torch scalar of c, rho, a0."""
+        d = self.build(c, rho, a0, gam)
+        return FdtdMisfit.apply(d, observed, checkpoint_every,
+                                *[d.diff_maps[k] for k in RAW_MAPS])
+
+
+def _pulse(grid, p0):
+    from .pulse import gaussian_modulated_sinusoidal_signal  # noqa: PLC0415
+
+    return gaussian_modulated_sinusoidal_signal(nt=grid.nt, duration=grid.duration, ncycles=2,
+                                                drop_off=2, f0=grid.f0, p0=p0).astype(np.float32)

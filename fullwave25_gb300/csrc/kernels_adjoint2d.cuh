@@ -1,0 +1,224 @@
+// Discrete adjoint of the 2D time step (beta = 0), for gradients of the sensor-trace misfit
+// J = 1/2 sum_n || p^{n+1}[outc] - d_n ||^2 with respect to the engine's coefficient maps.
+//
+// Reverse of step n uses the stored forward states S_n (before the step) and S_{n+1} (after):
+//   assemble  lam_p += sum_a D_a^T lam_g_a                      (from step n+1's velocity adjoint)
+//   io        lam_p[outc] += r_n ; lam_p[icczero] = 0 ; lam_p[icc] = 0 (n < nTic)
+//   pressure  d_a = D'_a v^{n+1/2};  L_nu = lam_phi_nu - k lam_p;
+//             lam_d_a = sum_nu ax_nu L_nu - k ikx lam_p;  lam_phi_nu = bx_nu L_nu
+//   velocity  lam_v_a += D'_a^T lam_d_a;  g_a = D_a p^n;  M_nu = lam_psi_nu - r lam_v_a;
+//             lam_g_a = sum_nu au_nu M_nu - r iku lam_v_a;  lam_psi_nu = bu_nu M_nu
+// Gradient contributions are summed over time in FP64, one array per coefficient map.
+// The transposes D^T are gathers: output cell q collects the terms of every body cell c whose
+// stencil touches q, each weighted by c's own taps.
+#pragma once
+#include "engine_common.cuh"
+
+namespace fwgb {
+
+enum AdjGrad {
+  kGRdtRho = 0, kGDtK, kGInvKu, kGInvKx, kGAu1, kGBu1, kGAu2, kGBu2, kGAx1, kGBx1, kGAx2, kGBx2,
+  kNumGrad
+};
+
+struct AdjArgs {
+  Grid g;
+  Maps m;
+  const float* Sn;      // stored state before step n: 11 padded fields (state order)
+  const float* Sn1;     // stored state after step n
+  int64_t fs;           // field stride (padded cells)
+  float* lam_p;
+  float* lam_v[2];
+  float* lam_psi[2][2];
+  float* lam_phi[2][2];
+  float* lam_d[2];
+  float* lam_g[2];
+  double* grad[kNumGrad];
+};
+
+// state field indices (2D): p, vx, vy, psi[a][nu] = 3 + 2a + nu, phi[a][nu] = 7 + 2a + nu
+__device__ __forceinline__ const float* S_p(const float* S, int64_t) { return S; }
+__device__ __forceinline__ const float* S_v(const float* S, int64_t fs, int a) { return S + (1 + a) * fs; }
+__device__ __forceinline__ const float* S_psi(const float* S, int64_t fs, int a, int nu) {
+  return S + (3 + 2 * a + nu) * fs;
+}
+__device__ __forceinline__ const float* S_phi(const float* S, int64_t fs, int a, int nu) {
+  return S + (7 + 2 * a + nu) * fs;
+}
+
+__device__ __forceinline__ float tap_of(const Maps& m, int64_t c, int idx) {
+  return __ldg(m.taps + (size_t)__ldg(m.dcmap + c) * kTapStride + idx);
+}
+
+// D_a f at c (the velocity-kernel stencil), same operation order as the forward kernels
+__device__ __forceinline__ float grad_at(const Maps& m, const float* f, int64_t c, int64_t se,
+                                         int64_t sf, float inv_h) {
+  float cm[8], co;
+  load_taps(m.taps, __ldg(m.dcmap + c), cm, co);
+  float g = 0.f;
+#pragma unroll
+  for (int k = 1; k <= 8; ++k) g = fmaf(cm[k - 1], __ldg(f + c + k * se) - __ldg(f + c - (k - 1) * se), g);
+  g = fmaf(co, (__ldg(f + c + se + sf) - __ldg(f + c + sf)) + (__ldg(f + c + se - sf) - __ldg(f + c - sf)), g);
+  return g * inv_h;
+}
+
+// D'_a v at c (the pressure-kernel stencil)
+__device__ __forceinline__ float div_at(const Maps& m, const float* v, int64_t c, int64_t se,
+                                        int64_t sf, float inv_h) {
+  float cm[8], co;
+  load_taps(m.taps, __ldg(m.dcmap + c), cm, co);
+  float d = 0.f;
+#pragma unroll
+  for (int k = 1; k <= 8; ++k) d = fmaf(cm[k - 1], __ldg(v + c + (k - 1) * se) - __ldg(v + c - k * se), d);
+  d = fmaf(co, (__ldg(v + c + sf) - __ldg(v + c - se + sf)) + (__ldg(v + c - sf) - __ldg(v + c - se - sf)), d);
+  return d * inv_h;
+}
+
+// (D_a^T u)(q): u is zero outside the body
+__device__ __forceinline__ float grad_T_at(const Maps& m, const float* u, int64_t q, int64_t se,
+                                           int64_t sf, float inv_h) {
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 1; k <= 8; ++k) {
+    const int64_t c1 = q - k * se, c2 = q + (k - 1) * se;
+    acc += tap_of(m, c1, k - 1) * __ldg(u + c1) - tap_of(m, c2, k - 1) * __ldg(u + c2);
+  }
+#pragma unroll
+  for (int s = -1; s <= 1; s += 2) {
+    const int64_t c1 = q - se - s * sf, c2 = q - s * sf;
+    acc += tap_of(m, c1, 8) * __ldg(u + c1) - tap_of(m, c2, 8) * __ldg(u + c2);
+  }
+  return acc * inv_h;
+}
+
+// (D'_a^T u)(q)
+__device__ __forceinline__ float div_T_at(const Maps& m, const float* u, int64_t q, int64_t se,
+                                          int64_t sf, float inv_h) {
+  float acc = 0.f;
+#pragma unroll
+  for (int k = 1; k <= 8; ++k) {
+    const int64_t c1 = q - (k - 1) * se, c2 = q + k * se;
+    acc += tap_of(m, c1, k - 1) * __ldg(u + c1) - tap_of(m, c2, k - 1) * __ldg(u + c2);
+  }
+#pragma unroll
+  for (int s = -1; s <= 1; s += 2) {
+    const int64_t c1 = q - s * sf, c2 = q + se - s * sf;
+    acc += tap_of(m, c1, 8) * __ldg(u + c1) - tap_of(m, c2, 8) * __ldg(u + c2);
+  }
+  return acc * inv_h;
+}
+
+__device__ __forceinline__ bool adj_cell(const Grid& g, int64_t* c) {
+  const int j = kGhost + blockIdx.x * blockDim.x + threadIdx.x;
+  const int i = kGhost + blockIdx.y * blockDim.y + threadIdx.y;
+  if (i >= g.nx - kGhost || j >= g.ny - kGhost) return false;
+  *c = (int64_t)i * g.sx + j;
+  return true;
+}
+
+// lam_p += sum_a D_a^T lam_g_a
+__global__ void __launch_bounds__(256) adj2d_assemble(const AdjArgs A) {
+  int64_t q;
+  if (!adj_cell(A.g, &q)) return;
+  const float add = grad_T_at(A.m, A.lam_g[0], q, A.g.sx, 1, A.g.inv_h[0]) +
+                    grad_T_at(A.m, A.lam_g[1], q, 1, A.g.sx, A.g.inv_h[1]);
+  A.lam_p[q] += add;
+}
+
+// record adjoint and projections for step n
+__global__ void adj2d_io(const AdjArgs A, const Lists L, const float* residual, int n,
+                         int n_src, int n_zero, int n_rec) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;
+  if (n % L.mod_t == 0) {
+    const float* row = residual + (size_t)(n / L.mod_t) * L.ncoordsout;
+    for (int e = t; e < n_rec; e += stride) atomicAdd(A.lam_p + L.rec_cell[e], row[L.rec_k[e]]);
+  }
+}
+
+__global__ void adj2d_zero(const AdjArgs A, const Lists L, int n, int n_src, int n_zero) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int stride = gridDim.x * blockDim.x;
+  for (int e = t; e < n_zero; e += stride) A.lam_p[L.zero_cell[e]] = 0.f;
+  if (n < L.nt_ic)
+    for (int e = t; e < n_src; e += stride) A.lam_p[L.src_cell[e]] = 0.f;
+}
+
+__global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
+  int64_t c;
+  if (!adj_cell(A.g, &c)) return;
+  const Grid& g = A.g;
+  const int64_t fs = A.fs;
+  const float lp = A.lam_p[c];
+  const float k = __ldg(A.m.dt_k + c), ikx = __ldg(A.m.inv_kx + c);
+  const float ax[2] = {__ldg(A.m.ax[0] + c), __ldg(A.m.ax[1] + c)};
+  const float bx[2] = {__ldg(A.m.bx[0] + c), __ldg(A.m.bx[1] + c)};
+  double g_dtk = 0.0, g_ikx = 0.0, g_ax[2] = {0.0, 0.0}, g_bx[2] = {0.0, 0.0};
+  float div = 0.f;
+  const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    const float d = div_at(A.m, S_v(A.Sn1, fs, a), c, se[a], sf[a], g.inv_h[a]);
+    const float n1 = __ldg(S_phi(A.Sn1, fs, a, 0) + c), n2 = __ldg(S_phi(A.Sn1, fs, a, 1) + c);
+    div += fmaf(d, ikx, n1) + n2;
+    float lam_d = -k * ikx * lp;
+#pragma unroll
+    for (int nu = 0; nu < 2; ++nu) {
+      const float L = A.lam_phi[a][nu][c] - k * lp;
+      lam_d = fmaf(ax[nu], L, lam_d);
+      g_ax[nu] += (double)L * d;
+      g_bx[nu] += (double)L * __ldg(S_phi(A.Sn, fs, a, nu) + c);
+      A.lam_phi[a][nu][c] = bx[nu] * L;
+    }
+    g_ikx -= (double)k * lp * d;
+    A.lam_d[a][c] = lam_d;
+  }
+  g_dtk -= (double)div * lp;
+  A.grad[kGDtK][c] += g_dtk;
+  A.grad[kGInvKx][c] += g_ikx;
+  A.grad[kGAx1][c] += g_ax[0];
+  A.grad[kGAx2][c] += g_ax[1];
+  A.grad[kGBx1][c] += g_bx[0];
+  A.grad[kGBx2][c] += g_bx[1];
+}
+
+__global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
+  int64_t c;
+  if (!adj_cell(A.g, &c)) return;
+  const Grid& g = A.g;
+  const int64_t fs = A.fs;
+  const float r = __ldg(A.m.rdt_rho + c), iku = __ldg(A.m.inv_ku + c);
+  const float au[2] = {__ldg(A.m.au[0] + c), __ldg(A.m.au[1] + c)};
+  const float bu[2] = {__ldg(A.m.bu[0] + c), __ldg(A.m.bu[1] + c)};
+  double g_r = 0.0, g_iku = 0.0, g_au[2] = {0.0, 0.0}, g_bu[2] = {0.0, 0.0};
+  const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    const float lv = A.lam_v[a][c] + div_T_at(A.m, A.lam_d[a], c, se[a], sf[a], g.inv_h[a]);
+    const float gr = grad_at(A.m, S_p(A.Sn, fs), c, se[a], sf[a], g.inv_h[a]);
+    const float p1 = __ldg(S_psi(A.Sn1, fs, a, 0) + c), p2 = __ldg(S_psi(A.Sn1, fs, a, 1) + c);
+    float lam_g = -r * iku * lv;
+#pragma unroll
+    for (int nu = 0; nu < 2; ++nu) {
+      const float M = A.lam_psi[a][nu][c] - r * lv;
+      lam_g = fmaf(au[nu], M, lam_g);
+      g_au[nu] += (double)M * gr;
+      g_bu[nu] += (double)M * __ldg(S_psi(A.Sn, fs, a, nu) + c);
+      A.lam_psi[a][nu][c] = bu[nu] * M;
+    }
+    g_r -= (double)lv * (fmaf(gr, iku, p1) + p2);
+    g_iku -= (double)r * gr * lv;
+    A.lam_v[a][c] = lv;
+    A.lam_g[a][c] = lam_g;
+  }
+  A.grad[kGRdtRho][c] += g_r;
+  A.grad[kGInvKu][c] += g_iku;
+  A.grad[kGAu1][c] += g_au[0];
+  A.grad[kGAu2][c] += g_au[1];
+  A.grad[kGBu1][c] += g_bu[0];
+  A.grad[kGBu2][c] += g_bu[1];
+}
+
+__global__ void set_step_counter(int* step, int value) { *step = value; }
+
+}  // namespace fwgb

@@ -23,7 +23,7 @@ EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_source_signa
             "fw_set_source_columns", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
             "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_launches_per_step",
-            "fw_destroy", "fw_group_create", "fw_group_run", "fw_group_set_members",
+            "fw_destroy", "fw_adjoint_forward", "fw_adjoint_backward", "fw_group_create", "fw_group_run", "fw_group_set_members",
             "fw_group_advance", "fw_group_destroy",
             "fw_run_noalloc", "fw_last_error")
 
@@ -48,6 +48,11 @@ class FwFields(C.Structure):
                 ("apmlu2", _FP), ("bpmlu2", _FP), ("apmlx2", _FP), ("bpmlx2", _FP),
                 ("icc", _IP), ("outc", _IP), ("icczero", _IP), ("icmat", _FP),
                 ("on_device", C.c_int32)]
+
+
+# order of the gradient arrays returned by fw_adjoint_backward
+ADJOINT_MAPS = ("rdt_rho", "dt_k", "inv_ku", "inv_kx", "au1", "bu1", "au2", "bu2",
+                "ax1", "bx1", "ax2", "bx2")
 
 
 class EngineError(RuntimeError):
@@ -90,6 +95,8 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_kernel_variant": (C.c_int, [H, _IP]),
         "fw_launches_per_step": (C.c_int, [H, _IP]),
         "fw_destroy": (C.c_int, [H]),
+        "fw_adjoint_forward": (C.c_int, [H, vp, C.c_int32]),
+        "fw_adjoint_backward": (C.c_int, [H, vp, _FP, C.POINTER(C.c_double)]),
         "fw_group_create": (C.c_int, [C.POINTER(C.c_void_p), C.c_int32, C.POINTER(C.c_void_p)]),
         "fw_group_run": (C.c_int, [C.c_void_p, vp]),
         "fw_group_set_members": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32]),
@@ -264,6 +271,16 @@ class Engine:
         out = np.empty(self.inputs.shape, dtype=np.float32)
         self._call("fw_get_field", C.c_void_p(stream or 0), int(field), _fp(out), 0)
         return out
+
+    def adjoint_forward(self, checkpoint_every: int, stream: int | None = None) -> None:
+        self._call("fw_adjoint_forward", C.c_void_p(stream or 0), int(checkpoint_every))
+
+    def adjoint_backward(self, residual_ptr: int, grad_ptr: int, stream: int | None = None) -> None:
+        """``residual_ptr``: device float32 [n_out, ncoordsout]; ``grad_ptr``: device float64
+        [12, nx, ny] (order of ``ADJOINT_MAPS``)."""
+        self._call("fw_adjoint_backward", C.c_void_p(stream or 0),
+                   C.cast(C.c_void_p(residual_ptr), _FP),
+                   C.cast(C.c_void_p(grad_ptr), C.POINTER(C.c_double)))
 
     @property
     def current_step(self) -> int:

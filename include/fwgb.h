@@ -144,6 +144,22 @@ FWGB_API int fw_launches_per_step(const fw_handle *h, int32_t *n);
 /* Release all device memory of the handle. */
 FWGB_API int fw_destroy(fw_handle *h);
 
+/* Gradient of the sensor-trace misfit J = 1/2 sum ||traces - observed||^2 (2D, beta = 0), with
+ * respect to the engine's coefficient maps, by the discrete adjoint of the time step. No
+ * counterpart in the reference (it has no gradient computation).
+ * fw_adjoint_forward: run the full forward solve from rest, keeping a checkpoint of the wavefield
+ * every `checkpoint_every` steps (device memory: nt / checkpoint_every + checkpoint_every + 1
+ * wavefield copies); the traces are then available from fw_read_traces. */
+FWGB_API int fw_adjoint_forward(fw_handle *h, void *stream, int32_t checkpoint_every);
+
+/* Reverse pass: recompute each segment from its checkpoint and run the adjoint step backwards,
+ * accumulating the gradient in FP64. `residual` = traces - observed, device float32
+ * [n_out][ncoordsout]. `grad_out`: device FP64 [12][nx][ny] in the order dt/rho, dt*K, 1/kappau,
+ * 1/kappax, au1, bu1, au2, bu2, ax1, bx1, ax2, bx2 (ghost cells zero). The wavefield left in the
+ * handle afterwards is the first segment's recomputation. */
+FWGB_API int fw_adjoint_backward(fw_handle *h, void *stream, const float *residual,
+                                 double *grad_out);
+
 /* A group runs many independent 2D simulations together: every time step is one velocity
  * launch and one pressure launch over a device work list of (simulation, tile) pairs, so small
  * simulations share the GPU instead of each leaving it mostly idle; blocks of 64 steps are

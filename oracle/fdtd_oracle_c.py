@@ -96,14 +96,16 @@ class OracleC:
         if not self.h:
             raise MemoryError("oracle_create failed")
         self.steps = 0
+        self.traces = np.zeros((inp.n_out, inp.outc.shape[0]))
 
     def run(self, n_steps=None):
-        n_steps = self.inp.nt if n_steps is None else n_steps
-        n_out = (self.steps + n_steps + self.inp.mod_t - 1) // self.inp.mod_t
-        out = np.zeros((n_out, self.inp.outc.shape[0]))
-        self.lib.oracle_run(self.h, int(n_steps), out.ctypes.data_as(_DP))
+        """Advance ``n_steps`` (default: to nT); returns the traces recorded so far."""
+        n_steps = self.inp.nt - self.steps if n_steps is None else n_steps
+        if self.steps + n_steps > self.inp.nt:
+            raise ValueError("cannot step past nT")
+        self.lib.oracle_run(self.h, int(n_steps), self.traces.ctypes.data_as(_DP))
         self.steps += n_steps
-        return out
+        return self.traces[: (self.steps + self.inp.mod_t - 1) // self.inp.mod_t].copy()
 
     def close(self):
         if self.h:

@@ -1,0 +1,65 @@
+"""The FP64 NumPy adjoint against central finite differences of the FP64 oracle."""
+
+import numpy as np
+import pytest
+
+from fdtd_adjoint import GRAD_KEYS, AdjointOracle, misfit, misfit_and_gradient
+from fdtd_oracle import GHOST, Oracle
+from golden_io import load_case_inputs
+
+
+def _small(name, nt):
+    inp = load_case_inputs(name)
+    inp.nt = nt
+    inp.icmat = np.ascontiguousarray(inp.icmat[:, :nt])
+    return inp
+
+
+@pytest.fixture(scope="module")
+def case():
+    inp = _small("2d_small", 70)
+    # observed data: the same experiment with a slightly different medium
+    obs_inp = _small("2d_small", 70)
+    obs_inp.maps = dict(obs_inp.maps)
+    obs_inp.maps["K"] = (obs_inp.maps["K"] * np.float32(1.02)).astype(np.float32)
+    observed = Oracle(obs_inp).run()
+    J, G, traces = misfit_and_gradient(inp, observed)
+    return inp, observed, J, G
+
+
+def _base_map(o, key):
+    return {"rdt_rho": o.rdt_rho, "dt_k": o.dt_k, "inv_ku": o.inv_kappa_u,
+            "inv_kx": o.inv_kappa_x}.get(key) if key in ("rdt_rho", "dt_k", "inv_ku", "inv_kx") \
+        else getattr(o, key[:2])[int(key[2]) - 1]
+
+
+@pytest.mark.parametrize("key", GRAD_KEYS)
+def test_gradient_matches_central_differences(case, key):
+    inp, observed, J, G = case
+    o = Oracle(inp)
+    base = _base_map(o, key)
+    rng = np.random.default_rng(sum(map(ord, key)))
+    # cells near the source/sensor rows and in the medium interior
+    cells = [(int(rng.integers(2, base.shape[0] - 2)), int(rng.integers(2, base.shape[1] - 2)))
+             for _ in range(3)]
+    for c in cells:
+        mag = abs(base[c]) if base[c] != 0 else float(np.abs(base).mean())
+        h = 1e-4 * mag
+        plus, minus = base.copy(), base.copy()
+        plus[c] += h
+        minus[c] -= h
+        fd = (misfit(inp, observed, {key: plus}) - misfit(inp, observed, {key: minus})) / (2 * h)
+        ad = G[key][c]
+        # central differences of an FP64 quadratic: agreement to ~1e-6 relative, with an
+        # absolute floor for cells the traces barely depend on
+        floor = 1e-10 * abs(J) / mag
+        assert abs(fd - ad) <= 1e-5 * max(abs(fd), abs(ad)) + floor, \
+            f"{key} at {c}: adjoint {ad:.6e} vs finite difference {fd:.6e}"
+
+
+def test_gradient_is_nonzero_and_finite(case):
+    inp, observed, J, G = case
+    assert J > 0
+    for k in GRAD_KEYS:
+        assert np.isfinite(G[k]).all()
+    assert np.abs(G["dt_k"]).max() > 0 and np.abs(G["rdt_rho"]).max() > 0

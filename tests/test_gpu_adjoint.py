@@ -1,0 +1,125 @@
+"""GPU adjoint (FP32 wavefields, FP64 gradient accumulation) against the FP64 NumPy adjoint and
+against central finite differences of the FP64 oracle.
+
+Tolerances: engine-map gradients within 1e-3 relative L2 of the FP64 adjoint; physical-map
+gradients (c, rho, alpha0) within 2e-2 of central differences (h = 1e-3 relative, tap sets
+held fixed) at 16 random cells, relative to the larger of the two values plus 1e-3 of the
+field's largest gradient.
+"""
+
+import numpy as np
+import pytest
+
+from fdtd_adjoint import GRAD_KEYS, misfit_and_gradient
+from fdtd_oracle import GHOST, Oracle
+from golden_io import load_case_inputs
+
+pytestmark = pytest.mark.gpu
+
+
+def _small(name, nt):
+    inp = load_case_inputs(name)
+    inp.nt = nt
+    inp.icmat = np.ascontiguousarray(inp.icmat[:, :nt])
+    return inp
+
+
+@pytest.mark.parametrize("name,nt,every", [("2d_small", 90, 25), ("2d_nopml", 75, 75)])
+def test_engine_map_gradients_match_fp64_adjoint(engine_lib, cuda, name, nt, every):
+    torch = cuda
+    from fullwave25_gb300.engine import ADJOINT_MAPS, Engine
+
+    inp = _small(name, nt)
+    obs_inp = _small(name, nt)
+    obs_inp.maps = dict(obs_inp.maps)
+    obs_inp.maps["K"] = (obs_inp.maps["K"] * np.float32(1.02)).astype(np.float32)
+    observed = Oracle(obs_inp).run()
+    J, G, traces64 = misfit_and_gradient(inp, observed)
+    with Engine(inp) as eng:
+        eng.adjoint_forward(every)
+        traces = eng.read_traces()
+        res = torch.as_tensor((traces - observed.astype(np.float32)), device="cuda").contiguous()
+        g = torch.zeros((12,) + inp.shape, dtype=torch.float64, device="cuda")
+        eng.adjoint_backward(res.data_ptr(), g.data_ptr())
+        torch.cuda.synchronize()
+    g = g.cpu().numpy()
+    body = tuple(slice(GHOST, n - GHOST) for n in inp.shape)
+    for i, key in enumerate(ADJOINT_MAPS):
+        ref = G[key]
+        got = g[i][body]
+        err = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+        assert err < 1e-3, f"{name} {key}: rel-L2 {err:.3e}"
+        outside = g[i].copy()
+        outside[body] = 0
+        assert not outside.any()
+
+
+@pytest.fixture(scope="module")
+def problem(cuda):
+    torch = cuda
+    from fullwave25_gb300.adjoint import AdjointProblem
+    from fullwave25_gb300.workloads import ellipse_medium_2d
+
+    shape = (72, 64)
+    c, rho, a0, gam = ellipse_medium_2d(shape, 1540 / 3e6 / 12, seed=11, n_ellipses=4)
+    dev = torch.device("cuda")
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=dev)  # noqa: E731
+    true = (t(c), t(rho), t(a0), t(gam))
+    start = (t(np.full(shape, 1540.0)), t(np.full(shape, 1000.0)), t(np.full(shape, 0.5)), true[3])
+    prob = AdjointProblem(shape, nt=420, n_pml=12, n_transition=12, c_ref=start[0],
+                          device=dev, sensor_row=40)
+    from fullwave25_gb300.engine import Engine
+
+    with Engine(prob.build(*true), validate=False) as e:
+        observed = torch.as_tensor(e.run(), device=dev)
+    return prob, start, observed
+
+
+def test_physical_gradients_match_finite_differences(engine_lib, cuda, problem):
+    torch = cuda
+    from fdtd_oracle_c import run_oracle_c
+    from fullwave25_gb300.workloads3d import to_host_inputs
+
+    prob, start, observed = problem
+    c, rho, a0, gam = [x.clone().requires_grad_(i < 3) for i, x in enumerate(start)]
+    J = prob.misfit(c, rho, a0, gam, observed, checkpoint_every=100)
+    J.backward()
+    grads = {"c": c.grad, "rho": rho.grad, "a0": a0.grad}
+    obs = observed.cpu().numpy().astype(np.float64)
+
+    def J64(cc, rr, aa):
+        h = to_host_inputs(prob.build(cc, rr, aa, start[3]))
+        tr = run_oracle_c(h)
+        return 0.5 * float(np.sum((tr - obs) ** 2))
+
+    rng = np.random.default_rng(3)
+    nx, ny = prob.shape
+    cells = [(int(rng.integers(0, nx)), int(rng.integers(0, ny))) for _ in range(16)]
+    checked = 0
+    for name, base in (("c", start[0]), ("rho", start[1]), ("a0", start[2])):
+        gmax = float(grads[name].abs().max())
+        for cell in (cells if name == "c" else cells[:4]):
+            h = 1e-3 * abs(float(base[cell]))
+            args = [start[0], start[1], start[2]]
+            k = ("c", "rho", "a0").index(name)
+            plus = [a.clone() for a in args]
+            minus = [a.clone() for a in args]
+            plus[k][cell] += h
+            minus[k][cell] -= h
+            fd = (J64(*plus) - J64(*minus)) / (2 * h)
+            ad = float(grads[name][cell])
+            assert abs(fd - ad) <= 2e-2 * max(abs(fd), abs(ad)) + 1e-3 * gmax, \
+                f"d J / d {name} at {cell}: adjoint {ad:.6e}, finite difference {fd:.6e}"
+            checked += 1
+    assert checked == 24
+
+
+def test_adjoint_rejects_3d_and_beta(engine_lib, cuda):
+    from fullwave25_gb300.engine import Engine, EngineError
+
+    with Engine(load_case_inputs("3d_small")) as e:
+        with pytest.raises(EngineError, match="FW_ERR_UNSUPPORTED"):
+            e.adjoint_forward(10)
+    with Engine(load_case_inputs("2d_air_beta")) as e:
+        with pytest.raises(EngineError, match="FW_ERR_UNSUPPORTED"):
+            e.adjoint_forward(10)
