@@ -19,6 +19,8 @@ stand-in lookup table), so alpha0 has a gradient; the relaxation rates depend on
 
 from __future__ import annotations
 
+import dataclasses
+
 import numpy as np
 
 from . import coefficients
@@ -82,10 +84,10 @@ class FdtdMisfit:
         class _Fn(torch.autograd.Function):
             @staticmethod
             def forward(ctx, *tensors):
-                inp = DeviceInputs(**{**template.__dict__, "maps": {
+                inp = dataclasses.replace(template, maps={
                     **template.maps,
                     **{k: t.detach().to(torch.float32).contiguous()
-                       for k, t in zip(RAW_MAPS, tensors)}}})
+                       for k, t in zip(RAW_MAPS, tensors)}})
                 with Engine(inp, validate=False) as eng:
                     J, traces, grads = map_gradients(eng, observed, checkpoint_every)
                 ctx.grads = [grads[k] for k in RAW_MAPS]

@@ -65,6 +65,7 @@ struct fw_handle {
   void* lists = nullptr;       // one allocation for all per-tile lists
   size_t bytes = 0;
   bool has_beta = false, fields_set = false;
+  bool aniso = false;          // per-axis relaxation maps (the anisotropic engine)
   int n_out = 0;
   int32_t host_step = 0;
   Tiling tiling{};
@@ -106,8 +107,12 @@ int fail(fw_handle* h, int code, const char* fmt, ...) {
 int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
 int n_state(int ndim) { return 1 + ndim + 4 * ndim; }
-// maps: rdt_rho, dt_k, beta2dt, inv_ku, inv_kx, au1 bu1 au2 bu2 ax1 bx1 ax2 bx2
+// maps: rdt_rho, dt_k, beta2dt, inv_ku, inv_kx, au1 bu1 au2 bu2 ax1 bx1 ax2 bx2 (x axis, or every
+// axis in the isotropic engine), then for the anisotropic engine per further axis a >= 1:
+// inv_ku, au1 bu1 au2 bu2, inv_kx, ax1 bx1 ax2 bx2 at 13 + 10 (a - 1) + k
 constexpr int kMaps = 13;
+int n_maps(const fw_handle* h) { return kMaps + (h->aniso ? 10 * (h->ndim - 1) : 0); }
+int axis_map(int a, int k) { return kMaps + 10 * (a - 1) + k; }
 
 Tiling make_tiling(const fw_handle* h) {
   Tiling t{};
@@ -145,16 +150,21 @@ int64_t padded_index(const fw_handle* h, int64_t i, int64_t j, int64_t k) {
 }
 
 __global__ void transform_maps(float* rho_to_rdt, float* k_to_dtk, float* beta_to_2dt,
-                               float* inv_ku, float* inv_kx, int64_t n, float dt) {
+                               int64_t n, float dt) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
        c += (int64_t)gridDim.x * blockDim.x) {
     const float r = rho_to_rdt[c];
     rho_to_rdt[c] = r != 0.f ? dt / r : 0.f;
     k_to_dtk[c] = dt * k_to_dtk[c];
     beta_to_2dt[c] = 2.f * dt * beta_to_2dt[c];
-    const float ku = inv_ku[c], kx = inv_kx[c];
-    inv_ku[c] = ku != 0.f ? 1.f / ku : 0.f;
-    inv_kx[c] = kx != 0.f ? 1.f / kx : 0.f;
+  }
+}
+
+__global__ void invert_map(float* kappa_to_inv, int64_t n) {
+  for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
+       c += (int64_t)gridDim.x * blockDim.x) {
+    const float k = kappa_to_inv[c];
+    kappa_to_inv[c] = k != 0.f ? 1.f / k : 0.f;
   }
 }
 
@@ -196,23 +206,40 @@ void launch_step(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
   if (h->ndim == 3 && h->variant == kMarch) {
     dim3 grid(t.n[2], t.n[1], t.n[0]), block(kMTZ, kMTY);
-    vel3d_march<kMarchXC><<<grid, block, 0, s>>>(h->args, h->tmaps.p);
-    if (h->has_beta)
-      prs3d_march<kMarchXC, true><<<grid, block, 0, s>>>(h->args, h->tmaps.vx, h->tmaps.vy, h->tmaps.vz);
-    else
-      prs3d_march<kMarchXC, false><<<grid, block, 0, s>>>(h->args, h->tmaps.vx, h->tmaps.vy, h->tmaps.vz);
+    const MarchMaps& tm = h->tmaps;
+    if (h->aniso) {
+      vel3d_march<kMarchXC, true><<<grid, block, 0, s>>>(h->args, tm.p);
+      if (h->has_beta) prs3d_march<kMarchXC, true, true><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
+      else prs3d_march<kMarchXC, false, true><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
+    } else {
+      vel3d_march<kMarchXC, false><<<grid, block, 0, s>>>(h->args, tm.p);
+      if (h->has_beta) prs3d_march<kMarchXC, true, false><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
+      else prs3d_march<kMarchXC, false, false><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
+    }
     return;
   }
   if (h->ndim == 2) {
     dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
-    vel2d_direct<<<grid, block, 0, s>>>(h->args);
-    if (h->has_beta) prs2d_direct<true><<<grid, block, 0, s>>>(h->args);
-    else prs2d_direct<false><<<grid, block, 0, s>>>(h->args);
+    if (h->aniso) {
+      vel2d_direct<true><<<grid, block, 0, s>>>(h->args);
+      if (h->has_beta) prs2d_direct<true, true><<<grid, block, 0, s>>>(h->args);
+      else prs2d_direct<false, true><<<grid, block, 0, s>>>(h->args);
+    } else {
+      vel2d_direct<false><<<grid, block, 0, s>>>(h->args);
+      if (h->has_beta) prs2d_direct<true, false><<<grid, block, 0, s>>>(h->args);
+      else prs2d_direct<false, false><<<grid, block, 0, s>>>(h->args);
+    }
   } else {
     dim3 grid(t.n[2], t.n[1], t.n[0]), block(kD3TZ, kD3TY, kD3TX);
-    vel3d_direct<<<grid, block, 0, s>>>(h->args);
-    if (h->has_beta) prs3d_direct<true><<<grid, block, 0, s>>>(h->args);
-    else prs3d_direct<false><<<grid, block, 0, s>>>(h->args);
+    if (h->aniso) {
+      vel3d_direct<true><<<grid, block, 0, s>>>(h->args);
+      if (h->has_beta) prs3d_direct<true, true><<<grid, block, 0, s>>>(h->args);
+      else prs3d_direct<false, true><<<grid, block, 0, s>>>(h->args);
+    } else {
+      vel3d_direct<false><<<grid, block, 0, s>>>(h->args);
+      if (h->has_beta) prs3d_direct<true, false><<<grid, block, 0, s>>>(h->args);
+      else prs3d_direct<false, false><<<grid, block, 0, s>>>(h->args);
+    }
   }
 }
 
@@ -282,8 +309,8 @@ int check_desc(const fw_desc* d) {
     return fail(nullptr, FW_ERR_ARGUMENT, "negative count or modT/ndmap < 1");
   if (!(d->dt > 0.f) || !(d->dx > 0.f) || !(d->dy > 0.f) || (d->ndim == 3 && !(d->dz > 0.f)))
     return fail(nullptr, FW_ERR_ARGUMENT, "grid spacing and time step must be positive");
-  if (d->isotropic != 1)
-    return fail(nullptr, FW_ERR_UNSUPPORTED, "only the isotropic relaxation engine is implemented");
+  if (d->isotropic != 0 && d->isotropic != 1)
+    return fail(nullptr, FW_ERR_ARGUMENT, "isotropic must be 0 or 1 (got %d)", d->isotropic);
   if (d->n_relax != 2)
     return fail(nullptr, FW_ERR_UNSUPPORTED, "only n_relax = 2 is implemented (got %d)", d->n_relax);
   return FW_OK;
@@ -307,6 +334,7 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   h->nx = desc->nx;
   h->ny = desc->ny;
   h->nz = desc->ndim == 3 ? desc->nz : 1;
+  h->aniso = desc->isotropic == 0;
   h->pitch = round_up(h->ndim == 2 ? h->ny : h->nz, 32);
   h->ncells_padded = h->ndim == 2 ? h->nx * h->pitch : h->nx * h->ny * h->pitch;
   h->n_out = (desc->nt + desc->mod_t - 1) / desc->mod_t;
@@ -328,7 +356,7 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   };
   const size_t cells = (size_t)h->ncells_padded;
   if ((st = alloc((void**)&h->state, cells * n_state(h->ndim) * sizeof(float))) ||
-      (st = alloc((void**)&h->maps, cells * kMaps * sizeof(float))) ||
+      (st = alloc((void**)&h->maps, cells * n_maps(h) * sizeof(float))) ||
       (st = alloc((void**)&h->dcmap, cells * sizeof(int32_t))) ||
       (st = alloc((void**)&h->taps, (size_t)desc->ndmap * kTapStride * sizeof(float))) ||
       (st = alloc((void**)&h->icmat_t, (size_t)desc->ncoords * desc->nt_ic * sizeof(float))) ||
@@ -343,7 +371,7 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   }
   // zero everything once: ghost cells, padding and memory variables start at zero
   if (cudaMemset(h->state, 0, cells * n_state(h->ndim) * sizeof(float)) != cudaSuccess ||
-      cudaMemset(h->maps, 0, cells * kMaps * sizeof(float)) != cudaSuccess ||
+      cudaMemset(h->maps, 0, cells * n_maps(h) * sizeof(float)) != cudaSuccess ||
       cudaMemset(h->dcmap, 0, cells * sizeof(int32_t)) != cudaSuccess ||
       cudaMemset(h->step, 0, sizeof(int) * 4) != cudaSuccess) {
     fw_destroy(h);
@@ -367,12 +395,19 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   A.m.rdt_rho = map_field(h, 0);
   A.m.dt_k = map_field(h, 1);
   A.m.beta2dt = map_field(h, 2);
-  A.m.inv_ku = map_field(h, 3);
-  A.m.inv_kx = map_field(h, 4);
-  A.m.au[0] = map_field(h, 5); A.m.bu[0] = map_field(h, 6);
-  A.m.au[1] = map_field(h, 7); A.m.bu[1] = map_field(h, 8);
-  A.m.ax[0] = map_field(h, 9); A.m.bx[0] = map_field(h, 10);
-  A.m.ax[1] = map_field(h, 11); A.m.bx[1] = map_field(h, 12);
+  for (int a = 0; a < 3; ++a) {
+    const bool own = h->aniso && a >= 1 && a < h->ndim;
+    A.m.inv_ku[a] = own ? map_field(h, axis_map(a, 0)) : map_field(h, 3);
+    A.m.au[a][0] = own ? map_field(h, axis_map(a, 1)) : map_field(h, 5);
+    A.m.bu[a][0] = own ? map_field(h, axis_map(a, 2)) : map_field(h, 6);
+    A.m.au[a][1] = own ? map_field(h, axis_map(a, 3)) : map_field(h, 7);
+    A.m.bu[a][1] = own ? map_field(h, axis_map(a, 4)) : map_field(h, 8);
+    A.m.inv_kx[a] = own ? map_field(h, axis_map(a, 5)) : map_field(h, 4);
+    A.m.ax[a][0] = own ? map_field(h, axis_map(a, 6)) : map_field(h, 9);
+    A.m.bx[a][0] = own ? map_field(h, axis_map(a, 7)) : map_field(h, 10);
+    A.m.ax[a][1] = own ? map_field(h, axis_map(a, 8)) : map_field(h, 11);
+    A.m.bx[a][1] = own ? map_field(h, axis_map(a, 9)) : map_field(h, 12);
+  }
   A.m.dcmap = h->dcmap;
   A.m.taps = h->taps;
   A.l.icmat_t = h->icmat_t;
@@ -396,9 +431,17 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   return FW_OK;
 }
 
-int fw_set_fields(fw_handle* h, const fw_fields* f) {
+}  // extern "C"
+
+namespace {
+
+int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   if (!f) return fail(h, FW_ERR_ARGUMENT, "fields is NULL");
+  if (h->aniso && !an)
+    return fail(h, FW_ERR_ARGUMENT, "an anisotropic handle (isotropic = 0) needs fw_set_fields_aniso");
+  if (!h->aniso && an)
+    return fail(h, FW_ERR_ARGUMENT, "per-direction maps given to an isotropic handle");
   const fw_desc& d = h->d;
   const float* need[] = {f->d, f->dmap, f->c, f->rho, f->K, f->beta, f->kappax, f->kappau,
                          f->apmlu1, f->bpmlu1, f->apmlx1, f->bpmlx1, f->apmlu2, f->bpmlu2,
@@ -526,9 +569,30 @@ int fw_set_fields(fw_handle* h, const fw_fields* f) {
       {f->apmlx1, 9}, {f->bpmlx1, 10}, {f->apmlx2, 11}, {f->bpmlx2, 12}};
   for (auto& m : mapsrc)
     if ((st = upload_grid(h, map_field(h, m.idx), m.src, sizeof(float), dev, s))) return st;
+  std::vector<int> kappa_maps = {3, 4};
+  if (h->aniso) {
+    // axis y: kappaw/apmlw*/bpmlw* (gradient), kappay/apmly*/bpmly* (divergence); axis z: v, z
+    const float* per_axis[3][10] = {
+        {},
+        {an->kappaw, an->apmlw1, an->bpmlw1, an->apmlw2, an->bpmlw2,
+         an->kappay, an->apmly1, an->bpmly1, an->apmly2, an->bpmly2},
+        {an->kappav, an->apmlv1, an->bpmlv1, an->apmlv2, an->bpmlv2,
+         an->kappaz, an->apmlz1, an->bpmlz1, an->apmlz2, an->bpmlz2}};
+    for (int a = 1; a < h->ndim; ++a)
+      for (int k = 0; k < 10; ++k) {
+        if (!per_axis[a][k]) return fail(h, FW_ERR_ARGUMENT, "a per-direction map for axis %d is NULL", a);
+        if ((st = upload_grid(h, map_field(h, axis_map(a, k)), per_axis[a][k], sizeof(float), dev, s)))
+          return st;
+      }
+    for (int a = 1; a < h->ndim; ++a) {
+      kappa_maps.push_back(axis_map(a, 0));
+      kappa_maps.push_back(axis_map(a, 5));
+    }
+  }
   if ((st = upload_grid(h, h->dcmap, dcm.data(), sizeof(int32_t), false, s))) return st;
   transform_maps<<<1024, 256, 0, s>>>(map_field(h, 0), map_field(h, 1), map_field(h, 2),
-                                      map_field(h, 3), map_field(h, 4), h->ncells_padded, d.dt);
+                                      h->ncells_padded, d.dt);
+  for (int idx : kappa_maps) invert_map<<<1024, 256, 0, s>>>(map_field(h, idx), h->ncells_padded);
   FW_CUDA(h, cudaGetLastError());
   // beta: use the nonlinear kernel only when some cell has beta != 0
   any_nonzero<<<1024, 256, 0, s>>>(map_field(h, 2), h->ncells_padded, h->step + 2);
@@ -558,6 +622,17 @@ int fw_set_fields(fw_handle* h, const fw_fields* f) {
   if (st) return st;
   FW_CUDA(h, cudaStreamSynchronize(s));
   return FW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int fw_set_fields(fw_handle* h, const fw_fields* f) { return set_fields_impl(h, f, nullptr); }
+
+int fw_set_fields_aniso(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an) {
+  if (!an) return fail(h, FW_ERR_ARGUMENT, "per-direction maps are NULL");
+  return set_fields_impl(h, f, an);
 }
 
 int fw_set_source_signal(fw_handle* h, const float* icmat, int32_t on_device) {
@@ -705,6 +780,7 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   if (h->ndim != 2) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint is implemented for 2D grids");
   if (h->has_beta) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs beta = 0 everywhere");
+  if (h->aniso) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint covers the isotropic engine");
   if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called first");
   if (checkpoint_every < 1) return fail(h, FW_ERR_ARGUMENT, "checkpoint_every must be >= 1");
   const size_t state_elems = (size_t)h->ncells_padded * n_state(h->ndim);
@@ -884,8 +960,9 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
   for (int i = 0; i < n; ++i) {
     const fw_handle* h = handles[i];
     if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle %d is NULL", i);
-    if (h->ndim != 2 || h->variant != kDirect)
-      return fail(nullptr, FW_ERR_UNSUPPORTED, "group members must be 2D simulations (member %d)", i);
+    if (h->ndim != 2 || h->variant != kDirect || h->aniso)
+      return fail(nullptr, FW_ERR_UNSUPPORTED,
+                  "group members must be isotropic 2D simulations (member %d)", i);
     if (!h->fields_set) return fail(nullptr, FW_ERR_STATE, "member %d has no fields set", i);
   }
   std::vector<fw_handle*> m(handles, handles + n);

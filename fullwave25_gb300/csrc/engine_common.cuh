@@ -52,12 +52,14 @@ struct Maps {
   const float* rdt_rho;      // dt / rho
   const float* dt_k;         // dt * K
   const float* beta2dt;      // 2 dt beta, or nullptr when beta == 0 everywhere
-  const float* inv_ku;       // 1 / kappau
-  const float* inv_kx;       // 1 / kappax
-  const float* au[2];
-  const float* bu[2];
-  const float* ax[2];
-  const float* bx[2];
+  // relaxation coefficients per derivative axis; the isotropic engine points every axis at the
+  // same arrays (u maps for the pressure gradient, x maps for the velocity divergence)
+  const float* inv_ku[3];    // 1 / kappa{u,w,v}
+  const float* inv_kx[3];    // 1 / kappa{x,y,z}
+  const float* au[3][2];
+  const float* bu[3][2];
+  const float* ax[3][2];
+  const float* bx[3][2];
   const int32_t* dcmap;
   const float* taps;         // [ndmap][12]
 };
@@ -79,20 +81,25 @@ __device__ __forceinline__ void load_taps(const float* taps, int dc, float (&c)[
 }
 
 // Point-wise operands of one cell for the velocity update, loaded together (all loads issued
-// before any use) and written back together. NDIM velocity components.
-template <int NDIM>
+// before any use) and written back together. NDIM velocity components; kAniso: one set of
+// relaxation coefficients per axis (NA = NDIM sets), else one set shared by every axis.
+template <int NDIM, bool kAniso = false>
 struct CellVelT {
+  static constexpr int NA = kAniso ? NDIM : 1;
   int dc;
-  float iku, rr, a1, b1, a2, b2;
+  float rr, iku[NA], a1[NA], b1[NA], a2[NA], b2[NA];
   float v[NDIM], s1[NDIM], s2[NDIM];
   __device__ __forceinline__ void load(const StepArgs& A, int64_t c) {
     dc = __ldg(A.m.dcmap + c);
-    iku = __ldg(A.m.inv_ku + c);
     rr = __ldg(A.m.rdt_rho + c);
-    a1 = __ldg(A.m.au[0] + c);
-    b1 = __ldg(A.m.bu[0] + c);
-    a2 = __ldg(A.m.au[1] + c);
-    b2 = __ldg(A.m.bu[1] + c);
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+      iku[a] = __ldg(A.m.inv_ku[a] + c);
+      a1[a] = __ldg(A.m.au[a][0] + c);
+      b1[a] = __ldg(A.m.bu[a][0] + c);
+      a2[a] = __ldg(A.m.au[a][1] + c);
+      b2[a] = __ldg(A.m.bu[a][1] + c);
+    }
 #pragma unroll
     for (int a = 0; a < NDIM; ++a) {
       v[a] = A.f.v[a][c];
@@ -104,29 +111,34 @@ struct CellVelT {
   __device__ __forceinline__ void update_store(const StepArgs& A, int64_t c, const float* g) {
 #pragma unroll
     for (int a = 0; a < NDIM; ++a) {
-      const float n1 = fmaf(b1, s1[a], a1 * g[a]);
-      const float n2 = fmaf(b2, s2[a], a2 * g[a]);
+      const int q = kAniso ? a : 0;
+      const float n1 = fmaf(b1[q], s1[a], a1[q] * g[a]);
+      const float n2 = fmaf(b2[q], s2[a], a2[q] * g[a]);
       A.f.psi[a][0][c] = n1;
       A.f.psi[a][1][c] = n2;
-      A.f.v[a][c] = fmaf(-rr, fmaf(g[a], iku, n1) + n2, v[a]);
+      A.f.v[a][c] = fmaf(-rr, fmaf(g[a], iku[q], n1) + n2, v[a]);
     }
   }
 };
 
-template <int NDIM, bool kBeta>
+template <int NDIM, bool kBeta, bool kAniso = false>
 struct CellPrsT {
+  static constexpr int NA = kAniso ? NDIM : 1;
   int dc;
-  float ikx, dtk, b2dt, a1, b1, a2, b2, pc;
+  float dtk, b2dt, pc, ikx[NA], a1[NA], b1[NA], a2[NA], b2[NA];
   float f1[NDIM], f2[NDIM];
   __device__ __forceinline__ void load(const StepArgs& A, int64_t c) {
     dc = __ldg(A.m.dcmap + c);
-    ikx = __ldg(A.m.inv_kx + c);
     dtk = __ldg(A.m.dt_k + c);
     b2dt = kBeta ? __ldg(A.m.beta2dt + c) : 0.f;
-    a1 = __ldg(A.m.ax[0] + c);
-    b1 = __ldg(A.m.bx[0] + c);
-    a2 = __ldg(A.m.ax[1] + c);
-    b2 = __ldg(A.m.bx[1] + c);
+#pragma unroll
+    for (int a = 0; a < NA; ++a) {
+      ikx[a] = __ldg(A.m.inv_kx[a] + c);
+      a1[a] = __ldg(A.m.ax[a][0] + c);
+      b1[a] = __ldg(A.m.bx[a][0] + c);
+      a2[a] = __ldg(A.m.ax[a][1] + c);
+      b2[a] = __ldg(A.m.bx[a][1] + c);
+    }
     pc = A.f.p[c];
 #pragma unroll
     for (int a = 0; a < NDIM; ++a) {
@@ -139,20 +151,17 @@ struct CellPrsT {
     float div = 0.f;
 #pragma unroll
     for (int a = 0; a < NDIM; ++a) {
-      const float n1 = fmaf(b1, f1[a], a1 * d[a]);
-      const float n2 = fmaf(b2, f2[a], a2 * d[a]);
+      const int q = kAniso ? a : 0;
+      const float n1 = fmaf(b1[q], f1[a], a1[q] * d[a]);
+      const float n2 = fmaf(b2[q], f2[a], a2[q] * d[a]);
       A.f.phi[a][0][c] = n1;
       A.f.phi[a][1][c] = n2;
-      div += fmaf(d[a], ikx, n1) + n2;
+      div += fmaf(d[a], ikx[q], n1) + n2;
     }
     const float coef = kBeta ? fmaf(b2dt, pc, dtk) : dtk;
     A.f.p[c] = fmaf(-coef, div, pc);
   }
 };
-
-using CellVel = CellVelT<3>;
-template <bool kBeta>
-using CellPrs = CellPrsT<3, kBeta>;
 
 // Source injection, air zeroing and sensor recording for the cells owned by this block's tile.
 // Called by every thread of kernel B after its pressure writes; `tid`/`nthr` span the block.

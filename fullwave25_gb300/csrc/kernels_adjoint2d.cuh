@@ -150,9 +150,9 @@ __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
   const Grid& g = A.g;
   const int64_t fs = A.fs;
   const float lp = A.lam_p[c];
-  const float k = __ldg(A.m.dt_k + c), ikx = __ldg(A.m.inv_kx + c);
-  const float ax[2] = {__ldg(A.m.ax[0] + c), __ldg(A.m.ax[1] + c)};
-  const float bx[2] = {__ldg(A.m.bx[0] + c), __ldg(A.m.bx[1] + c)};
+  const float k = __ldg(A.m.dt_k + c), ikx = __ldg(A.m.inv_kx[0] + c);
+  const float ax[2] = {__ldg(A.m.ax[0][0] + c), __ldg(A.m.ax[0][1] + c)};
+  const float bx[2] = {__ldg(A.m.bx[0][0] + c), __ldg(A.m.bx[0][1] + c)};
   double g_dtk = 0.0, g_ikx = 0.0, g_ax[2] = {0.0, 0.0}, g_bx[2] = {0.0, 0.0};
   float div = 0.f;
   const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
@@ -187,9 +187,9 @@ __global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
   if (!adj_cell(A.g, &c)) return;
   const Grid& g = A.g;
   const int64_t fs = A.fs;
-  const float r = __ldg(A.m.rdt_rho + c), iku = __ldg(A.m.inv_ku + c);
-  const float au[2] = {__ldg(A.m.au[0] + c), __ldg(A.m.au[1] + c)};
-  const float bu[2] = {__ldg(A.m.bu[0] + c), __ldg(A.m.bu[1] + c)};
+  const float r = __ldg(A.m.rdt_rho + c), iku = __ldg(A.m.inv_ku[0] + c);
+  const float au[2] = {__ldg(A.m.au[0][0] + c), __ldg(A.m.au[0][1] + c)};
+  const float bu[2] = {__ldg(A.m.bu[0][0] + c), __ldg(A.m.bu[0][1] + c)};
   double g_r = 0.0, g_iku = 0.0, g_au[2] = {0.0, 0.0}, g_bu[2] = {0.0, 0.0};
   const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
 #pragma unroll

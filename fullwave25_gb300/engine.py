@@ -11,7 +11,7 @@ from pathlib import Path
 
 import numpy as np
 
-from .inputs import ISOTROPIC_MAPS, EngineInputs
+from .inputs import ISOTROPIC_MAPS, EngineInputs, anisotropic_extra_maps
 
 LIB_PATH = Path(__file__).resolve().parent / "libfwgb.so"
 
@@ -19,7 +19,8 @@ FW_STATUS = {0: "FW_OK", 1: "FW_ERR_ARGUMENT", 2: "FW_ERR_CUDA", 3: "FW_ERR_STAT
              4: "FW_ERR_OOM", 5: "FW_ERR_DEVICE", 6: "FW_ERR_UNSUPPORTED"}
 
 # every symbol include/fwgb.h declares
-EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_source_signal",
+EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_fields_aniso",
+            "fw_set_source_signal",
             "fw_set_source_columns", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
             "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_launches_per_step",
@@ -55,6 +56,15 @@ ADJOINT_MAPS = ("rdt_rho", "dt_k", "inv_ku", "inv_kx", "au1", "bu1", "au2", "bu2
                 "ax1", "bx1", "ax2", "bx2")
 
 
+ANISO_FIELDS = tuple(f"{k}{ax}{nu}" if k != "kappa" else f"kappa{ax}"
+                     for ax in ("w", "y", "v", "z")
+                     for k, nu in (("kappa", ""), ("apml", 1), ("bpml", 1), ("apml", 2), ("bpml", 2)))
+
+
+class FwFieldsAniso(C.Structure):
+    _fields_ = [(n, _FP) for n in ANISO_FIELDS]
+
+
 class EngineError(RuntimeError):
     """A C-ABI call returned a non-zero status."""
 
@@ -82,6 +92,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_abi_version": (C.c_int, []),
         "fw_create": (C.c_int, [C.POINTER(FwDesc), C.POINTER(H)]),
         "fw_set_fields": (C.c_int, [H, C.POINTER(FwFields)]),
+        "fw_set_fields_aniso": (C.c_int, [H, C.POINTER(FwFields), C.POINTER(FwFieldsAniso)]),
         "fw_set_source_signal": (C.c_int, [H, _FP, C.c_int32]),
         "fw_set_source_columns": (C.c_int, [H, vp, _FP, C.c_int32, C.c_int32, C.c_int32]),
         "fw_run": (C.c_int, [H, vp, _FP, C.c_int32]),
@@ -137,8 +148,8 @@ def desc_from_inputs(inp) -> FwDesc:
                   nt_ic=int(inp.icmat.shape[1]), mod_t=inp.mod_t, dx=inp.spacing[0],
                   dy=inp.spacing[1], dz=dz,
                   dt=inp.dt, c0=inp.c0, ncoords=inp.icc.shape[0], ncoordsout=inp.outc.shape[0],
-                  ncoordszero=inp.icczero.shape[0], ndmap=inp.dmap.shape[2], isotropic=1,
-                  n_relax=2)
+                  ncoordszero=inp.icczero.shape[0], ndmap=inp.dmap.shape[2],
+                  isotropic=int("kappay" not in inp.maps), n_relax=2)
 
 
 class Engine:
@@ -189,7 +200,12 @@ class Engine:
             icmat=_fp(f("icmat", inp.icmat, _c_f32)),
             **{k: _fp(f(k, m[k], _c_f32)) for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)},
         )
-        self._call("fw_set_fields", C.byref(fields))
+        if inp.isotropic:
+            self._call("fw_set_fields", C.byref(fields))
+        else:
+            an = FwFieldsAniso(**{k: _fp(f(k, m[k], _c_f32))
+                                  for k in anisotropic_extra_maps(inp.ndim)})
+            self._call("fw_set_fields_aniso", C.byref(fields), C.byref(an))
 
     def _set_device_fields(self, inp) -> None:
         """Fields given as CUDA tensors (``workloads3d.DeviceInputs``): no host round trip."""
@@ -209,7 +225,13 @@ class Engine:
             icmat=fptr(inp.icmat), on_device=1,
             **{k: fptr(m[k]) for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)})
         torch.cuda.synchronize(dev)
-        self._call("fw_set_fields", C.byref(fields))
+        if "kappay" in m:
+            for k in anisotropic_extra_maps(inp.ndim):
+                assert m[k].dtype == torch.float32 and m[k].is_contiguous() and m[k].is_cuda, k
+            an = FwFieldsAniso(**{k: fptr(m[k]) for k in anisotropic_extra_maps(inp.ndim)})
+            self._call("fw_set_fields_aniso", C.byref(fields), C.byref(an))
+        else:
+            self._call("fw_set_fields", C.byref(fields))
 
     def set_source_columns(self, cols: np.ndarray, n0: int, stream: int | None = None) -> None:
         """Upload source samples of steps ``[n0, n0 + len(cols))`` (time-major, host)."""

@@ -32,6 +32,25 @@ logger = logging.getLogger("__main__." + __name__)
 ISOTROPIC_MAPS = ("kappax", "kappau", "apmlu1", "bpmlu1", "apmlx1", "bpmlx1",
                   "apmlu2", "bpmlu2", "apmlx2", "bpmlx2")
 
+# Gradient (nabla_1) maps per derivative axis x, y, z and divergence (nabla_2) maps per axis, as
+# the anisotropic build reads them (input_file_writer.py:592-620): u/w/v for the pressure
+# gradient along x/y/z, x/y/z for the velocity divergence along x/y/z.
+GRAD_AXIS_LETTER = ("u", "w", "v")
+DIV_AXIS_LETTER = ("x", "y", "z")
+
+
+def axis_maps(letter: str) -> tuple:
+    return (f"kappa{letter}", f"apml{letter}1", f"bpml{letter}1", f"apml{letter}2",
+            f"bpml{letter}2")
+
+
+def anisotropic_extra_maps(ndim: int) -> tuple:
+    """Maps the anisotropic engine reads in addition to ISOTROPIC_MAPS."""
+    out = []
+    for a in range(1, ndim):
+        out += axis_maps(GRAD_AXIS_LETTER[a]) + axis_maps(DIV_AXIS_LETTER[a])
+    return tuple(out)
+
 
 @dataclass
 class EngineInputs:
@@ -55,6 +74,11 @@ class EngineInputs:
     @property
     def ndim(self) -> int:
         return len(self.shape)
+
+    @property
+    def isotropic(self) -> bool:
+        """True unless per-direction relaxation maps (kappay, apmlw1, ...) are present."""
+        return "kappay" not in self.maps
 
     @property
     def n_cells(self) -> int:
@@ -81,7 +105,10 @@ class EngineInputs:
             raise ValueError(f"every axis needs more than {2 * coefficients.N_TAPS} cells: {self.shape}")
         if self.nt < 0 or self.mod_t < 1:
             raise ValueError(f"bad nT={self.nt} or modT={self.mod_t}")
-        for name in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS):
+        names = ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)
+        if not self.isotropic:
+            names += anisotropic_extra_maps(self.ndim)
+        for name in names:
             if name not in self.maps:
                 raise ValueError(f"missing map {name}")
             if tuple(self.maps[name].shape) != tuple(self.shape):
@@ -109,9 +136,14 @@ def build_inputs(grid, medium, source, sensor) -> EngineInputs:
     d = coefficients.d_matrix(grid.cfl, is_3d=grid.is_3d)
     dmap = coefficients.d_map(c, grid.dt, grid.dx, is_3d=grid.is_3d)
     fw2 = medium.relaxation_param_dict_for_fw2
-    names = {"kappax": "kappa_x", "kappau": "kappa_u"}
-    for nu in (1, 2):
-        for ax in ("u", "x"):
+    letters = ["u", "x"]
+    if "kappa_y" in fw2:  # anisotropic: one set of maps per derivative direction
+        nd = 3 if grid.is_3d else 2
+        letters = list(GRAD_AXIS_LETTER[:nd]) + list(DIV_AXIS_LETTER[:nd])
+    names = {}
+    for ax in letters:
+        names[f"kappa{ax}"] = f"kappa_{ax}"
+        for nu in (1, 2):
             names[f"apml{ax}{nu}"] = f"a_pml_{ax}{nu}"
             names[f"bpml{ax}{nu}"] = f"b_pml_{ax}{nu}"
     maps = {"c": c.astype(np.float32), "rho": medium.density.astype(np.float32),
@@ -163,7 +195,10 @@ def read_simulation_dir(sim_dir: Path) -> EngineInputs:
     dmap = dmap.reshape(9, 2, -1)
     if ndmap != dmap.shape[2] and not (ndmap == 1 and dmap.shape[2] >= 1):
         raise ValueError(f"ndmap={ndmap} disagrees with dmap.dat ({dmap.shape[2]} tap sets)")
-    maps = {n: grid_map(n) for n in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)}
+    names = ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)
+    if (sim_dir / "kappay.dat").exists():
+        names += anisotropic_extra_maps(len(shape))
+    maps = {n: grid_map(n) for n in names}
     coords = lambda n, k: _read(sim_dir / f"{n}.dat", np.int32).reshape(k, ndim)  # noqa: E731
     icczero = (coords("icczero", ncoordszero) if ncoordszero
                else np.zeros((0, ndim), np.int32))

@@ -31,8 +31,6 @@ class Solver:
                  cuda_device_id: str | int | list | None = None) -> None:
         if use_exponential_attenuation:
             raise NotImplementedError("the exponential-attenuation engine is not implemented")
-        if not use_isotropic_relaxation:
-            raise NotImplementedError("the anisotropic relaxation engine is not implemented")
         if not use_gpu:
             raise NotImplementedError("Currently, only GPU version is supported.")
         if transducer is not None:
@@ -57,10 +55,12 @@ class Solver:
         if n_transition_layer is None:
             n_transition_layer = grid.ppw * 3
         self.cuda_device_id = cuda_device_id
+        self.use_isotropic_relaxation = use_isotropic_relaxation
+        medium.use_isotropic_relaxation = use_isotropic_relaxation   # as solver.py:457-476 does
         self.pml_builder = PMLBuilder(grid, medium, source, sensor, m_spatial_order=m_spatial_order,
                                       n_pml_layer=pml_layer_thickness_px,
                                       n_transition_layer=n_transition_layer,
-                                      use_isotropic_relaxation=True)
+                                      use_isotropic_relaxation=use_isotropic_relaxation)
         self.last_timing: dict = {}
 
     @staticmethod
@@ -70,6 +70,9 @@ class Solver:
     def build_engine_inputs(self, *, record_whole_domain: bool = False,
                             sampling_modulus_time_whole_domain: int = 1):
         ext_medium = self.pml_builder.run(use_pml=self.use_pml)
+        if not self.use_isotropic_relaxation and not self.use_pml:
+            ext_medium.relaxation_param_dict_for_fw2 = ext_medium.calc_relaxation_param_dict_for_fw2(
+                use_isotropic_relaxation=False)
         if record_whole_domain:
             sensor = Sensor(np.ones(self.pml_builder.extended_grid.shape, dtype=bool),
                             sampling_modulus_time=sampling_modulus_time_whole_domain)

@@ -154,6 +154,10 @@ class DeviceInputs:
         return len(self.shape)
 
     @property
+    def isotropic(self):
+        return "kappay" not in self.maps
+
+    @property
     def nt_ic(self):
         return int(self.icmat.shape[1])
 

@@ -54,7 +54,8 @@ typedef struct fw_desc {
     int32_t ncoordsout;     /* sensor cells */
     int32_t ncoordszero;    /* air (zero-pressure) cells */
     int32_t ndmap;          /* tap sets in dmap */
-    int32_t isotropic;      /* must be 1: the isotropic relaxation build */
+    int32_t isotropic;      /* 1: isotropic relaxation maps (fw_set_fields); 0: one set of maps
+                               per derivative axis (fw_set_fields_aniso) */
     int32_t n_relax;        /* must be 2 relaxation mechanisms */
 } fw_desc;
 
@@ -76,6 +77,18 @@ typedef struct fw_fields {
     int32_t on_device;
 } fw_fields;
 
+/* The anisotropic build's additional maps (same layout as the maps of fw_fields): the pressure
+ * gradient along y uses kappaw, apmlw1, bpmlw1, apmlw2, bpmlw2 and along z the "v" maps; the
+ * velocity divergence along y uses the "y" maps and along z the "z" maps; along x the fw_fields
+ * maps ("u" for the gradient, "x" for the divergence) (input_file_writer.py:592-620).
+ * The z and v maps are ignored for 2D grids. */
+typedef struct fw_fields_aniso {
+    const float *kappaw, *apmlw1, *bpmlw1, *apmlw2, *bpmlw2;
+    const float *kappay, *apmly1, *bpmly1, *apmly2, *bpmly2;
+    const float *kappav, *apmlv1, *bpmlv1, *apmlv2, *bpmlv2;
+    const float *kappaz, *apmlz1, *bpmlz1, *apmlz2, *bpmlz2;
+} fw_fields_aniso;
+
 typedef struct fw_handle fw_handle;
 
 /* Library ABI version (FWGB_ABI_VERSION). */
@@ -90,6 +103,10 @@ FWGB_API int fw_create(const fw_desc *desc, fw_handle **out);
  * Replaces: the executable reading d dmap dcmap c rho K beta kappa* apml* bpml* icc outc icmat
  * icczero (InputFileWriter._save_variables_into_dat_file, input_file_writer.py:563-645). */
 FWGB_API int fw_set_fields(fw_handle *h, const fw_fields *f);
+
+/* fw_set_fields for a handle created with isotropic = 0 (the anisotropic build,
+ * use_isotropic_relaxation=False in the reference: medium.py:374-406). */
+FWGB_API int fw_set_fields_aniso(fw_handle *h, const fw_fields *f, const fw_fields_aniso *an);
 
 /* Replace only the source signals (a new transmit event on the same medium), float32
  * [ncoords][nt_ic]. Replaces: the is_static_map re-run that rewrites icmat.dat only

@@ -31,8 +31,11 @@ typedef struct {
     /* inputs (float32, dense C order) */
     const float *dmap;  /* [9][2][ndmap] */
     const int32_t *dcmap;
-    const float *rho, *K, *beta, *kappax, *kappau;
-    const float *au[2], *bu[2], *ax[2], *bx[2];
+    const float *rho, *K, *beta;
+    /* per derivative axis (the isotropic build passes the same maps for every axis):
+       gradient maps kappa{u,w,v}, apml/bpml{u,w,v}{1,2}; divergence maps kappa{x,y,z}, ... */
+    const float *kappau[3], *kappax[3];
+    const float *au[3][2], *bu[3][2], *ax[3][2], *bx[3][2];
     const int32_t *icc, *outc, *icczero;
     const float *icmat; /* [ncoords][nt_ic] */
 } oracle_desc;
@@ -42,7 +45,7 @@ typedef struct {
     int64_t cells, s[3];
     double *p, *v[3], *psi[3][2], *phi[3][2];
     double *taps;   /* per cell: 9 values */
-    double *rdt_rho, *dtk, *b2dt, *iku, *ikx;
+    double *rdt_rho, *dtk, *b2dt, *iku[3], *ikx[3];
     int has_beta;
     int64_t *icc_lin, *outc_lin, *zero_lin;
     int32_t *src_keep;
@@ -78,7 +81,7 @@ oracle_state *oracle_create(const oracle_desc *d) {
                          &o->psi[1][0], &o->psi[1][1], &o->psi[2][0], &o->psi[2][1],
                          &o->phi[0][0], &o->phi[0][1], &o->phi[1][0], &o->phi[1][1],
                          &o->phi[2][0], &o->phi[2][1], &o->rdt_rho, &o->dtk, &o->b2dt,
-                         &o->iku, &o->ikx};
+                         &o->iku[0], &o->iku[1], &o->iku[2], &o->ikx[0], &o->ikx[1], &o->ikx[2]};
     for (size_t f = 0; f < sizeof fields / sizeof fields[0]; ++f) {
         *fields[f] = calloc((size_t)n, sizeof(double));
         if (!*fields[f]) return NULL;
@@ -92,8 +95,10 @@ oracle_state *oracle_create(const oracle_desc *d) {
         o->dtk[c] = d->dt * (double)d->K[c];
         o->b2dt[c] = 2.0 * d->dt * (double)d->beta[c];
         if (d->beta[c] != 0.f) o->has_beta = 1;
-        o->iku[c] = 1.0 / (double)d->kappau[c];
-        o->ikx[c] = 1.0 / (double)d->kappax[c];
+        for (int a = 0; a < d->ndim; ++a) {
+            o->iku[a][c] = 1.0 / (double)d->kappau[a][c];
+            o->ikx[a][c] = 1.0 / (double)d->kappax[a][c];
+        }
     }
     o->icc_lin = malloc(sizeof(int64_t) * (d->ncoords + 1));
     o->outc_lin = malloc(sizeof(int64_t) * (d->ncoordsout + 1));
@@ -118,7 +123,8 @@ void oracle_destroy(oracle_state *o) {
     double *fields[] = {o->p, o->v[0], o->v[1], o->v[2], o->psi[0][0], o->psi[0][1],
                         o->psi[1][0], o->psi[1][1], o->psi[2][0], o->psi[2][1], o->phi[0][0],
                         o->phi[0][1], o->phi[1][0], o->phi[1][1], o->phi[2][0], o->phi[2][1],
-                        o->rdt_rho, o->dtk, o->b2dt, o->iku, o->ikx, o->taps};
+                        o->rdt_rho, o->dtk, o->b2dt, o->iku[0], o->iku[1], o->iku[2],
+                        o->ikx[0], o->ikx[1], o->ikx[2], o->taps};
     for (size_t f = 0; f < sizeof fields / sizeof fields[0]; ++f) free(fields[f]);
     free(o->icc_lin); free(o->outc_lin); free(o->zero_lin); free(o->src_keep);
     free(o);
@@ -153,9 +159,9 @@ void oracle_step(oracle_state *o, double *record_row) {
                 off += p[c + sa - sb] - p[c - sb];
             }
             const double g = (acc + t[8] * off) / h;
-            s1[c] = o->d.bu[0][c] * s1[c] + o->d.au[0][c] * g;
-            s2[c] = o->d.bu[1][c] * s2[c] + o->d.au[1][c] * g;
-            va[c] -= o->rdt_rho[c] * (g * o->iku[c] + s1[c] + s2[c]);
+            s1[c] = o->d.bu[a][0][c] * s1[c] + o->d.au[a][0][c] * g;
+            s2[c] = o->d.bu[a][1][c] * s2[c] + o->d.au[a][1][c] * g;
+            va[c] -= o->rdt_rho[c] * (g * o->iku[a][c] + s1[c] + s2[c]);
         })
     }
     /* divergence accumulated per cell over axes in order, like the NumPy oracle */
@@ -177,9 +183,9 @@ void oracle_step(oracle_state *o, double *record_row) {
                 }
                 const double dv = (acc + t[8] * off) / o->d.h[a];
                 double *f1 = o->phi[a][0], *f2 = o->phi[a][1];
-                f1[c] = o->d.bx[0][c] * f1[c] + o->d.ax[0][c] * dv;
-                f2[c] = o->d.bx[1][c] * f2[c] + o->d.ax[1][c] * dv;
-                dsum += dv * o->ikx[c] + f1[c] + f2[c];
+                f1[c] = o->d.bx[a][0][c] * f1[c] + o->d.ax[a][0][c] * dv;
+                f2[c] = o->d.bx[a][1][c] * f2[c] + o->d.ax[a][1][c] * dv;
+                dsum += dv * o->ikx[a][c] + f1[c] + f2[c];
             }
             const double pb = p[c];
             if (o->has_beta) p[c] = pb - (o->dtk[c] + o->b2dt[c] * pb) * dsum;

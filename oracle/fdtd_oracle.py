@@ -24,7 +24,9 @@ Scheme restated from these reference sources:
   fullwave/solver/pml_builder.py:794-810):
       psi_nu <- b_nu psi_nu + a_nu D f ;  D~ f = D f / kappa + psi_1 + psi_2
   with ``kappau/apmlu/bpmlu`` for the pressure gradient and ``kappax/apmlx/bpmlx`` for the
-  velocity divergence (fullwave/medium.py:357-372).
+  velocity divergence (fullwave/medium.py:357-372); the anisotropic build reads one set per
+  derivative axis: u/w/v for the gradient along x/y/z and x/y/z for the divergence
+  (fullwave/medium.py:374-406, input_file_writer.py:592-620).
 * Leapfrog: velocities then pressure each step; body region ``[8, n-8)`` on every axis (the
   8-cell ghost layer of pml_builder.py:270-276); ghost cells stay zero.
 * Nonlinearity: ``p <- p - dT (K + 2 beta p) div`` (beta = 0 in every benchmark workload).
@@ -96,6 +98,16 @@ class Oracle:
         self.bu = (m["bpmlu1"], m["bpmlu2"])
         self.ax = (m["apmlx1"], m["apmlx2"])
         self.bx = (m["bpmlx1"], m["bpmlx2"])
+        # per derivative axis (anisotropic build): gradient maps u/w/v, divergence maps x/y/z;
+        # the isotropic build uses the u and x maps on every axis
+        iso = "kappay" not in m
+        gl, dl = ("u", "w", "v"), ("x", "y", "z")
+        self.axis_u = [(1.0 / m[f"kappa{gl[a]}"], (m[f"apml{gl[a]}1"], m[f"apml{gl[a]}2"]),
+                        (m[f"bpml{gl[a]}1"], m[f"bpml{gl[a]}2"])) if not iso else None
+                       for a in range(nd)]
+        self.axis_x = [(1.0 / m[f"kappa{dl[a]}"], (m[f"apml{dl[a]}1"], m[f"apml{dl[a]}2"]),
+                        (m[f"bpml{dl[a]}1"], m[f"bpml{dl[a]}2"])) if not iso else None
+                       for a in range(nd)]
         lin = lambda c: (np.ravel_multi_index(tuple(np.asarray(c).T), self.shape)  # noqa: E731
                          if len(c) else np.zeros(0, np.int64))
         self.icc = lin(inputs.icc)
@@ -151,17 +163,18 @@ class Oracle:
     def step(self, record=None):
         st, body, n = self.state, _body(self.shape), self.step_index
         for a in range(self.nd):
+            ik, au, bu = self.axis_u[a] or (self.inv_kappa_u, self.au, self.bu)
             g = self.grad(st.p, a)
             for nu in range(2):
-                st.psi[a][nu][body] = self.bu[nu] * st.psi[a][nu][body] + self.au[nu] * g
-            st.v[a][body] -= self.rdt_rho * (g * self.inv_kappa_u + st.psi[a][0][body]
-                                             + st.psi[a][1][body])
+                st.psi[a][nu][body] = bu[nu] * st.psi[a][nu][body] + au[nu] * g
+            st.v[a][body] -= self.rdt_rho * (g * ik + st.psi[a][0][body] + st.psi[a][1][body])
         div = np.zeros(tuple(k - 2 * GHOST for k in self.shape))
         for a in range(self.nd):
+            ik, ax, bx = self.axis_x[a] or (self.inv_kappa_x, self.ax, self.bx)
             dv = self.div_component(st.v[a], a)
             for nu in range(2):
-                st.phi[a][nu][body] = self.bx[nu] * st.phi[a][nu][body] + self.ax[nu] * dv
-            div += dv * self.inv_kappa_x + st.phi[a][0][body] + st.phi[a][1][body]
+                st.phi[a][nu][body] = bx[nu] * st.phi[a][nu][body] + ax[nu] * dv
+            div += dv * ik + st.phi[a][0][body] + st.phi[a][1][body]
         pb = st.p[body]
         if self.has_beta:
             st.p[body] = pb - (self.dt_k + self.beta2dt * pb) * div

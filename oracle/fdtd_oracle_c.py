@@ -28,9 +28,9 @@ class OracleDesc(C.Structure):
                 ("nt", C.c_int), ("nt_ic", C.c_int), ("mod_t", C.c_int), ("ncoords", C.c_int),
                 ("ncoordsout", C.c_int), ("ncoordszero", C.c_int), ("ndmap", C.c_int),
                 ("dmap", _FP), ("dcmap", _IP), ("rho", _FP), ("K", _FP), ("beta", _FP),
-                ("kappax", _FP), ("kappau", _FP), ("au", _FP * 2), ("bu", _FP * 2),
-                ("ax", _FP * 2), ("bx", _FP * 2), ("icc", _IP), ("outc", _IP), ("icczero", _IP),
-                ("icmat", _FP)]
+                ("kappau", _FP * 3), ("kappax", _FP * 3), ("au", (_FP * 2) * 3),
+                ("bu", (_FP * 2) * 3), ("ax", (_FP * 2) * 3), ("bx", (_FP * 2) * 3),
+                ("icc", _IP), ("outc", _IP), ("icczero", _IP), ("icmat", _FP)]
 
 
 def build(force: bool = False) -> Path:
@@ -71,9 +71,11 @@ class OracleC:
         self._keep = k = {
             "dmap": f32(inp.dmap), "dcmap": i32(inp.dcmap), "icc": i32(inp.icc),
             "outc": i32(inp.outc), "icczero": i32(inp.icczero), "icmat": f32(inp.icmat),
-            **{n: f32(m[n]) for n in ("rho", "K", "beta", "kappax", "kappau", "apmlu1",
-                                      "apmlu2", "bpmlu1", "bpmlu2", "apmlx1", "apmlx2",
-                                      "bpmlx1", "bpmlx2")}}
+            **{n: f32(v) for n, v in m.items() if n not in ("c",)}}
+        iso = "kappay" not in m
+        gl = ["u"] * 3 if iso else ["u", "w", "v"]
+        dl = ["x"] * 3 if iso else ["x", "y", "z"]
+        nd = inp.ndim
         fp = lambda a: a.ctypes.data_as(_FP)  # noqa: E731
         ip = lambda a: a.ctypes.data_as(_IP) if a.size else None  # noqa: E731
         shape = list(inp.shape) + [1] * (3 - inp.ndim)
@@ -83,11 +85,17 @@ class OracleC:
                        ncoords=inp.icc.shape[0], ncoordsout=inp.outc.shape[0],
                        ncoordszero=inp.icczero.shape[0], ndmap=inp.dmap.shape[2],
                        dmap=fp(k["dmap"]), dcmap=ip(k["dcmap"]), rho=fp(k["rho"]), K=fp(k["K"]),
-                       beta=fp(k["beta"]), kappax=fp(k["kappax"]), kappau=fp(k["kappau"]),
-                       au=(_FP * 2)(fp(k["apmlu1"]), fp(k["apmlu2"])),
-                       bu=(_FP * 2)(fp(k["bpmlu1"]), fp(k["bpmlu2"])),
-                       ax=(_FP * 2)(fp(k["apmlx1"]), fp(k["apmlx2"])),
-                       bx=(_FP * 2)(fp(k["bpmlx1"]), fp(k["bpmlx2"])),
+                       beta=fp(k["beta"]),
+                       kappau=(_FP * 3)(*[fp(k[f"kappa{gl[a]}"]) for a in range(nd)]),
+                       kappax=(_FP * 3)(*[fp(k[f"kappa{dl[a]}"]) for a in range(nd)]),
+                       au=((_FP * 2) * 3)(*[(_FP * 2)(fp(k[f"apml{gl[a]}1"]), fp(k[f"apml{gl[a]}2"]))
+                                           for a in range(nd)]),
+                       bu=((_FP * 2) * 3)(*[(_FP * 2)(fp(k[f"bpml{gl[a]}1"]), fp(k[f"bpml{gl[a]}2"]))
+                                           for a in range(nd)]),
+                       ax=((_FP * 2) * 3)(*[(_FP * 2)(fp(k[f"apml{dl[a]}1"]), fp(k[f"apml{dl[a]}2"]))
+                                           for a in range(nd)]),
+                       bx=((_FP * 2) * 3)(*[(_FP * 2)(fp(k[f"bpml{dl[a]}1"]), fp(k[f"bpml{dl[a]}2"]))
+                                           for a in range(nd)]),
                        icc=ip(k["icc"]), outc=ip(k["outc"]), icczero=ip(k["icczero"]),
                        icmat=fp(k["icmat"]))
         self._desc = d

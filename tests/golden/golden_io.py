@@ -7,7 +7,7 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-CASE_NAMES = ("2d_small", "2d_air_beta", "2d_nopml", "3d_small")
+CASE_NAMES = ("2d_small", "2d_air_beta", "2d_nopml", "3d_small", "2d_aniso", "3d_aniso")
 
 
 def load_case(name: str):
@@ -47,10 +47,12 @@ def rebuild_case_inputs(name: str):
     g = Grid.from_cells(shape, f0=float(z["f0"]), nt=int(z["nt"]), ppw=int(z["ppw"]),
                         cfl=float(z["cfl"]))
     relax = {k[6:]: z[k] for k in z.files if k.startswith("relax/")}
-    med = MediumRelaxationMaps(g, z["c"], z["rho"], z["beta"], relax, air_map=z["air_map"])
+    iso = bool(z["isotropic"]) if "isotropic" in z.files else True
+    med = MediumRelaxationMaps(g, z["c"], z["rho"], z["beta"], relax, air_map=z["air_map"],
+                               use_isotropic_relaxation=iso)
     src = Source(z["p0"], z["src_mask"])
     sen = Sensor(z["sens_mask"], int(z["mod_t"]))
     b = PMLBuilder(g, med, src, sen, n_pml_layer=int(z["n_pml"]),
-                   n_transition_layer=int(z["n_transition"]))
+                   n_transition_layer=int(z["n_transition"]), use_isotropic_relaxation=iso)
     em = b.run(use_pml=bool(z["use_pml"]))
     return build_inputs(b.extended_grid, em, b.extended_source, b.extended_sensor)

@@ -78,16 +78,20 @@ def smooth(rng, shape, lo, hi, blobs=3):
 
 
 CASES = {
-    # name: (shape, f0, nt, ppw, cfl, n_pml, n_transition, mod_t, beta, air, use_pml, src_layers)
+    # name: (shape, f0, nt, ppw, cfl, n_pml, n_transition, mod_t, beta, air, use_pml, src_layers
+    #        [, isotropic])
     "2d_small": ((40, 36), 3e6, 240, 12, 0.2, 6, 6, 1, 0.0, False, True, 3),
     "2d_air_beta": ((36, 32), 3e6, 200, 12, 0.25, 5, 5, 3, 3.5, True, True, 2),
     "2d_nopml": ((30, 28), 2e6, 150, 10, 0.3, 0, 0, 2, 0.0, False, False, 1),
     "3d_small": ((16, 14, 12), 2e6, 120, 10, 0.2, 3, 3, 2, 0.0, False, True, 2),
+    "2d_aniso": ((34, 30), 3e6, 160, 12, 0.2, 5, 5, 1, 0.0, False, True, 2, False),
+    "3d_aniso": ((14, 12, 12), 2e6, 90, 10, 0.2, 3, 3, 1, 0.0, False, True, 1, False),
 }
 
 
 def build_case(fw, name, spec, tmp: Path):
-    shape, f0, nt, ppw, cfl, n_pml, n_tr, mod_t, beta, air, use_pml, layers = spec
+    shape, f0, nt, ppw, cfl, n_pml, n_tr, mod_t, beta, air, use_pml, layers = spec[:12]
+    iso = spec[12] if len(spec) > 12 else True
     rng = np.random.default_rng(sum(map(ord, name)))
     c0 = 1540.0
     dx = c0 / f0 / ppw
@@ -103,7 +107,7 @@ def build_case(fw, name, spec, tmp: Path):
         air_map[tuple(slice(n - 6, n - 2) for n in shape)] = True
     relax = relaxation_maps(rng, shape)
     medium = fw.MediumRelaxationMaps(grid, c, rho, beta_map, relax, air_map=air_map,
-                                     use_isotropic_relaxation=True)
+                                     use_isotropic_relaxation=iso)
     src_mask = np.zeros(shape, dtype=bool)
     src_mask[:layers] = True
     coords = np.array(np.where(src_mask)).T
@@ -124,19 +128,20 @@ def build_case(fw, name, spec, tmp: Path):
     from fullwave.solver.pml_builder import PMLBuilder  # noqa: PLC0415
 
     builder = PMLBuilder(grid, medium, source, sensor, m_spatial_order=8, n_pml_layer=n_pml,
-                         n_transition_layer=n_tr, use_isotropic_relaxation=True)
+                         n_transition_layer=n_tr, use_isotropic_relaxation=iso)
     ext_medium = builder.run(use_pml=use_pml)
     dummy_bin = tmp / "engine_placeholder"
     dummy_bin.write_text("placeholder: the engine executable is not copied into fixtures\n")
     writer = InputFileWriter(work_dir=tmp / "work", grid=builder.extended_grid,
                              medium=ext_medium, source=builder.extended_source,
                              sensor=builder.extended_sensor, path_fullwave_simulation_bin=dummy_bin,
-                             use_isotropic_relaxation=True)
+                             use_isotropic_relaxation=iso)
     sim_dir = writer.run(name)
     files = {f"dat/{p.stem}": np.frombuffer(p.read_bytes(), dtype=np.uint8)
              for p in sorted(sim_dir.glob("*.dat"))}
     scenario = {"shape": np.array(shape), "f0": f0, "nt": nt, "ppw": ppw, "cfl": cfl,
                 "n_pml": n_pml, "n_transition": n_tr, "mod_t": mod_t, "use_pml": use_pml,
+                "isotropic": iso,
                 "c": c, "rho": rho, "beta": beta_map, "air_map": air_map, "p0": p0,
                 "src_mask": src_mask, "sens_mask": sens_mask,
                 **{f"relax/{k}": v for k, v in relax.items()}}

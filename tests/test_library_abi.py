@@ -28,7 +28,7 @@ def test_library_exports_every_declared_symbol(engine_lib):
 
 
 @pytest.mark.parametrize("field,value,code", [
-    ("ndim", 4, 1), ("nx", 10, 1), ("mod_t", 0, 1), ("isotropic", 0, 6), ("n_relax", 3, 6),
+    ("ndim", 4, 1), ("nx", 10, 1), ("mod_t", 0, 1), ("isotropic", 2, 1), ("n_relax", 3, 6),
     ("dt", 0.0, 1),
 ])
 def test_create_rejects_bad_descriptor(engine_lib, field, value, code):

@@ -79,3 +79,25 @@ def test_wavefront_speed_in_homogeneous_lossless_medium():
     src_onset = np.argmax(np.abs(src) > 0.05 * np.abs(src).max())
     expected = src_onset + (row - 8) / cfl
     assert abs(onset - expected) < 0.1 * (row - 8) / cfl
+
+
+@pytest.mark.parametrize("name", ["2d_aniso", "3d_aniso"])
+def test_anisotropic_maps_equal_across_directions_give_isotropic_result(name):
+    """The reference's own pre-processing gives every direction the same maps
+    (pml_builder.py:926-1025 ramps all of them alike), so dropping the extra maps is exact."""
+    from fullwave25_gb300.inputs import anisotropic_extra_maps
+
+    inp = load_case_inputs(name)
+    assert not inp.isotropic
+    iso = load_case_inputs(name)
+    iso.maps = {k: v for k, v in iso.maps.items() if k not in anisotropic_extra_maps(iso.ndim)}
+    assert iso.isotropic
+    np.testing.assert_array_equal(run_oracle(inp, 40), run_oracle(iso, 40))
+
+
+def test_truly_anisotropic_maps_change_the_result():
+    inp = load_case_inputs("2d_aniso")
+    base = run_oracle(inp, 80)
+    inp.maps = dict(inp.maps)
+    inp.maps["apmlw1"] = (inp.maps["apmlw1"] * np.float32(3.0)).astype(np.float32)
+    assert rel_l2(run_oracle(inp, 80), base) > 1e-6
