@@ -11,7 +11,8 @@ import logging
 from .grid import Grid
 from .inputs import EngineInputs, build_inputs, load_dat_data, read_simulation_dir, write_simulation_dir
 from .launcher import Launcher, SimulationError
-from .medium import MediumRelaxationMaps
+from .exponential import MediumExponentialAttenuation, PMLBuilderExponentialAttenuation
+from .medium import Medium, MediumRelaxationMaps
 from .pml import PMLBuilder
 from .pulse import gaussian_modulated_sinusoidal_signal
 from .solver import Solver
@@ -22,7 +23,8 @@ __version__ = "0.1.0"
 logging.getLogger("__main__." + __name__).addHandler(logging.NullHandler())
 
 __all__ = [
-    "EngineInputs", "Grid", "Launcher", "MediumRelaxationMaps", "PMLBuilder", "Sensor",
+    "EngineInputs", "Grid", "Launcher", "Medium", "MediumExponentialAttenuation",
+    "MediumRelaxationMaps", "PMLBuilder", "PMLBuilderExponentialAttenuation", "Sensor",
     "SimulationError", "Solver", "Source", "build_inputs", "gaussian_modulated_sinusoidal_signal",
     "load_dat_data", "read_simulation_dir", "write_simulation_dir",
 ]

@@ -66,6 +66,7 @@ struct fw_handle {
   size_t bytes = 0;
   bool has_beta = false, fields_set = false;
   bool aniso = false;          // per-axis relaxation maps (the anisotropic engine)
+  bool exp = false;            // exponential-attenuation engine (n_relax = 0, map a_exp)
   int n_out = 0;
   int32_t host_step = 0;
   Tiling tiling{};
@@ -202,44 +203,44 @@ int upload_grid(fw_handle* h, void* dst, const void* src, size_t elem, bool on_d
   return FW_OK;
 }
 
-void launch_step(fw_handle* h, cudaStream_t s) {
+// One time step: velocity kernel, then pressure kernel (+ tile epilogue), with the cell physics
+// CV/CP (isotropic, anisotropic or exponential attenuation) of the handle.
+template <int ND, class CV, class CP, int kMin>
+void launch_typed(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
-  if (h->ndim == 3 && h->variant == kMarch) {
+  if (ND == 2) {
+    dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
+    vel2d_direct<CV><<<grid, block, 0, s>>>(h->args);
+    prs2d_direct<CP><<<grid, block, 0, s>>>(h->args);
+  } else if (h->variant == kMarch) {
     dim3 grid(t.n[2], t.n[1], t.n[0]), block(kMTZ, kMTY);
     const MarchMaps& tm = h->tmaps;
-    if (h->aniso) {
-      vel3d_march<kMarchXC, true><<<grid, block, 0, s>>>(h->args, tm.p);
-      if (h->has_beta) prs3d_march<kMarchXC, true, true><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
-      else prs3d_march<kMarchXC, false, true><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
-    } else {
-      vel3d_march<kMarchXC, false><<<grid, block, 0, s>>>(h->args, tm.p);
-      if (h->has_beta) prs3d_march<kMarchXC, true, false><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
-      else prs3d_march<kMarchXC, false, false><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
-    }
-    return;
-  }
-  if (h->ndim == 2) {
-    dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
-    if (h->aniso) {
-      vel2d_direct<true><<<grid, block, 0, s>>>(h->args);
-      if (h->has_beta) prs2d_direct<true, true><<<grid, block, 0, s>>>(h->args);
-      else prs2d_direct<false, true><<<grid, block, 0, s>>>(h->args);
-    } else {
-      vel2d_direct<false><<<grid, block, 0, s>>>(h->args);
-      if (h->has_beta) prs2d_direct<true, false><<<grid, block, 0, s>>>(h->args);
-      else prs2d_direct<false, false><<<grid, block, 0, s>>>(h->args);
-    }
+    vel3d_march<kMarchXC, CV, kMin><<<grid, block, 0, s>>>(h->args, tm.p);
+    prs3d_march<kMarchXC, CP, kMin><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
   } else {
     dim3 grid(t.n[2], t.n[1], t.n[0]), block(kD3TZ, kD3TY, kD3TX);
-    if (h->aniso) {
-      vel3d_direct<true><<<grid, block, 0, s>>>(h->args);
-      if (h->has_beta) prs3d_direct<true, true><<<grid, block, 0, s>>>(h->args);
-      else prs3d_direct<false, true><<<grid, block, 0, s>>>(h->args);
-    } else {
-      vel3d_direct<false><<<grid, block, 0, s>>>(h->args);
-      if (h->has_beta) prs3d_direct<true, false><<<grid, block, 0, s>>>(h->args);
-      else prs3d_direct<false, false><<<grid, block, 0, s>>>(h->args);
-    }
+    vel3d_direct<CV><<<grid, block, 0, s>>>(h->args);
+    prs3d_direct<CP><<<grid, block, 0, s>>>(h->args);
+  }
+}
+
+template <int ND, bool kBeta>
+void launch_nd(fw_handle* h, cudaStream_t s) {
+  if (h->exp)
+    launch_typed<ND, CellVelExpT<ND>, CellPrsExpT<ND, kBeta>, 3>(h, s);
+  else if (h->aniso)
+    launch_typed<ND, CellVelT<ND, true>, CellPrsT<ND, kBeta, true>, 2>(h, s);
+  else
+    launch_typed<ND, CellVelT<ND, false>, CellPrsT<ND, kBeta, false>, 3>(h, s);
+}
+
+void launch_step(fw_handle* h, cudaStream_t s) {
+  if (h->ndim == 2) {
+    if (h->has_beta) launch_nd<2, true>(h, s);
+    else launch_nd<2, false>(h, s);
+  } else {
+    if (h->has_beta) launch_nd<3, true>(h, s);
+    else launch_nd<3, false>(h, s);
   }
 }
 
@@ -311,8 +312,12 @@ int check_desc(const fw_desc* d) {
     return fail(nullptr, FW_ERR_ARGUMENT, "grid spacing and time step must be positive");
   if (d->isotropic != 0 && d->isotropic != 1)
     return fail(nullptr, FW_ERR_ARGUMENT, "isotropic must be 0 or 1 (got %d)", d->isotropic);
-  if (d->n_relax != 2)
-    return fail(nullptr, FW_ERR_UNSUPPORTED, "only n_relax = 2 is implemented (got %d)", d->n_relax);
+  if (d->n_relax != 2 && d->n_relax != 0)
+    return fail(nullptr, FW_ERR_UNSUPPORTED,
+                "n_relax must be 2 (relaxation engine) or 0 (exponential attenuation), got %d",
+                d->n_relax);
+  if (d->n_relax == 0 && d->isotropic != 1)
+    return fail(nullptr, FW_ERR_ARGUMENT, "the exponential-attenuation engine has no per-axis maps");
   return FW_OK;
 }
 
@@ -335,6 +340,7 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   h->ny = desc->ny;
   h->nz = desc->ndim == 3 ? desc->nz : 1;
   h->aniso = desc->isotropic == 0;
+  h->exp = desc->n_relax == 0;
   h->pitch = round_up(h->ndim == 2 ? h->ny : h->nz, 32);
   h->ncells_padded = h->ndim == 2 ? h->nx * h->pitch : h->nx * h->ny * h->pitch;
   h->n_out = (desc->nt + desc->mod_t - 1) / desc->mod_t;
@@ -408,6 +414,7 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
     A.m.ax[a][1] = own ? map_field(h, axis_map(a, 8)) : map_field(h, 11);
     A.m.bx[a][1] = own ? map_field(h, axis_map(a, 9)) : map_field(h, 12);
   }
+  A.m.a_exp = map_field(h, 5);  // exponential engine: a_exp in the first relaxation slot
   A.m.dcmap = h->dcmap;
   A.m.taps = h->taps;
   A.l.icmat_t = h->icmat_t;
@@ -435,19 +442,27 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
 
 namespace {
 
-int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an) {
+int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an,
+                    const float* a_exp) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   if (!f) return fail(h, FW_ERR_ARGUMENT, "fields is NULL");
+  if (h->exp != (a_exp != nullptr))
+    return fail(h, FW_ERR_ARGUMENT, h->exp ? "an exponential-attenuation handle (n_relax = 0) needs "
+                                             "fw_set_fields_exp"
+                                           : "a_exp given to a relaxation handle");
   if (h->aniso && !an)
     return fail(h, FW_ERR_ARGUMENT, "an anisotropic handle (isotropic = 0) needs fw_set_fields_aniso");
   if (!h->aniso && an)
     return fail(h, FW_ERR_ARGUMENT, "per-direction maps given to an isotropic handle");
   const fw_desc& d = h->d;
-  const float* need[] = {f->d, f->dmap, f->c, f->rho, f->K, f->beta, f->kappax, f->kappau,
-                         f->apmlu1, f->bpmlu1, f->apmlx1, f->bpmlx1, f->apmlu2, f->bpmlu2,
-                         f->apmlx2, f->bpmlx2};
+  const float* need[] = {f->d, f->dmap, f->c, f->rho, f->K, f->beta};
   for (const float* p : need)
     if (!p) return fail(h, FW_ERR_ARGUMENT, "a required map or table pointer is NULL");
+  const float* need_relax[] = {f->kappax, f->kappau, f->apmlu1, f->bpmlu1, f->apmlx1, f->bpmlx1,
+                               f->apmlu2, f->bpmlu2, f->apmlx2, f->bpmlx2};
+  if (!h->exp)
+    for (const float* p : need_relax)
+      if (!p) return fail(h, FW_ERR_ARGUMENT, "a required relaxation map pointer is NULL");
   if (!f->dcmap) return fail(h, FW_ERR_ARGUMENT, "dcmap is NULL");
   if ((d.ncoords && (!f->icc || (d.nt_ic && !f->icmat))) || (d.ncoordsout && !f->outc) ||
       (d.ncoordszero && !f->icczero))
@@ -567,9 +582,13 @@ int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an)
       {f->rho, 0}, {f->K, 1}, {f->beta, 2}, {f->kappau, 3}, {f->kappax, 4},
       {f->apmlu1, 5}, {f->bpmlu1, 6}, {f->apmlu2, 7}, {f->bpmlu2, 8},
       {f->apmlx1, 9}, {f->bpmlx1, 10}, {f->apmlx2, 11}, {f->bpmlx2, 12}};
-  for (auto& m : mapsrc)
+  for (auto& m : mapsrc) {
+    if (h->exp && m.idx >= 3) continue;  // no relaxation maps in the exponential engine
     if ((st = upload_grid(h, map_field(h, m.idx), m.src, sizeof(float), dev, s))) return st;
-  std::vector<int> kappa_maps = {3, 4};
+  }
+  if (h->exp && (st = upload_grid(h, map_field(h, 5), a_exp, sizeof(float), dev, s))) return st;
+  std::vector<int> kappa_maps;
+  if (!h->exp) kappa_maps = {3, 4};
   if (h->aniso) {
     // axis y: kappaw/apmlw*/bpmlw* (gradient), kappay/apmly*/bpmly* (divergence); axis z: v, z
     const float* per_axis[3][10] = {
@@ -628,11 +647,18 @@ int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an)
 
 extern "C" {
 
-int fw_set_fields(fw_handle* h, const fw_fields* f) { return set_fields_impl(h, f, nullptr); }
+int fw_set_fields(fw_handle* h, const fw_fields* f) {
+  return set_fields_impl(h, f, nullptr, nullptr);
+}
 
 int fw_set_fields_aniso(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an) {
   if (!an) return fail(h, FW_ERR_ARGUMENT, "per-direction maps are NULL");
-  return set_fields_impl(h, f, an);
+  return set_fields_impl(h, f, an, nullptr);
+}
+
+int fw_set_fields_exp(fw_handle* h, const fw_fields* f, const float* a_exp) {
+  if (!a_exp) return fail(h, FW_ERR_ARGUMENT, "a_exp is NULL");
+  return set_fields_impl(h, f, nullptr, a_exp);
 }
 
 int fw_set_source_signal(fw_handle* h, const float* icmat, int32_t on_device) {
@@ -780,7 +806,8 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   if (h->ndim != 2) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint is implemented for 2D grids");
   if (h->has_beta) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs beta = 0 everywhere");
-  if (h->aniso) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint covers the isotropic engine");
+  if (h->aniso || h->exp)
+    return fail(h, FW_ERR_UNSUPPORTED, "the adjoint covers the isotropic relaxation engine");
   if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called first");
   if (checkpoint_every < 1) return fail(h, FW_ERR_ARGUMENT, "checkpoint_every must be >= 1");
   const size_t state_elems = (size_t)h->ncells_padded * n_state(h->ndim);
@@ -960,7 +987,7 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
   for (int i = 0; i < n; ++i) {
     const fw_handle* h = handles[i];
     if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle %d is NULL", i);
-    if (h->ndim != 2 || h->variant != kDirect || h->aniso)
+    if (h->ndim != 2 || h->variant != kDirect || h->aniso || h->exp)
       return fail(nullptr, FW_ERR_UNSUPPORTED,
                   "group members must be isotropic 2D simulations (member %d)", i);
     if (!h->fields_set) return fail(nullptr, FW_ERR_STATE, "member %d has no fields set", i);

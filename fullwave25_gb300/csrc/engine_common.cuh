@@ -60,6 +60,7 @@ struct Maps {
   const float* bu[3][2];
   const float* ax[3][2];
   const float* bx[3][2];
+  const float* a_exp;        // exponential-attenuation engine: amplitude kept per field update
   const int32_t* dcmap;
   const float* taps;         // [ndmap][12]
 };
@@ -160,6 +161,45 @@ struct CellPrsT {
     }
     const float coef = kBeta ? fmaf(b2dt, pc, dtk) : dtk;
     A.f.p[c] = fmaf(-coef, div, pc);
+  }
+};
+
+// Exponential-attenuation engine (no memory variables, kappa = 1):
+//   v <- a_exp (v - dt/rho g);   p <- a_exp (p - dt (K + 2 beta p) sum_a d_a)
+template <int NDIM>
+struct CellVelExpT {
+  int dc;
+  float rr, ae, v[NDIM];
+  __device__ __forceinline__ void load(const StepArgs& A, int64_t c) {
+    dc = __ldg(A.m.dcmap + c);
+    rr = __ldg(A.m.rdt_rho + c);
+    ae = __ldg(A.m.a_exp + c);
+#pragma unroll
+    for (int a = 0; a < NDIM; ++a) v[a] = A.f.v[a][c];
+  }
+  __device__ __forceinline__ void update_store(const StepArgs& A, int64_t c, const float* g) {
+#pragma unroll
+    for (int a = 0; a < NDIM; ++a) A.f.v[a][c] = ae * fmaf(-rr, g[a], v[a]);
+  }
+};
+
+template <int NDIM, bool kBeta>
+struct CellPrsExpT {
+  int dc;
+  float dtk, b2dt, ae, pc;
+  __device__ __forceinline__ void load(const StepArgs& A, int64_t c) {
+    dc = __ldg(A.m.dcmap + c);
+    dtk = __ldg(A.m.dt_k + c);
+    b2dt = kBeta ? __ldg(A.m.beta2dt + c) : 0.f;
+    ae = __ldg(A.m.a_exp + c);
+    pc = A.f.p[c];
+  }
+  __device__ __forceinline__ void update_store(const StepArgs& A, int64_t c, const float* d) {
+    float div = 0.f;
+#pragma unroll
+    for (int a = 0; a < NDIM; ++a) div += d[a];
+    const float coef = kBeta ? fmaf(b2dt, pc, dtk) : dtk;
+    A.f.p[c] = ae * fmaf(-coef, div, pc);
   }
 };
 

@@ -16,7 +16,7 @@ constexpr int kD3TZ = 32, kD3TY = 4, kD3TX = 2;  // 3D tile
 // ---------------------------------------------------------------------------------------- 2D
 // Bodies take the tile (ty along y, tx along x) explicitly so that the single-simulation kernels
 // (tile = block index) and the group kernels (tile from a work list) share them.
-template <bool kAniso>
+template <class CV>
 __device__ __forceinline__ void vel2d_body(const StepArgs& A, int tile_y, int tile_x) {
   const Grid& g = A.g;
   const int j = kGhost + tile_y * kD2TY + threadIdx.x;
@@ -25,7 +25,7 @@ __device__ __forceinline__ void vel2d_body(const StepArgs& A, int tile_y, int ti
   const int64_t sx = g.sx;
   const int64_t c = i * sx + j;
   const float* __restrict__ p = A.f.p;
-  CellVelT<2, kAniso> cv;
+  CV cv;
   cv.load(A, c);
   float cm[8], co;
   load_taps(A.m.taps, cv.dc, cm, co);
@@ -41,7 +41,7 @@ __device__ __forceinline__ void vel2d_body(const StepArgs& A, int tile_y, int ti
   cv.update_store(A, c, gg);
 }
 
-template <bool kBeta, bool kAniso>
+template <class CP>
 __device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int tile_x, int tile) {
   const Grid& g = A.g;
   const int j = kGhost + tile_y * kD2TY + threadIdx.x;
@@ -52,7 +52,7 @@ __device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int ti
     const int64_t c = i * sx + j;
     const float* __restrict__ vx = A.f.v[0];
     const float* __restrict__ vy = A.f.v[1];
-    CellPrsT<2, kBeta, kAniso> cp;
+    CP cp;
     cp.load(A, c);
     float cm[8], co;
     load_taps(A.m.taps, cp.dc, cm, co);
@@ -70,15 +70,15 @@ __device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int ti
   tile_epilogue(A, p, tile, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
 }
 
-template <bool kAniso>
+template <class CV>
 __global__ void __launch_bounds__(256) vel2d_direct(const StepArgs A) {
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *A.step += 1;
-  vel2d_body<kAniso>(A, blockIdx.x, blockIdx.y);
+  vel2d_body<CV>(A, blockIdx.x, blockIdx.y);
 }
 
-template <bool kBeta, bool kAniso>
+template <class CP>
 __global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
-  prs2d_body<kBeta, kAniso>(A, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x);
+  prs2d_body<CP>(A, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // Group (batched) kernels: block b works on tiles[b] = {simulation, tile_y, tile_x, tile index
@@ -90,18 +90,18 @@ __global__ void __launch_bounds__(256) vel2d_group(const StepArgs* __restrict__ 
   const int4 t = tiles[blockIdx.x];
   const StepArgs& A = sims[t.x];
   if (t.w == 0 && threadIdx.x == 0 && threadIdx.y == 0) *A.step += 1;
-  vel2d_body<false>(A, t.y, t.z);
+  vel2d_body<CellVelT<2, false>>(A, t.y, t.z);
 }
 
 template <bool kBeta>
 __global__ void __launch_bounds__(256) prs2d_group(const StepArgs* __restrict__ sims,
                                                    const int4* __restrict__ tiles) {
   const int4 t = tiles[blockIdx.x];
-  prs2d_body<kBeta, false>(sims[t.x], t.y, t.z, t.w);
+  prs2d_body<CellPrsT<2, kBeta, false>>(sims[t.x], t.y, t.z, t.w);
 }
 
 // ---------------------------------------------------------------------------------------- 3D
-template <bool kAniso>
+template <class CV>
 __global__ void __launch_bounds__(256) vel3d_direct(const StepArgs A) {
   const Grid& g = A.g;
   const int k = kGhost + blockIdx.x * kD3TZ + threadIdx.x;
@@ -114,7 +114,7 @@ __global__ void __launch_bounds__(256) vel3d_direct(const StepArgs A) {
   const int64_t sx = g.sx, sy = g.sy;
   const int64_t c = i * sx + j * sy + k;
   const float* __restrict__ p = A.f.p;
-  CellVelT<3, kAniso> cv;
+  CV cv;
   cv.load(A, c);
   float cm[8], co;
   load_taps(A.m.taps, cv.dc, cm, co);
@@ -133,7 +133,7 @@ __global__ void __launch_bounds__(256) vel3d_direct(const StepArgs A) {
   cv.update_store(A, c, gg);
 }
 
-template <bool kBeta, bool kAniso>
+template <class CP>
 __global__ void __launch_bounds__(256) prs3d_direct(const StepArgs A) {
   const Grid& g = A.g;
   const int k = kGhost + blockIdx.x * kD3TZ + threadIdx.x;
@@ -146,7 +146,7 @@ __global__ void __launch_bounds__(256) prs3d_direct(const StepArgs A) {
     const float* __restrict__ vx = A.f.v[0];
     const float* __restrict__ vy = A.f.v[1];
     const float* __restrict__ vz = A.f.v[2];
-    CellPrsT<3, kBeta, kAniso> cp;
+    CP cp;
     cp.load(A, c);
     float cm[8], co;
     load_taps(A.m.taps, cp.dc, cm, co);

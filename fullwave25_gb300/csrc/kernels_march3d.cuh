@@ -31,8 +31,8 @@ struct MarchMaps {
   CUtensorMap p, vx, vy, vz;
 };
 
-template <int XC, bool kAniso>
-__global__ void __launch_bounds__(kMThreads, kAniso ? 2 : 3)
+template <int XC, class CV, int kMinBlocks = 3>
+__global__ void __launch_bounds__(kMThreads, kMinBlocks)
 vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
   __shared__ alignas(128) float ring[kRing][kPSlot];
   __shared__ alignas(8) uint64_t bar[kRing];
@@ -69,7 +69,7 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
     const int64_t c = (int64_t)x * sx + col;
     // point-wise operands of this plane: issued before the block barrier and the TMA wait so
     // their HBM latency overlaps them
-    CellVelT<3, kAniso> cv;
+    CV cv;
     if (active) cv.load(A, c);
     const float qn = (active && x + 9 < g.nx) ? __ldg(p + (int64_t)(x + 9) * sx + col) : 0.f;
     __syncthreads();  // the slot of plane x-2 is no longer read
@@ -112,8 +112,8 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
   }
 }
 
-template <int XC, bool kBeta, bool kAniso>
-__global__ void __launch_bounds__(kMThreads, kAniso ? 2 : 3)
+template <int XC, class CP, int kMinBlocks = 3>
+__global__ void __launch_bounds__(kMThreads, kMinBlocks)
 prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
             const __grid_constant__ CUtensorMap tm_vy, const __grid_constant__ CUtensorMap tm_vz) {
   __shared__ alignas(128) float rx[kRing][kXSlot];
@@ -155,7 +155,7 @@ prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
   for (int x = xb; x < xe; ++x) {
     const int it = x - xb;
     const int64_t c = (int64_t)x * sx + col;
-    CellPrsT<3, kBeta, kAniso> cp;
+    CP cp;
     if (active) cp.load(A, c);
     const float rn = active ? __ldg(vx + (int64_t)(x + 8) * sx + col) : 0.f;
     __syncthreads();

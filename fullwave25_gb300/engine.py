@@ -20,6 +20,7 @@ FW_STATUS = {0: "FW_OK", 1: "FW_ERR_ARGUMENT", 2: "FW_ERR_CUDA", 3: "FW_ERR_STAT
 
 # every symbol include/fwgb.h declares
 EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_fields_aniso",
+            "fw_set_fields_exp",
             "fw_set_source_signal",
             "fw_set_source_columns", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
@@ -93,6 +94,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_create": (C.c_int, [C.POINTER(FwDesc), C.POINTER(H)]),
         "fw_set_fields": (C.c_int, [H, C.POINTER(FwFields)]),
         "fw_set_fields_aniso": (C.c_int, [H, C.POINTER(FwFields), C.POINTER(FwFieldsAniso)]),
+        "fw_set_fields_exp": (C.c_int, [H, C.POINTER(FwFields), _FP]),
         "fw_set_source_signal": (C.c_int, [H, _FP, C.c_int32]),
         "fw_set_source_columns": (C.c_int, [H, vp, _FP, C.c_int32, C.c_int32, C.c_int32]),
         "fw_run": (C.c_int, [H, vp, _FP, C.c_int32]),
@@ -149,7 +151,8 @@ def desc_from_inputs(inp) -> FwDesc:
                   dy=inp.spacing[1], dz=dz,
                   dt=inp.dt, c0=inp.c0, ncoords=inp.icc.shape[0], ncoordsout=inp.outc.shape[0],
                   ncoordszero=inp.icczero.shape[0], ndmap=inp.dmap.shape[2],
-                  isotropic=int("kappay" not in inp.maps), n_relax=2)
+                  isotropic=int("kappay" not in inp.maps),
+                  n_relax=0 if "a_exp" in inp.maps else 2)
 
 
 class Engine:
@@ -198,9 +201,12 @@ class Engine:
             icc=_ip(f("icc", inp.icc, _c_i32)), outc=_ip(f("outc", inp.outc, _c_i32)),
             icczero=_ip(f("icczero", inp.icczero, _c_i32)),
             icmat=_fp(f("icmat", inp.icmat, _c_f32)),
-            **{k: _fp(f(k, m[k], _c_f32)) for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)},
+            **{k: _fp(f(k, m[k], _c_f32)) for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)
+               if k in m},
         )
-        if inp.isotropic:
+        if "a_exp" in m:
+            self._call("fw_set_fields_exp", C.byref(fields), _fp(f("a_exp", m["a_exp"], _c_f32)))
+        elif inp.isotropic:
             self._call("fw_set_fields", C.byref(fields))
         else:
             an = FwFieldsAniso(**{k: _fp(f(k, m[k], _c_f32))

@@ -34,6 +34,10 @@ class Grid:
         self.is_3d = len(self.domain_size) == 3
 
     @property
+    def omega(self) -> float:
+        return 2 * np.pi * self.f0
+
+    @property
     def wavelength(self) -> float:
         return self.c0 / self.f0
 

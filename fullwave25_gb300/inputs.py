@@ -81,6 +81,11 @@ class EngineInputs:
         return "kappay" not in self.maps
 
     @property
+    def exponential(self) -> bool:
+        """The exponential-attenuation engine (map a_exp, no relaxation memory variables)."""
+        return "a_exp" in self.maps
+
+    @property
     def n_cells(self) -> int:
         return int(np.prod(self.shape))
 
@@ -108,6 +113,8 @@ class EngineInputs:
         names = ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)
         if not self.isotropic:
             names += anisotropic_extra_maps(self.ndim)
+        if self.exponential:
+            names = ("c", "rho", "K", "beta", "a_exp")
         for name in names:
             if name not in self.maps:
                 raise ValueError(f"missing map {name}")
@@ -161,6 +168,26 @@ def build_inputs(grid, medium, source, sensor) -> EngineInputs:
     )
 
 
+def build_inputs_exponential(grid, medium, source, sensor) -> EngineInputs:
+    """In-memory equivalent of ``InputFileWriter`` with ``use_exponential_attenuation=True``
+    (input_file_writer.py:629-645): maps c, K, rho, beta, a_exp plus the shared contract."""
+    c = medium.sound_speed
+    maps = {"c": c.astype(np.float32), "rho": medium.density.astype(np.float32),
+            "K": medium.bulk_modulus.astype(np.float32), "beta": medium.beta.astype(np.float32),
+            "a_exp": medium.alpha_exp.astype(np.float32)}
+    spacing = (grid.dx, grid.dy, grid.dz) if grid.is_3d else (grid.dx, grid.dy)
+    return EngineInputs(
+        shape=tuple(grid.shape), nt=int(grid.nt), spacing=spacing, dt=grid.dt, c0=grid.c0,
+        mod_t=int(sensor.sampling_modulus_time),
+        d=coefficients.d_matrix(grid.cfl, is_3d=grid.is_3d),
+        dmap=coefficients.d_map(c, grid.dt, grid.dx, is_3d=grid.is_3d),
+        dcmap=coefficients.dc_map(c), maps=maps,
+        icc=source.incoords.astype(np.int32), icmat=np.asarray(source.icmat, dtype=np.float32),
+        outc=sensor.outcoords.astype(np.int32),
+        icczero=map_to_coords(medium.air_map).astype(np.int32).reshape(-1, grid.is_3d + 2),
+    )
+
+
 # -- simulation-directory (.dat) contract -------------------------------------------------------
 
 def _read(path: Path, dtype, count=-1) -> np.ndarray:
@@ -198,6 +225,8 @@ def read_simulation_dir(sim_dir: Path) -> EngineInputs:
     names = ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)
     if (sim_dir / "kappay.dat").exists():
         names += anisotropic_extra_maps(len(shape))
+    if (sim_dir / "a_exp.dat").exists() and not (sim_dir / "kappax.dat").exists():
+        names = ("c", "rho", "K", "beta", "a_exp")
     maps = {n: grid_map(n) for n in names}
     coords = lambda n, k: _read(sim_dir / f"{n}.dat", np.int32).reshape(k, ndim)  # noqa: E731
     icczero = (coords("icczero", ncoordszero) if ncoordszero

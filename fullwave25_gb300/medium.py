@@ -125,3 +125,51 @@ class MediumRelaxationMaps:
 
     def build(self) -> "MediumRelaxationMaps":
         return self
+
+
+class Medium:
+    """Medium given by attenuation maps (mirrors ``fullwave/medium.py:753-1156``).
+
+    ``build()`` maps (alpha0, gamma) to relaxation parameters by table lookup
+    (:class:`fullwave25_gb300.relaxation.RelaxationTable`; the reference's ``.mat`` table when
+    one is given, else the stand-in table) and returns a :class:`MediumRelaxationMaps`;
+    ``build_exponential()`` returns the exponential-attenuation medium (medium.py:1068-1111).
+    """
+
+    def __init__(self, grid, sound_speed, density, alpha_coeff, alpha_power, beta, *,
+                 air_map=None, relaxation_table=None, n_relaxation_mechanisms: int = 2,
+                 use_isotropic_relaxation: bool = True) -> None:
+        if n_relaxation_mechanisms != 2:
+            raise ValueError("Only n_relaxation_mechanisms=2 are supported currently.")
+        self.grid = grid
+        self.is_3d = grid.is_3d
+        self.sound_speed = np.atleast_2d(np.asarray(sound_speed, dtype=np.float64))
+        self.density = np.atleast_2d(np.asarray(density, dtype=np.float64))
+        self.alpha_coeff = np.atleast_2d(np.asarray(alpha_coeff, dtype=np.float64))
+        self.alpha_power = np.atleast_2d(np.asarray(alpha_power, dtype=np.float64))
+        self.beta = np.atleast_2d(np.asarray(beta, dtype=np.float64))
+        self.air_map = (np.zeros_like(self.sound_speed, dtype=bool) if air_map is None
+                        else np.asarray(air_map))
+        self.relaxation_table = relaxation_table
+        self.n_relaxation_mechanisms = n_relaxation_mechanisms
+        self.use_isotropic_relaxation = use_isotropic_relaxation
+
+    @property
+    def bulk_modulus(self):
+        return np.multiply(self.sound_speed**2, self.density)
+
+    def build(self) -> MediumRelaxationMaps:
+        from .relaxation import default_table  # noqa: PLC0415
+
+        table = self.relaxation_table or default_table()
+        params = table.lookup(self.alpha_coeff, self.alpha_power)
+        return MediumRelaxationMaps(self.grid, self.sound_speed, self.density, self.beta, params,
+                                    air_map=self.air_map,
+                                    use_isotropic_relaxation=self.use_isotropic_relaxation)
+
+    def build_exponential(self):
+        from .exponential import MediumExponentialAttenuation, db_mhz_cm_to_a_exp  # noqa: PLC0415
+
+        return MediumExponentialAttenuation(self.grid, self.sound_speed, self.density,
+                                            db_mhz_cm_to_a_exp(self.alpha_coeff, self.grid),
+                                            self.beta, air_map=self.air_map)

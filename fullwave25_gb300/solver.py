@@ -14,7 +14,9 @@ from pathlib import Path
 
 import numpy as np
 
-from .inputs import build_inputs, write_simulation_dir
+from .exponential import PMLBuilderExponentialAttenuation
+from .inputs import build_inputs, build_inputs_exponential, write_simulation_dir
+from .medium import Medium
 from .pml import PMLBuilder
 from .source import Sensor
 
@@ -29,8 +31,6 @@ class Solver:
                  run_on_memory: bool = False, use_gpu: bool = True,
                  use_exponential_attenuation: bool = False, use_isotropic_relaxation: bool = True,
                  cuda_device_id: str | int | list | None = None) -> None:
-        if use_exponential_attenuation:
-            raise NotImplementedError("the exponential-attenuation engine is not implemented")
         if not use_gpu:
             raise NotImplementedError("Currently, only GPU version is supported.")
         if transducer is not None:
@@ -56,11 +56,22 @@ class Solver:
             n_transition_layer = grid.ppw * 3
         self.cuda_device_id = cuda_device_id
         self.use_isotropic_relaxation = use_isotropic_relaxation
+        self.use_exponential_attenuation = use_exponential_attenuation
         medium.use_isotropic_relaxation = use_isotropic_relaxation   # as solver.py:457-476 does
-        self.pml_builder = PMLBuilder(grid, medium, source, sensor, m_spatial_order=m_spatial_order,
-                                      n_pml_layer=pml_layer_thickness_px,
-                                      n_transition_layer=n_transition_layer,
-                                      use_isotropic_relaxation=use_isotropic_relaxation)
+        if use_exponential_attenuation:
+            if not isinstance(medium, Medium):
+                raise TypeError("the exponential-attenuation engine needs a Medium (alpha_coeff)")
+            self.pml_builder = PMLBuilderExponentialAttenuation(
+                grid, medium.sound_speed, medium.density, medium.alpha_coeff, medium.beta,
+                source, sensor, air_map=medium.air_map, m_spatial_order=m_spatial_order,
+                n_pml_layer=pml_layer_thickness_px)
+        else:
+            maps = medium.build() if isinstance(medium, Medium) else medium
+            self.pml_builder = PMLBuilder(grid, maps, source, sensor,
+                                          m_spatial_order=m_spatial_order,
+                                          n_pml_layer=pml_layer_thickness_px,
+                                          n_transition_layer=n_transition_layer,
+                                          use_isotropic_relaxation=use_isotropic_relaxation)
         self.last_timing: dict = {}
 
     @staticmethod
@@ -70,6 +81,12 @@ class Solver:
     def build_engine_inputs(self, *, record_whole_domain: bool = False,
                             sampling_modulus_time_whole_domain: int = 1):
         ext_medium = self.pml_builder.run(use_pml=self.use_pml)
+        if self.use_exponential_attenuation:
+            sensor = (Sensor(np.ones(self.pml_builder.extended_grid.shape, dtype=bool),
+                             sampling_modulus_time=sampling_modulus_time_whole_domain)
+                      if record_whole_domain else self.pml_builder.extended_sensor)
+            return build_inputs_exponential(self.pml_builder.extended_grid, ext_medium,
+                                            self.pml_builder.extended_source, sensor), sensor
         if not self.use_isotropic_relaxation and not self.use_pml:
             ext_medium.relaxation_param_dict_for_fw2 = ext_medium.calc_relaxation_param_dict_for_fw2(
                 use_isotropic_relaxation=False)

@@ -56,7 +56,8 @@ typedef struct fw_desc {
     int32_t ndmap;          /* tap sets in dmap */
     int32_t isotropic;      /* 1: isotropic relaxation maps (fw_set_fields); 0: one set of maps
                                per derivative axis (fw_set_fields_aniso) */
-    int32_t n_relax;        /* must be 2 relaxation mechanisms */
+    int32_t n_relax;        /* 2: the relaxation engine; 0: the exponential-attenuation engine
+                               (fw_set_fields_exp, no relaxation maps) */
 } fw_desc;
 
 /* Arrays of the file contract. Maps are float32 [nx*ny*nz] C order; dcmap int32 of the same
@@ -107,6 +108,12 @@ FWGB_API int fw_set_fields(fw_handle *h, const fw_fields *f);
 /* fw_set_fields for a handle created with isotropic = 0 (the anisotropic build,
  * use_isotropic_relaxation=False in the reference: medium.py:374-406). */
 FWGB_API int fw_set_fields_aniso(fw_handle *h, const fw_fields *f, const fw_fields_aniso *an);
+
+/* fw_set_fields for a handle created with n_relax = 0: the exponential-attenuation build
+ * (use_exponential_attenuation=True in the reference: medium.py:560-750, input_file_writer.py:
+ * 629-645). The relaxation map pointers of `f` are ignored; `a_exp` is the per-cell amplitude kept
+ * per field update (same layout and on_device flag as the other maps). */
+FWGB_API int fw_set_fields_exp(fw_handle *h, const fw_fields *f, const float *a_exp);
 
 /* Replace only the source signals (a new transmit event on the same medium), float32
  * [ncoords][nt_ic]. Replaces: the is_static_map re-run that rewrites icmat.dat only

@@ -38,6 +38,7 @@ typedef struct {
     const float *au[3][2], *bu[3][2], *ax[3][2], *bx[3][2];
     const int32_t *icc, *outc, *icczero;
     const float *icmat; /* [ncoords][nt_ic] */
+    const float *a_exp; /* non-NULL: exponential-attenuation engine (no memory variables) */
 } oracle_desc;
 
 typedef struct {
@@ -45,7 +46,7 @@ typedef struct {
     int64_t cells, s[3];
     double *p, *v[3], *psi[3][2], *phi[3][2];
     double *taps;   /* per cell: 9 values */
-    double *rdt_rho, *dtk, *b2dt, *iku[3], *ikx[3];
+    double *rdt_rho, *dtk, *b2dt, *iku[3], *ikx[3], *aexp;
     int has_beta;
     int64_t *icc_lin, *outc_lin, *zero_lin;
     int32_t *src_keep;
@@ -81,7 +82,8 @@ oracle_state *oracle_create(const oracle_desc *d) {
                          &o->psi[1][0], &o->psi[1][1], &o->psi[2][0], &o->psi[2][1],
                          &o->phi[0][0], &o->phi[0][1], &o->phi[1][0], &o->phi[1][1],
                          &o->phi[2][0], &o->phi[2][1], &o->rdt_rho, &o->dtk, &o->b2dt,
-                         &o->iku[0], &o->iku[1], &o->iku[2], &o->ikx[0], &o->ikx[1], &o->ikx[2]};
+                         &o->iku[0], &o->iku[1], &o->iku[2], &o->ikx[0], &o->ikx[1], &o->ikx[2],
+                         &o->aexp};
     for (size_t f = 0; f < sizeof fields / sizeof fields[0]; ++f) {
         *fields[f] = calloc((size_t)n, sizeof(double));
         if (!*fields[f]) return NULL;
@@ -95,6 +97,10 @@ oracle_state *oracle_create(const oracle_desc *d) {
         o->dtk[c] = d->dt * (double)d->K[c];
         o->b2dt[c] = 2.0 * d->dt * (double)d->beta[c];
         if (d->beta[c] != 0.f) o->has_beta = 1;
+        if (d->a_exp) {
+            o->aexp[c] = (double)d->a_exp[c];
+            continue;
+        }
         for (int a = 0; a < d->ndim; ++a) {
             o->iku[a][c] = 1.0 / (double)d->kappau[a][c];
             o->ikx[a][c] = 1.0 / (double)d->kappax[a][c];
@@ -124,7 +130,7 @@ void oracle_destroy(oracle_state *o) {
                         o->psi[1][0], o->psi[1][1], o->psi[2][0], o->psi[2][1], o->phi[0][0],
                         o->phi[0][1], o->phi[1][0], o->phi[1][1], o->phi[2][0], o->phi[2][1],
                         o->rdt_rho, o->dtk, o->b2dt, o->iku[0], o->iku[1], o->iku[2],
-                        o->ikx[0], o->ikx[1], o->ikx[2], o->taps};
+                        o->ikx[0], o->ikx[1], o->ikx[2], o->aexp, o->taps};
     for (size_t f = 0; f < sizeof fields / sizeof fields[0]; ++f) free(fields[f]);
     free(o->icc_lin); free(o->outc_lin); free(o->zero_lin); free(o->src_keep);
     free(o);
@@ -142,8 +148,55 @@ void oracle_destroy(oracle_state *o) {
             }                                                                                \
         }
 
+static void step_exponential(oracle_state *o) {
+    const int nd = o->d.ndim;
+    for (int a = 0; a < nd; ++a) {
+        const int64_t sa = o->s[a];
+        const double h = o->d.h[a];
+        double *p = o->p, *va = o->v[a];
+        BODY_LOOP(o, {
+            const double *t = o->taps + c * 9;
+            double acc = 0.0, off = 0.0;
+            for (int m = 1; m <= 8; ++m) acc += t[m - 1] * (p[c + m * sa] - p[c - (m - 1) * sa]);
+            for (int b = 0; b < nd; ++b) {
+                if (b == a) continue;
+                const int64_t sb = o->s[b];
+                off += p[c + sa + sb] - p[c + sb];
+                off += p[c + sa - sb] - p[c - sb];
+            }
+            const double g = (acc + t[8] * off) / h;
+            va[c] = o->aexp[c] * (va[c] - o->rdt_rho[c] * g);
+        })
+    }
+    double *p = o->p;
+    BODY_LOOP(o, {
+        const double *t = o->taps + c * 9;
+        double dsum = 0.0;
+        for (int a = 0; a < nd; ++a) {
+            const int64_t sa = o->s[a];
+            const double *g = o->v[a];
+            double acc = 0.0, off = 0.0;
+            for (int m = 1; m <= 8; ++m) acc += t[m - 1] * (g[c + (m - 1) * sa] - g[c - m * sa]);
+            for (int b = 0; b < nd; ++b) {
+                if (b == a) continue;
+                const int64_t sb = o->s[b];
+                off += g[c + sb] - g[c - sa + sb];
+                off += g[c - sb] - g[c - sa - sb];
+            }
+            dsum += (acc + t[8] * off) / o->d.h[a];
+        }
+        const double pb = p[c];
+        const double coef = o->has_beta ? o->dtk[c] + o->b2dt[c] * pb : o->dtk[c];
+        p[c] = o->aexp[c] * (pb - coef * dsum);
+    })
+}
+
 void oracle_step(oracle_state *o, double *record_row) {
     const int nd = o->d.ndim;
+    if (o->d.a_exp) {
+        step_exponential(o);
+        goto finish;
+    }
     for (int a = 0; a < nd; ++a) {
         const int64_t sa = o->s[a];
         const double h = o->d.h[a];
@@ -192,6 +245,7 @@ void oracle_step(oracle_state *o, double *record_row) {
             else p[c] = pb - o->dtk[c] * dsum;
         })
     }
+finish:;
     const int n = o->step;
     if (n < o->d.nt_ic)
         for (int q = 0; q < o->n_keep; ++q) {

@@ -30,6 +30,9 @@ Scheme restated from these reference sources:
 * Leapfrog: velocities then pressure each step; body region ``[8, n-8)`` on every axis (the
   8-cell ghost layer of pml_builder.py:270-276); ghost cells stay zero.
 * Nonlinearity: ``p <- p - dT (K + 2 beta p) div`` (beta = 0 in every benchmark workload).
+* Exponential-attenuation engine (maps ``a_exp`` instead of relaxation maps): no memory
+  variables, ``kappa = 1``; after each field update the field is multiplied by ``a_exp``
+  (``exp(-dt alpha c0 / 2)``, so the two updates of a step attenuate by ``exp(-dt alpha c0)``).
 * Source: hard source ``p[icc[k]] = icmat[k, n]`` for ``n < nTic`` after the pressure update;
   air cells ``icczero`` forced to zero; sensors recorded after that whenever ``n % modT == 0``
   (fullwave/source.py:25-77, fullwave/sensor.py:24-50, input_file_writer.py:753-762).
@@ -92,6 +95,13 @@ class Oracle:
         self.dt_k = self.dt * m["K"]
         self.beta2dt = 2.0 * self.dt * m["beta"]
         self.has_beta = bool(np.any(m["beta"] != 0))
+        # exponential-attenuation engine: no relaxation maps; each field update is followed by
+        # a multiplication with a_exp (fullwave/medium.py:1068-1090)
+        self.a_exp = m.get("a_exp")
+        if self.a_exp is not None:
+            self.axis_u = self.axis_x = [None] * nd
+            self._init_io(inputs)
+            return
         self.inv_kappa_u = 1.0 / m["kappau"]
         self.inv_kappa_x = 1.0 / m["kappax"]
         self.au = (m["apmlu1"], m["apmlu2"])
@@ -108,6 +118,10 @@ class Oracle:
         self.axis_x = [(1.0 / m[f"kappa{dl[a]}"], (m[f"apml{dl[a]}1"], m[f"apml{dl[a]}2"]),
                         (m[f"bpml{dl[a]}1"], m[f"bpml{dl[a]}2"])) if not iso else None
                        for a in range(nd)]
+        self._init_io(inputs)
+
+    def _init_io(self, inputs):
+        f64 = lambda a: np.asarray(a, dtype=np.float32).astype(np.float64)  # noqa: E731
         lin = lambda c: (np.ravel_multi_index(tuple(np.asarray(c).T), self.shape)  # noqa: E731
                          if len(c) else np.zeros(0, np.int64))
         self.icc = lin(inputs.icc)
@@ -162,6 +176,8 @@ class Oracle:
     # -- one time step ------------------------------------------------------------------------
     def step(self, record=None):
         st, body, n = self.state, _body(self.shape), self.step_index
+        if self.a_exp is not None:
+            return self._step_exponential(record)
         for a in range(self.nd):
             ik, au, bu = self.axis_u[a] or (self.inv_kappa_u, self.au, self.bu)
             g = self.grad(st.p, a)
@@ -180,6 +196,30 @@ class Oracle:
             st.p[body] = pb - (self.dt_k + self.beta2dt * pb) * div
         else:
             st.p[body] = pb - self.dt_k * div
+        flat = st.p.reshape(-1)
+        if n < self.icmat.shape[1] and self.src_keep.size:
+            flat[self.icc[self.src_keep]] = self.icmat[self.src_keep, n]
+        if self.icczero.size:
+            flat[self.icczero] = 0.0
+        if record is not None and n % self.inp.mod_t == 0:
+            record[n // self.inp.mod_t] = flat[self.outc]
+        self.step_index += 1
+
+    def _step_exponential(self, record):
+        """v <- a_exp (v - dt/rho D p);  p <- a_exp (p - dt (K + 2 beta p) sum_a D'_a v_a)."""
+        st, body, n = self.state, _body(self.shape), self.step_index
+        for a in range(self.nd):
+            st.v[a][body] = self.a_exp * (st.v[a][body] - self.rdt_rho * self.grad(st.p, a))
+        div = np.zeros(tuple(k - 2 * GHOST for k in self.shape))
+        for a in range(self.nd):
+            div += self.div_component(st.v[a], a)
+        pb = st.p[body]
+        coef = self.dt_k + self.beta2dt * pb if self.has_beta else self.dt_k
+        st.p[body] = self.a_exp * (pb - coef * div)
+        self._finish_step(record)
+
+    def _finish_step(self, record):
+        st, n = self.state, self.step_index
         flat = st.p.reshape(-1)
         if n < self.icmat.shape[1] and self.src_keep.size:
             flat[self.icc[self.src_keep]] = self.icmat[self.src_keep, n]

@@ -30,7 +30,7 @@ class OracleDesc(C.Structure):
                 ("dmap", _FP), ("dcmap", _IP), ("rho", _FP), ("K", _FP), ("beta", _FP),
                 ("kappau", _FP * 3), ("kappax", _FP * 3), ("au", (_FP * 2) * 3),
                 ("bu", (_FP * 2) * 3), ("ax", (_FP * 2) * 3), ("bx", (_FP * 2) * 3),
-                ("icc", _IP), ("outc", _IP), ("icczero", _IP), ("icmat", _FP)]
+                ("icc", _IP), ("outc", _IP), ("icczero", _IP), ("icmat", _FP), ("a_exp", _FP)]
 
 
 def build(force: bool = False) -> Path:
@@ -76,6 +76,11 @@ class OracleC:
         gl = ["u"] * 3 if iso else ["u", "w", "v"]
         dl = ["x"] * 3 if iso else ["x", "y", "z"]
         nd = inp.ndim
+        exp = "a_exp" in m
+        if exp:  # the exponential engine has no relaxation maps; pass the K map as filler
+            for ax in ("u", "x"):
+                k[f"kappa{ax}"] = k[f"apml{ax}1"] = k[f"apml{ax}2"] = k["K"]
+                k[f"bpml{ax}1"] = k[f"bpml{ax}2"] = k["K"]
         fp = lambda a: a.ctypes.data_as(_FP)  # noqa: E731
         ip = lambda a: a.ctypes.data_as(_IP) if a.size else None  # noqa: E731
         shape = list(inp.shape) + [1] * (3 - inp.ndim)
@@ -97,7 +102,7 @@ class OracleC:
                        bx=((_FP * 2) * 3)(*[(_FP * 2)(fp(k[f"bpml{dl[a]}1"]), fp(k[f"bpml{dl[a]}2"]))
                                            for a in range(nd)]),
                        icc=ip(k["icc"]), outc=ip(k["outc"]), icczero=ip(k["icczero"]),
-                       icmat=fp(k["icmat"]))
+                       icmat=fp(k["icmat"]), a_exp=fp(k["a_exp"]) if exp else None)
         self._desc = d
         self.lib = _load()
         self.h = self.lib.oracle_create(C.byref(d))

@@ -7,7 +7,8 @@ from pathlib import Path
 import numpy as np
 
 HERE = Path(__file__).resolve().parent
-CASE_NAMES = ("2d_small", "2d_air_beta", "2d_nopml", "3d_small", "2d_aniso", "3d_aniso")
+CASE_NAMES = ("2d_small", "2d_air_beta", "2d_nopml", "3d_small", "2d_aniso", "3d_aniso",
+              "2d_exp", "3d_exp")
 
 
 def load_case(name: str):
@@ -46,6 +47,15 @@ def rebuild_case_inputs(name: str):
     shape = tuple(int(v) for v in z["shape"])
     g = Grid.from_cells(shape, f0=float(z["f0"]), nt=int(z["nt"]), ppw=int(z["ppw"]),
                         cfl=float(z["cfl"]))
+    if "alpha_coeff" in z.files:  # exponential-attenuation case
+        from fullwave25_gb300.exponential import PMLBuilderExponentialAttenuation  # noqa: PLC0415
+        from fullwave25_gb300.inputs import build_inputs_exponential  # noqa: PLC0415
+
+        b = PMLBuilderExponentialAttenuation(
+            g, z["c"], z["rho"], z["alpha_coeff"], np.zeros(shape), Source(z["p0"], z["src_mask"]),
+            Sensor(z["sens_mask"], int(z["mod_t"])), n_pml_layer=int(z["n_pml"]))
+        m = b.run(use_pml=bool(z["use_pml"]))
+        return build_inputs_exponential(b.extended_grid, m, b.extended_source, b.extended_sensor)
     relax = {k[6:]: z[k] for k in z.files if k.startswith("relax/")}
     iso = bool(z["isotropic"]) if "isotropic" in z.files else True
     med = MediumRelaxationMaps(g, z["c"], z["rho"], z["beta"], relax, air_map=z["air_map"],

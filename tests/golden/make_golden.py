@@ -149,6 +149,63 @@ def build_case(fw, name, spec, tmp: Path):
     print(f"case {name}: extended grid {builder.extended_grid.shape}, {len(files)} files")
 
 
+EXP_CASES = {
+    # name: (shape, f0, nt, ppw, cfl, n_pml, mod_t, use_pml)
+    "2d_exp": ((36, 30), 3e6, 160, 12, 0.2, 8, 1, True),
+    "3d_exp": ((14, 12, 12), 2e6, 90, 10, 0.2, 4, 2, True),
+}
+
+
+def build_exp_case(fw, name, spec, tmp: Path):
+    """Exponential-attenuation input set (PMLBuilderExponentialAttenuation + InputFileWriter
+    with use_exponential_attenuation=True). The relaxation lookup table is not read on this
+    path; Medium only checks that its file exists, so an empty placeholder is passed."""
+    shape, f0, nt, ppw, cfl, n_pml, mod_t, use_pml = spec
+    rng = np.random.default_rng(sum(map(ord, name)))
+    c0 = 1540.0
+    dx = c0 / f0 / ppw
+    dt = cfl * dx / c0
+    grid = fw.Grid(domain_size=tuple(n * dx for n in shape), f0=f0, duration=nt * dt, c0=c0,
+                   ppw=ppw, cfl=cfl)
+    c = smooth(rng, shape, 1480.0, 1620.0)
+    rho = smooth(rng, shape, 950.0, 1080.0)
+    a0 = smooth(rng, shape, 0.2, 1.2)
+    placeholder = tmp / "lut_placeholder.mat"
+    placeholder.write_bytes(b"")
+    medium = fw.Medium(grid, c, rho, a0, np.full(shape, 1.1), np.zeros(shape),
+                       path_relaxation_parameters_database=placeholder)
+    src_mask = np.zeros(shape, dtype=bool)
+    src_mask[0] = True
+    n_src = int(src_mask.sum())
+    p0 = np.tile(fw.utils.pulse.gaussian_modulated_sinusoidal_signal(
+        nt=nt, duration=grid.duration, ncycles=2, drop_off=2, f0=f0, p0=1e5), (n_src, 1))
+    source = fw.Source(p0, src_mask)
+    sens_mask = np.zeros(shape, dtype=bool)
+    sens_mask[4] = True
+    sensor = fw.Sensor(sens_mask, sampling_modulus_time=mod_t)
+
+    from fullwave.solver.input_file_writer import InputFileWriter  # noqa: PLC0415
+    from fullwave.solver.pml_builder import PMLBuilderExponentialAttenuation  # noqa: PLC0415
+
+    builder = PMLBuilderExponentialAttenuation(grid, medium, source, sensor, m_spatial_order=8,
+                                               n_pml_layer=n_pml)
+    ext_medium = builder.run(use_pml=use_pml)
+    dummy_bin = tmp / "engine_placeholder"
+    dummy_bin.write_text("placeholder\n")
+    writer = InputFileWriter(work_dir=tmp / "work", grid=builder.extended_grid,
+                             medium=ext_medium, source=builder.extended_source,
+                             sensor=builder.extended_sensor, path_fullwave_simulation_bin=dummy_bin,
+                             use_exponential_attenuation=True)
+    sim_dir = writer.run(name)
+    files = {f"dat/{p.stem}": np.frombuffer(p.read_bytes(), dtype=np.uint8)
+             for p in sorted(sim_dir.glob("*.dat"))}
+    scenario = {"shape": np.array(shape), "f0": f0, "nt": nt, "ppw": ppw, "cfl": cfl,
+                "n_pml": n_pml, "mod_t": mod_t, "use_pml": use_pml, "c": c, "rho": rho,
+                "alpha_coeff": a0, "p0": p0, "src_mask": src_mask, "sens_mask": sens_mask}
+    np.savez_compressed(HERE / f"case_{name}.npz", **files, **scenario)
+    print(f"exp case {name}: extended grid {builder.extended_grid.shape}, {len(files)} files")
+
+
 def coefficient_tables(fw, tmp: Path):
     from fullwave.solver.input_file_writer import InputFileWriter  # noqa: PLC0415
 
@@ -188,6 +245,8 @@ def main():
         coefficient_tables(fw, tmp)
         for name, spec in CASES.items():
             build_case(fw, name, spec, tmp)
+        for name, spec in EXP_CASES.items():
+            build_exp_case(fw, name, spec, tmp)
 
 
 if __name__ == "__main__":

@@ -33,7 +33,7 @@ def test_direction_dependent_maps_match_oracle(engine_lib, cuda, name):
 
 
 def test_aniso_march_equals_direct_bitwise(engine_lib, cuda):
-    from test_gpu_parity import _engine_with_variant
+    from helpers import engine_with_variant as _engine_with_variant
 
     inp = _skew(load_case_inputs("3d_aniso"))
     with _engine_with_variant(inp, "march") as a, _engine_with_variant(inp, "direct") as b:

@@ -142,20 +142,7 @@ def test_full_size_determinism_linearity_shift(engine_lib, cuda, plain_2d_full):
     assert not d[:shift].any()
 
 
-def _engine_with_variant(inp, variant):
-    import os
-
-    from fullwave25_gb300.engine import Engine
-
-    old = os.environ.get("FWGB_VARIANT")
-    os.environ["FWGB_VARIANT"] = variant
-    try:
-        return Engine(inp, validate=False)
-    finally:
-        if old is None:
-            del os.environ["FWGB_VARIANT"]
-        else:
-            os.environ["FWGB_VARIANT"] = old
+from helpers import engine_with_variant as _engine_with_variant  # noqa: E402
 
 
 @pytest.fixture(scope="module")
