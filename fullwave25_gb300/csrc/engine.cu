@@ -63,6 +63,9 @@ struct fw_handle {
   float* traces = nullptr;     // [n_out][ncoordsout]
   int* step = nullptr;
   void* lists = nullptr;       // one allocation for all per-tile lists
+  std::vector<int32_t> rec_k_host;   // sensor index of each record entry (entry order)
+  void* groups = nullptr;      // rec_group (int32) + rec_w (float) per record entry
+  int32_t n_cols = 0;          // trace row length: ncoordsout, or n_groups with sensor groups
   size_t bytes = 0;
   bool has_beta = false, fields_set = false;
   bool aniso = false;          // per-axis relaxation maps (the anisotropic engine)
@@ -344,6 +347,7 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   h->pitch = round_up(h->ndim == 2 ? h->ny : h->nz, 32);
   h->ncells_padded = h->ndim == 2 ? h->nx * h->pitch : h->nx * h->ny * h->pitch;
   h->n_out = (desc->nt + desc->mod_t - 1) / desc->mod_t;
+  h->n_cols = desc->ncoordsout;
   {
     const char* v = std::getenv("FWGB_VARIANT");
     h->variant = (h->ndim == 3 && !(v && std::strcmp(v, "direct") == 0)) ? kMarch : kDirect;
@@ -563,6 +567,21 @@ int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an,
   for (size_t e = 0; e < es.size(); ++e) { src_k[e] = es[e].k; src_cell[e] = es[e].cell; }
   for (size_t e = 0; e < ez.size(); ++e) zero_cell[e] = ez[e].cell;
   for (size_t e = 0; e < eo.size(); ++e) { rec_k[e] = eo[e].k; rec_cell[e] = eo[e].cell; }
+  h->rec_k_host.assign(rec_k, rec_k + eo.size());
+  if (h->groups) {  // new sensor lists: previous groups no longer apply
+    cudaFree(h->groups);
+    h->groups = nullptr;
+    h->args.l.rec_group = nullptr;
+    h->args.l.rec_w = nullptr;
+    if (h->n_cols != d.ncoordsout) {
+      cudaFree(h->traces);
+      h->traces = nullptr;
+      FW_CUDA(h, cudaMalloc(&h->traces, (size_t)h->n_out * std::max(d.ncoordsout, 1) * sizeof(float)));
+      h->args.l.traces = h->traces;
+    }
+    h->n_cols = d.ncoordsout;
+    h->args.l.ncoordsout = d.ncoordsout;
+  }
   if (h->lists) { cudaFree(h->lists); h->lists = nullptr; }
   FW_CUDA(h, cudaMalloc(&h->lists, blob.size()));
   FW_CUDA(h, cudaMemcpy(h->lists, blob.data(), blob.size(), cudaMemcpyHostToDevice));
@@ -683,6 +702,57 @@ int fw_set_source_signal(fw_handle* h, const float* icmat, int32_t on_device) {
   return FW_OK;
 }
 
+int fw_set_sensor_groups(fw_handle* h, const int32_t* group_of_sensor, const float* weight,
+                         int32_t n_groups) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called first");
+  if (n_groups < 0 || (n_groups > 0 && (!group_of_sensor || !weight)))
+    return fail(h, FW_ERR_ARGUMENT, "bad sensor groups");
+  const fw_desc& d = h->d;
+  if (h->graph) {
+    cudaGraphExecDestroy(h->graph);
+    h->graph = nullptr;
+    h->graph_steps = 0;
+  }
+  if (h->groups) {
+    cudaFree(h->groups);
+    h->groups = nullptr;
+  }
+  const int32_t cols = n_groups > 0 ? n_groups : d.ncoordsout;
+  if (cols != h->n_cols) {
+    cudaFree(h->traces);
+    h->traces = nullptr;
+    FW_CUDA(h, cudaMalloc(&h->traces, (size_t)h->n_out * std::max(cols, 1) * sizeof(float)));
+    h->args.l.traces = h->traces;
+    h->n_cols = cols;
+  }
+  h->args.l.ncoordsout = cols;
+  h->args.l.rec_group = nullptr;
+  h->args.l.rec_w = nullptr;
+  if (n_groups > 0) {
+    const size_t ne = h->rec_k_host.size();
+    std::vector<int32_t> grp(ne);
+    std::vector<float> w(ne);
+    for (size_t e = 0; e < ne; ++e) {
+      const int k = h->rec_k_host[e];
+      grp[e] = group_of_sensor[k];
+      w[e] = weight[k];
+      if (grp[e] >= n_groups) return fail(h, FW_ERR_ARGUMENT, "sensor %d: group %d >= %d", k, grp[e], n_groups);
+    }
+    FW_CUDA(h, cudaMalloc(&h->groups, ne * 8 + 16));
+    int32_t* dg = static_cast<int32_t*>(h->groups);
+    float* dw = reinterpret_cast<float*>(dg + ne);
+    FW_CUDA(h, cudaMemcpy(dg, grp.data(), ne * 4, cudaMemcpyHostToDevice));
+    FW_CUDA(h, cudaMemcpy(dw, w.data(), ne * 4, cudaMemcpyHostToDevice));
+    h->args.l.rec_group = dg;
+    h->args.l.rec_w = dw;
+  }
+  int st = fw_reset(h, h->capture_stream);
+  if (st) return st;
+  FW_CUDA(h, cudaStreamSynchronize(h->capture_stream));
+  return FW_OK;
+}
+
 int fw_set_source_columns(fw_handle* h, void* stream, const float* cols, int32_t n0,
                           int32_t ncols, int32_t on_device) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
@@ -702,7 +772,7 @@ int fw_reset(fw_handle* h, void* stream) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   FW_CUDA(h, cudaMemsetAsync(h->state, 0, (size_t)h->ncells_padded * n_state(h->ndim) * sizeof(float), s));
-  FW_CUDA(h, cudaMemsetAsync(h->traces, 0, (size_t)h->n_out * h->d.ncoordsout * sizeof(float) + 0, s));
+  FW_CUDA(h, cudaMemsetAsync(h->traces, 0, (size_t)h->n_out * h->n_cols * sizeof(float), s));
   FW_CUDA(h, cudaMemsetAsync(h->step, 0, 2 * sizeof(int), s));
   h->host_step = 0;
   return FW_OK;
@@ -748,8 +818,8 @@ int fw_read_traces(fw_handle* h, void* stream, int32_t row0, int32_t n_rows, flo
     return fail(h, FW_ERR_ARGUMENT, "trace rows [%d, %d) outside [0, %d)", row0, row0 + n_rows, h->n_out);
   if (!dst && n_rows) return fail(h, FW_ERR_ARGUMENT, "dst is NULL");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const size_t n = (size_t)n_rows * h->d.ncoordsout;
-  if (n) FW_CUDA(h, cudaMemcpyAsync(dst, h->traces + (size_t)row0 * h->d.ncoordsout, n * sizeof(float),
+  const size_t n = (size_t)n_rows * h->n_cols;
+  if (n) FW_CUDA(h, cudaMemcpyAsync(dst, h->traces + (size_t)row0 * h->n_cols, n * sizeof(float),
                                     on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyDeviceToHost, s));
   if (!on_device) {
     FW_CUDA(h, cudaStreamSynchronize(s));
@@ -922,7 +992,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
 int fw_destroy(fw_handle* h) {
   if (!h) return FW_OK;
   {
-    void* bufs[] = {h->adj_ckpt, h->adj_store, h->adj_lam, h->adj_grad};
+    void* bufs[] = {h->adj_ckpt, h->adj_store, h->adj_lam, h->adj_grad, h->groups};
     for (void* b : bufs)
       if (b) cudaFree(b);
   }

@@ -31,7 +31,9 @@ struct Lists {
   const int64_t* rec_cell;
   const int32_t* rec_k;     // sensor index (column of the traces)
   const float* icmat_t;     // [nt_ic][ncoords]
-  float* traces;            // [n_out][ncoordsout]
+  float* traces;            // [n_out][ncoordsout], or [n_out][n_groups] with sensor groups
+  const int32_t* rec_group; // per record entry: output column (sensor groups), or nullptr
+  const float* rec_w;       // per record entry: weight of the sample in its group
   int32_t ncoords, ncoordsout, nt_ic, mod_t;
 };
 
@@ -220,8 +222,13 @@ __device__ __forceinline__ void tile_epilogue(const StepArgs& A, float* p, int t
   __syncthreads();
   if (n % L.mod_t == 0) {
     float* row = L.traces + (size_t)(n / L.mod_t) * L.ncoordsout;
-    for (int e = L.rec_ptr[tile] + tid; e < L.rec_ptr[tile + 1]; e += nthr)
-      row[L.rec_k[e]] = p[L.rec_cell[e]];
+    if (L.rec_group) {  // weighted sums per sensor group (e.g. transducer elements)
+      for (int e = L.rec_ptr[tile] + tid; e < L.rec_ptr[tile + 1]; e += nthr)
+        if (L.rec_group[e] >= 0) atomicAdd(row + L.rec_group[e], L.rec_w[e] * p[L.rec_cell[e]]);
+    } else {
+      for (int e = L.rec_ptr[tile] + tid; e < L.rec_ptr[tile + 1]; e += nthr)
+        row[L.rec_k[e]] = p[L.rec_cell[e]];
+    }
   }
 }
 

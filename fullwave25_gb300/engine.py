@@ -22,7 +22,7 @@ FW_STATUS = {0: "FW_OK", 1: "FW_ERR_ARGUMENT", 2: "FW_ERR_CUDA", 3: "FW_ERR_STAT
 EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_fields_aniso",
             "fw_set_fields_exp",
             "fw_set_source_signal",
-            "fw_set_source_columns", "fw_run",
+            "fw_set_source_columns", "fw_set_sensor_groups", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
             "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_launches_per_step",
             "fw_destroy", "fw_adjoint_forward", "fw_adjoint_backward", "fw_group_create", "fw_group_run", "fw_group_set_members",
@@ -97,6 +97,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_set_fields_exp": (C.c_int, [H, C.POINTER(FwFields), _FP]),
         "fw_set_source_signal": (C.c_int, [H, _FP, C.c_int32]),
         "fw_set_source_columns": (C.c_int, [H, vp, _FP, C.c_int32, C.c_int32, C.c_int32]),
+        "fw_set_sensor_groups": (C.c_int, [H, _IP, _FP, C.c_int32]),
         "fw_run": (C.c_int, [H, vp, _FP, C.c_int32]),
         "fw_reset": (C.c_int, [H, vp]),
         "fw_advance": (C.c_int, [H, vp, C.c_int32]),
@@ -251,6 +252,19 @@ class Engine:
         self._call("fw_read_traces", C.c_void_p(stream or 0), int(row0), int(dst.shape[0]),
                    _fp(dst), 0)
 
+    def set_sensor_groups(self, group_of_sensor, weight, n_groups: int) -> None:
+        """Record weighted sums per sensor group (traces become ``[n_out, n_groups]``)."""
+        g = _c_i32(group_of_sensor)
+        w = _c_f32(weight)
+        if g.shape != (self.inputs.outc.shape[0],) or w.shape != g.shape:
+            raise ValueError("one group id and one weight per sensor")
+        self._call("fw_set_sensor_groups", _ip(g), _fp(w), int(n_groups))
+        self._n_cols = int(n_groups) or self.inputs.outc.shape[0]
+
+    @property
+    def n_cols(self) -> int:
+        return getattr(self, "_n_cols", self.inputs.outc.shape[0])
+
     def set_source_signal(self, icmat: np.ndarray) -> None:
         a = _c_f32(icmat)
         if a.shape != self.inputs.icmat.shape:
@@ -264,7 +278,7 @@ class Engine:
 
     def run(self, stream: int | None = None) -> np.ndarray:
         """Full solve; returns the float32 traces ``[n_out, ncoordsout]`` (genout layout)."""
-        out = np.empty((self.n_out, self.inputs.outc.shape[0]), dtype=np.float32)
+        out = np.empty((self.n_out, self.n_cols), dtype=np.float32)
         self._call("fw_run", C.c_void_p(stream or 0), _fp(out), 0)
         return out
 
@@ -281,7 +295,7 @@ class Engine:
     def read_traces(self, row0: int = 0, n_rows: int | None = None,
                     stream: int | None = None) -> np.ndarray:
         n_rows = self.n_out - row0 if n_rows is None else n_rows
-        out = np.empty((n_rows, self.inputs.outc.shape[0]), dtype=np.float32)
+        out = np.empty((n_rows, self.n_cols), dtype=np.float32)
         self._call("fw_read_traces", C.c_void_p(stream or 0), int(row0), int(n_rows), _fp(out), 0)
         return out
 

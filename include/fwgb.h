@@ -126,6 +126,15 @@ FWGB_API int fw_set_source_signal(fw_handle *h, const float *icmat, int32_t on_d
 FWGB_API int fw_set_source_columns(fw_handle *h, void *stream, const float *cols, int32_t n0,
                                    int32_t ncols, int32_t on_device);
 
+/* Record sensor groups instead of single sensors: from now on every recorded step writes
+ * row[g] = sum over the sensors k with group_of_sensor[k] = g of weight[k] * p (sensors with
+ * group -1 are dropped), so traces become [n_out][n_groups]. With weights 1/(sensors in the group)
+ * this is the per-element averaging of Transducer.post_process_sensor_output
+ * (transducer.py:807-869) done inside the time loop, without per-sensor traces. n_groups = 0
+ * returns to per-sensor traces. Host arrays of ncoordsout entries. Resets the wavefield. */
+FWGB_API int fw_set_sensor_groups(fw_handle *h, const int32_t *group_of_sensor,
+                                  const float *weight, int32_t n_groups);
+
 /* Full solve: reset the wavefield, run nt steps on `stream`, and copy the traces
  * [n_out][ncoordsout] (n_out = ceil(nt / mod_t)) to `out` (host memory unless
  * out_on_device = 1). Synchronises `stream` before returning when out is host memory.
