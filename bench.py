@@ -302,7 +302,8 @@ def run_gpu(args):
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {**desc, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "wall_s_timed": wall},
+                   "wall_s_timed": wall, "kernels": engine.kernel_variant,
+                   "block_tile_xyz": list(engine.block_tile)},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": (tr * cells if tr is not None else None),
@@ -402,7 +403,12 @@ def run_batch(args):
             ev[2 * i + 1].record(stream)
         torch.cuda.synchronize(dev)
     group_ms = sum(ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(args.steps)) / args.steps
-    # the same simulations one by one (each a full solve on the same device-resident inputs)
+    # the same simulations one by one (each a full solve on the same device-resident inputs);
+    # one untimed advance first, so that each grid size's kernel-shape autotuning is not timed
+    for e in engines:
+        e.reset(sptr)
+        e.advance(1, sptr)
+    torch.cuda.synchronize(dev)
     lat = []
     for e in engines:
         a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)

@@ -12,7 +12,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <array>
 #include <map>
+#include <mutex>
 #include <new>
 #include <string>
 #include <vector>
@@ -21,6 +23,7 @@
 #include "engine_common.cuh"
 #include "kernels_direct.cuh"
 #include "kernels_march3d.cuh"
+#include "kernels_march2d.cuh"
 #include "kernels_adjoint2d.cuh"
 
 using namespace fwgb;
@@ -37,6 +40,14 @@ void fwgb_set_global_error(const char* msg) { g_create_error = msg; }
 namespace {
 
 constexpr int kMarchXC = 64;  // x planes per block of the 3D plane-march kernels
+
+// 2D kernel shapes the autotuner chooses from: 0 = direct kernels (one block per 32 y x 8 x tile),
+// else the row-march kernels with TY threads (y columns) walking XC rows. TY + 16 <= 256 (TMA box
+// limit), TY a multiple of 32 and XC of 8 (whole list tiles per block).
+struct Shape2D { int ty, xc; };
+constexpr Shape2D kShapes2D[] = {{0, 0}, {64, 16}, {64, 32}, {128, 16}, {128, 32}, {128, 64}};
+constexpr int kNumShapes2D = sizeof(kShapes2D) / sizeof(kShapes2D[0]);
+constexpr int kTuneSteps = 64;   // time steps per autotuning trial (one graph)
 
 enum Variant { kDirect = 0, kMarch = 1 };
 
@@ -78,7 +89,10 @@ struct fw_handle {
   cudaGraphExec_t graph = nullptr;
   int graph_steps = 0;
   int variant = kDirect;
+  int shape2d = 0;             // index into kShapes2D (2D handles)
+  bool shape_fixed = false;    // 2D shape forced (FWGB_SHAPE2D / FWGB_VARIANT) or already tuned
   MarchMaps tmaps{};
+  March2Maps tmaps2{};
   // adjoint (2D): checkpoints every adj_every steps, per-segment state store, adjoint fields
   int adj_every = 0, adj_nckpt = 0;
   float* adj_ckpt = nullptr;     // adj_nckpt states
@@ -118,6 +132,8 @@ constexpr int kMaps = 13;
 int n_maps(const fw_handle* h) { return kMaps + (h->aniso ? 10 * (h->ndim - 1) : 0); }
 int axis_map(int a, int k) { return kMaps + 10 * (a - 1) + k; }
 
+// Tiling of the per-tile source/air/sensor lists, which is also the direct kernels' block tiling
+// (and in 3D the plane-march kernels'). 2D march blocks own whole rectangles of these tiles.
 Tiling make_tiling(const fw_handle* h) {
   Tiling t{};
   if (h->ndim == 2) {
@@ -208,13 +224,34 @@ int upload_grid(fw_handle* h, void* dst, const void* src, size_t elem, bool on_d
 
 // One time step: velocity kernel, then pressure kernel (+ tile epilogue), with the cell physics
 // CV/CP (isotropic, anisotropic or exponential attenuation) of the handle.
+template <int TY, int XC, class CV, class CP>
+void launch_march2d(fw_handle* h, cudaStream_t s) {
+  const Tiling& t = h->tiling;
+  const int body_x = (int)h->nx - 2 * kGhost, body_y = (int)h->ny - 2 * kGhost;
+  dim3 grid((body_y + TY - 1) / TY, (body_x + XC - 1) / XC);
+  vel2d_march<TY, XC, CV><<<grid, TY, 0, s>>>(h->args, h->tmaps2.p);
+  prs2d_march<TY, XC, CP><<<grid, TY, 0, s>>>(h->args, h->tmaps2.vx, h->tmaps2.vy,
+                                               make_int2(t.n[0], t.n[1]));
+}
+
 template <int ND, class CV, class CP, int kMin>
 void launch_typed(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
-  if (ND == 2) {
-    dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
-    vel2d_direct<CV><<<grid, block, 0, s>>>(h->args);
-    prs2d_direct<CP><<<grid, block, 0, s>>>(h->args);
+  if constexpr (ND == 2) {
+    static_assert(kNumShapes2D == 6, "one case per 2D march shape");
+    switch (h->shape2d) {
+      case 0: {
+        dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
+        vel2d_direct<CV><<<grid, block, 0, s>>>(h->args);
+        prs2d_direct<CP><<<grid, block, 0, s>>>(h->args);
+        break;
+      }
+      case 1: launch_march2d<64, 16, CV, CP>(h, s); break;
+      case 2: launch_march2d<64, 32, CV, CP>(h, s); break;
+      case 3: launch_march2d<128, 16, CV, CP>(h, s); break;
+      case 4: launch_march2d<128, 32, CV, CP>(h, s); break;
+      default: launch_march2d<128, 64, CV, CP>(h, s); break;
+    }
   } else if (h->variant == kMarch) {
     dim3 grid(t.n[2], t.n[1], t.n[0]), block(kMTZ, kMTY);
     const MarchMaps& tm = h->tmaps;
@@ -269,8 +306,8 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t
                                    const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-// 3D float32 tensor map over one padded field: dims (pitch, ny, nx), box (bz, by, 1).
-int encode_field_map(fw_handle* h, CUtensorMap* map, float* base, uint32_t bz, uint32_t by) {
+int encode_map(fw_handle* h, CUtensorMap* map, float* base, cuuint32_t rank,
+               const cuuint64_t* dims, const cuuint64_t* strides, const cuuint32_t* box) {
   static EncodeTiledFn encode = nullptr;
   if (!encode) {
     void* fn = nullptr;
@@ -281,14 +318,43 @@ int encode_field_map(fw_handle* h, CUtensorMap* map, float* base, uint32_t bz, u
       return fail(h, FW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     encode = reinterpret_cast<EncodeTiledFn>(fn);
   }
-  const cuuint64_t dims[3] = {(cuuint64_t)h->pitch, (cuuint64_t)h->ny, (cuuint64_t)h->nx};
-  const cuuint64_t strides[2] = {(cuuint64_t)h->pitch * 4, (cuuint64_t)(h->pitch * h->ny) * 4};
-  const cuuint32_t box[3] = {bz, by, 1};
   const cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, base, dims, strides, box, estr,
+  CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, base, dims, strides, box, estr,
                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(h, FW_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return FW_OK;
+}
+
+// 3D float32 tensor map over one padded field: dims (pitch, ny, nx), box (bz, by, 1).
+int encode_field_map(fw_handle* h, CUtensorMap* map, float* base, uint32_t bz, uint32_t by) {
+  const cuuint64_t dims[3] = {(cuuint64_t)h->pitch, (cuuint64_t)h->ny, (cuuint64_t)h->nx};
+  const cuuint64_t strides[2] = {(cuuint64_t)h->pitch * 4, (cuuint64_t)(h->pitch * h->ny) * 4};
+  const cuuint32_t box[3] = {bz, by, 1};
+  return encode_map(h, map, base, 3, dims, strides, box);
+}
+
+// 2D float32 tensor map over one padded 2D field: dims (pitch, nx), box (bw, 1) = one row segment.
+int encode_row_map(fw_handle* h, CUtensorMap* map, float* base, uint32_t bw) {
+  const cuuint64_t dims[2] = {(cuuint64_t)h->pitch, (cuuint64_t)h->nx};
+  const cuuint64_t strides[1] = {(cuuint64_t)h->pitch * 4};
+  const cuuint32_t box[2] = {bw, 1};
+  return encode_map(h, map, base, 2, dims, strides, box);
+}
+
+// Select 2D kernel shape k: encode the row tensor maps for its width, drop the step graph.
+int set_shape2d(fw_handle* h, int k) {
+  if (k > 0) {
+    const uint32_t ty = (uint32_t)kShapes2D[k].ty;
+    int st;
+    if ((st = encode_row_map(h, &h->tmaps2.p, h->args.f.p, ty + 16)) ||
+        (st = encode_row_map(h, &h->tmaps2.vx, h->args.f.v[0], ty + 8)) ||
+        (st = encode_row_map(h, &h->tmaps2.vy, h->args.f.v[1], ty + 16)))
+      return st;
+  }
+  h->shape2d = k;
+  h->variant = k > 0 ? kMarch : kDirect;
+  h->graph_steps = 0;   // the next advance captures a graph with the new kernels
   return FW_OK;
 }
 
@@ -428,7 +494,32 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   A.l.nt_ic = desc->nt_ic;
   A.l.mod_t = desc->mod_t;
   A.step = h->step;
-  if (h->variant == kMarch) {
+  if (h->ndim == 2) {
+    // 2D kernel shape: forced by FWGB_VARIANT=direct or FWGB_SHAPE2D=<k>, else the direct kernels
+    // until the autotuner (first advance from step 0) has measured the shapes for this grid
+    const char* v = std::getenv("FWGB_VARIANT");
+    const char* sh = std::getenv("FWGB_SHAPE2D");
+    int k = 0;
+    if (v && std::strcmp(v, "direct") == 0) {
+      h->shape_fixed = true;
+    } else if (sh && *sh) {
+      k = std::atoi(sh);
+      if (k < 0 || k >= kNumShapes2D) {
+        fw_destroy(h);
+        return fail(nullptr, FW_ERR_ARGUMENT, "FWGB_SHAPE2D=%s outside [0, %d)", sh, kNumShapes2D);
+      }
+      h->shape_fixed = true;
+    } else if (v && std::strcmp(v, "march") == 0) {
+      k = 4;
+      h->shape_fixed = true;
+    }
+    if ((st = set_shape2d(h, k))) {
+      g_create_error = h->err;
+      fw_destroy(h);
+      return st;
+    }
+  }
+  if (h->variant == kMarch && h->ndim == 3) {
     if ((st = encode_field_map(h, &h->tmaps.p, A.f.p, kPW, kPH)) ||
         (st = encode_field_map(h, &h->tmaps.vx, A.f.v[0], kXW, kXH)) ||
         (st = encode_field_map(h, &h->tmaps.vy, A.f.v[1], kYW, kYH)) ||
@@ -778,6 +869,65 @@ int fw_reset(fw_handle* h, void* stream) {
   return FW_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+std::mutex g_tune_mutex;
+std::map<std::array<int64_t, 6>, int> g_tuned;   // (device, nx, ny, aniso, exp, beta) -> shape
+
+// 2D kernel-shape autotuner. Called on the first advance from step 0, when the state is all zero:
+// every shape of kShapes2D runs kTuneSteps steps twice (the second timed with events on the
+// caller's stream), the handle is reset after each trial, and the fastest shape is kept. All
+// shapes give bit-identical results, so the choice changes speed only. The choice is cached per
+// device, grid size and cell physics, so later handles of the same kind skip the trials.
+int autotune_2d(fw_handle* h, cudaStream_t s) {
+  int dev = 0;
+  FW_CUDA(h, cudaGetDevice(&dev));
+  const std::array<int64_t, 6> key{dev, h->nx, h->ny, h->aniso, h->exp, h->has_beta};
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mutex);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) {
+      h->shape_fixed = true;
+      return it->second == h->shape2d ? FW_OK : set_shape2d(h, it->second);
+    }
+  }
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FW_CUDA(h, cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(h, FW_ERR_CUDA, "cudaEventCreate failed");
+  }
+  int st = FW_OK, best = 0;
+  float best_ms = 0.f;
+  for (int k = 0; k < kNumShapes2D && st == FW_OK; ++k) {
+    float ms = 0.f;
+    if ((st = set_shape2d(h, k)) || (st = build_graph(h, kTuneSteps))) break;
+    if (cudaGraphLaunch(h->graph, s) != cudaSuccess || cudaEventRecord(e0, s) != cudaSuccess ||
+        cudaGraphLaunch(h->graph, s) != cudaSuccess || cudaEventRecord(e1, s) != cudaSuccess ||
+        cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      st = fail(h, FW_ERR_CUDA, "autotuning trial of 2D shape %d failed: %s", k,
+                cudaGetErrorString(cudaGetLastError()));
+      break;
+    }
+    if ((st = check_device_status(h, s)) || (st = fw_reset(h, s))) break;
+    if (k == 0 || ms < best_ms) { best_ms = ms; best = k; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  if ((st = set_shape2d(h, best))) return st;
+  h->shape_fixed = true;
+  std::lock_guard<std::mutex> lk(g_tune_mutex);
+  g_tuned[key] = best;
+  return FW_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int fw_advance(fw_handle* h, void* stream, int32_t n_steps) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called before stepping");
@@ -785,6 +935,18 @@ int fw_advance(fw_handle* h, void* stream, int32_t n_steps) {
     return fail(h, FW_ERR_ARGUMENT, "cannot advance %d steps from step %d (nt = %d)", n_steps,
                 h->host_step, h->d.nt);
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (h->ndim == 2 && !h->shape_fixed && h->host_step == 0 && n_steps > 0) {
+    // autotune unless disabled (FWGB_AUTOTUNE=0), too short, or inside a stream capture
+    const char* a = std::getenv("FWGB_AUTOTUNE");
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    FW_CUDA(h, cudaStreamIsCapturing(s, &cs));
+    if ((a && std::strcmp(a, "0") == 0) || h->d.nt < 2 * kTuneSteps) {
+      h->shape_fixed = true;
+    } else if (cs == cudaStreamCaptureStatusNone) {
+      int st = autotune_2d(h, s);
+      if (st) return st;
+    }
+  }
   constexpr int kGraphSteps = 64;
   int left = n_steps;
   if (left >= kGraphSteps) {
@@ -863,6 +1025,18 @@ int fw_device_bytes(const fw_handle* h, uint64_t* bytes) {
 int fw_kernel_variant(const fw_handle* h, int32_t* variant) {
   if (!h || !variant) return FW_ERR_ARGUMENT;
   *variant = h->variant;
+  return FW_OK;
+}
+
+int fw_block_tile(const fw_handle* h, int32_t tile[3]) {
+  if (!h || !tile) return FW_ERR_ARGUMENT;
+  if (h->ndim == 2 && h->shape2d > 0) {
+    tile[0] = kShapes2D[h->shape2d].xc;
+    tile[1] = kShapes2D[h->shape2d].ty;
+    tile[2] = 1;
+  } else {
+    for (int a = 0; a < 3; ++a) tile[a] = h->tiling.t[a];
+  }
   return FW_OK;
 }
 
@@ -1057,7 +1231,7 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
   for (int i = 0; i < n; ++i) {
     const fw_handle* h = handles[i];
     if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle %d is NULL", i);
-    if (h->ndim != 2 || h->variant != kDirect || h->aniso || h->exp)
+    if (h->ndim != 2 || h->aniso || h->exp)
       return fail(nullptr, FW_ERR_UNSUPPORTED,
                   "group members must be isotropic 2D simulations (member %d)", i);
     if (!h->fields_set) return fail(nullptr, FW_ERR_STATE, "member %d has no fields set", i);

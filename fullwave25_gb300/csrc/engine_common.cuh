@@ -205,31 +205,44 @@ struct CellPrsExpT {
   }
 };
 
-// Source injection, air zeroing and sensor recording for the cells owned by this block's tile.
-// Called by every thread of kernel B after its pressure writes; `tid`/`nthr` span the block.
-__device__ __forceinline__ void tile_epilogue(const StepArgs& A, float* p, int tile, int tid,
-                                              int nthr) {
+// Source injection, air zeroing and sensor recording for the cells owned by a block. The per-tile
+// lists are indexed tile = tx * n_ty + ty; a block owns the tiles [tx0, tx1) x [ty0, ty1), whose
+// entries are contiguous per tx. Called by every thread of the pressure kernel after its pressure
+// writes; `tid`/`nthr` span the block. Order per cell: source, air, record.
+__device__ __forceinline__ void span_epilogue(const StepArgs& A, float* p, int tx0, int tx1,
+                                              int ty0, int ty1, int n_ty, int tid, int nthr) {
   const Lists& L = A.l;
   const int n = *A.step - 1;
   __syncthreads();
   if (n < L.nt_ic) {
     const float* col = L.icmat_t + (size_t)n * L.ncoords;
-    for (int e = L.src_ptr[tile] + tid; e < L.src_ptr[tile + 1]; e += nthr)
-      p[L.src_cell[e]] = col[L.src_k[e]];
+    for (int tx = tx0; tx < tx1; ++tx)
+      for (int e = L.src_ptr[tx * n_ty + ty0] + tid; e < L.src_ptr[tx * n_ty + ty1]; e += nthr)
+        p[L.src_cell[e]] = col[L.src_k[e]];
   }
   __syncthreads();
-  for (int e = L.zero_ptr[tile] + tid; e < L.zero_ptr[tile + 1]; e += nthr) p[L.zero_cell[e]] = 0.f;
+  for (int tx = tx0; tx < tx1; ++tx)
+    for (int e = L.zero_ptr[tx * n_ty + ty0] + tid; e < L.zero_ptr[tx * n_ty + ty1]; e += nthr)
+      p[L.zero_cell[e]] = 0.f;
   __syncthreads();
   if (n % L.mod_t == 0) {
     float* row = L.traces + (size_t)(n / L.mod_t) * L.ncoordsout;
-    if (L.rec_group) {  // weighted sums per sensor group (e.g. transducer elements)
-      for (int e = L.rec_ptr[tile] + tid; e < L.rec_ptr[tile + 1]; e += nthr)
-        if (L.rec_group[e] >= 0) atomicAdd(row + L.rec_group[e], L.rec_w[e] * p[L.rec_cell[e]]);
-    } else {
-      for (int e = L.rec_ptr[tile] + tid; e < L.rec_ptr[tile + 1]; e += nthr)
-        row[L.rec_k[e]] = p[L.rec_cell[e]];
+    for (int tx = tx0; tx < tx1; ++tx) {
+      const int b = L.rec_ptr[tx * n_ty + ty0], end = L.rec_ptr[tx * n_ty + ty1];
+      if (L.rec_group) {  // weighted sums per sensor group (e.g. transducer elements)
+        for (int e = b + tid; e < end; e += nthr)
+          if (L.rec_group[e] >= 0) atomicAdd(row + L.rec_group[e], L.rec_w[e] * p[L.rec_cell[e]]);
+      } else {
+        for (int e = b + tid; e < end; e += nthr) row[L.rec_k[e]] = p[L.rec_cell[e]];
+      }
     }
   }
+}
+
+// The epilogue of one tile (the direct kernels: one block per tile).
+__device__ __forceinline__ void tile_epilogue(const StepArgs& A, float* p, int tile, int tid,
+                                              int nthr) {
+  span_epilogue(A, p, tile, tile + 1, 0, 1, 1, tid, nthr);
 }
 
 }  // namespace fwgb

@@ -1,0 +1,200 @@
+// 2D step kernels that march along x (depth, the slow axis).
+//
+// Block = TY threads, one per y column (y is contiguous), walking XC consecutive x rows. Per row:
+//   * x taps come from a 16-entry register queue of the thread's column (one new coalesced load
+//     per row, prefetched one row ahead);
+//   * y taps and the off-axis taps come from shared-memory copies of rows x-1, x, x+1 with the y
+//     halo they need, brought in by TMA (2D tiled loads) into a 4-slot ring, row x+2 in flight
+//     while row x is computed; one mbarrier per slot, bounded waits;
+//   * the point-wise state and maps of the cell are loaded before the row barrier and written
+//     once, coalesced.
+// Same arithmetic (operation order, fused multiply-adds) as the 2D direct kernels, so the results
+// are bit-identical to theirs. The per-tile source/air/sensor lists stay those of the direct
+// kernels' 32 (y) x 8 (x) tiles: TY is a multiple of 32 and XC of 8, so a march block owns a
+// rectangle of list tiles and the tile shape can change without rebuilding the lists.
+#pragma once
+#include "engine_common.cuh"
+#include "tma.cuh"
+
+namespace fwgb {
+
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+constexpr int kRing2 = 4;
+
+// Row boxes: p and vy with a y halo of 8 (start y0 - 8), vx with a halo of 4 (start y0 - 4).
+template <int TY>
+struct Row2 {
+  static constexpr int kWide = TY + 16;   // floats, multiple of 4
+  static constexpr int kNarrow = TY + 8;
+  static constexpr int kWideSlot = (kWide * 4 + 127) / 128 * 32;   // floats, 128-byte aligned
+  static constexpr int kNarrowSlot = (kNarrow * 4 + 127) / 128 * 32;
+};
+
+struct March2Maps {
+  CUtensorMap p, vx, vy;
+};
+
+template <int TY, int XC, class CV>
+__global__ void __launch_bounds__(TY)
+vel2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
+  using R = Row2<TY>;
+  __shared__ alignas(128) float ring[kRing2][R::kWideSlot];
+  __shared__ alignas(8) uint64_t bar[kRing2];
+  const Grid& g = A.g;
+  int* status = A.step + 1;
+  const int tj = threadIdx.x;
+  const int y0 = kGhost + blockIdx.x * TY;
+  const int xb = kGhost + blockIdx.y * XC;
+  const int xe = min(xb + XC, g.nx - kGhost);
+  const int j = y0 + tj;
+  const bool active = j < g.ny - kGhost;
+  if (blockIdx.x == 0 && blockIdx.y == 0 && tj == 0) *A.step += 1;
+  if (tj == 0) {
+    for (int s = 0; s < kRing2; ++s) mbar_init(&bar[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  constexpr uint32_t kBytes = R::kWide * 4;
+  if (tj == 0)
+    for (int s = 0; s < 3; ++s) {
+      mbar_arrive_expect_tx(&bar[s], kBytes);
+      tma_load_2d(ring[s], &tm_p, &bar[s], y0 - 8, xb - 1 + s);
+    }
+  const int64_t sx = g.sx;
+  const float* __restrict__ p = A.f.p;
+  float q[16];  // q[t] = p[x - 7 + t]
+#pragma unroll
+  for (int t = 0; t < 16; ++t) q[t] = active ? __ldg(p + (int64_t)(xb - 7 + t) * sx + j) : 0.f;
+  const int si = tj + 8;
+  for (int x = xb; x < xe; ++x) {
+    const int it = x - xb;
+    const int64_t c = (int64_t)x * sx + j;
+    CV cv;
+    if (active) cv.load(A, c);
+    const float qn = (active && x + 9 < g.nx) ? __ldg(p + (int64_t)(x + 9) * sx + j) : 0.f;
+    __syncthreads();
+    if (tj == 0 && x + 1 < xe) {
+      const int s = (it + 3) % kRing2;
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(&bar[s], kBytes);
+      tma_load_2d(ring[s], &tm_p, &bar[s], y0 - 8, x + 2);
+    }
+    if (it == 0) {
+      mbar_wait_bounded(&bar[0], 0, status);
+      mbar_wait_bounded(&bar[1], 0, status);
+    }
+    mbar_wait_bounded(&bar[(it + 2) % kRing2], ((it + 2) / kRing2) & 1, status);
+    const float* Rm = ring[it % kRing2];
+    const float* R0 = ring[(it + 1) % kRing2];
+    const float* R1 = ring[(it + 2) % kRing2];
+    if (active) {
+      float cm[8], co;
+      load_taps(A.m.taps, cv.dc, cm, co);
+      float gx = 0.f, gy = 0.f;
+#pragma unroll
+      for (int m = 1; m <= 8; ++m) {
+        gx = fmaf(cm[m - 1], q[7 + m] - q[8 - m], gx);
+        gy = fmaf(cm[m - 1], R0[si + m] - R0[si - (m - 1)], gy);
+      }
+      gx = fmaf(co, (R1[si + 1] - R0[si + 1]) + (R1[si - 1] - R0[si - 1]), gx);
+      gy = fmaf(co, (R1[si + 1] - R1[si]) + (Rm[si + 1] - Rm[si]), gy);
+      const float gg[2] = {gx * g.inv_h[0], gy * g.inv_h[1]};
+      cv.update_store(A, c, gg);
+    }
+#pragma unroll
+    for (int t = 0; t < 15; ++t) q[t] = q[t + 1];
+    q[15] = qn;
+  }
+}
+
+template <int TY, int XC, class CP>
+__global__ void __launch_bounds__(TY)
+prs2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
+            const __grid_constant__ CUtensorMap tm_vy, const int2 list_tiles) {
+  static_assert(TY % 32 == 0 && XC % 8 == 0, "a march block must own whole 32 x 8 list tiles");
+  using R = Row2<TY>;
+  __shared__ alignas(128) float rx[kRing2][R::kNarrowSlot];
+  __shared__ alignas(128) float ry[kRing2][R::kWideSlot];
+  __shared__ alignas(8) uint64_t bar[kRing2];
+  const Grid& g = A.g;
+  int* status = A.step + 1;
+  const int tj = threadIdx.x;
+  const int y0 = kGhost + blockIdx.x * TY;
+  const int xb = kGhost + blockIdx.y * XC;
+  const int xe = min(xb + XC, g.nx - kGhost);
+  const int j = y0 + tj;
+  const bool active = j < g.ny - kGhost;
+  if (tj == 0) {
+    for (int s = 0; s < kRing2; ++s) mbar_init(&bar[s], 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  constexpr uint32_t kBytes = (R::kNarrow + R::kWide) * 4;
+  auto issue = [&](int s, int x) {
+    mbar_arrive_expect_tx(&bar[s], kBytes);
+    tma_load_2d(rx[s], &tm_vx, &bar[s], y0 - 4, x);
+    tma_load_2d(ry[s], &tm_vy, &bar[s], y0 - 8, x);
+  };
+  if (tj == 0)
+    for (int s = 0; s < 3; ++s) issue(s, xb - 1 + s);
+  const int64_t sx = g.sx;
+  const float* __restrict__ vx = A.f.v[0];
+  float* p = A.f.p;
+  float r[16];  // r[t] = vx[x - 8 + t]
+#pragma unroll
+  for (int t = 0; t < 16; ++t) r[t] = active ? __ldg(vx + (int64_t)(xb - 8 + t) * sx + j) : 0.f;
+  const int xi = tj + 4, yi = tj + 8;
+  for (int x = xb; x < xe; ++x) {
+    const int it = x - xb;
+    const int64_t c = (int64_t)x * sx + j;
+    CP cp;
+    if (active) cp.load(A, c);
+    const float rn = active ? __ldg(vx + (int64_t)(x + 8) * sx + j) : 0.f;
+    __syncthreads();
+    if (tj == 0 && x + 1 < xe) {
+      fence_proxy_async_smem();
+      issue((it + 3) % kRing2, x + 2);
+    }
+    if (it == 0) {
+      mbar_wait_bounded(&bar[0], 0, status);
+      mbar_wait_bounded(&bar[1], 0, status);
+    }
+    mbar_wait_bounded(&bar[(it + 2) % kRing2], ((it + 2) / kRing2) & 1, status);
+    const float* Xm = rx[it % kRing2];
+    const float* X0 = rx[(it + 1) % kRing2];
+    const float* Ym = ry[it % kRing2];
+    const float* Y0 = ry[(it + 1) % kRing2];
+    const float* Y1 = ry[(it + 2) % kRing2];
+    if (active) {
+      float cm[8], co;
+      load_taps(A.m.taps, cp.dc, cm, co);
+      float dx = 0.f, dy = 0.f;
+#pragma unroll
+      for (int m = 1; m <= 8; ++m) {
+        dx = fmaf(cm[m - 1], r[7 + m] - r[8 - m], dx);
+        dy = fmaf(cm[m - 1], Y0[yi + (m - 1)] - Y0[yi - m], dy);
+      }
+      dx = fmaf(co, (X0[xi + 1] - Xm[xi + 1]) + (X0[xi - 1] - Xm[xi - 1]), dx);
+      dy = fmaf(co, (Y1[yi] - Y1[yi - 1]) + (Ym[yi] - Ym[yi - 1]), dy);
+      const float dd[2] = {dx * g.inv_h[0], dy * g.inv_h[1]};
+      cp.update_store(A, c, dd);
+    }
+#pragma unroll
+    for (int t = 0; t < 15; ++t) r[t] = r[t + 1];
+    r[15] = rn;
+  }
+  // list tiles: list_tiles.x along x (8 rows each), list_tiles.y along y (32 columns each)
+  const int tx0 = blockIdx.y * (XC / 8), ty0 = blockIdx.x * (TY / 32);
+  span_epilogue(A, p, tx0, min(tx0 + XC / 8, list_tiles.x), ty0, min(ty0 + TY / 32, list_tiles.y),
+                list_tiles.y, tj, TY);
+}
+
+}  // namespace fwgb

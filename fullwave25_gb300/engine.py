@@ -24,7 +24,7 @@ EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_fields_aniso
             "fw_set_source_signal",
             "fw_set_source_columns", "fw_set_sensor_groups", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
-            "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_launches_per_step",
+            "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_block_tile", "fw_launches_per_step",
             "fw_destroy", "fw_adjoint_forward", "fw_adjoint_backward", "fw_group_create", "fw_group_run", "fw_group_set_members",
             "fw_group_advance", "fw_group_destroy",
             "fw_run_noalloc", "fw_last_error")
@@ -107,6 +107,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_current_step": (C.c_int, [H, _IP]),
         "fw_device_bytes": (C.c_int, [H, C.POINTER(C.c_uint64)]),
         "fw_kernel_variant": (C.c_int, [H, _IP]),
+        "fw_block_tile": (C.c_int, [H, _IP]),
         "fw_launches_per_step": (C.c_int, [H, _IP]),
         "fw_destroy": (C.c_int, [H]),
         "fw_adjoint_forward": (C.c_int, [H, vp, C.c_int32]),
@@ -341,6 +342,14 @@ class Engine:
         v = C.c_int32()
         self._call("fw_kernel_variant", C.byref(v))
         return {0: "direct", 1: "march"}[v.value]
+
+    @property
+    def block_tile(self) -> tuple:
+        """Cells per block of the kernels in use along (x, y, z); 2D handles report the shape
+        the autotuner picked once the first advance from step 0 has run."""
+        v = (C.c_int32 * 3)()
+        self._call("fw_block_tile", v)
+        return tuple(v)
 
     @property
     def launches_per_step(self) -> int:
