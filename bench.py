@@ -433,7 +433,9 @@ def run_batch(args):
                                    "size (512-2048 x 512-1536 + PML 40 + transition 40), "
                                    "nt 3000-8000, 128-element transmits",
                        "bench_step": "one group run = every simulation to its own nt",
-                       "device_build_s": build_s},
+                       "device_build_s": build_s,
+                       "group_block_tile_xyz": list(grp.block_tile),
+                       "one_by_one_block_tiles": sorted({str(e.block_tile) for e in engines})},
             "sims_per_s": {"batched": len(insts) / (group_ms / 1e3),
                            "one_by_one": len(insts) / (serial_ms / 1e3),
                            "batched_over_one_by_one": serial_ms / group_ms},

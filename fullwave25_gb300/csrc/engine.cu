@@ -226,12 +226,10 @@ int upload_grid(fw_handle* h, void* dst, const void* src, size_t elem, bool on_d
 // CV/CP (isotropic, anisotropic or exponential attenuation) of the handle.
 template <int TY, int XC, class CV, class CP>
 void launch_march2d(fw_handle* h, cudaStream_t s) {
-  const Tiling& t = h->tiling;
   const int body_x = (int)h->nx - 2 * kGhost, body_y = (int)h->ny - 2 * kGhost;
   dim3 grid((body_y + TY - 1) / TY, (body_x + XC - 1) / XC);
   vel2d_march<TY, XC, CV><<<grid, TY, 0, s>>>(h->args, h->tmaps2.p);
-  prs2d_march<TY, XC, CP><<<grid, TY, 0, s>>>(h->args, h->tmaps2.vx, h->tmaps2.vy,
-                                               make_int2(t.n[0], t.n[1]));
+  prs2d_march<TY, XC, CP><<<grid, TY, 0, s>>>(h->args, h->tmaps2.vx, h->tmaps2.vy);
 }
 
 template <int ND, class CV, class CP, int kMin>
@@ -1187,8 +1185,13 @@ const char* fw_last_error(const fw_handle* h) { return h ? h->err.c_str() : g_cr
 struct fw_group {
   std::vector<fw_handle*> members;  // sorted by steps left, descending (tiles in the same order)
   StepArgs* d_args = nullptr;       // one argument block per member (its own step counter)
-  int4* d_tiles = nullptr;          // {member, tile_y, tile_x, tile index within the member}
+  // work list: direct kernels {member, tile_y, tile_x, tile index within the member};
+  //            march kernels  {member, y block, x chunk, 1 for the block that counts the step}
+  int4* d_tiles = nullptr;
+  CUtensorMap* d_maps = nullptr;    // march kernels: row maps p, vx, vy per member
   size_t args_cap = 0, tiles_cap = 0;
+  int shape = 0;                    // index into kShapes2D (0 = direct group kernels)
+  bool shape_fixed = false;         // forced by the environment or already tuned
   std::vector<int> tiles_upto;      // tiles of the first k members (k = 0..n)
   bool beta = false;
   cudaStream_t capture_stream = nullptr;
@@ -1199,11 +1202,29 @@ namespace {
 
 constexpr int kGroupGraphSteps = 64;
 
+template <int TY, int XC>
+void group_launch_march(fw_group* g, int n_blocks, cudaStream_t s) {
+  vel2d_march_group<TY, XC><<<n_blocks, TY, 0, s>>>(g->d_args, g->d_maps, g->d_tiles);
+  if (g->beta) prs2d_march_group<TY, XC, true><<<n_blocks, TY, 0, s>>>(g->d_args, g->d_maps, g->d_tiles);
+  else prs2d_march_group<TY, XC, false><<<n_blocks, TY, 0, s>>>(g->d_args, g->d_maps, g->d_tiles);
+}
+
 void group_launch_step(fw_group* g, int n_tiles, cudaStream_t s) {
-  const dim3 block(kD2TY, kD2TX);
-  vel2d_group<<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
-  if (g->beta) prs2d_group<true><<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
-  else prs2d_group<false><<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
+  static_assert(kNumShapes2D == 6, "one case per 2D march shape");
+  switch (g->shape) {
+    case 0: {
+      const dim3 block(kD2TY, kD2TX);
+      vel2d_group<<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
+      if (g->beta) prs2d_group<true><<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
+      else prs2d_group<false><<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
+      break;
+    }
+    case 1: group_launch_march<64, 16>(g, n_tiles, s); break;
+    case 2: group_launch_march<64, 32>(g, n_tiles, s); break;
+    case 3: group_launch_march<128, 16>(g, n_tiles, s); break;
+    case 4: group_launch_march<128, 32>(g, n_tiles, s); break;
+    default: group_launch_march<128, 64>(g, n_tiles, s); break;
+  }
 }
 
 int group_graph(fw_group* g, int n_tiles, cudaGraphExec_t* out) {
@@ -1242,6 +1263,7 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
   });
   std::vector<StepArgs> args(n);
   std::vector<int4> tiles;
+  std::vector<CUtensorMap> maps;
   g->members = m;
   g->tiles_upto.assign(1, 0);
   g->beta = false;
@@ -1251,9 +1273,23 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
     args[r] = h->args;
     // members without beta read their (all-zero) beta buffer when the group uses the beta kernel
     args[r].m.beta2dt = map_field(h, 2);
-    const Tiling& t = h->tiling;
-    for (int tx = 0; tx < t.n[0]; ++tx)
-      for (int ty = 0; ty < t.n[1]; ++ty) tiles.push_back(make_int4(r, ty, tx, tx * t.n[1] + ty));
+    if (g->shape == 0) {
+      const Tiling& t = h->tiling;
+      for (int tx = 0; tx < t.n[0]; ++tx)
+        for (int ty = 0; ty < t.n[1]; ++ty) tiles.push_back(make_int4(r, ty, tx, tx * t.n[1] + ty));
+    } else {
+      const int ty_ = kShapes2D[g->shape].ty, xc = kShapes2D[g->shape].xc;
+      const int nby = (int)(h->ny - 2 * kGhost + ty_ - 1) / ty_;
+      const int nbx = (int)(h->nx - 2 * kGhost + xc - 1) / xc;
+      for (int bx = 0; bx < nbx; ++bx)
+        for (int by = 0; by < nby; ++by) tiles.push_back(make_int4(r, by, bx, bx == 0 && by == 0));
+      CUtensorMap tm[3];
+      if (encode_row_map(h, &tm[0], h->args.f.p, ty_ + 16) ||
+          encode_row_map(h, &tm[1], h->args.f.v[0], ty_ + 8) ||
+          encode_row_map(h, &tm[2], h->args.f.v[1], ty_ + 16))
+        return fail(nullptr, FW_ERR_CUDA, "row tensor map of member %d: %s", r, h->err.c_str());
+      maps.insert(maps.end(), tm, tm + 3);
+    }
     g->tiles_upto.push_back((int)tiles.size());
   }
   if ((size_t)n > g->args_cap || tiles.size() > g->tiles_cap) {
@@ -1261,12 +1297,15 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
     g->graphs.clear();
     if (g->d_args) cudaFree(g->d_args);
     if (g->d_tiles) cudaFree(g->d_tiles);
+    if (g->d_maps) cudaFree(g->d_maps);
     g->d_args = nullptr;
     g->d_tiles = nullptr;
+    g->d_maps = nullptr;
     g->args_cap = std::max<size_t>(n, 2 * g->args_cap);
     g->tiles_cap = std::max<size_t>(tiles.size(), 2 * g->tiles_cap);
     if (cudaMalloc(&g->d_args, sizeof(StepArgs) * g->args_cap) != cudaSuccess ||
-        cudaMalloc(&g->d_tiles, sizeof(int4) * g->tiles_cap) != cudaSuccess) {
+        cudaMalloc(&g->d_tiles, sizeof(int4) * g->tiles_cap) != cudaSuccess ||
+        cudaMalloc(&g->d_maps, sizeof(CUtensorMap) * 3 * g->args_cap) != cudaSuccess) {
       g->args_cap = g->tiles_cap = 0;
       return fail(nullptr, FW_ERR_OOM, "group device allocation failed");
     }
@@ -1276,8 +1315,60 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
                                    cudaMemcpyHostToDevice, g->capture_stream));
   FW_CUDA(nullptr, cudaMemcpyAsync(g->d_tiles, tiles.data(), sizeof(int4) * tiles.size(),
                                    cudaMemcpyHostToDevice, g->capture_stream));
+  if (!maps.empty())
+    FW_CUDA(nullptr, cudaMemcpyAsync(g->d_maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
+                                     cudaMemcpyHostToDevice, g->capture_stream));
   FW_CUDA(nullptr, cudaStreamSynchronize(g->capture_stream));
   return FW_OK;
+}
+
+// Switch the group's kernel shape: drop the captured graphs and rebuild the work list.
+int group_set_shape(fw_group* g, int k) {
+  for (auto& kv : g->graphs) cudaGraphExecDestroy(kv.second);
+  g->graphs.clear();
+  g->shape = k;
+  std::vector<fw_handle*> m = g->members;
+  return m.empty() ? FW_OK : group_set(g, m.data(), (int)m.size());
+}
+
+int group_advance(fw_group* g, cudaStream_t s, int n_steps);
+
+// Group kernel-shape autotuner, run by the first fw_group_run (every member reset to step 0):
+// each shape advances the group kTuneSteps steps untimed, then kTuneSteps steps timed with events
+// on the caller's stream; the members are reset after each trial and the fastest shape is kept.
+// All shapes give bit-identical results.
+int group_autotune(fw_group* g, cudaStream_t s) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  FW_CUDA(nullptr, cudaEventCreate(&e0));
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return fail(nullptr, FW_ERR_CUDA, "cudaEventCreate failed");
+  }
+  int st = FW_OK, best = 0;
+  float best_ms = 0.f;
+  for (int k = 0; k < kNumShapes2D && st == FW_OK; ++k) {
+    float ms = 0.f;
+    if ((st = group_set_shape(g, k)) || (st = group_advance(g, s, kTuneSteps))) break;
+    if (cudaEventRecord(e0, s) != cudaSuccess) { st = fail(nullptr, FW_ERR_CUDA, "event record failed"); break; }
+    if ((st = group_advance(g, s, kTuneSteps))) break;
+    if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      st = fail(nullptr, FW_ERR_CUDA, "group autotuning trial of shape %d failed", k);
+      break;
+    }
+    for (fw_handle* h : g->members) {
+      if ((st = check_device_status(h, s)) || (st = fw_reset(h, s))) {
+        st = fail(nullptr, st, "group autotuning: %s", h->err.c_str());
+        break;
+      }
+    }
+    if (k == 0 || ms < best_ms) { best_ms = ms; best = k; }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  g->shape_fixed = true;
+  return best == g->shape ? FW_OK : group_set_shape(g, best);
 }
 
 // Advance every member by up to n_steps, each stopping at its own nt.
@@ -1320,6 +1411,28 @@ int fw_group_create(fw_handle* const* handles, int32_t n, fw_group** out) {
   *out = nullptr;
   fw_group* g = new (std::nothrow) fw_group();
   if (!g) return fail(nullptr, FW_ERR_OOM, "host allocation failed");
+  {
+    // kernel shape: FWGB_VARIANT=direct or FWGB_SHAPE2D=<k> fix it; otherwise the 128 x 32 row
+    // march until the first fw_group_run has timed every shape on the group itself
+    const char* v = std::getenv("FWGB_VARIANT");
+    const char* sh = std::getenv("FWGB_SHAPE2D");
+    const char* a = std::getenv("FWGB_AUTOTUNE");
+    g->shape = 4;
+    if (v && std::strcmp(v, "direct") == 0) {
+      g->shape = 0;
+      g->shape_fixed = true;
+    } else if (sh && *sh) {
+      const int k = std::atoi(sh);
+      if (k < 0 || k >= kNumShapes2D) {
+        delete g;
+        return fail(nullptr, FW_ERR_ARGUMENT, "FWGB_SHAPE2D=%s outside [0, %d)", sh, kNumShapes2D);
+      }
+      g->shape = k;
+      g->shape_fixed = true;
+    } else if (a && std::strcmp(a, "0") == 0) {
+      g->shape_fixed = true;
+    }
+  }
   if (cudaStreamCreateWithFlags(&g->capture_stream, cudaStreamNonBlocking) != cudaSuccess) {
     delete g;
     return fail(nullptr, FW_ERR_CUDA, "stream creation failed");
@@ -1362,7 +1475,23 @@ int fw_group_run(fw_group* g, void* stream) {
     if (st) return fail(nullptr, st, "member reset failed: %s", h->err.c_str());
     max_nt = std::max(max_nt, (int)h->d.nt);
   }
+  if (!g->shape_fixed && !g->members.empty()) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cs) == cudaSuccess &&
+        cs == cudaStreamCaptureStatusNone) {
+      int st = group_autotune(g, static_cast<cudaStream_t>(stream));
+      if (st) return st;
+    }
+  }
   return fw_group_advance(g, stream, max_nt);
+}
+
+int fw_group_block_tile(const fw_group* g, int32_t tile[3]) {
+  if (!g || !tile) return FW_ERR_ARGUMENT;
+  tile[0] = g->shape ? kShapes2D[g->shape].xc : kD2TX;
+  tile[1] = g->shape ? kShapes2D[g->shape].ty : kD2TY;
+  tile[2] = 1;
+  return FW_OK;
 }
 
 int fw_group_destroy(fw_group* g) {
@@ -1371,6 +1500,7 @@ int fw_group_destroy(fw_group* g) {
   if (g->capture_stream) cudaStreamDestroy(g->capture_stream);
   if (g->d_args) cudaFree(g->d_args);
   if (g->d_tiles) cudaFree(g->d_tiles);
+  if (g->d_maps) cudaFree(g->d_maps);
   delete g;
   return FW_OK;
 }

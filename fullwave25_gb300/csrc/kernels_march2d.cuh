@@ -14,6 +14,7 @@
 // rectangle of list tiles and the tile shape can change without rebuilding the lists.
 #pragma once
 #include "engine_common.cuh"
+#include "kernels_direct.cuh"
 #include "tma.cuh"
 
 namespace fwgb {
@@ -42,21 +43,23 @@ struct March2Maps {
   CUtensorMap p, vx, vy;
 };
 
+// Bodies take the block's y block (by) and x chunk (bx) explicitly and the tensor maps by address
+// (kernel parameters or global memory), so that the single-simulation kernels and the group
+// kernels (block from a work list, one argument block and map set per simulation) share them.
 template <int TY, int XC, class CV>
-__global__ void __launch_bounds__(TY)
-vel2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
+__device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const CUtensorMap* tm_p,
+                                                 int by, int bx) {
   using R = Row2<TY>;
   __shared__ alignas(128) float ring[kRing2][R::kWideSlot];
   __shared__ alignas(8) uint64_t bar[kRing2];
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tj = threadIdx.x;
-  const int y0 = kGhost + blockIdx.x * TY;
-  const int xb = kGhost + blockIdx.y * XC;
+  const int y0 = kGhost + by * TY;
+  const int xb = kGhost + bx * XC;
   const int xe = min(xb + XC, g.nx - kGhost);
   const int j = y0 + tj;
   const bool active = j < g.ny - kGhost;
-  if (blockIdx.x == 0 && blockIdx.y == 0 && tj == 0) *A.step += 1;
   if (tj == 0) {
     for (int s = 0; s < kRing2; ++s) mbar_init(&bar[s], 1);
     fence_barrier_init();
@@ -66,7 +69,7 @@ vel2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
   if (tj == 0)
     for (int s = 0; s < 3; ++s) {
       mbar_arrive_expect_tx(&bar[s], kBytes);
-      tma_load_2d(ring[s], &tm_p, &bar[s], y0 - 8, xb - 1 + s);
+      tma_load_2d(ring[s], tm_p, &bar[s], y0 - 8, xb - 1 + s);
     }
   const int64_t sx = g.sx;
   const float* __restrict__ p = A.f.p;
@@ -85,7 +88,7 @@ vel2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
       const int s = (it + 3) % kRing2;
       fence_proxy_async_smem();
       mbar_arrive_expect_tx(&bar[s], kBytes);
-      tma_load_2d(ring[s], &tm_p, &bar[s], y0 - 8, x + 2);
+      tma_load_2d(ring[s], tm_p, &bar[s], y0 - 8, x + 2);
     }
     if (it == 0) {
       mbar_wait_bounded(&bar[0], 0, status);
@@ -116,10 +119,9 @@ vel2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
 }
 
 template <int TY, int XC, class CP>
-__global__ void __launch_bounds__(TY)
-prs2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
-            const __grid_constant__ CUtensorMap tm_vy, const int2 list_tiles) {
-  static_assert(TY % 32 == 0 && XC % 8 == 0, "a march block must own whole 32 x 8 list tiles");
+__device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const CUtensorMap* tm_vx,
+                                                 const CUtensorMap* tm_vy, int by, int bx) {
+  static_assert(TY % kD2TY == 0 && XC % kD2TX == 0, "a march block must own whole list tiles");
   using R = Row2<TY>;
   __shared__ alignas(128) float rx[kRing2][R::kNarrowSlot];
   __shared__ alignas(128) float ry[kRing2][R::kWideSlot];
@@ -127,8 +129,8 @@ prs2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tj = threadIdx.x;
-  const int y0 = kGhost + blockIdx.x * TY;
-  const int xb = kGhost + blockIdx.y * XC;
+  const int y0 = kGhost + by * TY;
+  const int xb = kGhost + bx * XC;
   const int xe = min(xb + XC, g.nx - kGhost);
   const int j = y0 + tj;
   const bool active = j < g.ny - kGhost;
@@ -140,8 +142,8 @@ prs2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
   constexpr uint32_t kBytes = (R::kNarrow + R::kWide) * 4;
   auto issue = [&](int s, int x) {
     mbar_arrive_expect_tx(&bar[s], kBytes);
-    tma_load_2d(rx[s], &tm_vx, &bar[s], y0 - 4, x);
-    tma_load_2d(ry[s], &tm_vy, &bar[s], y0 - 8, x);
+    tma_load_2d(rx[s], tm_vx, &bar[s], y0 - 4, x);
+    tma_load_2d(ry[s], tm_vy, &bar[s], y0 - 8, x);
   };
   if (tj == 0)
     for (int s = 0; s < 3; ++s) issue(s, xb - 1 + s);
@@ -191,10 +193,61 @@ prs2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
     for (int t = 0; t < 15; ++t) r[t] = r[t + 1];
     r[15] = rn;
   }
-  // list tiles: list_tiles.x along x (8 rows each), list_tiles.y along y (32 columns each)
-  const int tx0 = blockIdx.y * (XC / 8), ty0 = blockIdx.x * (TY / 32);
-  span_epilogue(A, p, tx0, min(tx0 + XC / 8, list_tiles.x), ty0, min(ty0 + TY / 32, list_tiles.y),
-                list_tiles.y, tj, TY);
+  // the block's list tiles: rows [tx0, tx0 + XC / kD2TX) x columns [ty0, ty0 + TY / kD2TY)
+  const int n_tx = (g.nx - 2 * kGhost + kD2TX - 1) / kD2TX;
+  const int n_ty = (g.ny - 2 * kGhost + kD2TY - 1) / kD2TY;
+  const int tx0 = bx * (XC / kD2TX), ty0 = by * (TY / kD2TY);
+  span_epilogue(A, p, tx0, min(tx0 + XC / kD2TX, n_tx), ty0, min(ty0 + TY / kD2TY, n_ty), n_ty,
+                tj, TY);
+}
+
+// Single simulation: grid (y blocks, x chunks).
+template <int TY, int XC, class CV>
+__global__ void __launch_bounds__(TY)
+vel2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
+  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *A.step += 1;
+  vel2d_march_body<TY, XC, CV>(A, &tm_p, blockIdx.x, blockIdx.y);
+}
+
+template <int TY, int XC, class CP>
+__global__ void __launch_bounds__(TY)
+prs2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
+            const __grid_constant__ CUtensorMap tm_vy) {
+  prs2d_march_body<TY, XC, CP>(A, &tm_vx, &tm_vy, blockIdx.x, blockIdx.y);
+}
+
+// Group (batched) kernels: block b works on work[b] = {simulation, y block, x chunk, 1 if the
+// block advances that simulation's step counter}. `sims` holds one argument block per simulation
+// and `maps` three row tensor maps (p, vx, vy) per simulation, in global memory. The argument
+// block is copied to shared memory first: stores to the fields then cannot alias it.
+__device__ __forceinline__ void stage_args(StepArgs& dst, const StepArgs& src) {
+  static_assert(sizeof(StepArgs) % 4 == 0, "word copy");
+  const int* s = reinterpret_cast<const int*>(&src);
+  int* d = reinterpret_cast<int*>(&dst);
+  for (int w = threadIdx.x; w < (int)(sizeof(StepArgs) / 4); w += blockDim.x) d[w] = s[w];
+  __syncthreads();
+}
+
+template <int TY, int XC>
+__global__ void __launch_bounds__(TY)
+vel2d_march_group(const StepArgs* __restrict__ sims, const CUtensorMap* __restrict__ maps,
+                  const int4* __restrict__ work) {
+  __shared__ alignas(16) StepArgs A;
+  const int4 t = work[blockIdx.x];
+  stage_args(A, sims[t.x]);
+  if (t.w && threadIdx.x == 0) *A.step += 1;
+  vel2d_march_body<TY, XC, CellVelT<2, false>>(A, maps + 3 * t.x, t.y, t.z);
+}
+
+template <int TY, int XC, bool kBeta>
+__global__ void __launch_bounds__(TY)
+prs2d_march_group(const StepArgs* __restrict__ sims, const CUtensorMap* __restrict__ maps,
+                  const int4* __restrict__ work) {
+  __shared__ alignas(16) StepArgs A;
+  const int4 t = work[blockIdx.x];
+  stage_args(A, sims[t.x]);
+  prs2d_march_body<TY, XC, CellPrsT<2, kBeta, false>>(A, maps + 3 * t.x + 1, maps + 3 * t.x + 2,
+                                                       t.y, t.z);
 }
 
 }  // namespace fwgb

@@ -26,7 +26,7 @@ EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_fields_aniso
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
             "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_block_tile", "fw_launches_per_step",
             "fw_destroy", "fw_adjoint_forward", "fw_adjoint_backward", "fw_group_create", "fw_group_run", "fw_group_set_members",
-            "fw_group_advance", "fw_group_destroy",
+            "fw_group_advance", "fw_group_block_tile", "fw_group_destroy",
             "fw_run_noalloc", "fw_last_error")
 
 
@@ -116,6 +116,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_group_run": (C.c_int, [C.c_void_p, vp]),
         "fw_group_set_members": (C.c_int, [C.c_void_p, C.POINTER(C.c_void_p), C.c_int32]),
         "fw_group_advance": (C.c_int, [C.c_void_p, vp, C.c_int32]),
+        "fw_group_block_tile": (C.c_int, [C.c_void_p, _IP]),
         "fw_group_destroy": (C.c_int, [C.c_void_p]),
         "fw_run_noalloc": (C.c_int, [C.POINTER(FwDesc), C.POINTER(FwFields), vp, _FP]),
         "fw_last_error": (C.c_char_p, [H]),
@@ -406,6 +407,15 @@ class EngineGroup:
 
     def traces(self) -> list:
         return [e.read_traces() for e in self.engines]
+
+    @property
+    def block_tile(self) -> tuple:
+        """Cells per block of the group's kernels along (x, y, z)."""
+        v = (C.c_int32 * 3)()
+        st = self.lib.fw_group_block_tile(self._g, v)
+        if st:
+            raise EngineError("fw_group_block_tile", st, "")
+        return tuple(v)
 
     def close(self) -> None:
         if getattr(self, "_g", None) and self._g.value:

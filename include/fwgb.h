@@ -226,6 +226,12 @@ FWGB_API int fw_group_set_members(fw_group *g, fw_handle *const *handles, int32_
 FWGB_API int fw_group_advance(fw_group *g, void *stream, int32_t n_steps);
 
 /* Release the group (not its members). */
+/* Cells per block of the group's kernels along (x, y, z). The group starts on the 128 x 32 row
+ * march (or the shape FWGB_VARIANT / FWGB_SHAPE2D fix at creation); the first fw_group_run
+ * times every 2D kernel shape on the group itself (members reset after each trial) and keeps the
+ * fastest. FWGB_AUTOTUNE=0 disables the trials. No counterpart in the reference. */
+FWGB_API int fw_group_block_tile(const fw_group *g, int32_t tile[3]);
+
 FWGB_API int fw_group_destroy(fw_group *g);
 
 /* Bytes of the file-scope device array that fw_run_noalloc keeps its wavefield in (32 MiB):

@@ -57,3 +57,62 @@ def test_group_rejects_3d_member(engine_lib, cuda):
     with Engine(load_case_inputs("3d_small")) as e3:
         with pytest.raises(EngineError, match="FW_ERR_UNSUPPORTED"):
             EngineGroup([e3])
+
+
+def _group(engines, **env):
+    import os
+
+    from fullwave25_gb300.engine import EngineGroup
+
+    keys = ("FWGB_VARIANT", "FWGB_SHAPE2D", "FWGB_AUTOTUNE")
+    old = {k: os.environ.get(k) for k in keys}
+    for k in keys:
+        os.environ.pop(k, None)
+    os.environ.update({k: str(v) for k, v in env.items()})
+    try:
+        return EngineGroup(engines)
+    finally:
+        for k, v in old.items():
+            if v is None:
+                os.environ.pop(k, None)
+            else:
+                os.environ[k] = v
+
+
+SHAPE_TILES = {0: (8, 32, 1), 1: (16, 64, 1), 2: (32, 64, 1), 3: (16, 128, 1), 4: (32, 128, 1),
+               5: (64, 128, 1)}
+
+
+@pytest.mark.parametrize("shape", sorted(SHAPE_TILES))
+def test_group_every_kernel_shape_equals_alone(engine_lib, cuda, instances, shape):
+    """Group row-march kernels (per-member TMA maps in global memory, staged argument blocks),
+    with a beta/air member mixed in so the beta pressure kernel runs: bitwise equal to solo runs."""
+    from fullwave25_gb300.engine import Engine
+    from golden_io import load_case_inputs
+
+    engines = [d.make_engine() for d in instances[:4]]
+    engines.append(Engine(load_case_inputs("2d_air_beta"), validate=False))
+    alone = [e.run() for e in engines]
+    with _group(engines, FWGB_SHAPE2D=shape) as grp:
+        assert grp.block_tile == SHAPE_TILES[shape]
+        grp.run()
+        for a, t in zip(alone, grp.traces()):
+            np.testing.assert_array_equal(a, t)
+    for e in engines:
+        e.close()
+
+
+def test_group_autotune_keeps_results(engine_lib, cuda, instances):
+    engines = [d.make_engine() for d in instances]
+    alone = [e.run() for e in engines]
+    with _group(engines) as grp:
+        grp.run()                          # first run times every shape, then solves
+        tile = grp.block_tile
+        for a, t in zip(alone, grp.traces()):
+            np.testing.assert_array_equal(a, t)
+        grp.run()
+        assert grp.block_tile == tile      # tuned once
+        for a, t in zip(alone, grp.traces()):
+            np.testing.assert_array_equal(a, t)
+    for e in engines:
+        e.close()
