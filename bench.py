@@ -118,32 +118,41 @@ def traffic_from_profiles(workload: str):
 
 
 # --------------------------------------------------------------------------------- workloads
+def workload_desc(name: str, grid: int = 0) -> dict:
+    """The ``config`` description of a workload (shared by the GPU arm and the reference arm)."""
+    if name == "plain2d":
+        return {"workload": "plain 2D forward, 768x512 + PML 40 + transition 40 (944x688), "
+                            "nt 4000, 8 random ellipses, 2 relaxation mechanisms",
+                "grid": [944, 688], "nt": 4000, "steps_per_bench_step": 4000,
+                "l2": "flushed (256 MB write) before every bench step; working set 60 MB"}
+    if name == "plain3d":
+        edge = grid or 512
+        return {"workload": f"plain 3D forward, {edge}^3 + PML 32 + transition 32 "
+                            f"({edge + 144}^3), nt 3000, "
+                            "layered fat/muscle/liver with perturbed interfaces and 0.5% scatterers,"
+                            " 64-element plane-wave source, 256x256 sensor plane",
+                "grid": [edge + 144] * 3, "nt": 3000, "steps_per_bench_step": 100,
+                "l2": "inputs larger than L2 (working set ~30 GB)"}
+    raise ValueError(f"unknown workload {name}")
+
+
 def make_workload(name: str, rank: int, grid: int = 0):
     """Return (inputs-or-builder, steps_per_bench_step, description dict).
 
     ``grid`` > 0 replaces the 3D workload's 512^3 cells by grid^3 (small profiling cases)."""
+    desc = workload_desc(name, grid)
     if name == "plain2d":
         from fullwave25_gb300.workloads import plain_2d_inputs
 
         inp = plain_2d_inputs(seed=rank)
-        desc = {"workload": "plain 2D forward, 768x512 + PML 40 + transition 40 (944x688), "
-                            "nt 4000, 8 random ellipses, 2 relaxation mechanisms",
-                "grid": list(inp.shape), "nt": inp.nt, "steps_per_bench_step": inp.nt,
-                "l2": "flushed (256 MB write) before every bench step; working set 60 MB"}
+        assert list(inp.shape) == desc["grid"] and inp.nt == desc["nt"]
         return inp, inp.nt, desc
-    if name == "plain3d":
-        from fullwave25_gb300.workloads3d import plain_3d_device_inputs
+    from fullwave25_gb300.workloads3d import plain_3d_device_inputs
 
-        edge = grid or 512
-        dinp = plain_3d_device_inputs(seed=rank, shape=(edge, edge, edge))
-        desc = {"workload": f"plain 3D forward, {edge}^3 + PML 32 + transition 32 "
-                            f"({edge + 144}^3), nt 3000, "
-                            "layered fat/muscle/liver with perturbed interfaces and 0.5% scatterers,"
-                            " 64-element plane-wave source, 256x256 sensor plane",
-                "grid": list(dinp.shape), "nt": dinp.nt, "steps_per_bench_step": 100,
-                "l2": "inputs larger than L2 (working set ~30 GB)"}
-        return dinp, 100, desc
-    raise ValueError(f"unknown workload {name}")
+    edge = grid or 512
+    dinp = plain_3d_device_inputs(seed=rank, shape=(edge, edge, edge))
+    assert list(dinp.shape) == desc["grid"] and dinp.nt == desc["nt"]
+    return dinp, 100, desc
 
 
 # --------------------------------------------------------------------------------- CPU baseline
@@ -210,8 +219,11 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {"workload": args.workload, "engine": "FP64 C oracle restatement "
-                       "(reference engine is a closed x86-64 CUDA executable; no CPU engine)"},
+            "config": {**workload_desc(args.workload, args.grid),
+                       "parallelism": "single GPU" if world == 1 else f"replicas x{world}",
+                       "engine": "FP64 C oracle restatement on the host cores (the reference "
+                                 "engine is a closed x86-64 CUDA executable; it has no CPU "
+                                 "engine)"},
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": r["cores"], "kind": "port",
                              "sample": r["sample"]},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
@@ -384,10 +396,13 @@ def run_batch(args):
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     ids = rank_instances(rank, world, args.batch)
+    torch.zeros(1, device=dev)  # context creation outside the timed build
+    torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     insts = [batch_instance(i) for i in ids]
-    build_s = time.perf_counter() - t0
     engines = [d.make_engine() for d in insts]
+    torch.cuda.synchronize(dev)
+    build_s = time.perf_counter() - t0
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
     units = sum(int(np.prod(d.shape)) * d.nt for d in insts)
@@ -403,6 +418,10 @@ def run_batch(args):
             ev[2 * i + 1].record(stream)
         torch.cuda.synchronize(dev)
     group_ms = sum(ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(args.steps)) / args.steps
+    # end to end, batched: device build (timed above) + group solve + every trace to the host
+    t0 = time.perf_counter()
+    traces = grp.traces()
+    readback_s = time.perf_counter() - t0
     # the same simulations one by one (each a full solve on the same device-resident inputs);
     # one untimed advance first, so that each grid size's kernel-shape autotuning is not timed
     for e in engines:
@@ -419,12 +438,41 @@ def run_batch(args):
         torch.cuda.synchronize(dev)
         lat.append(a.elapsed_time(b))
     serial_ms = sum(lat)
+    batched_e2e_s = build_s + group_ms / 1e3 + readback_s
+    # end to end, one by one through the host-side API (the reference's call sequence: NumPy
+    # pre-processing, engine creation and upload, solve, traces back), on a sample of instances
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.workloads_batch import batch_inputs_host
+
+    sample = list(ids[:args.host_sample])
+    host_s, host_err = [], []
+    for n, i in enumerate(sample):
+        t0 = time.perf_counter()
+        with Engine(batch_inputs_host(i), validate=False) as e:
+            tr = e.run(sptr)
+        host_s.append(time.perf_counter() - t0)
+        ref = traces[n]
+        host_err.append(float(np.linalg.norm(tr - ref) / max(np.linalg.norm(ref), 1e-30)))
+    dev_sample_s = sum(lat[:len(sample)]) / 1e3
+    # the sample's own batched throughput (same simulations as the host-API runs)
+    grp_sample_s = None
+    if sample:
+        with EngineGroup(engines[:len(sample)]) as gs:
+            gs.run(sptr)  # untimed: shape autotuning of this group
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            gs.run(sptr)
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            grp_sample_s = a.elapsed_time(b) / 1e3
     from fullwave25_gb300.workloads import algorithmic_bytes_per_cell
 
     achieved = units * algorithmic_bytes_per_cell(2) / (group_ms / 1e3) / 1e9
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (
         ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
+    tr = traffic_from_profiles("batch2d")
+    cells_all = sum(int(np.prod(d.shape)) for d in insts)
     line = {"metric": METRIC, "value": units / (group_ms / 1e3) / 1e9, "unit": METRIC,
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": group_ms, "higher_is_better": True, "scaling": "weak",
@@ -439,11 +487,35 @@ def run_batch(args):
             "sims_per_s": {"batched": len(insts) / (group_ms / 1e3),
                            "one_by_one": len(insts) / (serial_ms / 1e3),
                            "batched_over_one_by_one": serial_ms / group_ms},
+            "e2e": {"value": units / batched_e2e_s / 1e9, "unit": METRIC,
+                    "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": int(sum(t.nbytes for t in traces)),
+                    "sims_per_s": len(insts) / batched_e2e_s,
+                    "api": "device-side build of every instance + fw_group_run + "
+                           "fw_read_traces of every member (media built on the GPU)"},
+            "one_by_one_host_api": {
+                "sample_instances": sample,
+                "sims_per_s": len(sample) / sum(host_s) if sample else None,
+                "device_resident_sims_per_s_same_sample":
+                    len(sample) / dev_sample_s if sample else None,
+                "batched_sims_per_s_same_sample":
+                    len(sample) / grp_sample_s if grp_sample_s else None,
+                "batched_over_host_api_same_sample":
+                    sum(host_s) / grp_sample_s if grp_sample_s else None,
+                "rel_l2_vs_batched_traces_max": max(host_err) if host_err else None,
+                "api": "NumPy pre-processing (relaxation lookup, PML builder) + Engine "
+                       "(fw_create, fw_set_fields host) + fw_run with host traces, per instance"},
             "one_by_one_latency_ms": {"p50": float(np.percentile(lat, 50)),
                                       "p99": float(np.percentile(lat, 99)),
                                       "max": float(max(lat))},
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                         "frac": achieved / peak, "traffic": None},
+                         "frac": achieved / peak,
+                         "traffic": (tr * cells_all if tr is not None else None),
+                         "kernel": "group time step = velocity + pressure group kernels, "
+                                   "every member active",
+                         "algorithmic_bytes_per_cell_update": algorithmic_bytes_per_cell(2),
+                         "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
+                         else "fallback 6800 GB/s"},
             "gpu_launches": 2 * max(d.nt for d in insts) * args.steps,
             "clocks": clocks.summary()}
     if rank == 0:
@@ -567,6 +639,8 @@ def main():
     ap.add_argument("--scale", type=float, default=0.5, help="serve2d: instance size scale")
     ap.add_argument("--budget-gb", type=int, default=150, help="serve2d: device memory budget")
     ap.add_argument("--batch", type=int, default=64, help="simulations per rank (batch2d)")
+    ap.add_argument("--host-sample", type=int, default=8,
+                    help="batch2d: instances also run one by one through the host-side API")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=0,
                     help="3D workload edge in cells (default 512; smaller for profiling)")

@@ -153,3 +153,44 @@ def batch_instance(i: int, device=None, n_pml: int = 40, n_transition: int = 40,
                      outc=i32(outc), icczero=i32(np.zeros((0, 2))))
     d.spec = spec
     return d
+
+
+def batch_problem_host(i: int, n_pml: int = 40, n_transition: int = 40, scale: float = 1.0):
+    """Instance ``i`` through the host-side API (the reference's call sequence): Grid, a NumPy
+    medium with the same seeded draws, relaxation-table lookup, Source/Sensor masks; returns
+    (grid, medium, source, sensor, (n_pml, n_transition)) for :class:`PMLBuilder` /
+    :class:`fullwave25_gb300.Solver`. Same physics as :func:`batch_instance`."""
+    from .medium import MediumRelaxationMaps  # noqa: PLC0415
+    from .source import Sensor, Source  # noqa: PLC0415
+    from .workloads import ellipse_medium_2d  # noqa: PLC0415
+
+    spec = instance_spec(i)
+    nx = max(32, int(spec["nx"] * scale))
+    ny = max(N_ELEMENTS, int(spec["ny"] * scale) // N_ELEMENTS * N_ELEMENTS)
+    nt = max(50, int(spec["nt"] * scale))
+    spec = {**spec, "nx": nx, "ny": ny, "nt": nt}
+    grid = Grid.from_cells((nx, ny), f0=spec["f0"], nt=nt, ppw=12, cfl=0.2)
+    c, rho, a0, gam = ellipse_medium_2d((nx, ny), grid.dx, seed=spec["seed"])
+    medium = MediumRelaxationMaps(grid, c, rho, np.zeros((nx, ny)),
+                                  default_table().lookup(a0, gam))
+    w = ny // N_ELEMENTS
+    sig = np.stack([gaussian_modulated_sinusoidal_signal(
+        nt=nt, duration=grid.duration, ncycles=2, drop_off=2, f0=spec["f0"], p0=1e6,
+        delay_sec=float(d)) for d in transmit_delays(spec, grid.dx)])
+    mask = np.zeros((nx, ny), dtype=bool)
+    mask[0, :N_ELEMENTS * w] = True
+    source = Source(np.repeat(sig, w, axis=0), mask)
+    smask = np.zeros((nx, ny), dtype=bool)
+    smask[1, :] = True
+    sensor = Sensor(smask, sampling_modulus_time=1)
+    return grid, medium, source, sensor, (n_pml, n_transition)
+
+
+def batch_inputs_host(i: int, **kw):
+    """Host :class:`EngineInputs` of instance ``i`` built by the NumPy pre-processing path."""
+    from .inputs import build_inputs  # noqa: PLC0415
+    from .pml import PMLBuilder  # noqa: PLC0415
+
+    grid, medium, source, sensor, (n_pml, n_tr) = batch_problem_host(i, **kw)
+    b = PMLBuilder(grid, medium, source, sensor, n_pml_layer=n_pml, n_transition_layer=n_tr)
+    return build_inputs(b.extended_grid, b.run(), b.extended_source, b.extended_sensor)

@@ -116,3 +116,22 @@ def test_group_autotune_keeps_results(engine_lib, cuda, instances):
             np.testing.assert_array_equal(a, t)
     for e in engines:
         e.close()
+
+
+def test_host_api_instance_matches_device_built_instance(engine_lib, cuda):
+    """The batched workload built on the device and the same instance built through the host-side
+    API (NumPy medium, relaxation lookup, PML builder) give the same traces."""
+    from fdtd_oracle import rel_l2
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.workloads_batch import batch_inputs_host, batch_instance
+
+    kw = dict(scale=0.12, n_pml=10, n_transition=10)
+    for i in (0, 5):
+        d = batch_instance(i, **kw)
+        h = batch_inputs_host(i, **kw)
+        assert tuple(h.shape) == tuple(d.shape) and h.nt == d.nt
+        with d.make_engine() as a, Engine(h) as b:
+            ta, tb = a.run(), b.run()
+        assert np.abs(ta).max() > 0
+        err = rel_l2(tb, ta)
+        assert err < 1e-5, f"instance {i}: rel-L2 {err:.3e}"
