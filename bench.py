@@ -526,45 +526,63 @@ def run_batch(args):
 
 
 def run_serve(args):
-    """Serving stream: Poisson arrivals of forward solves, continuous batching vs FIFO."""
+    """Serving stream: Poisson arrivals of forward and gradient solves, continuous batching vs
+    FIFO one at a time."""
     import torch
 
     from fullwave25_gb300.server import (Request, engine_bytes, poisson_arrivals,
                                          serve_continuous, serve_fifo)
-    from fullwave25_gb300.workloads_batch import batch_instance
+    from fullwave25_gb300.workloads_batch import batch_instance, gradient_job
 
     torch.cuda.set_device(0)
     arrivals = poisson_arrivals(args.rate, args.duration, seed=0)
     scale = args.scale
+    kinds = np.where(np.random.default_rng(1).random(len(arrivals)) < args.grad_frac,
+                     "gradient", "forward")
 
-    def make(i, t):
-        return Request(rid=i, arrival=float(t), build=lambda i=i: batch_instance(i, scale=scale))
-
-    reqs = [make(i, t) for i, t in enumerate(arrivals)]
-    for r in reqs:  # memory need from the instance geometry (built once to measure)
-        d = r.build()
-        r.bytes_needed = engine_bytes(d.shape, d.nt, d.outc.shape[0])
-        del d
+    reqs = []
+    for i, (t, kind) in enumerate(zip(arrivals, kinds)):
+        if kind == "gradient":
+            # the request's input data (starting medium, observed traces) exists before it arrives
+            job = gradient_job(i, scale=scale)
+            reqs.append(Request(rid=i, arrival=float(t), build=(lambda j=job: j), kind="gradient",
+                                bytes_needed=job.bytes_needed()))
+        else:
+            r = Request(rid=i, arrival=float(t), build=lambda i=i: batch_instance(i, scale=scale))
+            d = r.build()  # memory need from the instance geometry (built once to measure)
+            r.bytes_needed = engine_bytes(d.shape, d.nt, d.outc.shape[0])
+            del d
+            reqs.append(r)
     torch.cuda.synchronize()
     # warm-up: one small continuous run so that graphs and kernels are loaded
-    serve_continuous(reqs[:3], budget_bytes=args.budget_gb << 30)
+    warm = [r for r in reqs if r.kind == "forward"][:3] + [r for r in reqs if r.kind == "gradient"][:1]
+    serve_continuous(warm, budget_bytes=args.budget_gb << 30)
+    for r in warm:
+        r.admitted = r.finished = -1.0
+        r.traces = r.result = None
     with ClockSampler(0) as clocks:
         cont = serve_continuous(reqs, budget_bytes=args.budget_gb << 30, chunk_steps=256)
-    cont_lat = [r.latency for r in reqs]
+    for r in reqs:
+        r.result = None
     fifo = serve_fifo(reqs)
+    for r in reqs:
+        r.result = None
+    n_grad = int((kinds == "gradient").sum())
     line = {"metric": "simulations/s (serving stream)", "value": cont["sims_per_s"],
             "unit": "sims/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": f"Poisson {args.rate} req/s for {args.duration} s of 2D forward "
-                                   f"solves (batched-workload instances at scale {scale}), "
-                                   f"device budget {args.budget_gb} GB, blocks of 256 steps",
-                       "requests": len(reqs)},
+            "config": {"workload": f"Poisson {args.rate} req/s for {args.duration} s: 2D forward "
+                                   f"solves (batched-workload instances) and "
+                                   f"{args.grad_frac:.0%} gradient solves (512-1024 square "
+                                   f"grids, nt 6000 at 1024), sizes scaled by {scale}; device "
+                                   f"budget {args.budget_gb} GB, blocks of 256 steps, "
+                                   "2 gradient worker streams",
+                       "requests": len(reqs), "gradient_requests": n_grad},
             "continuous": cont, "fifo_one_at_a_time": fifo,
             "sims_per_s_ratio": cont["sims_per_s"] / fifo["sims_per_s"],
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
-    del cont_lat
 
 
 def run_adjoint(args):
@@ -638,6 +656,8 @@ def main():
     ap.add_argument("--duration", type=float, default=10.0, help="serve2d: stream length [s]")
     ap.add_argument("--scale", type=float, default=0.5, help="serve2d: instance size scale")
     ap.add_argument("--budget-gb", type=int, default=150, help="serve2d: device memory budget")
+    ap.add_argument("--grad-frac", type=float, default=0.2,
+                    help="serve2d: fraction of gradient requests")
     ap.add_argument("--batch", type=int, default=64, help="simulations per rank (batch2d)")
     ap.add_argument("--host-sample", type=int, default=8,
                     help="batch2d: instances also run one by one through the host-side API")

@@ -43,34 +43,38 @@ def _torch():
 def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=None):
     """Misfit and raw-map gradients for ``engine`` (its current fields) against ``observed``.
 
-    ``observed``: CUDA float32 tensor ``[n_out, ncoordsout]``. Returns ``(J, traces, grads)`` with
-    ``grads[name]`` a float64 CUDA tensor of the grid shape for every name in ``RAW_MAPS``.
+    ``observed``: CUDA float32 tensor ``[n_out, ncoordsout]``. ``stream``: a torch CUDA stream
+    (None: the current one); all work is ordered on it and only it is synchronised, so gradient
+    evaluations on other streams overlap. Returns ``(J, traces, grads)`` with ``grads[name]`` a
+    float64 CUDA tensor of the grid shape for every name in ``RAW_MAPS``.
     """
     torch = _torch()
     inp = engine.inputs
     dev = observed.device
-    engine.adjoint_forward(checkpoint_every, stream)
-    traces = torch.empty_like(observed)
-    engine.read_traces_into(0, inp.n_out, traces.data_ptr(), stream)
-    torch.cuda.synchronize(dev)
-    residual = (traces - observed).contiguous()
-    J = 0.5 * float(torch.sum(residual.double() ** 2))
-    g = torch.zeros((len(ADJOINT_MAPS),) + tuple(inp.shape), dtype=torch.float64, device=dev)
-    engine.adjoint_backward(residual.data_ptr(), g.data_ptr(), stream)
-    torch.cuda.synchronize(dev)
-    gm = dict(zip(ADJOINT_MAPS, g))
-    m = {k: inp.maps[k].double() for k in ("rho", "K", "kappau", "kappax")}
-    dt = float(np.float32(inp.dt))
-    grads = {
-        "rho": gm["rdt_rho"] * (-dt / m["rho"] ** 2),
-        "K": gm["dt_k"] * dt,
-        "kappau": gm["inv_ku"] * (-1.0 / m["kappau"] ** 2),
-        "kappax": gm["inv_kx"] * (-1.0 / m["kappax"] ** 2),
-    }
-    for nu in (1, 2):
-        for ax in ("u", "x"):
-            grads[f"apml{ax}{nu}"] = gm[f"a{ax}{nu}"]
-            grads[f"bpml{ax}{nu}"] = gm[f"b{ax}{nu}"]
+    ts = stream if stream is not None else torch.cuda.current_stream(dev)
+    raw = ts.cuda_stream
+    with torch.cuda.stream(ts):
+        engine.adjoint_forward(checkpoint_every, raw)
+        traces = torch.empty_like(observed)
+        engine.read_traces_into(0, inp.n_out, traces.data_ptr(), raw)
+        residual = (traces - observed).contiguous()
+        J = 0.5 * float(torch.sum(residual.double() ** 2))
+        g = torch.zeros((len(ADJOINT_MAPS),) + tuple(inp.shape), dtype=torch.float64, device=dev)
+        engine.adjoint_backward(residual.data_ptr(), g.data_ptr(), raw)
+        gm = dict(zip(ADJOINT_MAPS, g))
+        m = {k: inp.maps[k].double() for k in ("rho", "K", "kappau", "kappax")}
+        dt = float(np.float32(inp.dt))
+        grads = {
+            "rho": gm["rdt_rho"] * (-dt / m["rho"] ** 2),
+            "K": gm["dt_k"] * dt,
+            "kappau": gm["inv_ku"] * (-1.0 / m["kappau"] ** 2),
+            "kappax": gm["inv_kx"] * (-1.0 / m["kappax"] ** 2),
+        }
+        for nu in (1, 2):
+            for ax in ("u", "x"):
+                grads[f"apml{ax}{nu}"] = gm[f"a{ax}{nu}"]
+                grads[f"bpml{ax}{nu}"] = gm[f"b{ax}{nu}"]
+    ts.synchronize()
     return J, traces, grads
 
 

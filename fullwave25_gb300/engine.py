@@ -233,7 +233,9 @@ class Engine:
             icc=iptr(inp.icc), outc=iptr(inp.outc), icczero=iptr(inp.icczero),
             icmat=fptr(inp.icmat), on_device=1,
             **{k: fptr(m[k]) for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)})
-        torch.cuda.synchronize(dev)
+        # the tensors were produced on the caller's current stream: wait for that stream only,
+        # so that work on other streams (other simulations) keeps running
+        torch.cuda.current_stream(dev).synchronize()
         if "kappay" in m:
             for k in anisotropic_extra_maps(inp.ndim):
                 assert m[k].dtype == torch.float32 and m[k].is_contiguous() and m[k].is_cuda, k

@@ -194,3 +194,38 @@ def batch_inputs_host(i: int, **kw):
     grid, medium, source, sensor, (n_pml, n_tr) = batch_problem_host(i, **kw)
     b = PMLBuilder(grid, medium, source, sensor, n_pml_layer=n_pml, n_transition_layer=n_tr)
     return build_inputs(b.extended_grid, b.run(), b.extended_source, b.extended_sensor)
+
+
+GRADIENT_SIZES = (512, 768, 1024)
+
+
+def gradient_job(i: int, scale: float = 1.0, device=None, checkpoint_every: int = 200):
+    """Gradient request ``i`` of the serving mix (seed = i): a square grid drawn from
+    {512, 768, 1024}^2 (times ``scale``), nt = 6000 at 1024 scaled with the grid, f0 = 3 MHz,
+    sensors every other cell of depth row 5; the starting medium is the seeded true medium
+    Gaussian-blurred with sigma = 2 mm, and the observed traces are the true medium's forward
+    solve (computed here, as the request's input data)."""
+    from scipy.ndimage import gaussian_filter  # noqa: PLC0415
+
+    from .adjoint import AdjointProblem  # noqa: PLC0415
+    from .engine import Engine  # noqa: PLC0415
+    from .server import GradientJob  # noqa: PLC0415
+    from .workloads import ellipse_medium_2d  # noqa: PLC0415
+
+    torch = _torch()
+    device = device or torch.device("cuda", torch.cuda.current_device())
+    rng = np.random.default_rng(10_000 + i)
+    n = max(64, int(int(rng.choice(GRADIENT_SIZES)) * scale))
+    nt = max(100, int(round(6000 * n / 1024)))
+    dx = 1540 / 3e6 / 12
+    c, rho, a0, gam = ellipse_medium_2d((n, n), dx, seed=10_000 + i)
+    sig = 2e-3 / dx
+    t = lambda a: torch.as_tensor(a, dtype=torch.float64, device=device)  # noqa: E731
+    blur = lambda a: t(gaussian_filter(a, sig, mode="nearest"))  # noqa: E731
+    start = (blur(c), blur(rho), blur(a0), t(gam))
+    prob = AdjointProblem((n, n), nt=nt, n_pml=40, n_transition=40, c_ref=start[0],
+                          device=device, sensor_step=2, sensor_row=5)
+    with Engine(prob.build(t(c), t(rho), t(a0), t(gam)), validate=False) as e:
+        observed = torch.as_tensor(e.run(), device=device)
+    return GradientJob(problem=prob, start=start, observed=observed,
+                       checkpoint_every=min(checkpoint_every, nt))

@@ -44,3 +44,30 @@ def test_budget_limits_concurrency(engine_lib, cuda):
     order = sorted(reqs, key=lambda r: r.admitted)
     for a, b in zip(order, order[1:]):
         assert b.admitted >= a.finished - 1e-9
+
+
+def test_forward_and_gradient_mix_equal_alone(engine_lib, cuda):
+    """Gradient requests run on worker streams while forward requests step in the group: every
+    forward result and every gradient equals the one computed alone."""
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.server import Request, serve_continuous
+    from fullwave25_gb300.workloads_batch import gradient_job
+
+    reqs = _requests(6, 0.12, rate_hz=40.0)
+    jobs = [gradient_job(i, scale=0.12) for i in range(3)]
+    for k, j in enumerate(jobs):
+        reqs.append(Request(rid=100 + k, arrival=0.02 * k, build=(lambda j=j: j),
+                            kind="gradient", bytes_needed=j.bytes_needed()))
+    stats = serve_continuous(reqs, budget_bytes=8 << 30, chunk_steps=64, gradient_workers=2)
+    assert stats["requests"] == 9 and set(stats["by_kind"]) == {"forward", "gradient"}
+    for r in reqs:
+        assert r.finished >= r.admitted >= r.arrival - 1e-9
+        if r.kind == "forward":
+            with Engine(r.build(), validate=False) as e:
+                np.testing.assert_array_equal(r.traces, e.run())
+        else:
+            alone = r.build().run()
+            assert r.result["J"] == alone["J"] and alone["J"] > 0
+            for k, g in alone["grads"].items():
+                np.testing.assert_allclose(r.result["grads"][k].cpu().numpy(), g.cpu().numpy(),
+                                           rtol=1e-12, atol=0, err_msg=k)
