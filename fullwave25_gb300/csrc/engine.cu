@@ -24,6 +24,7 @@
 #include "kernels_direct.cuh"
 #include "kernels_march3d.cuh"
 #include "kernels_march2d.cuh"
+#include "kernels_persistent2d.cuh"
 #include "kernels_adjoint2d.cuh"
 
 using namespace fwgb;
@@ -42,14 +43,18 @@ namespace {
 constexpr int kMarchXC = 64;  // x planes per block of the 3D plane-march kernels
 
 // 2D kernel shapes the autotuner chooses from: 0 = direct kernels (one block per 32 y x 8 x tile),
-// else the row-march kernels with TY threads (y columns) walking XC rows. TY + 16 <= 256 (TMA box
-// limit), TY a multiple of 32 and XC of 8 (whole list tiles per block).
-struct Shape2D { int ty, xc; };
-constexpr Shape2D kShapes2D[] = {{0, 0}, {64, 16}, {64, 32}, {128, 16}, {128, 32}, {128, 64}};
+// 1-5 = row-march kernels with TY threads (y columns) walking XC rows (TY + 16 <= 256, the TMA box
+// limit; TY a multiple of 32 and XC of 8, whole list tiles per block), 6 = the persistent kernel
+// (direct bodies, one cooperative launch per block of steps, grid barriers between phases).
+struct Shape2D { int ty, xc; bool persistent; };
+constexpr Shape2D kShapes2D[] = {{0, 0, false},   {64, 16, false},  {64, 32, false},
+                                 {128, 16, false}, {128, 32, false}, {128, 64, false},
+                                 {0, 0, true}};
+constexpr int kPersistentShape = 6;
 constexpr int kNumShapes2D = sizeof(kShapes2D) / sizeof(kShapes2D[0]);
 constexpr int kTuneSteps = 64;   // time steps per autotuning trial (one graph)
 
-enum Variant { kDirect = 0, kMarch = 1 };
+enum Variant { kDirect = 0, kMarch = 1, kPersistent = 2 };
 
 struct Tiling {
   int t[3];   // tile extent along x, y, z (z unused in 2D)
@@ -73,6 +78,7 @@ struct fw_handle {
   float* icmat_t = nullptr;    // [nt_ic][ncoords]
   float* traces = nullptr;     // [n_out][ncoordsout]
   int* step = nullptr;
+  unsigned* bar = nullptr;     // persistent 2D kernel: grid-barrier words (kBarWords)
   void* lists = nullptr;       // one allocation for all per-tile lists
   std::vector<int32_t> rec_k_host;   // sensor index of each record entry (entry order)
   void* groups = nullptr;      // rec_group (int32) + rec_w (float) per record entry
@@ -236,9 +242,10 @@ template <int ND, class CV, class CP, int kMin>
 void launch_typed(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
   if constexpr (ND == 2) {
-    static_assert(kNumShapes2D == 6, "one case per 2D march shape");
+    static_assert(kNumShapes2D == 7, "one case per 2D kernel shape");
     switch (h->shape2d) {
-      case 0: {
+      case 0:
+      case kPersistentShape: {  // the persistent shape issues the direct kernels when captured
         dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
         vel2d_direct<CV><<<grid, block, 0, s>>>(h->args);
         prs2d_direct<CP><<<grid, block, 0, s>>>(h->args);
@@ -248,7 +255,7 @@ void launch_typed(fw_handle* h, cudaStream_t s) {
       case 2: launch_march2d<64, 32, CV, CP>(h, s); break;
       case 3: launch_march2d<128, 16, CV, CP>(h, s); break;
       case 4: launch_march2d<128, 32, CV, CP>(h, s); break;
-      default: launch_march2d<128, 64, CV, CP>(h, s); break;
+      case 5: launch_march2d<128, 64, CV, CP>(h, s); break;
     }
   } else if (h->variant == kMarch) {
     dim3 grid(t.n[2], t.n[1], t.n[0]), block(kMTZ, kMTY);
@@ -280,6 +287,43 @@ void launch_step(fw_handle* h, cudaStream_t s) {
     if (h->has_beta) launch_nd<3, true>(h, s);
     else launch_nd<3, false>(h, s);
   }
+}
+
+// Persistent 2D kernel: steps n0 .. n0 + n_steps - 1 in one cooperative launch. Each block owns
+// an equal share of the 32 x 8 tiles; the grid is at most the co-resident block count.
+template <class CV, class CP>
+int launch_persistent_typed(fw_handle* h, cudaStream_t s, int n0, int n_steps) {
+  auto kern = step2d_persistent<CV, CP>;
+  int per_sm = 0, dev = 0, sms = 0;
+  FW_CUDA(h, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kD2TY * kD2TX, 0));
+  FW_CUDA(h, cudaGetDevice(&dev));
+  FW_CUDA(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  int n_tiles = h->tiling.count(), n_ty = h->tiling.n[1];
+  const int max_blocks = std::min(per_sm * sms, kBarGroup * kBarMaxGroups);
+  if (max_blocks < 1) return fail(h, FW_ERR_CUDA, "persistent kernel: no block fits an SM");
+  const int per_block = (n_tiles + max_blocks - 1) / max_blocks;
+  const int grid = (n_tiles + per_block - 1) / per_block;
+  if (!h->bar) FW_CUDA(h, cudaMalloc(&h->bar, kBarWords * sizeof(unsigned)));
+  FW_CUDA(h, cudaMemsetAsync(h->bar, 0, kBarWords * sizeof(unsigned), s));
+  void* args[] = {&h->args, &h->bar, &n0, &n_steps, &n_tiles, &n_ty};
+  FW_CUDA(h, cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(grid),
+                                         dim3(kD2TY, kD2TX), args, 0, s));
+  return FW_OK;
+}
+
+template <bool kBeta>
+int launch_persistent_nd(fw_handle* h, cudaStream_t s, int n0, int n_steps) {
+  if (h->exp)
+    return launch_persistent_typed<CellVelExpT<2>, CellPrsExpT<2, kBeta>>(h, s, n0, n_steps);
+  if (h->aniso)
+    return launch_persistent_typed<CellVelT<2, true>, CellPrsT<2, kBeta, true>>(h, s, n0, n_steps);
+  return launch_persistent_typed<CellVelT<2, false>, CellPrsT<2, kBeta, false>>(h, s, n0, n_steps);
+}
+
+int launch_persistent(fw_handle* h, cudaStream_t s, int n0, int n_steps) {
+  if (n_steps <= 0) return FW_OK;
+  return h->has_beta ? launch_persistent_nd<true>(h, s, n0, n_steps)
+                     : launch_persistent_nd<false>(h, s, n0, n_steps);
 }
 
 int build_graph(fw_handle* h, int steps) {
@@ -342,7 +386,7 @@ int encode_row_map(fw_handle* h, CUtensorMap* map, float* base, uint32_t bw) {
 
 // Select 2D kernel shape k: encode the row tensor maps for its width, drop the step graph.
 int set_shape2d(fw_handle* h, int k) {
-  if (k > 0) {
+  if (kShapes2D[k].ty > 0) {
     const uint32_t ty = (uint32_t)kShapes2D[k].ty;
     int st;
     if ((st = encode_row_map(h, &h->tmaps2.p, h->args.f.p, ty + 16)) ||
@@ -351,7 +395,7 @@ int set_shape2d(fw_handle* h, int k) {
       return st;
   }
   h->shape2d = k;
-  h->variant = k > 0 ? kMarch : kDirect;
+  h->variant = kShapes2D[k].persistent ? kPersistent : kShapes2D[k].ty > 0 ? kMarch : kDirect;
   h->graph_steps = 0;   // the next advance captures a graph with the new kernels
   return FW_OK;
 }
@@ -901,13 +945,26 @@ int autotune_2d(fw_handle* h, cudaStream_t s) {
   float best_ms = 0.f;
   for (int k = 0; k < kNumShapes2D && st == FW_OK; ++k) {
     float ms = 0.f;
-    if ((st = set_shape2d(h, k)) || (st = build_graph(h, kTuneSteps))) break;
-    if (cudaGraphLaunch(h->graph, s) != cudaSuccess || cudaEventRecord(e0, s) != cudaSuccess ||
-        cudaGraphLaunch(h->graph, s) != cudaSuccess || cudaEventRecord(e1, s) != cudaSuccess ||
-        cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
-      st = fail(h, FW_ERR_CUDA, "autotuning trial of 2D shape %d failed: %s", k,
-                cudaGetErrorString(cudaGetLastError()));
-      break;
+    if ((st = set_shape2d(h, k))) break;
+    if (kShapes2D[k].persistent) {
+      if ((st = launch_persistent(h, s, 0, kTuneSteps))) break;
+      if (cudaEventRecord(e0, s) != cudaSuccess) { st = fail(h, FW_ERR_CUDA, "event record failed"); break; }
+      if ((st = launch_persistent(h, s, kTuneSteps, kTuneSteps))) break;
+      if (cudaEventRecord(e1, s) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+          cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        st = fail(h, FW_ERR_CUDA, "autotuning trial of 2D shape %d failed: %s", k,
+                  cudaGetErrorString(cudaGetLastError()));
+        break;
+      }
+    } else {
+      if ((st = build_graph(h, kTuneSteps))) break;
+      if (cudaGraphLaunch(h->graph, s) != cudaSuccess || cudaEventRecord(e0, s) != cudaSuccess ||
+          cudaGraphLaunch(h->graph, s) != cudaSuccess || cudaEventRecord(e1, s) != cudaSuccess ||
+          cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+        st = fail(h, FW_ERR_CUDA, "autotuning trial of 2D shape %d failed: %s", k,
+                  cudaGetErrorString(cudaGetLastError()));
+        break;
+      }
     }
     if ((st = check_device_status(h, s)) || (st = fw_reset(h, s))) break;
     if (k == 0 || ms < best_ms) { best_ms = ms; best = k; }
@@ -943,6 +1000,18 @@ int fw_advance(fw_handle* h, void* stream, int32_t n_steps) {
     } else if (cs == cudaStreamCaptureStatusNone) {
       int st = autotune_2d(h, s);
       if (st) return st;
+    }
+  }
+  if (h->ndim == 2 && kShapes2D[h->shape2d].persistent) {
+    // one cooperative launch for all the steps; under a stream capture the direct kernels run
+    // instead (same results)
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    FW_CUDA(h, cudaStreamIsCapturing(s, &cs));
+    if (cs == cudaStreamCaptureStatusNone) {
+      int st = launch_persistent(h, s, h->host_step, n_steps);
+      if (st) return st;
+      h->host_step += n_steps;
+      return FW_OK;
     }
   }
   constexpr int kGraphSteps = 64;
@@ -1028,7 +1097,7 @@ int fw_kernel_variant(const fw_handle* h, int32_t* variant) {
 
 int fw_block_tile(const fw_handle* h, int32_t tile[3]) {
   if (!h || !tile) return FW_ERR_ARGUMENT;
-  if (h->ndim == 2 && h->shape2d > 0) {
+  if (h->ndim == 2 && kShapes2D[h->shape2d].ty > 0) {
     tile[0] = kShapes2D[h->shape2d].xc;
     tile[1] = kShapes2D[h->shape2d].ty;
     tile[2] = 1;
@@ -1170,7 +1239,8 @@ int fw_destroy(fw_handle* h) {
   }
   if (h->graph) cudaGraphExecDestroy(h->graph);
   if (h->capture_stream) cudaStreamDestroy(h->capture_stream);
-  void* ptrs[] = {h->state, h->maps, h->dcmap, h->taps, h->icmat_t, h->traces, h->step, h->lists};
+  void* ptrs[] = {h->state, h->maps, h->dcmap, h->taps, h->icmat_t, h->traces, h->step, h->lists,
+                  h->bar};
   for (void* p : ptrs)
     if (p) cudaFree(p);
   delete h;
@@ -1210,7 +1280,7 @@ void group_launch_march(fw_group* g, int n_blocks, cudaStream_t s) {
 }
 
 void group_launch_step(fw_group* g, int n_tiles, cudaStream_t s) {
-  static_assert(kNumShapes2D == 6, "one case per 2D march shape");
+  static_assert(kNumShapes2D == 7, "one case per 2D kernel shape");
   switch (g->shape) {
     case 0: {
       const dim3 block(kD2TY, kD2TX);
@@ -1223,7 +1293,8 @@ void group_launch_step(fw_group* g, int n_tiles, cudaStream_t s) {
     case 2: group_launch_march<64, 32>(g, n_tiles, s); break;
     case 3: group_launch_march<128, 16>(g, n_tiles, s); break;
     case 4: group_launch_march<128, 32>(g, n_tiles, s); break;
-    default: group_launch_march<128, 64>(g, n_tiles, s); break;
+    case 5: group_launch_march<128, 64>(g, n_tiles, s); break;
+    default: break;  // no persistent group kernel: group shapes are 0-5
   }
 }
 
@@ -1347,6 +1418,7 @@ int group_autotune(fw_group* g, cudaStream_t s) {
   int st = FW_OK, best = 0;
   float best_ms = 0.f;
   for (int k = 0; k < kNumShapes2D && st == FW_OK; ++k) {
+    if (kShapes2D[k].persistent) continue;  // single-simulation kernel only
     float ms = 0.f;
     if ((st = group_set_shape(g, k)) || (st = group_advance(g, s, kTuneSteps))) break;
     if (cudaEventRecord(e0, s) != cudaSuccess) { st = fail(nullptr, FW_ERR_CUDA, "event record failed"); break; }
@@ -1427,7 +1499,7 @@ int fw_group_create(fw_handle* const* handles, int32_t n, fw_group** out) {
         delete g;
         return fail(nullptr, FW_ERR_ARGUMENT, "FWGB_SHAPE2D=%s outside [0, %d)", sh, kNumShapes2D);
       }
-      g->shape = k;
+      g->shape = kShapes2D[k].persistent ? 0 : k;
       g->shape_fixed = true;
     } else if (a && std::strcmp(a, "0") == 0) {
       g->shape_fixed = true;

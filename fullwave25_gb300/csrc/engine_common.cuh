@@ -209,10 +209,12 @@ struct CellPrsExpT {
 // lists are indexed tile = tx * n_ty + ty; a block owns the tiles [tx0, tx1) x [ty0, ty1), whose
 // entries are contiguous per tx. Called by every thread of the pressure kernel after its pressure
 // writes; `tid`/`nthr` span the block. Order per cell: source, air, record.
+// `n` is the time step being completed (-1: take it from the device step counter).
 __device__ __forceinline__ void span_epilogue(const StepArgs& A, float* p, int tx0, int tx1,
-                                              int ty0, int ty1, int n_ty, int tid, int nthr) {
+                                              int ty0, int ty1, int n_ty, int tid, int nthr,
+                                              int n = -1) {
   const Lists& L = A.l;
-  const int n = *A.step - 1;
+  if (n < 0) n = *A.step - 1;
   __syncthreads();
   if (n < L.nt_ic) {
     const float* col = L.icmat_t + (size_t)n * L.ncoords;
@@ -241,8 +243,8 @@ __device__ __forceinline__ void span_epilogue(const StepArgs& A, float* p, int t
 
 // The epilogue of one tile (the direct kernels: one block per tile).
 __device__ __forceinline__ void tile_epilogue(const StepArgs& A, float* p, int tile, int tid,
-                                              int nthr) {
-  span_epilogue(A, p, tile, tile + 1, 0, 1, 1, tid, nthr);
+                                              int nthr, int n = -1) {
+  span_epilogue(A, p, tile, tile + 1, 0, 1, 1, tid, nthr, n);
 }
 
 }  // namespace fwgb

@@ -16,7 +16,16 @@ constexpr int kD3TZ = 32, kD3TY = 4, kD3TX = 2;  // 3D tile
 // ---------------------------------------------------------------------------------------- 2D
 // Bodies take the tile (ty along y, tx along x) explicitly so that the single-simulation kernels
 // (tile = block index) and the group kernels (tile from a work list) share them.
-template <class CV>
+// Stencil operand load: through the read-only path (__ldg) when the field is constant for the
+// whole launch, or a plain coherent load (ld.global.ca) in the persistent kernel, where the field
+// is rewritten by other blocks between grid barriers inside the same launch.
+template <bool kCoherent>
+__device__ __forceinline__ float ld_field(const float* q) {
+  if constexpr (kCoherent) return __ldca(q);
+  else return __ldg(q);
+}
+
+template <class CV, bool kCoherent = false>
 __device__ __forceinline__ void vel2d_body(const StepArgs& A, int tile_y, int tile_x) {
   const Grid& g = A.g;
   const int j = kGhost + tile_y * kD2TY + threadIdx.x;
@@ -24,7 +33,8 @@ __device__ __forceinline__ void vel2d_body(const StepArgs& A, int tile_y, int ti
   if (i >= g.nx - kGhost || j >= g.ny - kGhost) return;
   const int64_t sx = g.sx;
   const int64_t c = i * sx + j;
-  const float* __restrict__ p = A.f.p;
+  const float* p = A.f.p;
+  auto P = [&](int64_t o) { return ld_field<kCoherent>(p + c + o); };
   CV cv;
   cv.load(A, c);
   float cm[8], co;
@@ -32,17 +42,19 @@ __device__ __forceinline__ void vel2d_body(const StepArgs& A, int tile_y, int ti
   float gx = 0.f, gy = 0.f;
 #pragma unroll
   for (int m = 1; m <= 8; ++m) {
-    gx = fmaf(cm[m - 1], __ldg(p + c + m * sx) - __ldg(p + c - (m - 1) * sx), gx);
-    gy = fmaf(cm[m - 1], __ldg(p + c + m) - __ldg(p + c - (m - 1)), gy);
+    gx = fmaf(cm[m - 1], P(m * sx) - P(-(m - 1) * sx), gx);
+    gy = fmaf(cm[m - 1], P(m) - P(-(m - 1)), gy);
   }
-  gx = fmaf(co, (__ldg(p + c + sx + 1) - __ldg(p + c + 1)) + (__ldg(p + c + sx - 1) - __ldg(p + c - 1)), gx);
-  gy = fmaf(co, (__ldg(p + c + 1 + sx) - __ldg(p + c + sx)) + (__ldg(p + c + 1 - sx) - __ldg(p + c - sx)), gy);
+  gx = fmaf(co, (P(sx + 1) - P(1)) + (P(sx - 1) - P(-1)), gx);
+  gy = fmaf(co, (P(1 + sx) - P(sx)) + (P(1 - sx) - P(-sx)), gy);
   const float gg[2] = {gx * g.inv_h[0], gy * g.inv_h[1]};
   cv.update_store(A, c, gg);
 }
 
-template <class CP>
-__device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int tile_x, int tile) {
+// `n`: the time step being completed (-1: read the device step counter in the epilogue).
+template <class CP, bool kCoherent = false>
+__device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int tile_x, int tile,
+                                           int n = -1) {
   const Grid& g = A.g;
   const int j = kGhost + tile_y * kD2TY + threadIdx.x;
   const int i = kGhost + tile_x * kD2TX + threadIdx.y;
@@ -50,8 +62,10 @@ __device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int ti
   if (i < g.nx - kGhost && j < g.ny - kGhost) {
     const int64_t sx = g.sx;
     const int64_t c = i * sx + j;
-    const float* __restrict__ vx = A.f.v[0];
-    const float* __restrict__ vy = A.f.v[1];
+    const float* vx = A.f.v[0];
+    const float* vy = A.f.v[1];
+    auto X = [&](int64_t o) { return ld_field<kCoherent>(vx + c + o); };
+    auto Y = [&](int64_t o) { return ld_field<kCoherent>(vy + c + o); };
     CP cp;
     cp.load(A, c);
     float cm[8], co;
@@ -59,15 +73,15 @@ __device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int ti
     float dx = 0.f, dy = 0.f;
 #pragma unroll
     for (int m = 1; m <= 8; ++m) {
-      dx = fmaf(cm[m - 1], __ldg(vx + c + (m - 1) * sx) - __ldg(vx + c - m * sx), dx);
-      dy = fmaf(cm[m - 1], __ldg(vy + c + (m - 1)) - __ldg(vy + c - m), dy);
+      dx = fmaf(cm[m - 1], X((m - 1) * sx) - X(-m * sx), dx);
+      dy = fmaf(cm[m - 1], Y(m - 1) - Y(-m), dy);
     }
-    dx = fmaf(co, (__ldg(vx + c + 1) - __ldg(vx + c - sx + 1)) + (__ldg(vx + c - 1) - __ldg(vx + c - sx - 1)), dx);
-    dy = fmaf(co, (__ldg(vy + c + sx) - __ldg(vy + c + sx - 1)) + (__ldg(vy + c - sx) - __ldg(vy + c - sx - 1)), dy);
+    dx = fmaf(co, (X(1) - X(-sx + 1)) + (X(-1) - X(-sx - 1)), dx);
+    dy = fmaf(co, (Y(sx) - Y(sx - 1)) + (Y(-sx) - Y(-sx - 1)), dy);
     const float dd[2] = {dx * g.inv_h[0], dy * g.inv_h[1]};
     cp.update_store(A, c, dd);
   }
-  tile_epilogue(A, p, tile, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y);
+  tile_epilogue(A, p, tile, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y, n);
 }
 
 template <class CV>

@@ -167,13 +167,15 @@ FWGB_API int fw_current_step(const fw_handle *h, int32_t *step);
 FWGB_API int fw_device_bytes(const fw_handle *h, uint64_t *bytes);
 
 /* Kernel family in use: 0 = direct-addressed kernels, 1 = plane/row-march kernels (TMA-staged
- * halo planes in 3D, halo rows in 2D). 3D handles use 1 unless the environment variable
- * FWGB_VARIANT=direct was set when the handle was created. 2D handles start on 0 and the first
- * fw_advance from step 0 autotunes the kernel shape (direct, or a march block of TY columns x XC
- * rows), timing each shape for a few dozen steps on the handle itself and resetting it after each
- * trial; the choice is cached per device, grid size and physics. FWGB_AUTOTUNE=0 disables the
- * trials, FWGB_VARIANT=direct|march or FWGB_SHAPE2D=<index> fixes the shape at creation. Every
- * shape gives bit-identical results. No counterpart in the reference (one CUDA kernel family). */
+ * halo planes in 3D, halo rows in 2D), 2 = the persistent 2D kernel (one cooperative launch per
+ * fw_advance, grid barriers between the velocity and pressure phases). 3D handles use 1 unless
+ * the environment variable FWGB_VARIANT=direct was set when the handle was created. 2D handles
+ * start on 0 and the first fw_advance from step 0 autotunes the kernel shape (direct, a march
+ * block of TY columns x XC rows, or persistent), timing each shape for a few dozen steps on the
+ * handle itself and resetting it after each trial; the choice is cached per device, grid size and
+ * physics. FWGB_AUTOTUNE=0 disables the trials, FWGB_VARIANT=direct|march or
+ * FWGB_SHAPE2D=<index 0-6> fixes the shape at creation. Every shape gives bit-identical results.
+ * No counterpart in the reference (one CUDA kernel family). */
 FWGB_API int fw_kernel_variant(const fw_handle *h, int32_t *variant);
 
 /* Cells per block of the kernels in use, along (x, y, z) (z = 1 in 2D). No counterpart in the

@@ -16,7 +16,8 @@ from golden_io import load_case_inputs
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
-MARCH_SHAPES = (1, 2, 3, 4, 5)   # indices of the march shapes; 0 = direct kernels
+MARCH_SHAPES = (1, 2, 3, 4, 5, 6)   # march shapes 1-5, persistent kernel 6; 0 = direct kernels
+VARIANT = {1: "march", 2: "march", 3: "march", 4: "march", 5: "march", 6: "persistent"}
 
 
 def _engine(inp, **env):
@@ -68,7 +69,7 @@ def test_every_march_shape_equals_direct_bitwise(engine_lib, cuda, case):
     for k in MARCH_SHAPES:
         with _engine(inp, FWGB_SHAPE2D=k) as em:
             got = em.run()
-            assert em.kernel_variant == "march"
+            assert em.kernel_variant == VARIANT[k]
         np.testing.assert_array_equal(got, ref, err_msg=f"{case}: shape {k}")
 
 
@@ -81,11 +82,27 @@ def test_scattered_sources_air_sensors_every_shape(engine_lib, cuda, ragged_2d):
             tile = em.block_tile
             got = em.run()
             pf = em.get_field(0)
-        assert tile[1] % 32 == 0 and tile[0] % 8 == 0
+        assert tile[1] % 32 == 0 and tile[0] % 8 == 0 and tile[2] == 1
         np.testing.assert_array_equal(got, ref, err_msg=f"shape {k}")
         # air cells are zero after the final step
         z = ragged_2d.icczero
         assert not pf[z[:, 0], z[:, 1]].any()
+
+
+def test_persistent_kernel_in_uneven_advances(engine_lib, cuda, ragged_2d):
+    """The persistent kernel numbers its steps from the handle's step count: advancing in uneven
+    pieces (and one step at a time) gives the traces of one full run."""
+    with _engine(ragged_2d, FWGB_VARIANT="direct") as ed:
+        ref = ed.run()
+    with _engine(ragged_2d, FWGB_SHAPE2D=6) as e:
+        e.reset()
+        done = 0
+        for n in (1, 1, 37, 100, 5):
+            e.advance(n)
+            done += n
+        e.advance(ragged_2d.nt - done)
+        assert e.current_step == ragged_2d.nt
+        np.testing.assert_array_equal(e.read_traces(), ref)
 
 
 def test_autotuned_engine_matches_direct_and_oracle(engine_lib, cuda, ragged_2d):
