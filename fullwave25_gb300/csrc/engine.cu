@@ -25,6 +25,7 @@
 #include "kernels_march3d.cuh"
 #include "kernels_march2d.cuh"
 #include "kernels_persistent2d.cuh"
+#include "kernels_stream3d.cuh"
 #include "kernels_adjoint2d.cuh"
 
 using namespace fwgb;
@@ -54,7 +55,7 @@ constexpr int kPersistentShape = 6;
 constexpr int kNumShapes2D = sizeof(kShapes2D) / sizeof(kShapes2D[0]);
 constexpr int kTuneSteps = 64;   // time steps per autotuning trial (one graph)
 
-enum Variant { kDirect = 0, kMarch = 1, kPersistent = 2 };
+enum Variant { kDirect = 0, kMarch = 1, kPersistent = 2, kStream = 3 };
 
 struct Tiling {
   int t[3];   // tile extent along x, y, z (z unused in 2D)
@@ -99,6 +100,9 @@ struct fw_handle {
   bool shape_fixed = false;    // 2D shape forced (FWGB_SHAPE2D / FWGB_VARIANT) or already tuned
   MarchMaps tmaps{};
   March2Maps tmaps2{};
+  StreamMaps smaps{};
+  bool stream3d = false;       // 3D isotropic: point-wise operands staged by TMA too
+  int ps3d = 2;                // stages of the point-wise ring of the streaming kernels
   // adjoint (2D): checkpoints every adj_every steps, per-segment state store, adjoint fields
   int adj_every = 0, adj_nckpt = 0;
   float* adj_ckpt = nullptr;     // adj_nckpt states
@@ -131,9 +135,15 @@ int fail(fw_handle* h, int code, const char* fmt, ...) {
 int64_t round_up(int64_t v, int64_t m) { return (v + m - 1) / m * m; }
 
 int n_state(int ndim) { return 1 + ndim + 4 * ndim; }
-// maps: rdt_rho, dt_k, beta2dt, inv_ku, inv_kx, au1 bu1 au2 bu2 ax1 bx1 ax2 bx2 (x axis, or every
-// axis in the isotropic engine), then for the anisotropic engine per further axis a >= 1:
-// inv_ku, au1 bu1 au2 bu2, inv_kx, ax1 bx1 ax2 bx2 at 13 + 10 (a - 1) + k
+// maps, in the order the streaming 3D kernels fetch them (one contiguous run per kernel):
+// velocity rdt_rho inv_ku au1 bu1 au2 bu2 | pressure dt_k inv_kx ax1 bx1 ax2 bx2 | beta2dt
+// (x axis, or every axis in the isotropic engine); then for the anisotropic engine per further
+// axis a >= 1: inv_ku, au1 bu1 au2 bu2, inv_kx, ax1 bx1 ax2 bx2 at 13 + 10 (a - 1) + k
+enum MapSlot {
+  kMRdtRho = 0, kMInvKu, kMAu1, kMBu1, kMAu2, kMBu2,
+  kMDtK, kMInvKx, kMAx1, kMBx1, kMAx2, kMBx2,
+  kMBeta2dt
+};
 constexpr int kMaps = 13;
 int n_maps(const fw_handle* h) { return kMaps + (h->aniso ? 10 * (h->ndim - 1) : 0); }
 int axis_map(int a, int k) { return kMaps + 10 * (a - 1) + k; }
@@ -269,14 +279,40 @@ void launch_typed(fw_handle* h, cudaStream_t s) {
   }
 }
 
+// Streaming 3D kernels (isotropic engine): kPS-stage point-wise ring in dynamic shared memory.
+template <int kPS, bool kBeta>
+void launch_stream3d_ps(fw_handle* h, cudaStream_t s) {
+  const Tiling& t = h->tiling;
+  dim3 grid(t.n[2], t.n[1], t.n[0]), block(kMTZ, kMTY);
+  const MarchMaps& tm = h->tmaps;
+  const StreamMaps& sm = h->smaps;
+  vel3d_stream<kMarchXC, kPS, kMRdtRho><<<grid, block, vel_stream_smem<kPS>(), s>>>(
+      h->args, tm.p, sm.vstate, sm.vmaps, sm.dcmap);
+  prs3d_stream<kMarchXC, kPS, kBeta, kMDtK><<<grid, block, prs_stream_smem<kPS, kBeta>(), s>>>(
+      h->args, tm.vx, tm.vy, tm.vz, sm.pstate, sm.phi, kBeta ? sm.pmaps7 : sm.pmaps6, sm.dcmap);
+}
+
+template <bool kBeta>
+void launch_stream3d(fw_handle* h, cudaStream_t s) {
+  if (h->ps3d == 2) launch_stream3d_ps<2, kBeta>(h, s);
+  else launch_stream3d_ps<3, kBeta>(h, s);
+}
+
 template <int ND, bool kBeta>
 void launch_nd(fw_handle* h, cudaStream_t s) {
-  if (h->exp)
+  if (h->exp) {
     launch_typed<ND, CellVelExpT<ND>, CellPrsExpT<ND, kBeta>, 3>(h, s);
-  else if (h->aniso)
+  } else if (h->aniso) {
     launch_typed<ND, CellVelT<ND, true>, CellPrsT<ND, kBeta, true>, 2>(h, s);
-  else
+  } else {
+    if constexpr (ND == 3) {
+      if (h->stream3d && h->variant == kMarch) {
+        launch_stream3d<kBeta>(h, s);
+        return;
+      }
+    }
     launch_typed<ND, CellVelT<ND, false>, CellPrsT<ND, kBeta, false>, 3>(h, s);
+  }
 }
 
 void launch_step(fw_handle* h, cudaStream_t s) {
@@ -348,8 +384,9 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t
                                    const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
-int encode_map(fw_handle* h, CUtensorMap* map, float* base, cuuint32_t rank,
-               const cuuint64_t* dims, const cuuint64_t* strides, const cuuint32_t* box) {
+int encode_map(fw_handle* h, CUtensorMap* map, void* base, cuuint32_t rank,
+               const cuuint64_t* dims, const cuuint64_t* strides, const cuuint32_t* box,
+               CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_FLOAT32) {
   static EncodeTiledFn encode = nullptr;
   if (!encode) {
     void* fn = nullptr;
@@ -360,11 +397,41 @@ int encode_map(fw_handle* h, CUtensorMap* map, float* base, cuuint32_t rank,
       return fail(h, FW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
     encode = reinterpret_cast<EncodeTiledFn>(fn);
   }
-  const cuuint32_t estr[3] = {1, 1, 1};
-  CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, rank, base, dims, strides, box, estr,
+  const cuuint32_t estr[4] = {1, 1, 1, 1};
+  CUresult r = encode(map, type, rank, base, dims, strides, box, estr,
                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
                       CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   if (r != CUDA_SUCCESS) return fail(h, FW_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return FW_OK;
+}
+
+// 4D float32 tensor map over a stack of padded 3D fields (the state or the map allocation):
+// dims (pitch, ny, nx, n_fields), box (32, 8, 1, f): f consecutive fields of one plane tile.
+int encode_stack_map(fw_handle* h, CUtensorMap* map, float* base, int n_fields, uint32_t f) {
+  const cuuint64_t dims[4] = {(cuuint64_t)h->pitch, (cuuint64_t)h->ny, (cuuint64_t)h->nx,
+                              (cuuint64_t)n_fields};
+  const cuuint64_t strides[3] = {(cuuint64_t)h->pitch * 4, (cuuint64_t)(h->pitch * h->ny) * 4,
+                                 (cuuint64_t)h->ncells_padded * 4};
+  const cuuint32_t box[4] = {(cuuint32_t)kMTZ, (cuuint32_t)kMTY, 1, f};
+  return encode_map(h, map, base, 4, dims, strides, box);
+}
+
+// Tensor maps of the streaming 3D kernels (state and map stacks, tap-index map).
+int encode_stream_maps(fw_handle* h) {
+  StreamMaps& m = h->smaps;
+  const int ns = n_state(h->ndim), nm = n_maps(h);
+  const cuuint64_t dims[3] = {(cuuint64_t)h->pitch, (cuuint64_t)h->ny, (cuuint64_t)h->nx};
+  const cuuint64_t strides[2] = {(cuuint64_t)h->pitch * 4, (cuuint64_t)(h->pitch * h->ny) * 4};
+  const cuuint32_t box[3] = {(cuuint32_t)kMTZ, (cuuint32_t)kMTY, 1};
+  int st;
+  if ((st = encode_stack_map(h, &m.vstate, h->state, ns, kVelStateF)) ||
+      (st = encode_stack_map(h, &m.vmaps, h->maps, nm, kVelMapF)) ||
+      (st = encode_stack_map(h, &m.pstate, h->state, ns, 1)) ||
+      (st = encode_stack_map(h, &m.phi, h->state, ns, kPrsPhiF)) ||
+      (st = encode_stack_map(h, &m.pmaps6, h->maps, nm, kVelMapF)) ||
+      (st = encode_stack_map(h, &m.pmaps7, h->maps, nm, kVelMapF + 1)) ||
+      (st = encode_map(h, &m.dcmap, h->dcmap, 3, dims, strides, box, CU_TENSOR_MAP_DATA_TYPE_INT32)))
+    return st;
   return FW_OK;
 }
 
@@ -397,6 +464,39 @@ int set_shape2d(fw_handle* h, int k) {
   h->shape2d = k;
   h->variant = kShapes2D[k].persistent ? kPersistent : kShapes2D[k].ty > 0 ? kMarch : kDirect;
   h->graph_steps = 0;   // the next advance captures a graph with the new kernels
+  return FW_OK;
+}
+
+// Allow the streaming kernels their dynamic shared memory (once per process; before any capture).
+template <int kPS>
+cudaError_t stream3d_attributes() {
+  cudaError_t e;
+  if ((e = cudaFuncSetAttribute(vel3d_stream<kMarchXC, kPS, kMRdtRho>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)vel_stream_smem<kPS>())) != cudaSuccess)
+    return e;
+  if ((e = cudaFuncSetAttribute(prs3d_stream<kMarchXC, kPS, false, kMDtK>,
+                                cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                (int)prs_stream_smem<kPS, false>())) != cudaSuccess)
+    return e;
+  return cudaFuncSetAttribute(prs3d_stream<kMarchXC, kPS, true, kMDtK>,
+                              cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              (int)prs_stream_smem<kPS, true>());
+}
+
+int prepare_stream3d(fw_handle* h) {
+  static std::mutex mu;
+  static std::vector<int> done;   // devices whose attributes are set
+  int dev = 0;
+  FW_CUDA(h, cudaGetDevice(&dev));
+  std::lock_guard<std::mutex> lk(mu);
+  if (std::find(done.begin(), done.end(), dev) != done.end()) return FW_OK;
+  cudaError_t e = stream3d_attributes<2>();
+  if (e == cudaSuccess) e = stream3d_attributes<3>();
+  if (e != cudaSuccess)
+    return fail(h, FW_ERR_CUDA, "streaming 3D kernels: cudaFuncSetAttribute failed: %s",
+                cudaGetErrorString(e));
+  done.push_back(dev);
   return FW_OK;
 }
 
@@ -510,23 +610,23 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
     for (int nu = 0; nu < 2; ++nu) A.f.psi[a][nu] = a < h->ndim ? state_field(h, s++) : nullptr;
   for (int a = 0; a < 3; ++a)
     for (int nu = 0; nu < 2; ++nu) A.f.phi[a][nu] = a < h->ndim ? state_field(h, s++) : nullptr;
-  A.m.rdt_rho = map_field(h, 0);
-  A.m.dt_k = map_field(h, 1);
-  A.m.beta2dt = map_field(h, 2);
+  A.m.rdt_rho = map_field(h, kMRdtRho);
+  A.m.dt_k = map_field(h, kMDtK);
+  A.m.beta2dt = map_field(h, kMBeta2dt);
   for (int a = 0; a < 3; ++a) {
     const bool own = h->aniso && a >= 1 && a < h->ndim;
-    A.m.inv_ku[a] = own ? map_field(h, axis_map(a, 0)) : map_field(h, 3);
-    A.m.au[a][0] = own ? map_field(h, axis_map(a, 1)) : map_field(h, 5);
-    A.m.bu[a][0] = own ? map_field(h, axis_map(a, 2)) : map_field(h, 6);
-    A.m.au[a][1] = own ? map_field(h, axis_map(a, 3)) : map_field(h, 7);
-    A.m.bu[a][1] = own ? map_field(h, axis_map(a, 4)) : map_field(h, 8);
-    A.m.inv_kx[a] = own ? map_field(h, axis_map(a, 5)) : map_field(h, 4);
-    A.m.ax[a][0] = own ? map_field(h, axis_map(a, 6)) : map_field(h, 9);
-    A.m.bx[a][0] = own ? map_field(h, axis_map(a, 7)) : map_field(h, 10);
-    A.m.ax[a][1] = own ? map_field(h, axis_map(a, 8)) : map_field(h, 11);
-    A.m.bx[a][1] = own ? map_field(h, axis_map(a, 9)) : map_field(h, 12);
+    A.m.inv_ku[a] = own ? map_field(h, axis_map(a, 0)) : map_field(h, kMInvKu);
+    A.m.au[a][0] = own ? map_field(h, axis_map(a, 1)) : map_field(h, kMAu1);
+    A.m.bu[a][0] = own ? map_field(h, axis_map(a, 2)) : map_field(h, kMBu1);
+    A.m.au[a][1] = own ? map_field(h, axis_map(a, 3)) : map_field(h, kMAu2);
+    A.m.bu[a][1] = own ? map_field(h, axis_map(a, 4)) : map_field(h, kMBu2);
+    A.m.inv_kx[a] = own ? map_field(h, axis_map(a, 5)) : map_field(h, kMInvKx);
+    A.m.ax[a][0] = own ? map_field(h, axis_map(a, 6)) : map_field(h, kMAx1);
+    A.m.bx[a][0] = own ? map_field(h, axis_map(a, 7)) : map_field(h, kMBx1);
+    A.m.ax[a][1] = own ? map_field(h, axis_map(a, 8)) : map_field(h, kMAx2);
+    A.m.bx[a][1] = own ? map_field(h, axis_map(a, 9)) : map_field(h, kMBx2);
   }
-  A.m.a_exp = map_field(h, 5);  // exponential engine: a_exp in the first relaxation slot
+  A.m.a_exp = map_field(h, kMAu1);  // exponential engine: a_exp in the first relaxation slot
   A.m.dcmap = h->dcmap;
   A.m.taps = h->taps;
   A.l.icmat_t = h->icmat_t;
@@ -562,10 +662,18 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
     }
   }
   if (h->variant == kMarch && h->ndim == 3) {
+    // isotropic relaxation engine: point-wise operands staged by TMA as well, unless
+    // FWGB_STREAM3D=0; FWGB_PS3D=2|3 sets the depth of the point-wise ring (default 2: the next
+    // plane's operands are in flight while a plane is computed)
+    const char* sv = std::getenv("FWGB_STREAM3D");
+    const char* ps = std::getenv("FWGB_PS3D");
+    h->stream3d = !h->aniso && !h->exp && !(sv && std::strcmp(sv, "0") == 0);
+    h->ps3d = (ps && std::strcmp(ps, "3") == 0) ? 3 : 2;   // 2 stages measured fastest
     if ((st = encode_field_map(h, &h->tmaps.p, A.f.p, kPW, kPH)) ||
         (st = encode_field_map(h, &h->tmaps.vx, A.f.v[0], kXW, kXH)) ||
         (st = encode_field_map(h, &h->tmaps.vy, A.f.v[1], kYW, kYH)) ||
-        (st = encode_field_map(h, &h->tmaps.vz, A.f.v[2], kZW, kZH))) {
+        (st = encode_field_map(h, &h->tmaps.vz, A.f.v[2], kZW, kZH)) ||
+        (h->stream3d && ((st = encode_stream_maps(h)) || (st = prepare_stream3d(h))))) {
       g_create_error = h->err;
       fw_destroy(h);
       return st;
@@ -730,17 +838,20 @@ int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an,
   h->args.l.rec_cell = reinterpret_cast<int64_t*>(L + off64) + es.size() + ez.size();
 
   // -- maps -------------------------------------------------------------------------------------
-  struct { const float* src; int idx; } mapsrc[] = {
-      {f->rho, 0}, {f->K, 1}, {f->beta, 2}, {f->kappau, 3}, {f->kappax, 4},
-      {f->apmlu1, 5}, {f->bpmlu1, 6}, {f->apmlu2, 7}, {f->bpmlu2, 8},
-      {f->apmlx1, 9}, {f->bpmlx1, 10}, {f->apmlx2, 11}, {f->bpmlx2, 12}};
+  struct { const float* src; int idx; bool relax; } mapsrc[] = {
+      {f->rho, kMRdtRho, false}, {f->K, kMDtK, false}, {f->beta, kMBeta2dt, false},
+      {f->kappau, kMInvKu, true}, {f->kappax, kMInvKx, true},
+      {f->apmlu1, kMAu1, true}, {f->bpmlu1, kMBu1, true}, {f->apmlu2, kMAu2, true},
+      {f->bpmlu2, kMBu2, true}, {f->apmlx1, kMAx1, true}, {f->bpmlx1, kMBx1, true},
+      {f->apmlx2, kMAx2, true}, {f->bpmlx2, kMBx2, true}};
   for (auto& m : mapsrc) {
-    if (h->exp && m.idx >= 3) continue;  // no relaxation maps in the exponential engine
+    if (h->exp && m.relax) continue;  // no relaxation maps in the exponential engine
     if ((st = upload_grid(h, map_field(h, m.idx), m.src, sizeof(float), dev, s))) return st;
   }
-  if (h->exp && (st = upload_grid(h, map_field(h, 5), a_exp, sizeof(float), dev, s))) return st;
+  if (h->exp && (st = upload_grid(h, map_field(h, kMAu1), a_exp, sizeof(float), dev, s)))
+    return st;
   std::vector<int> kappa_maps;
-  if (!h->exp) kappa_maps = {3, 4};
+  if (!h->exp) kappa_maps = {kMInvKu, kMInvKx};
   if (h->aniso) {
     // axis y: kappaw/apmlw*/bpmlw* (gradient), kappay/apmly*/bpmly* (divergence); axis z: v, z
     const float* per_axis[3][10] = {
@@ -761,18 +872,18 @@ int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an,
     }
   }
   if ((st = upload_grid(h, h->dcmap, dcm.data(), sizeof(int32_t), false, s))) return st;
-  transform_maps<<<1024, 256, 0, s>>>(map_field(h, 0), map_field(h, 1), map_field(h, 2),
-                                      h->ncells_padded, d.dt);
+  transform_maps<<<1024, 256, 0, s>>>(map_field(h, kMRdtRho), map_field(h, kMDtK),
+                                      map_field(h, kMBeta2dt), h->ncells_padded, d.dt);
   for (int idx : kappa_maps) invert_map<<<1024, 256, 0, s>>>(map_field(h, idx), h->ncells_padded);
   FW_CUDA(h, cudaGetLastError());
   // beta: use the nonlinear kernel only when some cell has beta != 0
-  any_nonzero<<<1024, 256, 0, s>>>(map_field(h, 2), h->ncells_padded, h->step + 2);
+  any_nonzero<<<1024, 256, 0, s>>>(map_field(h, kMBeta2dt), h->ncells_padded, h->step + 2);
   FW_CUDA(h, cudaGetLastError());
   int flag = 0;
   FW_CUDA(h, cudaMemcpyAsync(&flag, h->step + 2, sizeof(int), cudaMemcpyDeviceToHost, s));
   FW_CUDA(h, cudaStreamSynchronize(s));
   h->has_beta = flag != 0;
-  h->args.m.beta2dt = h->has_beta ? map_field(h, 2) : nullptr;
+  h->args.m.beta2dt = h->has_beta ? map_field(h, kMBeta2dt) : nullptr;
 
   // -- tap table [ndmap][12] ----------------------------------------------------------------------
   std::vector<float> dmap((size_t)18 * d.ndmap), taps((size_t)d.ndmap * kTapStride, 0.f);
@@ -1091,7 +1202,7 @@ int fw_device_bytes(const fw_handle* h, uint64_t* bytes) {
 
 int fw_kernel_variant(const fw_handle* h, int32_t* variant) {
   if (!h || !variant) return FW_ERR_ARGUMENT;
-  *variant = h->variant;
+  *variant = (h->variant == kMarch && h->stream3d) ? kStream : h->variant;
   return FW_OK;
 }
 
@@ -1343,7 +1454,7 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
     fw_handle* h = m[r];
     args[r] = h->args;
     // members without beta read their (all-zero) beta buffer when the group uses the beta kernel
-    args[r].m.beta2dt = map_field(h, 2);
+    args[r].m.beta2dt = map_field(h, kMBeta2dt);
     if (g->shape == 0) {
       const Tiling& t = h->tiling;
       for (int tx = 0; tx < t.n[0]; ++tx)

@@ -344,7 +344,7 @@ class Engine:
     def kernel_variant(self) -> str:
         v = C.c_int32()
         self._call("fw_kernel_variant", C.byref(v))
-        return {0: "direct", 1: "march", 2: "persistent"}[v.value]
+        return {0: "direct", 1: "march", 2: "persistent", 3: "stream"}[v.value]
 
     @property
     def block_tile(self) -> tuple:

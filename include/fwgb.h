@@ -168,8 +168,10 @@ FWGB_API int fw_device_bytes(const fw_handle *h, uint64_t *bytes);
 
 /* Kernel family in use: 0 = direct-addressed kernels, 1 = plane/row-march kernels (TMA-staged
  * halo planes in 3D, halo rows in 2D), 2 = the persistent 2D kernel (one cooperative launch per
- * fw_advance, grid barriers between the velocity and pressure phases). 3D handles use 1 unless
- * the environment variable FWGB_VARIANT=direct was set when the handle was created. 2D handles
+ * fw_advance, grid barriers between the velocity and pressure phases), 3 = the 3D plane march
+ * with the point-wise state and maps staged by TMA as well (isotropic engine). 3D handles use 3
+ * (isotropic; 1 with FWGB_STREAM3D=0) or 1 (anisotropic, exponential) unless the environment
+ * variable FWGB_VARIANT=direct was set when the handle was created. 2D handles
  * start on 0 and the first fw_advance from step 0 autotunes the kernel shape (direct, a march
  * block of TY columns x XC rows, or persistent), timing each shape for a few dozen steps on the
  * handle itself and resetting it after each trial; the choice is cached per device, grid size and
