@@ -2,8 +2,9 @@
 
 Public surface (names follow the reference package ``fullwave``):
 ``Grid``, ``MediumRelaxationMaps``, ``Source``, ``Sensor``, ``PMLBuilder``, ``Solver``,
-``Launcher`` / ``SimulationError`` (drop-in for ``fullwave.solver.launcher``), and the engine
-binding ``Engine`` over the C ABI of ``include/fwgb.h``.
+``Launcher`` / ``SimulationError`` (drop-in for ``fullwave.solver.launcher``), ``signal_process``
+(whole-domain output reshapes), and the engine binding ``Engine`` over the C ABI of
+``include/fwgb.h``.
 """
 
 import logging
@@ -15,6 +16,7 @@ from .exponential import MediumExponentialAttenuation, PMLBuilderExponentialAtte
 from .medium import Medium, MediumRelaxationMaps
 from .pml import PMLBuilder
 from .pulse import gaussian_modulated_sinusoidal_signal
+from . import signal_process
 from .solver import Solver
 from .source import Sensor, Source
 
@@ -26,5 +28,5 @@ __all__ = [
     "EngineInputs", "Grid", "Launcher", "Medium", "MediumExponentialAttenuation",
     "MediumRelaxationMaps", "PMLBuilder", "PMLBuilderExponentialAttenuation", "Sensor",
     "SimulationError", "Solver", "Source", "build_inputs", "gaussian_modulated_sinusoidal_signal",
-    "load_dat_data", "read_simulation_dir", "write_simulation_dir",
+    "load_dat_data", "read_simulation_dir", "signal_process", "write_simulation_dir",
 ]

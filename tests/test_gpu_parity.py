@@ -180,3 +180,30 @@ def test_device_and_host_inputs_give_same_traces(engine_lib, cuda, plain_3d_smal
     d, host = plain_3d_small
     with d.make_engine() as a, Engine(host) as b:
         np.testing.assert_array_equal(a.run(), b.run())
+
+
+def test_solver_whole_domain_recording_movie(engine_lib, cuda):
+    """record_whole_domain=True records every cell of the extended grid every
+    ``sampling_modulus_time_whole_domain`` steps; reshaped to [nt, nx, ny] each frame is the
+    pressure field at that step (the last frame equals the field left in the engine)."""
+    from fullwave25_gb300 import Solver
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.signal_process import reshape_whole_sensor_to_nt_nx_ny
+    from fullwave25_gb300.workloads import plain_2d_problem
+
+    nt, mod = 120, 4
+    grid, medium, source, sensor, _ = plain_2d_problem(shape=(64, 48), nt=nt, seed=5)
+    solver = Solver(Path(tempfile.gettempdir()), grid, medium, source, sensor,
+                    pml_layer_thickness_px=8, n_transition_layer=8)
+    out = solver.run(record_whole_domain=True, sampling_modulus_time_whole_domain=mod)
+    ext = solver.pml_builder.extended_grid
+    movie = reshape_whole_sensor_to_nt_nx_ny(out, ext)
+    n_out = (nt + mod - 1) // mod
+    assert movie.shape == (n_out, ext.nx, ext.ny)
+    inputs, _ = solver.build_engine_inputs(record_whole_domain=True,
+                                           sampling_modulus_time_whole_domain=mod)
+    with Engine(inputs) as eng:
+        eng.reset()
+        eng.advance((n_out - 1) * mod + 1)   # the last recorded step is (n_out - 1) * mod
+        np.testing.assert_array_equal(movie[-1], eng.get_field(0))
+    assert np.abs(movie[-1]).max() > 0
