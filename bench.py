@@ -614,7 +614,7 @@ def run_adjoint(args):
         cc, rr, aa = [x.clone().requires_grad_(True) for x in start[:3]]
         J = prob.misfit(cc, rr, aa, start[3], observed, checkpoint_every=200)
         J.backward()
-        return float(J), cc.grad, rr.grad, aa.grad
+        return float(J.detach()), cc.grad, rr.grad, aa.grad
 
     for _ in range(args.warmup):
         evaluate()

@@ -1243,7 +1243,8 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
     h->adj_grad = nullptr;
     const size_t b_ckpt = state_elems * std::max(nckpt, 1) * sizeof(float);
     const size_t b_store = state_elems * (checkpoint_every + 1) * sizeof(float);
-    const size_t b_lam = (size_t)h->ncells_padded * 15 * sizeof(float);
+    // 15 adjoint fields and temporaries, then the FP32 per-segment gradient partials
+    const size_t b_lam = (size_t)h->ncells_padded * (15 + kNumGrad) * sizeof(float);
     const size_t b_grad = (size_t)h->ncells_padded * kNumGrad * sizeof(double);
     FW_CUDA(h, cudaMalloc(&h->adj_ckpt, b_ckpt));
     FW_CUDA(h, cudaMalloc(&h->adj_store, b_store));
@@ -1274,7 +1275,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int64_t fs = h->ncells_padded;
   const size_t state_elems = (size_t)fs * n_state(h->ndim);
-  FW_CUDA(h, cudaMemsetAsync(h->adj_lam, 0, (size_t)fs * 15 * sizeof(float), s));
+  FW_CUDA(h, cudaMemsetAsync(h->adj_lam, 0, (size_t)fs * (15 + kNumGrad) * sizeof(float), s));
   FW_CUDA(h, cudaMemsetAsync(h->adj_grad, 0, (size_t)fs * kNumGrad * sizeof(double), s));
   AdjArgs A{};
   A.g = h->args.g;
@@ -1290,7 +1291,14 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     A.lam_d[a] = h->adj_lam + (11 + a) * fs;
     A.lam_g[a] = h->adj_lam + (13 + a) * fs;
   }
-  for (int q = 0; q < kNumGrad; ++q) A.grad[q] = h->adj_grad + (size_t)q * fs;
+  for (int q = 0; q < kNumGrad; ++q) {
+    A.grad[q] = h->adj_grad + (size_t)q * fs;
+    A.g32[q] = h->adj_lam + (size_t)(15 + q) * fs;
+  }
+  // FWGB_ADJ_F64_STEPS=1: form and add every step's contributions in FP64 (slow on GB300's FP64
+  // pipe; kept to validate the default segmented FP32-partial / FP64-total accumulation)
+  const char* f64env = std::getenv("FWGB_ADJ_F64_STEPS");
+  const bool f64_steps = f64env && std::strcmp(f64env, "1") == 0;
   const Lists& L = h->args.l;
   const int n_src = L.ncoords ? 0 : 0;
   (void)n_src;
@@ -1327,9 +1335,15 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
       if (counts[2]) adj2d_io<<<(counts[2] + 255) / 256, 256, 0, s>>>(A, L, residual, n, 0, 0, counts[2]);
       if (counts[0] || counts[1])
         adj2d_zero<<<(std::max(counts[0], counts[1]) + 255) / 256, 256, 0, s>>>(A, L, n, counts[0], counts[1]);
-      adj2d_prs<<<grid, block, 0, s>>>(A);
-      adj2d_vel<<<grid, block, 0, s>>>(A);
+      if (f64_steps) {
+        adj2d_prs<true><<<grid, block, 0, s>>>(A);
+        adj2d_vel<true><<<grid, block, 0, s>>>(A);
+      } else {
+        adj2d_prs<false><<<grid, block, 0, s>>>(A);
+        adj2d_vel<false><<<grid, block, 0, s>>>(A);
+      }
     }
+    if (!f64_steps) adj2d_merge<<<grid, block, 0, s>>>(A);
     FW_CUDA(h, cudaGetLastError());
   }
   if (grad_out) {

@@ -12,6 +12,7 @@
 // The transposes D^T are gathers: output cell q collects the terms of every body cell c whose
 // stencil touches q, each weighted by c's own taps.
 #pragma once
+#include <type_traits>
 #include "engine_common.cuh"
 
 namespace fwgb {
@@ -33,7 +34,8 @@ struct AdjArgs {
   float* lam_phi[2][2];
   float* lam_d[2];
   float* lam_g[2];
-  double* grad[kNumGrad];
+  double* grad[kNumGrad];    // FP64 time sums
+  float* g32[kNumGrad];      // FP32 partial sums of the current segment (segmented mode)
 };
 
 // state field indices (2D): p, vx, vy, psi[a][nu] = 3 + 2a + nu, phi[a][nu] = 7 + 2a + nu
@@ -144,7 +146,13 @@ __global__ void adj2d_zero(const AdjArgs A, const Lists L, int n, int n_src, int
     for (int e = t; e < n_src; e += stride) A.lam_p[L.src_cell[e]] = 0.f;
 }
 
+// Gradient accumulation: kF64 = every step's contributions formed and added in FP64 (GB300's FP64
+// pipe is the bottleneck then); otherwise contributions are formed in FP32 (the precision of the
+// adjoint fields themselves) and summed per checkpoint segment in FP32 partials, which
+// adj2d_merge adds into the FP64 time sums at the end of every segment.
+template <bool kF64>
 __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
+  using acc_t = typename std::conditional<kF64, double, float>::type;
   int64_t c;
   if (!adj_cell(A.g, &c)) return;
   const Grid& g = A.g;
@@ -153,7 +161,7 @@ __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
   const float k = __ldg(A.m.dt_k + c), ikx = __ldg(A.m.inv_kx[0] + c);
   const float ax[2] = {__ldg(A.m.ax[0][0] + c), __ldg(A.m.ax[0][1] + c)};
   const float bx[2] = {__ldg(A.m.bx[0][0] + c), __ldg(A.m.bx[0][1] + c)};
-  double g_dtk = 0.0, g_ikx = 0.0, g_ax[2] = {0.0, 0.0}, g_bx[2] = {0.0, 0.0};
+  acc_t g_dtk = 0, g_ikx = 0, g_ax[2] = {0, 0}, g_bx[2] = {0, 0};
   float div = 0.f;
   const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
 #pragma unroll
@@ -166,23 +174,34 @@ __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
     for (int nu = 0; nu < 2; ++nu) {
       const float L = A.lam_phi[a][nu][c] - k * lp;
       lam_d = fmaf(ax[nu], L, lam_d);
-      g_ax[nu] += (double)L * d;
-      g_bx[nu] += (double)L * __ldg(S_phi(A.Sn, fs, a, nu) + c);
+      g_ax[nu] += (acc_t)L * d;
+      g_bx[nu] += (acc_t)L * __ldg(S_phi(A.Sn, fs, a, nu) + c);
       A.lam_phi[a][nu][c] = bx[nu] * L;
     }
-    g_ikx -= (double)k * lp * d;
+    g_ikx -= (acc_t)k * lp * d;
     A.lam_d[a][c] = lam_d;
   }
-  g_dtk -= (double)div * lp;
-  A.grad[kGDtK][c] += g_dtk;
-  A.grad[kGInvKx][c] += g_ikx;
-  A.grad[kGAx1][c] += g_ax[0];
-  A.grad[kGAx2][c] += g_ax[1];
-  A.grad[kGBx1][c] += g_bx[0];
-  A.grad[kGBx2][c] += g_bx[1];
+  g_dtk -= (acc_t)div * lp;
+  if constexpr (kF64) {
+    A.grad[kGDtK][c] += g_dtk;
+    A.grad[kGInvKx][c] += g_ikx;
+    A.grad[kGAx1][c] += g_ax[0];
+    A.grad[kGAx2][c] += g_ax[1];
+    A.grad[kGBx1][c] += g_bx[0];
+    A.grad[kGBx2][c] += g_bx[1];
+  } else {
+    A.g32[kGDtK][c] += g_dtk;
+    A.g32[kGInvKx][c] += g_ikx;
+    A.g32[kGAx1][c] += g_ax[0];
+    A.g32[kGAx2][c] += g_ax[1];
+    A.g32[kGBx1][c] += g_bx[0];
+    A.g32[kGBx2][c] += g_bx[1];
+  }
 }
 
+template <bool kF64>
 __global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
+  using acc_t = typename std::conditional<kF64, double, float>::type;
   int64_t c;
   if (!adj_cell(A.g, &c)) return;
   const Grid& g = A.g;
@@ -190,7 +209,7 @@ __global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
   const float r = __ldg(A.m.rdt_rho + c), iku = __ldg(A.m.inv_ku[0] + c);
   const float au[2] = {__ldg(A.m.au[0][0] + c), __ldg(A.m.au[0][1] + c)};
   const float bu[2] = {__ldg(A.m.bu[0][0] + c), __ldg(A.m.bu[0][1] + c)};
-  double g_r = 0.0, g_iku = 0.0, g_au[2] = {0.0, 0.0}, g_bu[2] = {0.0, 0.0};
+  acc_t g_r = 0, g_iku = 0, g_au[2] = {0, 0}, g_bu[2] = {0, 0};
   const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
@@ -202,21 +221,41 @@ __global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
     for (int nu = 0; nu < 2; ++nu) {
       const float M = A.lam_psi[a][nu][c] - r * lv;
       lam_g = fmaf(au[nu], M, lam_g);
-      g_au[nu] += (double)M * gr;
-      g_bu[nu] += (double)M * __ldg(S_psi(A.Sn, fs, a, nu) + c);
+      g_au[nu] += (acc_t)M * gr;
+      g_bu[nu] += (acc_t)M * __ldg(S_psi(A.Sn, fs, a, nu) + c);
       A.lam_psi[a][nu][c] = bu[nu] * M;
     }
-    g_r -= (double)lv * (fmaf(gr, iku, p1) + p2);
-    g_iku -= (double)r * gr * lv;
+    g_r -= (acc_t)lv * (fmaf(gr, iku, p1) + p2);
+    g_iku -= (acc_t)r * gr * lv;
     A.lam_v[a][c] = lv;
     A.lam_g[a][c] = lam_g;
   }
-  A.grad[kGRdtRho][c] += g_r;
-  A.grad[kGInvKu][c] += g_iku;
-  A.grad[kGAu1][c] += g_au[0];
-  A.grad[kGAu2][c] += g_au[1];
-  A.grad[kGBu1][c] += g_bu[0];
-  A.grad[kGBu2][c] += g_bu[1];
+  if constexpr (kF64) {
+    A.grad[kGRdtRho][c] += g_r;
+    A.grad[kGInvKu][c] += g_iku;
+    A.grad[kGAu1][c] += g_au[0];
+    A.grad[kGAu2][c] += g_au[1];
+    A.grad[kGBu1][c] += g_bu[0];
+    A.grad[kGBu2][c] += g_bu[1];
+  } else {
+    A.g32[kGRdtRho][c] += g_r;
+    A.g32[kGInvKu][c] += g_iku;
+    A.g32[kGAu1][c] += g_au[0];
+    A.g32[kGAu2][c] += g_au[1];
+    A.g32[kGBu1][c] += g_bu[0];
+    A.g32[kGBu2][c] += g_bu[1];
+  }
+}
+
+// End of a segment: FP64 time sums += FP32 segment partials; partials reset (body cells).
+__global__ void __launch_bounds__(256) adj2d_merge(const AdjArgs A) {
+  int64_t c;
+  if (!adj_cell(A.g, &c)) return;
+#pragma unroll
+  for (int q = 0; q < kNumGrad; ++q) {
+    A.grad[q][c] += (double)A.g32[q][c];
+    A.g32[q][c] = 0.f;
+  }
 }
 
 __global__ void set_step_counter(int* step, int value) { *step = value; }

@@ -199,7 +199,9 @@ FWGB_API int fw_destroy(fw_handle *h);
 FWGB_API int fw_adjoint_forward(fw_handle *h, void *stream, int32_t checkpoint_every);
 
 /* Reverse pass: recompute each segment from its checkpoint and run the adjoint step backwards,
- * accumulating the gradient in FP64. `residual` = traces - observed, device float32
+ * accumulating the gradient: each step's contributions are formed in FP32 (the precision of the
+ * adjoint fields) into per-segment FP32 partial sums that are added into FP64 time sums at the
+ * end of every segment (FWGB_ADJ_F64_STEPS=1: every step's contributions in FP64 instead). `residual` = traces - observed, device float32
  * [n_out][ncoordsout]. `grad_out`: device FP64 [12][nx][ny] in the order dt/rho, dt*K, 1/kappau,
  * 1/kappax, au1, bu1, au2, bu2, ax1, bx1, ax2, bx2 (ghost cells zero). The wavefield left in the
  * handle afterwards is the first segment's recomputation. */

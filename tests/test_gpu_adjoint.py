@@ -1,5 +1,6 @@
-"""GPU adjoint (FP32 wavefields, FP64 gradient accumulation) against the FP64 NumPy adjoint and
-against central finite differences of the FP64 oracle.
+"""GPU adjoint (FP32 wavefields; FP32 per-step contributions summed per checkpoint segment, FP64
+time sums across segments) against the FP64 NumPy adjoint, against the all-FP64 accumulation
+mode, and against central finite differences of the FP64 oracle.
 
 Tolerances: engine-map gradients within 1e-3 relative L2 of the FP64 adjoint; physical-map
 gradients (c, rho, alpha0) within 2e-2 of central differences (h = 1e-3 relative, tap sets
@@ -52,6 +53,41 @@ def test_engine_map_gradients_match_fp64_adjoint(engine_lib, cuda, name, nt, eve
         outside = g[i].copy()
         outside[body] = 0
         assert not outside.any()
+
+
+def test_segmented_accumulation_matches_fp64_steps(engine_lib, cuda):
+    """Default accumulation (FP32 contributions, FP32 segment partials, FP64 totals) against
+    every step formed and added in FP64 (FWGB_ADJ_F64_STEPS=1): within 1e-5 relative L2 per map,
+    on a run with several segments."""
+    import os
+
+    torch = cuda
+    from fullwave25_gb300.engine import Engine
+
+    inp = _small("2d_small", 120)
+    obs = _small("2d_small", 120)
+    obs.maps = dict(obs.maps)
+    obs.maps["rho"] = (obs.maps["rho"] * np.float32(0.97)).astype(np.float32)
+    observed = Oracle(obs).run().astype(np.float32)
+    out = {}
+    for mode in ("segmented", "f64"):
+        if mode == "f64":
+            os.environ["FWGB_ADJ_F64_STEPS"] = "1"
+        try:
+            with Engine(inp) as eng:
+                eng.adjoint_forward(30)
+                res = torch.as_tensor(eng.read_traces() - observed, device="cuda").contiguous()
+                g = torch.zeros((12,) + inp.shape, dtype=torch.float64, device="cuda")
+                eng.adjoint_backward(res.data_ptr(), g.data_ptr())
+                torch.cuda.synchronize()
+                out[mode] = g.cpu().numpy()
+        finally:
+            os.environ.pop("FWGB_ADJ_F64_STEPS", None)
+    for i in range(12):
+        a, b = out["segmented"][i], out["f64"][i]
+        assert np.abs(b).max() > 0
+        err = np.linalg.norm(a - b) / np.linalg.norm(b)
+        assert err < 1e-5, f"map {i}: rel-L2 {err:.3e}"
 
 
 @pytest.fixture(scope="module")
