@@ -1295,6 +1295,11 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     A.grad[q] = h->adj_grad + (size_t)q * fs;
     A.g32[q] = h->adj_lam + (size_t)(15 + q) * fs;
   }
+  A.ndmap = h->d.ndmap;
+  // the tap table goes to shared memory when it fits the default 48 KB of dynamic shared memory
+  const size_t tap_bytes = (size_t)h->d.ndmap * kTapStride * sizeof(float);
+  const bool smem_taps = tap_bytes <= 48 * 1024;
+  const size_t sm = smem_taps ? tap_bytes : 0;
   // FWGB_ADJ_F64_STEPS=1: form and add every step's contributions in FP64 (slow on GB300's FP64
   // pipe; kept to validate the default segmented FP32-partial / FP64-total accumulation)
   const char* f64env = std::getenv("FWGB_ADJ_F64_STEPS");
@@ -1330,17 +1335,26 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     for (int n = n1 - 1; n >= n0; --n) {
       A.Sn = h->adj_store + state_elems * (n - n0);
       A.Sn1 = h->adj_store + state_elems * (n - n0 + 1);
-      if (!first) adj2d_assemble<<<grid, block, 0, s>>>(A);
+      if (!first) {
+        if (smem_taps) adj2d_assemble<true><<<grid, block, sm, s>>>(A);
+        else adj2d_assemble<false><<<grid, block, 0, s>>>(A);
+      }
       first = false;
       if (counts[2]) adj2d_io<<<(counts[2] + 255) / 256, 256, 0, s>>>(A, L, residual, n, 0, 0, counts[2]);
       if (counts[0] || counts[1])
         adj2d_zero<<<(std::max(counts[0], counts[1]) + 255) / 256, 256, 0, s>>>(A, L, n, counts[0], counts[1]);
-      if (f64_steps) {
-        adj2d_prs<true><<<grid, block, 0, s>>>(A);
-        adj2d_vel<true><<<grid, block, 0, s>>>(A);
+      if (f64_steps && smem_taps) {
+        adj2d_prs<true, true><<<grid, block, sm, s>>>(A);
+        adj2d_vel<true, true><<<grid, block, sm, s>>>(A);
+      } else if (f64_steps) {
+        adj2d_prs<true, false><<<grid, block, 0, s>>>(A);
+        adj2d_vel<true, false><<<grid, block, 0, s>>>(A);
+      } else if (smem_taps) {
+        adj2d_prs<false, true><<<grid, block, sm, s>>>(A);
+        adj2d_vel<false, true><<<grid, block, sm, s>>>(A);
       } else {
-        adj2d_prs<false><<<grid, block, 0, s>>>(A);
-        adj2d_vel<false><<<grid, block, 0, s>>>(A);
+        adj2d_prs<false, false><<<grid, block, 0, s>>>(A);
+        adj2d_vel<false, false><<<grid, block, 0, s>>>(A);
       }
     }
     if (!f64_steps) adj2d_merge<<<grid, block, 0, s>>>(A);

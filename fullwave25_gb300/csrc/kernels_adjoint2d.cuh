@@ -34,6 +34,7 @@ struct AdjArgs {
   float* lam_phi[2][2];
   float* lam_d[2];
   float* lam_g[2];
+  int ndmap;                 // tap sets in m.taps
   double* grad[kNumGrad];    // FP64 time sums
   float* g32[kNumGrad];      // FP32 partial sums of the current segment (segmented mode)
 };
@@ -48,15 +49,53 @@ __device__ __forceinline__ const float* S_phi(const float* S, int64_t fs, int a,
   return S + (7 + 2 * a + nu) * fs;
 }
 
-__device__ __forceinline__ float tap_of(const Maps& m, int64_t c, int idx) {
-  return __ldg(m.taps + (size_t)__ldg(m.dcmap + c) * kTapStride + idx);
+// Tap table access: from a shared-memory copy of the table (kS, when it fits) or through the
+// read-only path. The transposed stencils read one tap of every neighbour, so the table is read
+// ~40 times per cell: the shared copy turns each of those into one L1-latency access.
+template <bool kS>
+struct TapSrc {
+  const float* t;
+  __device__ __forceinline__ float tap(int dc, int idx) const {
+    if constexpr (kS) return t[dc * kTapStride + idx];
+    else return __ldg(t + (size_t)dc * kTapStride + idx);
+  }
+  __device__ __forceinline__ void load(int dc, float (&c)[8], float& co) const {
+    if constexpr (kS) {
+      const float* r = t + dc * kTapStride;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) c[k] = r[k];
+      co = r[8];
+    } else {
+      load_taps(t, dc, c, co);
+    }
+  }
+};
+
+// Copy the tap table into shared memory (all threads of the block; before any early return).
+template <bool kS>
+__device__ __forceinline__ TapSrc<kS> stage_taps(const AdjArgs& A, float* s_taps) {
+  if constexpr (kS) {
+    const int n = A.ndmap * kTapStride;
+    const int tid = threadIdx.y * blockDim.x + threadIdx.x, nthr = blockDim.x * blockDim.y;
+    for (int i = tid; i < n; i += nthr) s_taps[i] = __ldg(A.m.taps + i);
+    __syncthreads();
+    return TapSrc<kS>{s_taps};
+  } else {
+    return TapSrc<kS>{A.m.taps};
+  }
+}
+
+template <bool kS>
+__device__ __forceinline__ float tap_of(const Maps& m, const TapSrc<kS>& T, int64_t c, int idx) {
+  return T.tap(__ldg(m.dcmap + c), idx);
 }
 
 // D_a f at c (the velocity-kernel stencil), same operation order as the forward kernels
-__device__ __forceinline__ float grad_at(const Maps& m, const float* f, int64_t c, int64_t se,
-                                         int64_t sf, float inv_h) {
+template <bool kS>
+__device__ __forceinline__ float grad_at(const Maps& m, const TapSrc<kS>& T, const float* f,
+                                         int64_t c, int64_t se, int64_t sf, float inv_h) {
   float cm[8], co;
-  load_taps(m.taps, __ldg(m.dcmap + c), cm, co);
+  T.load(__ldg(m.dcmap + c), cm, co);
   float g = 0.f;
 #pragma unroll
   for (int k = 1; k <= 8; ++k) g = fmaf(cm[k - 1], __ldg(f + c + k * se) - __ldg(f + c - (k - 1) * se), g);
@@ -65,10 +104,11 @@ __device__ __forceinline__ float grad_at(const Maps& m, const float* f, int64_t 
 }
 
 // D'_a v at c (the pressure-kernel stencil)
-__device__ __forceinline__ float div_at(const Maps& m, const float* v, int64_t c, int64_t se,
-                                        int64_t sf, float inv_h) {
+template <bool kS>
+__device__ __forceinline__ float div_at(const Maps& m, const TapSrc<kS>& T, const float* v,
+                                        int64_t c, int64_t se, int64_t sf, float inv_h) {
   float cm[8], co;
-  load_taps(m.taps, __ldg(m.dcmap + c), cm, co);
+  T.load(__ldg(m.dcmap + c), cm, co);
   float d = 0.f;
 #pragma unroll
   for (int k = 1; k <= 8; ++k) d = fmaf(cm[k - 1], __ldg(v + c + (k - 1) * se) - __ldg(v + c - k * se), d);
@@ -77,35 +117,37 @@ __device__ __forceinline__ float div_at(const Maps& m, const float* v, int64_t c
 }
 
 // (D_a^T u)(q): u is zero outside the body
-__device__ __forceinline__ float grad_T_at(const Maps& m, const float* u, int64_t q, int64_t se,
-                                           int64_t sf, float inv_h) {
+template <bool kS>
+__device__ __forceinline__ float grad_T_at(const Maps& m, const TapSrc<kS>& T, const float* u,
+                                           int64_t q, int64_t se, int64_t sf, float inv_h) {
   float acc = 0.f;
 #pragma unroll
   for (int k = 1; k <= 8; ++k) {
     const int64_t c1 = q - k * se, c2 = q + (k - 1) * se;
-    acc += tap_of(m, c1, k - 1) * __ldg(u + c1) - tap_of(m, c2, k - 1) * __ldg(u + c2);
+    acc += tap_of(m, T, c1, k - 1) * __ldg(u + c1) - tap_of(m, T, c2, k - 1) * __ldg(u + c2);
   }
 #pragma unroll
   for (int s = -1; s <= 1; s += 2) {
     const int64_t c1 = q - se - s * sf, c2 = q - s * sf;
-    acc += tap_of(m, c1, 8) * __ldg(u + c1) - tap_of(m, c2, 8) * __ldg(u + c2);
+    acc += tap_of(m, T, c1, 8) * __ldg(u + c1) - tap_of(m, T, c2, 8) * __ldg(u + c2);
   }
   return acc * inv_h;
 }
 
 // (D'_a^T u)(q)
-__device__ __forceinline__ float div_T_at(const Maps& m, const float* u, int64_t q, int64_t se,
-                                          int64_t sf, float inv_h) {
+template <bool kS>
+__device__ __forceinline__ float div_T_at(const Maps& m, const TapSrc<kS>& T, const float* u,
+                                          int64_t q, int64_t se, int64_t sf, float inv_h) {
   float acc = 0.f;
 #pragma unroll
   for (int k = 1; k <= 8; ++k) {
     const int64_t c1 = q - (k - 1) * se, c2 = q + k * se;
-    acc += tap_of(m, c1, k - 1) * __ldg(u + c1) - tap_of(m, c2, k - 1) * __ldg(u + c2);
+    acc += tap_of(m, T, c1, k - 1) * __ldg(u + c1) - tap_of(m, T, c2, k - 1) * __ldg(u + c2);
   }
 #pragma unroll
   for (int s = -1; s <= 1; s += 2) {
     const int64_t c1 = q - s * sf, c2 = q + se - s * sf;
-    acc += tap_of(m, c1, 8) * __ldg(u + c1) - tap_of(m, c2, 8) * __ldg(u + c2);
+    acc += tap_of(m, T, c1, 8) * __ldg(u + c1) - tap_of(m, T, c2, 8) * __ldg(u + c2);
   }
   return acc * inv_h;
 }
@@ -119,11 +161,14 @@ __device__ __forceinline__ bool adj_cell(const Grid& g, int64_t* c) {
 }
 
 // lam_p += sum_a D_a^T lam_g_a
+template <bool kS>
 __global__ void __launch_bounds__(256) adj2d_assemble(const AdjArgs A) {
+  extern __shared__ float s_taps[];
+  const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
   int64_t q;
   if (!adj_cell(A.g, &q)) return;
-  const float add = grad_T_at(A.m, A.lam_g[0], q, A.g.sx, 1, A.g.inv_h[0]) +
-                    grad_T_at(A.m, A.lam_g[1], q, 1, A.g.sx, A.g.inv_h[1]);
+  const float add = grad_T_at(A.m, T, A.lam_g[0], q, A.g.sx, 1, A.g.inv_h[0]) +
+                    grad_T_at(A.m, T, A.lam_g[1], q, 1, A.g.sx, A.g.inv_h[1]);
   A.lam_p[q] += add;
 }
 
@@ -150,9 +195,11 @@ __global__ void adj2d_zero(const AdjArgs A, const Lists L, int n, int n_src, int
 // pipe is the bottleneck then); otherwise contributions are formed in FP32 (the precision of the
 // adjoint fields themselves) and summed per checkpoint segment in FP32 partials, which
 // adj2d_merge adds into the FP64 time sums at the end of every segment.
-template <bool kF64>
+template <bool kF64, bool kS>
 __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
   using acc_t = typename std::conditional<kF64, double, float>::type;
+  extern __shared__ float s_taps[];
+  const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
   int64_t c;
   if (!adj_cell(A.g, &c)) return;
   const Grid& g = A.g;
@@ -166,7 +213,7 @@ __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
   const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
-    const float d = div_at(A.m, S_v(A.Sn1, fs, a), c, se[a], sf[a], g.inv_h[a]);
+    const float d = div_at(A.m, T, S_v(A.Sn1, fs, a), c, se[a], sf[a], g.inv_h[a]);
     const float n1 = __ldg(S_phi(A.Sn1, fs, a, 0) + c), n2 = __ldg(S_phi(A.Sn1, fs, a, 1) + c);
     div += fmaf(d, ikx, n1) + n2;
     float lam_d = -k * ikx * lp;
@@ -199,9 +246,11 @@ __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
   }
 }
 
-template <bool kF64>
+template <bool kF64, bool kS>
 __global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
   using acc_t = typename std::conditional<kF64, double, float>::type;
+  extern __shared__ float s_taps[];
+  const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
   int64_t c;
   if (!adj_cell(A.g, &c)) return;
   const Grid& g = A.g;
@@ -213,8 +262,8 @@ __global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
   const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
-    const float lv = A.lam_v[a][c] + div_T_at(A.m, A.lam_d[a], c, se[a], sf[a], g.inv_h[a]);
-    const float gr = grad_at(A.m, S_p(A.Sn, fs), c, se[a], sf[a], g.inv_h[a]);
+    const float lv = A.lam_v[a][c] + div_T_at(A.m, T, A.lam_d[a], c, se[a], sf[a], g.inv_h[a]);
+    const float gr = grad_at(A.m, T, S_p(A.Sn, fs), c, se[a], sf[a], g.inv_h[a]);
     const float p1 = __ldg(S_psi(A.Sn1, fs, a, 0) + c), p2 = __ldg(S_psi(A.Sn1, fs, a, 1) + c);
     float lam_g = -r * iku * lv;
 #pragma unroll
