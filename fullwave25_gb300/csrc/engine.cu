@@ -17,6 +17,7 @@
 #include <mutex>
 #include <new>
 #include <string>
+#include <utility>
 #include <vector>
 
 #include "../../include/fwgb.h"
@@ -238,14 +239,41 @@ int upload_grid(fw_handle* h, void* dst, const void* src, size_t elem, bool on_d
   return FW_OK;
 }
 
+// Time-step kernels are launched with programmatic dependent launch (FWGB_PDL=0 turns it off):
+// each may be scheduled while the previous kernel of the stream drains, and waits for it on the
+// device (pdl_entry). Captured into graphs as programmatic dependency edges.
+bool pdl_enabled() {
+  static const bool on = [] {
+    const char* v = std::getenv("FWGB_PDL");
+    return !(v && std::strcmp(v, "0") == 0);
+  }();
+  return on;
+}
+
+template <typename... KArgs, typename... Args>
+void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s,
+              Args&&... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = attr;
+  cfg.numAttrs = pdl_enabled() ? 1 : 0;
+  cudaLaunchKernelEx(&cfg, kernel, std::forward<Args>(args)...);
+}
+
 // One time step: velocity kernel, then pressure kernel (+ tile epilogue), with the cell physics
 // CV/CP (isotropic, anisotropic or exponential attenuation) of the handle.
 template <int TY, int XC, class CV, class CP>
 void launch_march2d(fw_handle* h, cudaStream_t s) {
   const int body_x = (int)h->nx - 2 * kGhost, body_y = (int)h->ny - 2 * kGhost;
   dim3 grid((body_y + TY - 1) / TY, (body_x + XC - 1) / XC);
-  vel2d_march<TY, XC, CV><<<grid, TY, 0, s>>>(h->args, h->tmaps2.p);
-  prs2d_march<TY, XC, CP><<<grid, TY, 0, s>>>(h->args, h->tmaps2.vx, h->tmaps2.vy);
+  launch_k(vel2d_march<TY, XC, CV>, grid, dim3(TY), 0, s, h->args, h->tmaps2.p);
+  launch_k(prs2d_march<TY, XC, CP>, grid, dim3(TY), 0, s, h->args, h->tmaps2.vx, h->tmaps2.vy);
 }
 
 template <int ND, class CV, class CP, int kMin>
@@ -257,8 +285,8 @@ void launch_typed(fw_handle* h, cudaStream_t s) {
       case 0:
       case kPersistentShape: {  // the persistent shape issues the direct kernels when captured
         dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
-        vel2d_direct<CV><<<grid, block, 0, s>>>(h->args);
-        prs2d_direct<CP><<<grid, block, 0, s>>>(h->args);
+        launch_k(vel2d_direct<CV>, grid, block, 0, s, h->args);
+        launch_k(prs2d_direct<CP>, grid, block, 0, s, h->args);
         break;
       }
       case 1: launch_march2d<64, 16, CV, CP>(h, s); break;
@@ -270,12 +298,12 @@ void launch_typed(fw_handle* h, cudaStream_t s) {
   } else if (h->variant == kMarch) {
     dim3 grid(t.n[2], t.n[1], t.n[0]), block(kMTZ, kMTY);
     const MarchMaps& tm = h->tmaps;
-    vel3d_march<kMarchXC, CV, kMin><<<grid, block, 0, s>>>(h->args, tm.p);
-    prs3d_march<kMarchXC, CP, kMin><<<grid, block, 0, s>>>(h->args, tm.vx, tm.vy, tm.vz);
+    launch_k(vel3d_march<kMarchXC, CV, kMin>, grid, block, 0, s, h->args, tm.p);
+    launch_k(prs3d_march<kMarchXC, CP, kMin>, grid, block, 0, s, h->args, tm.vx, tm.vy, tm.vz);
   } else {
     dim3 grid(t.n[2], t.n[1], t.n[0]), block(kD3TZ, kD3TY, kD3TX);
-    vel3d_direct<CV><<<grid, block, 0, s>>>(h->args);
-    prs3d_direct<CP><<<grid, block, 0, s>>>(h->args);
+    launch_k(vel3d_direct<CV>, grid, block, 0, s, h->args);
+    launch_k(prs3d_direct<CP>, grid, block, 0, s, h->args);
   }
 }
 
@@ -286,10 +314,11 @@ void launch_stream3d_ps(fw_handle* h, cudaStream_t s) {
   dim3 grid(t.n[2], t.n[1], t.n[0]), block(kMTZ, kMTY);
   const MarchMaps& tm = h->tmaps;
   const StreamMaps& sm = h->smaps;
-  vel3d_stream<kMarchXC, kPS, kMRdtRho><<<grid, block, vel_stream_smem<kPS>(), s>>>(
-      h->args, tm.p, sm.vstate, sm.vmaps, sm.dcmap);
-  prs3d_stream<kMarchXC, kPS, kBeta, kMDtK><<<grid, block, prs_stream_smem<kPS, kBeta>(), s>>>(
-      h->args, tm.vx, tm.vy, tm.vz, sm.pstate, sm.phi, kBeta ? sm.pmaps7 : sm.pmaps6, sm.dcmap);
+  launch_k(vel3d_stream<kMarchXC, kPS, kMRdtRho>, grid, block, vel_stream_smem<kPS>(), s,
+           h->args, tm.p, sm.vstate, sm.vmaps, sm.dcmap);
+  launch_k(prs3d_stream<kMarchXC, kPS, kBeta, kMDtK>, grid, block, prs_stream_smem<kPS, kBeta>(), s,
+           h->args, tm.vx, tm.vy, tm.vz, sm.pstate, sm.phi, kBeta ? sm.pmaps7 : sm.pmaps6,
+           sm.dcmap);
 }
 
 template <bool kBeta>
@@ -1413,9 +1442,12 @@ constexpr int kGroupGraphSteps = 64;
 
 template <int TY, int XC>
 void group_launch_march(fw_group* g, int n_blocks, cudaStream_t s) {
-  vel2d_march_group<TY, XC><<<n_blocks, TY, 0, s>>>(g->d_args, g->d_maps, g->d_tiles);
-  if (g->beta) prs2d_march_group<TY, XC, true><<<n_blocks, TY, 0, s>>>(g->d_args, g->d_maps, g->d_tiles);
-  else prs2d_march_group<TY, XC, false><<<n_blocks, TY, 0, s>>>(g->d_args, g->d_maps, g->d_tiles);
+  const StepArgs* a = g->d_args;
+  const CUtensorMap* m = g->d_maps;
+  const int4* w = g->d_tiles;
+  launch_k(vel2d_march_group<TY, XC>, dim3(n_blocks), dim3(TY), 0, s, a, m, w);
+  if (g->beta) launch_k(prs2d_march_group<TY, XC, true>, dim3(n_blocks), dim3(TY), 0, s, a, m, w);
+  else launch_k(prs2d_march_group<TY, XC, false>, dim3(n_blocks), dim3(TY), 0, s, a, m, w);
 }
 
 void group_launch_step(fw_group* g, int n_tiles, cudaStream_t s) {
@@ -1423,9 +1455,11 @@ void group_launch_step(fw_group* g, int n_tiles, cudaStream_t s) {
   switch (g->shape) {
     case 0: {
       const dim3 block(kD2TY, kD2TX);
-      vel2d_group<<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
-      if (g->beta) prs2d_group<true><<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
-      else prs2d_group<false><<<n_tiles, block, 0, s>>>(g->d_args, g->d_tiles);
+      const StepArgs* a = g->d_args;
+      const int4* w = g->d_tiles;
+      launch_k(vel2d_group, dim3(n_tiles), block, 0, s, a, w);
+      if (g->beta) launch_k(prs2d_group<true>, dim3(n_tiles), block, 0, s, a, w);
+      else launch_k(prs2d_group<false>, dim3(n_tiles), block, 0, s, a, w);
       break;
     }
     case 1: group_launch_march<64, 16>(g, n_tiles, s); break;

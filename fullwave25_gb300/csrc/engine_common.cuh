@@ -75,6 +75,16 @@ struct StepArgs {
   int* step;                 // device step counter: velocity kernel of step n sets it to n+1
 };
 
+// Programmatic dependent launch: every time-step kernel is launched allowed to start while the
+// previous kernel of the stream drains. It first waits for that kernel (and so, transitively,
+// every earlier one) to complete and its writes to be visible, then lets the next kernel launch:
+// the launch latency and the next kernel's block scheduling overlap this kernel's last wave.
+// Without the launch attribute both instructions are no-ops.
+__device__ __forceinline__ void pdl_entry() {
+  asm volatile("griddepcontrol.wait;" ::: "memory");
+  asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ void load_taps(const float* taps, int dc, float (&c)[8], float& co) {
   const float4* t = reinterpret_cast<const float4*>(taps + (size_t)dc * kTapStride);
   float4 a = __ldg(t), b = __ldg(t + 1), e = __ldg(t + 2);

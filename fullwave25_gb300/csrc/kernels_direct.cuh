@@ -86,12 +86,14 @@ __device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int ti
 
 template <class CV>
 __global__ void __launch_bounds__(256) vel2d_direct(const StepArgs A) {
+  pdl_entry();
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *A.step += 1;
   vel2d_body<CV>(A, blockIdx.x, blockIdx.y);
 }
 
 template <class CP>
 __global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
+  pdl_entry();
   prs2d_body<CP>(A, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x);
 }
 
@@ -101,6 +103,7 @@ __global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
 // every listed simulation by one step; simulations may be at different steps.
 __global__ void __launch_bounds__(256) vel2d_group(const StepArgs* __restrict__ sims,
                                                    const int4* __restrict__ tiles) {
+  pdl_entry();
   const int4 t = tiles[blockIdx.x];
   const StepArgs& A = sims[t.x];
   if (t.w == 0 && threadIdx.x == 0 && threadIdx.y == 0) *A.step += 1;
@@ -110,6 +113,7 @@ __global__ void __launch_bounds__(256) vel2d_group(const StepArgs* __restrict__ 
 template <bool kBeta>
 __global__ void __launch_bounds__(256) prs2d_group(const StepArgs* __restrict__ sims,
                                                    const int4* __restrict__ tiles) {
+  pdl_entry();
   const int4 t = tiles[blockIdx.x];
   prs2d_body<CellPrsT<2, kBeta, false>>(sims[t.x], t.y, t.z, t.w);
 }
@@ -117,6 +121,7 @@ __global__ void __launch_bounds__(256) prs2d_group(const StepArgs* __restrict__ 
 // ---------------------------------------------------------------------------------------- 3D
 template <class CV>
 __global__ void __launch_bounds__(256) vel3d_direct(const StepArgs A) {
+  pdl_entry();
   const Grid& g = A.g;
   const int k = kGhost + blockIdx.x * kD3TZ + threadIdx.x;
   const int j = kGhost + blockIdx.y * kD3TY + threadIdx.y;
@@ -149,6 +154,7 @@ __global__ void __launch_bounds__(256) vel3d_direct(const StepArgs A) {
 
 template <class CP>
 __global__ void __launch_bounds__(256) prs3d_direct(const StepArgs A) {
+  pdl_entry();
   const Grid& g = A.g;
   const int k = kGhost + blockIdx.x * kD3TZ + threadIdx.x;
   const int j = kGhost + blockIdx.y * kD3TY + threadIdx.y;

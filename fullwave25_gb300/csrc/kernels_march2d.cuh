@@ -205,6 +205,7 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const CUtens
 template <int TY, int XC, class CV>
 __global__ void __launch_bounds__(TY)
 vel2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
+  pdl_entry();
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *A.step += 1;
   vel2d_march_body<TY, XC, CV>(A, &tm_p, blockIdx.x, blockIdx.y);
 }
@@ -213,6 +214,7 @@ template <int TY, int XC, class CP>
 __global__ void __launch_bounds__(TY)
 prs2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
             const __grid_constant__ CUtensorMap tm_vy) {
+  pdl_entry();
   prs2d_march_body<TY, XC, CP>(A, &tm_vx, &tm_vy, blockIdx.x, blockIdx.y);
 }
 
@@ -233,6 +235,7 @@ __global__ void __launch_bounds__(TY)
 vel2d_march_group(const StepArgs* __restrict__ sims, const CUtensorMap* __restrict__ maps,
                   const int4* __restrict__ work) {
   __shared__ alignas(16) StepArgs A;
+  pdl_entry();
   const int4 t = work[blockIdx.x];
   stage_args(A, sims[t.x]);
   if (t.w && threadIdx.x == 0) *A.step += 1;
@@ -244,6 +247,7 @@ __global__ void __launch_bounds__(TY)
 prs2d_march_group(const StepArgs* __restrict__ sims, const CUtensorMap* __restrict__ maps,
                   const int4* __restrict__ work) {
   __shared__ alignas(16) StepArgs A;
+  pdl_entry();
   const int4 t = work[blockIdx.x];
   stage_args(A, sims[t.x]);
   prs2d_march_body<TY, XC, CellPrsT<2, kBeta, false>>(A, maps + 3 * t.x + 1, maps + 3 * t.x + 2,

@@ -34,6 +34,7 @@ struct MarchMaps {
 template <int XC, class CV, int kMinBlocks = 3>
 __global__ void __launch_bounds__(kMThreads, kMinBlocks)
 vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
+  pdl_entry();
   __shared__ alignas(128) float ring[kRing][kPSlot];
   __shared__ alignas(8) uint64_t bar[kRing];
   const Grid& g = A.g;
@@ -116,6 +117,7 @@ template <int XC, class CP, int kMinBlocks = 3>
 __global__ void __launch_bounds__(kMThreads, kMinBlocks)
 prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
             const __grid_constant__ CUtensorMap tm_vy, const __grid_constant__ CUtensorMap tm_vz) {
+  pdl_entry();
   __shared__ alignas(128) float rx[kRing][kXSlot];
   __shared__ alignas(128) float ry[kRing][kYSlot];
   __shared__ alignas(128) float rz[kRing][kZSlot];

@@ -52,6 +52,7 @@ __global__ void __launch_bounds__(kMThreads, 3)
 vel3d_stream(const StepArgs A, const __grid_constant__ CUtensorMap tm_p,
              const __grid_constant__ CUtensorMap tm_st, const __grid_constant__ CUtensorMap tm_mp,
              const __grid_constant__ CUtensorMap tm_dc) {
+  pdl_entry();
   __shared__ alignas(128) float ring[kRing][kPSlot];
   __shared__ alignas(8) uint64_t bar[kRing];
   __shared__ alignas(8) uint64_t pbar[kPS];
@@ -171,6 +172,7 @@ prs3d_stream(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
              const __grid_constant__ CUtensorMap tm_vy, const __grid_constant__ CUtensorMap tm_vz,
              const __grid_constant__ CUtensorMap tm_pp, const __grid_constant__ CUtensorMap tm_phi,
              const __grid_constant__ CUtensorMap tm_mp, const __grid_constant__ CUtensorMap tm_dc) {
+  pdl_entry();
   constexpr int kMapF = kVelMapF + (kBeta ? 1 : 0);
   __shared__ alignas(128) float rx[kRing][kXSlot];
   __shared__ alignas(128) float ry[kRing][kYSlot];
