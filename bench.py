@@ -190,6 +190,26 @@ def time_oracle(workload: str, budget_s: float):
     return out
 
 
+def time_numpy_oracle(workload: str, budget_s: float):
+    """The FP64 NumPy transcription of the scheme (``oracle/fdtd_oracle.py``) on the same bounded
+    sample as :func:`time_oracle`, for as many steps as fit in ``budget_s``; NumPy runs its
+    element-wise arrays on one host thread."""
+    sys.path.insert(0, str(ROOT / "oracle"))
+    from fdtd_oracle import Oracle
+
+    inp, _, _, label = time_oracle.last
+    o = Oracle(inp)
+    o.step(None)  # warm-up (no recording: the timed loop is the time step itself)
+    steps, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < budget_s and steps + 2 < inp.nt:
+        o.step(None)
+        steps += 1
+    el = time.perf_counter() - t0
+    cells = int(np.prod(inp.shape))
+    return {"value": cells * steps / el / 1e9, "unit": METRIC, "cores": 1, "kind": "port",
+            "sample": f"FP64 NumPy oracle (one thread), {label}, {steps} time steps in {el:.1f} s"}
+
+
 def parity_vs_oracle():
     """rel-L2 of the GPU engine's traces against the FP64 oracle on the CPU-baseline sample."""
     from fullwave25_gb300.engine import Engine
@@ -309,6 +329,8 @@ def run_gpu(args):
     cpu = time_oracle(args.workload, float(os.environ.get("FWGB_CPU_SAMPLE_S", "15"))) if (
         world == 1 and not args.no_cpu_baseline) else None
     parity = parity_vs_oracle() if cpu is not None else None
+    cpu_numpy = (time_numpy_oracle(args.workload, float(os.environ.get("FWGB_NUMPY_SAMPLE_S", "5")))
+                 if cpu is not None else None)
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
@@ -325,6 +347,7 @@ def run_gpu(args):
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
                      else "fallback 6800 GB/s"},
         "cpu_baseline": cpu,
+        "cpu_baseline_numpy": cpu_numpy,
         "parity": parity,
         "e2e": e2e,
         "gpu_launches": int(engine.launches_per_step * chunk * args.steps),
