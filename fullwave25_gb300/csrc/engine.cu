@@ -529,6 +529,22 @@ int prepare_stream3d(fw_handle* h) {
   return FW_OK;
 }
 
+// Self-test kernels for the bounded waits: each waits on something nothing will complete.
+__global__ void selftest_mbar_timeout(int* status) {
+  __shared__ alignas(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) mbar_wait_bounded(&bar, 0, status);   // no arrival: gives up
+}
+
+__global__ void selftest_grid_barrier_timeout(unsigned* bar, int* status) {
+  // one block, while the barrier counts two: the generation never advances
+  grid_barrier(bar, status, 2u);
+}
+
 // Device status word (step buffer slot 1): non-zero if a kernel gave up on a bounded wait.
 int check_device_status(fw_handle* h, cudaStream_t s) {
   int st = 0;
@@ -1250,6 +1266,33 @@ int fw_block_tile(const fw_handle* h, int32_t tile[3]) {
 int fw_launches_per_step(const fw_handle* h, int32_t* n) {
   if (!h || !n) return FW_ERR_ARGUMENT;
   *n = 2;
+  return FW_OK;
+}
+
+int fw_selftest_waits(int32_t status_out[2]) {
+  if (!status_out) return fail(nullptr, FW_ERR_ARGUMENT, "status_out is NULL");
+  int* st = nullptr;
+  unsigned* bar = nullptr;
+  if (cudaMalloc(&st, 2 * sizeof(int)) != cudaSuccess ||
+      cudaMalloc(&bar, kBarWords * sizeof(unsigned)) != cudaSuccess) {
+    cudaFree(st);
+    return fail(nullptr, FW_ERR_OOM, "self-test allocation failed");
+  }
+  cudaError_t e = cudaMemset(st, 0, 2 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(bar, 0, kBarWords * sizeof(unsigned));
+  if (e == cudaSuccess) {
+    selftest_mbar_timeout<<<1, 32>>>(st);
+    selftest_grid_barrier_timeout<<<1, dim3(kD2TY, kD2TX)>>>(bar, st + 1);
+    e = cudaDeviceSynchronize();
+  }
+  int h_st[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h_st, st, sizeof(h_st), cudaMemcpyDeviceToHost);
+  cudaFree(st);
+  cudaFree(bar);
+  if (e != cudaSuccess)
+    return fail(nullptr, FW_ERR_CUDA, "self-test failed: %s", cudaGetErrorString(e));
+  status_out[0] = h_st[0];
+  status_out[1] = h_st[1];
   return FW_OK;
 }
 

@@ -24,7 +24,8 @@ EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_fields_aniso
             "fw_set_source_signal",
             "fw_set_source_columns", "fw_set_sensor_groups", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
-            "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_block_tile", "fw_launches_per_step",
+            "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_block_tile", "fw_selftest_waits",
+            "fw_launches_per_step",
             "fw_destroy", "fw_adjoint_forward", "fw_adjoint_backward", "fw_group_create", "fw_group_run", "fw_group_set_members",
             "fw_group_advance", "fw_group_block_tile", "fw_group_destroy",
             "fw_run_noalloc", "fw_last_error")
@@ -108,6 +109,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_device_bytes": (C.c_int, [H, C.POINTER(C.c_uint64)]),
         "fw_kernel_variant": (C.c_int, [H, _IP]),
         "fw_block_tile": (C.c_int, [H, _IP]),
+        "fw_selftest_waits": (C.c_int, [_IP]),
         "fw_launches_per_step": (C.c_int, [H, _IP]),
         "fw_destroy": (C.c_int, [H]),
         "fw_adjoint_forward": (C.c_int, [H, vp, C.c_int32]),
@@ -376,6 +378,18 @@ class Engine:
             self.close()
         except Exception:
             pass
+
+
+def selftest_waits() -> tuple:
+    """Run the bounded-wait self-test (``fw_selftest_waits``): returns the status words of the
+    mbarrier-wait kernel and of the grid-barrier kernel, each of which waits on something that
+    never completes and must give up (expected ``(0x1, 0x4)``)."""
+    lib = load_library()
+    out = (C.c_int32 * 2)()
+    st = lib.fw_selftest_waits(out)
+    if st:
+        raise EngineError("fw_selftest_waits", st, lib.fw_last_error(None).decode())
+    return int(out[0]), int(out[1])
 
 
 class EngineGroup:

@@ -184,6 +184,13 @@ FWGB_API int fw_kernel_variant(const fw_handle *h, int32_t *variant);
  * reference. */
 FWGB_API int fw_block_tile(const fw_handle *h, int32_t tile[3]);
 
+/* Failure-detection self-test: runs a kernel that waits on an mbarrier nothing completes and a
+ * one-block kernel at a grid barrier that counts two blocks; each wait gives up after its limit
+ * (0.5 s, 1 s) and records it in a status word instead of hanging. status_out[0] = the mbarrier
+ * kernel's status (bit 0x1 expected), status_out[1] = the grid-barrier kernel's (bit 0x4
+ * expected). Takes about 1.5 s. No counterpart in the reference. */
+FWGB_API int fw_selftest_waits(int32_t status_out[2]);
+
 /* Kernel launches issued per time step (for launch accounting). */
 FWGB_API int fw_launches_per_step(const fw_handle *h, int32_t *n);
 
