@@ -1377,8 +1377,6 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   const char* f64env = std::getenv("FWGB_ADJ_F64_STEPS");
   const bool f64_steps = f64env && std::strcmp(f64env, "1") == 0;
   const Lists& L = h->args.l;
-  const int n_src = L.ncoords ? 0 : 0;
-  (void)n_src;
   // list lengths: sources after de-duplication, air cells, sensors
   int32_t counts[3] = {0, 0, 0};
   {
