@@ -42,7 +42,8 @@ void fwgb_set_global_error(const char* msg) { g_create_error = msg; }
 
 namespace {
 
-constexpr int kMarchXC = 64;  // x planes per block of the 3D plane-march kernels
+constexpr int kMarchXC = 64;   // x planes per block of the 3D register-load plane march
+constexpr int kStreamXC = 32;  // x planes per block of the streaming 3D march (default)
 
 // 2D kernel shapes the autotuner chooses from: 0 = direct kernels (one block per 32 y x 8 x tile),
 // 1-5 = row-march kernels with TY threads (y columns) walking XC rows (TY + 16 <= 256, the TMA box
@@ -104,6 +105,7 @@ struct fw_handle {
   StreamMaps smaps{};
   bool stream3d = false;       // 3D isotropic: point-wise operands staged by TMA too
   int ps3d = 2;                // stages of the point-wise ring of the streaming kernels
+  int march_xc = kMarchXC;     // x planes per block of the 3D march (streaming: kStreamXC)
   // adjoint (2D): checkpoints every adj_every steps, per-segment state store, adjoint fields
   int adj_every = 0, adj_nckpt = 0;
   float* adj_ckpt = nullptr;     // adj_nckpt states
@@ -156,7 +158,7 @@ Tiling make_tiling(const fw_handle* h) {
   if (h->ndim == 2) {
     t.t[0] = kD2TX; t.t[1] = kD2TY; t.t[2] = 1;
   } else if (h->variant == kMarch) {
-    t.t[0] = kMarchXC; t.t[1] = kMTY; t.t[2] = kMTZ;
+    t.t[0] = h->march_xc; t.t[1] = kMTY; t.t[2] = kMTZ;
   } else {
     t.t[0] = kD3TX; t.t[1] = kD3TY; t.t[2] = kD3TZ;
   }
@@ -307,24 +309,26 @@ void launch_typed(fw_handle* h, cudaStream_t s) {
   }
 }
 
-// Streaming 3D kernels (isotropic engine): kPS-stage point-wise ring in dynamic shared memory.
-template <int kPS, bool kBeta>
+// Streaming 3D kernels (isotropic engine): kPS-stage point-wise ring in dynamic shared memory,
+// XC x planes per block.
+template <int XC, int kPS, bool kBeta>
 void launch_stream3d_ps(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
   dim3 grid(t.n[2], t.n[1], t.n[0]), block(kMTZ, kMTY);
   const MarchMaps& tm = h->tmaps;
   const StreamMaps& sm = h->smaps;
-  launch_k(vel3d_stream<kMarchXC, kPS, kMRdtRho>, grid, block, vel_stream_smem<kPS>(), s,
+  launch_k(vel3d_stream<XC, kPS, kMRdtRho>, grid, block, vel_stream_smem<kPS>(), s,
            h->args, tm.p, sm.vstate, sm.vmaps, sm.dcmap);
-  launch_k(prs3d_stream<kMarchXC, kPS, kBeta, kMDtK>, grid, block, prs_stream_smem<kPS, kBeta>(), s,
+  launch_k(prs3d_stream<XC, kPS, kBeta, kMDtK>, grid, block, prs_stream_smem<kPS, kBeta>(), s,
            h->args, tm.vx, tm.vy, tm.vz, sm.pstate, sm.phi, kBeta ? sm.pmaps7 : sm.pmaps6,
            sm.dcmap);
 }
 
 template <bool kBeta>
 void launch_stream3d(fw_handle* h, cudaStream_t s) {
-  if (h->ps3d == 2) launch_stream3d_ps<2, kBeta>(h, s);
-  else launch_stream3d_ps<3, kBeta>(h, s);
+  if (h->march_xc == kStreamXC) launch_stream3d_ps<kStreamXC, 2, kBeta>(h, s);
+  else if (h->ps3d == 2) launch_stream3d_ps<kMarchXC, 2, kBeta>(h, s);
+  else launch_stream3d_ps<kMarchXC, 3, kBeta>(h, s);
 }
 
 template <int ND, bool kBeta>
@@ -497,18 +501,18 @@ int set_shape2d(fw_handle* h, int k) {
 }
 
 // Allow the streaming kernels their dynamic shared memory (once per process; before any capture).
-template <int kPS>
+template <int XC, int kPS>
 cudaError_t stream3d_attributes() {
   cudaError_t e;
-  if ((e = cudaFuncSetAttribute(vel3d_stream<kMarchXC, kPS, kMRdtRho>,
+  if ((e = cudaFuncSetAttribute(vel3d_stream<XC, kPS, kMRdtRho>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)vel_stream_smem<kPS>())) != cudaSuccess)
     return e;
-  if ((e = cudaFuncSetAttribute(prs3d_stream<kMarchXC, kPS, false, kMDtK>,
+  if ((e = cudaFuncSetAttribute(prs3d_stream<XC, kPS, false, kMDtK>,
                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
                                 (int)prs_stream_smem<kPS, false>())) != cudaSuccess)
     return e;
-  return cudaFuncSetAttribute(prs3d_stream<kMarchXC, kPS, true, kMDtK>,
+  return cudaFuncSetAttribute(prs3d_stream<XC, kPS, true, kMDtK>,
                               cudaFuncAttributeMaxDynamicSharedMemorySize,
                               (int)prs_stream_smem<kPS, true>());
 }
@@ -520,8 +524,9 @@ int prepare_stream3d(fw_handle* h) {
   FW_CUDA(h, cudaGetDevice(&dev));
   std::lock_guard<std::mutex> lk(mu);
   if (std::find(done.begin(), done.end(), dev) != done.end()) return FW_OK;
-  cudaError_t e = stream3d_attributes<2>();
-  if (e == cudaSuccess) e = stream3d_attributes<3>();
+  cudaError_t e = stream3d_attributes<kStreamXC, 2>();
+  if (e == cudaSuccess) e = stream3d_attributes<kMarchXC, 2>();
+  if (e == cudaSuccess) e = stream3d_attributes<kMarchXC, 3>();
   if (e != cudaSuccess)
     return fail(h, FW_ERR_CUDA, "streaming 3D kernels: cudaFuncSetAttribute failed: %s",
                 cudaGetErrorString(e));
@@ -604,6 +609,21 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   {
     const char* v = std::getenv("FWGB_VARIANT");
     h->variant = (h->ndim == 3 && !(v && std::strcmp(v, "direct") == 0)) ? kMarch : kDirect;
+    if (h->variant == kMarch) {
+      // isotropic relaxation engine: point-wise operands staged by TMA as well, unless
+      // FWGB_STREAM3D=0. Streaming blocks march 32 planes with a two-stage point-wise ring (the
+      // next plane's operands in flight while a plane is computed); FWGB_XC3D=64 marches 64
+      // planes and FWGB_PS3D=3 then deepens the ring to three stages. Measured on the plain 3D
+      // workload (Gcell/s): 32 planes 33.74, 64 planes 33.37 (3 stages 31.36), 16 planes
+      // 33.30, 128 planes 32.34.
+      const char* sv = std::getenv("FWGB_STREAM3D");
+      const char* ps = std::getenv("FWGB_PS3D");
+      const char* xc = std::getenv("FWGB_XC3D");
+      h->stream3d = !h->aniso && !h->exp && !(sv && std::strcmp(sv, "0") == 0);
+      h->ps3d = (ps && std::strcmp(ps, "3") == 0) ? 3 : 2;
+      const bool x64 = (xc && std::strcmp(xc, "64") == 0) || h->ps3d == 3;
+      if (h->stream3d && !x64) h->march_xc = kStreamXC;
+    }
   }
   h->tiling = make_tiling(h);
   auto alloc = [&](void** p, size_t bytes) -> int {
@@ -707,13 +727,6 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
     }
   }
   if (h->variant == kMarch && h->ndim == 3) {
-    // isotropic relaxation engine: point-wise operands staged by TMA as well, unless
-    // FWGB_STREAM3D=0; FWGB_PS3D=2|3 sets the depth of the point-wise ring (default 2: the next
-    // plane's operands are in flight while a plane is computed)
-    const char* sv = std::getenv("FWGB_STREAM3D");
-    const char* ps = std::getenv("FWGB_PS3D");
-    h->stream3d = !h->aniso && !h->exp && !(sv && std::strcmp(sv, "0") == 0);
-    h->ps3d = (ps && std::strcmp(ps, "3") == 0) ? 3 : 2;   // 2 stages measured fastest
     if ((st = encode_field_map(h, &h->tmaps.p, A.f.p, kPW, kPH)) ||
         (st = encode_field_map(h, &h->tmaps.vx, A.f.v[0], kXW, kXH)) ||
         (st = encode_field_map(h, &h->tmaps.vy, A.f.v[1], kYW, kYH)) ||

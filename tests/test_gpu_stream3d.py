@@ -22,7 +22,7 @@ TOL = 1e-4
 def _engine(inp, **env):
     from fullwave25_gb300.engine import Engine
 
-    keys = ("FWGB_VARIANT", "FWGB_STREAM3D", "FWGB_PS3D")
+    keys = ("FWGB_VARIANT", "FWGB_STREAM3D", "FWGB_PS3D", "FWGB_XC3D")
     old = {k: os.environ.get(k) for k in keys}
     for k in keys:
         os.environ.pop(k, None)
@@ -65,10 +65,10 @@ def test_stream_equals_register_march_and_direct(engine_lib, cuda, case):
     with _engine(inp, FWGB_STREAM3D=0) as er:
         assert er.kernel_variant == "march"
         np.testing.assert_array_equal(er.run(), ref)
-    for ps in (2, 3):
-        with _engine(inp, FWGB_PS3D=ps) as es:
+    for env in ({}, {"FWGB_XC3D": 64}, {"FWGB_PS3D": 3}):
+        with _engine(inp, **env) as es:
             assert es.kernel_variant == "stream"
-            np.testing.assert_array_equal(es.run(), ref, err_msg=f"{case}: PS3D={ps}")
+            np.testing.assert_array_equal(es.run(), ref, err_msg=f"{case}: {env}")
 
 
 def test_stream_with_beta_matches_oracle(engine_lib, cuda):
@@ -90,6 +90,9 @@ def test_plain_3d_reduced_stream_vs_register(engine_lib, cuda):
 
     d = plain_3d_device_inputs(shape=(160, 40, 72), nt=200, n_pml=8, n_transition=8,
                                sensor_plane=24, element_height=8)
-    with _engine(d) as es, _engine(d, FWGB_STREAM3D=0) as er:
-        assert es.kernel_variant == "stream"
-        np.testing.assert_array_equal(es.run(), er.run())
+    with _engine(d) as es, _engine(d, FWGB_STREAM3D=0) as er, _engine(d, FWGB_XC3D=64) as e8:
+        assert es.kernel_variant == "stream" and es.block_tile[0] == 32
+        assert e8.block_tile[0] == 64
+        ref = er.run()
+        np.testing.assert_array_equal(es.run(), ref)
+        np.testing.assert_array_equal(e8.run(), ref)
