@@ -102,6 +102,7 @@ struct fw_handle {
   bool shape_fixed = false;    // 2D shape forced (FWGB_SHAPE2D / FWGB_VARIANT) or already tuned
   MarchMaps tmaps{};
   March2Maps tmaps2{};
+  bool stream2d = false;       // 2D isotropic row march: point-wise operands staged by TMA too
   StreamMaps smaps{};
   bool stream3d = false;       // 3D isotropic: point-wise operands staged by TMA too
   int ps3d = 2;                // stages of the point-wise ring of the streaming kernels
@@ -274,8 +275,31 @@ template <int TY, int XC, class CV, class CP>
 void launch_march2d(fw_handle* h, cudaStream_t s) {
   const int body_x = (int)h->nx - 2 * kGhost, body_y = (int)h->ny - 2 * kGhost;
   dim3 grid((body_y + TY - 1) / TY, (body_x + XC - 1) / XC);
-  launch_k(vel2d_march<TY, XC, CV>, grid, dim3(TY), 0, s, h->args, h->tmaps2.p);
-  launch_k(prs2d_march<TY, XC, CP>, grid, dim3(TY), 0, s, h->args, h->tmaps2.vx, h->tmaps2.vy);
+  launch_k(vel2d_march<TY, XC, CV>, grid, dim3(TY), 0, s, h->args, h->tmaps2);
+  launch_k(prs2d_march<TY, XC, CP>, grid, dim3(TY), 0, s, h->args, h->tmaps2);
+}
+
+// Streaming row march (isotropic engine): point-wise operands by TMA as well.
+template <int TY, int XC, bool kBeta>
+void launch_stream2d_shape(fw_handle* h, cudaStream_t s) {
+  const int body_x = (int)h->nx - 2 * kGhost, body_y = (int)h->ny - 2 * kGhost;
+  dim3 grid((body_y + TY - 1) / TY, (body_x + XC - 1) / XC);
+  launch_k(vel2d_march<TY, XC, CellVelT<2, false>, true, kMRdtRho>, grid, dim3(TY), 0, s,
+           h->args, h->tmaps2);
+  launch_k(prs2d_march<TY, XC, CellPrsT<2, kBeta, false>, true, kBeta, kMDtK>, grid, dim3(TY), 0,
+           s, h->args, h->tmaps2);
+}
+
+template <bool kBeta>
+void launch_stream2d(fw_handle* h, cudaStream_t s) {
+  switch (h->shape2d) {
+    case 1: launch_stream2d_shape<64, 16, kBeta>(h, s); break;
+    case 2: launch_stream2d_shape<64, 32, kBeta>(h, s); break;
+    case 3: launch_stream2d_shape<128, 16, kBeta>(h, s); break;
+    case 4: launch_stream2d_shape<128, 32, kBeta>(h, s); break;
+    case 5: launch_stream2d_shape<128, 64, kBeta>(h, s); break;
+    default: break;
+  }
 }
 
 template <int ND, class CV, class CP, int kMin>
@@ -341,6 +365,11 @@ void launch_nd(fw_handle* h, cudaStream_t s) {
     if constexpr (ND == 3) {
       if (h->stream3d && h->variant == kMarch) {
         launch_stream3d<kBeta>(h, s);
+        return;
+      }
+    } else {
+      if (h->stream2d && kShapes2D[h->shape2d].ty > 0) {
+        launch_stream2d<kBeta>(h, s);
         return;
       }
     }
@@ -484,15 +513,45 @@ int encode_row_map(fw_handle* h, CUtensorMap* map, float* base, uint32_t bw) {
   return encode_map(h, map, base, 2, dims, strides, box);
 }
 
+// 3D float32 tensor map over a stack of padded 2D fields: dims (pitch, nx, n_fields), box
+// (ty, 1, f): f consecutive fields of one row segment.
+int encode_row_stack_map(fw_handle* h, CUtensorMap* map, float* base, int n_fields, uint32_t ty,
+                         uint32_t f) {
+  const cuuint64_t dims[3] = {(cuuint64_t)h->pitch, (cuuint64_t)h->nx, (cuuint64_t)n_fields};
+  const cuuint64_t strides[2] = {(cuuint64_t)h->pitch * 4, (cuuint64_t)h->ncells_padded * 4};
+  const cuuint32_t box[3] = {ty, 1, f};
+  return encode_map(h, map, base, 3, dims, strides, box);
+}
+
+// Every tensor map of the 2D row march for block width ty (the point-wise ones only for the
+// isotropic relaxation engine).
+int encode_march2_maps(fw_handle* h, uint32_t ty, March2Maps* m) {
+  int st;
+  if ((st = encode_row_map(h, &m->p, h->args.f.p, ty + 16)) ||
+      (st = encode_row_map(h, &m->vx, h->args.f.v[0], ty + 8)) ||
+      (st = encode_row_map(h, &m->vy, h->args.f.v[1], ty + 16)))
+    return st;
+  if (h->aniso || h->exp) return FW_OK;
+  const int ns = n_state(h->ndim), nm = n_maps(h);
+  const cuuint64_t dims[2] = {(cuuint64_t)h->pitch, (cuuint64_t)h->nx};
+  const cuuint64_t strides[1] = {(cuuint64_t)h->pitch * 4};
+  const cuuint32_t box[2] = {ty, 1};
+  if ((st = encode_row_stack_map(h, &m->vst, h->state, ns, ty, kV2StateF)) ||
+      (st = encode_row_stack_map(h, &m->vmp, h->maps, nm, ty, kV2MapF)) ||
+      (st = encode_row_stack_map(h, &m->pp, h->state, ns, ty, 1)) ||
+      (st = encode_row_stack_map(h, &m->phi, h->state, ns, ty, kP2PhiF)) ||
+      (st = encode_row_stack_map(h, &m->pmp6, h->maps, nm, ty, kV2MapF)) ||
+      (st = encode_row_stack_map(h, &m->pmp7, h->maps, nm, ty, kV2MapF + 1)) ||
+      (st = encode_map(h, &m->dc, h->dcmap, 2, dims, strides, box, CU_TENSOR_MAP_DATA_TYPE_INT32)))
+    return st;
+  return FW_OK;
+}
+
 // Select 2D kernel shape k: encode the row tensor maps for its width, drop the step graph.
 int set_shape2d(fw_handle* h, int k) {
   if (kShapes2D[k].ty > 0) {
-    const uint32_t ty = (uint32_t)kShapes2D[k].ty;
-    int st;
-    if ((st = encode_row_map(h, &h->tmaps2.p, h->args.f.p, ty + 16)) ||
-        (st = encode_row_map(h, &h->tmaps2.vx, h->args.f.v[0], ty + 8)) ||
-        (st = encode_row_map(h, &h->tmaps2.vy, h->args.f.v[1], ty + 16)))
-      return st;
+    int st = encode_march2_maps(h, (uint32_t)kShapes2D[k].ty, &h->tmaps2);
+    if (st) return st;
   }
   h->shape2d = k;
   h->variant = kShapes2D[k].persistent ? kPersistent : kShapes2D[k].ty > 0 ? kMarch : kDirect;
@@ -702,6 +761,10 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   A.l.mod_t = desc->mod_t;
   A.step = h->step;
   if (h->ndim == 2) {
+    // isotropic relaxation engine: the row-march shapes stage the point-wise operands by TMA too,
+    // unless FWGB_STREAM2D=0
+    const char* s2 = std::getenv("FWGB_STREAM2D");
+    h->stream2d = !h->aniso && !h->exp && !(s2 && std::strcmp(s2, "0") == 0);
     // 2D kernel shape: forced by FWGB_VARIANT=direct or FWGB_SHAPE2D=<k>, else the direct kernels
     // until the autotuner (first advance from step 0) has measured the shapes for this grid
     const char* v = std::getenv("FWGB_VARIANT");
@@ -1480,7 +1543,8 @@ struct fw_group {
   // work list: direct kernels {member, tile_y, tile_x, tile index within the member};
   //            march kernels  {member, y block, x chunk, 1 for the block that counts the step}
   int4* d_tiles = nullptr;
-  CUtensorMap* d_maps = nullptr;    // march kernels: row maps p, vx, vy per member
+  March2Maps* d_maps = nullptr;     // march kernels: one March2Maps per member
+  bool stream = true;               // march kernels with TMA-staged point-wise operands
   size_t args_cap = 0, tiles_cap = 0;
   int shape = 0;                    // index into kShapes2D (0 = direct group kernels)
   bool shape_fixed = false;         // forced by the environment or already tuned
@@ -1494,14 +1558,21 @@ namespace {
 
 constexpr int kGroupGraphSteps = 64;
 
+template <int TY, int XC, bool kStream>
+void group_launch_march_t(fw_group* g, int n_blocks, cudaStream_t s) {
+  const StepArgs* a = g->d_args;
+  const March2Maps* m = g->d_maps;
+  const int4* w = g->d_tiles;
+  const dim3 grid(n_blocks), block(TY);
+  launch_k(vel2d_march_group<TY, XC, kStream, kMRdtRho>, grid, block, 0, s, a, m, w);
+  if (g->beta) launch_k(prs2d_march_group<TY, XC, true, kStream, kMDtK>, grid, block, 0, s, a, m, w);
+  else launch_k(prs2d_march_group<TY, XC, false, kStream, kMDtK>, grid, block, 0, s, a, m, w);
+}
+
 template <int TY, int XC>
 void group_launch_march(fw_group* g, int n_blocks, cudaStream_t s) {
-  const StepArgs* a = g->d_args;
-  const CUtensorMap* m = g->d_maps;
-  const int4* w = g->d_tiles;
-  launch_k(vel2d_march_group<TY, XC>, dim3(n_blocks), dim3(TY), 0, s, a, m, w);
-  if (g->beta) launch_k(prs2d_march_group<TY, XC, true>, dim3(n_blocks), dim3(TY), 0, s, a, m, w);
-  else launch_k(prs2d_march_group<TY, XC, false>, dim3(n_blocks), dim3(TY), 0, s, a, m, w);
+  if (g->stream) group_launch_march_t<TY, XC, true>(g, n_blocks, s);
+  else group_launch_march_t<TY, XC, false>(g, n_blocks, s);
 }
 
 void group_launch_step(fw_group* g, int n_tiles, cudaStream_t s) {
@@ -1561,7 +1632,7 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
   });
   std::vector<StepArgs> args(n);
   std::vector<int4> tiles;
-  std::vector<CUtensorMap> maps;
+  std::vector<March2Maps> maps;
   g->members = m;
   g->tiles_upto.assign(1, 0);
   g->beta = false;
@@ -1581,12 +1652,10 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
       const int nbx = (int)(h->nx - 2 * kGhost + xc - 1) / xc;
       for (int bx = 0; bx < nbx; ++bx)
         for (int by = 0; by < nby; ++by) tiles.push_back(make_int4(r, by, bx, bx == 0 && by == 0));
-      CUtensorMap tm[3];
-      if (encode_row_map(h, &tm[0], h->args.f.p, ty_ + 16) ||
-          encode_row_map(h, &tm[1], h->args.f.v[0], ty_ + 8) ||
-          encode_row_map(h, &tm[2], h->args.f.v[1], ty_ + 16))
-        return fail(nullptr, FW_ERR_CUDA, "row tensor map of member %d: %s", r, h->err.c_str());
-      maps.insert(maps.end(), tm, tm + 3);
+      March2Maps tm{};
+      if (encode_march2_maps(h, (uint32_t)ty_, &tm))
+        return fail(nullptr, FW_ERR_CUDA, "row tensor maps of member %d: %s", r, h->err.c_str());
+      maps.push_back(tm);
     }
     g->tiles_upto.push_back((int)tiles.size());
   }
@@ -1603,7 +1672,7 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
     g->tiles_cap = std::max<size_t>(tiles.size(), 2 * g->tiles_cap);
     if (cudaMalloc(&g->d_args, sizeof(StepArgs) * g->args_cap) != cudaSuccess ||
         cudaMalloc(&g->d_tiles, sizeof(int4) * g->tiles_cap) != cudaSuccess ||
-        cudaMalloc(&g->d_maps, sizeof(CUtensorMap) * 3 * g->args_cap) != cudaSuccess) {
+        cudaMalloc(&g->d_maps, sizeof(March2Maps) * g->args_cap) != cudaSuccess) {
       g->args_cap = g->tiles_cap = 0;
       return fail(nullptr, FW_ERR_OOM, "group device allocation failed");
     }
@@ -1614,7 +1683,7 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
   FW_CUDA(nullptr, cudaMemcpyAsync(g->d_tiles, tiles.data(), sizeof(int4) * tiles.size(),
                                    cudaMemcpyHostToDevice, g->capture_stream));
   if (!maps.empty())
-    FW_CUDA(nullptr, cudaMemcpyAsync(g->d_maps, maps.data(), sizeof(CUtensorMap) * maps.size(),
+    FW_CUDA(nullptr, cudaMemcpyAsync(g->d_maps, maps.data(), sizeof(March2Maps) * maps.size(),
                                      cudaMemcpyHostToDevice, g->capture_stream));
   FW_CUDA(nullptr, cudaStreamSynchronize(g->capture_stream));
   return FW_OK;
@@ -1716,6 +1785,8 @@ int fw_group_create(fw_handle* const* handles, int32_t n, fw_group** out) {
     const char* v = std::getenv("FWGB_VARIANT");
     const char* sh = std::getenv("FWGB_SHAPE2D");
     const char* a = std::getenv("FWGB_AUTOTUNE");
+    const char* s2 = std::getenv("FWGB_STREAM2D");
+    g->stream = !(s2 && std::strcmp(s2, "0") == 0);
     g->shape = 4;
     if (v && std::strcmp(v, "direct") == 0) {
       g->shape = 0;

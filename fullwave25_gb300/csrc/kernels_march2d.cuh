@@ -39,19 +39,44 @@ struct Row2 {
   static constexpr int kNarrowSlot = (kNarrow * 4 + 127) / 128 * 32;
 };
 
+// Tensor maps of one 2D simulation for the row-march kernels: the three halo-row maps, then the
+// point-wise maps of the streaming bodies (isotropic engine): 3D boxes {TY, 1, F} over the state
+// and map allocations (fields stacked on the third axis) and the tap-index map.
 struct March2Maps {
-  CUtensorMap p, vx, vy;
+  CUtensorMap p, vx, vy;        // halo rows
+  CUtensorMap vst, vmp;         // velocity: v_x v_y psi_x1 psi_x2 psi_y1 psi_y2 | rdt_rho .. bu2
+  CUtensorMap pp, phi;          // pressure: p | phi_x1 phi_x2 phi_y1 phi_y2
+  CUtensorMap pmp6, pmp7;       // pressure maps dt_k .. bx2 (+ beta2dt)
+  CUtensorMap dc;               // int32 tap index
 };
+constexpr int kMarch2Maps = sizeof(March2Maps) / sizeof(CUtensorMap);   // 10
+
+// Point-wise field counts of the streaming 2D bodies and their first fields in the stacks.
+constexpr int kV2StateF = 6, kV2MapF = 6, kP2PhiF = 4;
+constexpr int kState2V0 = 1, kState2Phi0 = 7;
+
+__device__ __forceinline__ void tma_load_3d_row(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                                int y, int x, int f) {
+  tma_load_3d(dst, map, bar, y, x, f);
+}
 
 // Bodies take the block's y block (by) and x chunk (bx) explicitly and the tensor maps by address
 // (kernel parameters or global memory), so that the single-simulation kernels and the group
 // kernels (block from a work list, one argument block and map set per simulation) share them.
-template <int TY, int XC, class CV>
-__device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const CUtensorMap* tm_p,
+// kStream (isotropic engine): the point-wise operands of a row come by TMA too — state, maps and
+// tap index of row x+1 are in flight (two-stage ring) while row x is computed; the cell update
+// is CellVelT's / CellPrsT's, so results stay bit-identical.
+template <int TY, int XC, class CV, bool kStream = false, int kMapSlotVel = 0>
+__device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const March2Maps* tm,
                                                  int by, int bx) {
   using R = Row2<TY>;
+  const CUtensorMap* tm_p = &tm->p;
   __shared__ alignas(128) float ring[kRing2][R::kWideSlot];
   __shared__ alignas(8) uint64_t bar[kRing2];
+  __shared__ alignas(128) float pst[kStream ? 2 : 1][kStream ? kV2StateF : 1][kStream ? TY : 1];
+  __shared__ alignas(128) float pmp[kStream ? 2 : 1][kStream ? kV2MapF : 1][kStream ? TY : 1];
+  __shared__ alignas(128) int pdc[kStream ? 2 : 1][kStream ? TY : 1];
+  __shared__ alignas(8) uint64_t pbar[2];
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tj = threadIdx.x;
@@ -62,15 +87,27 @@ __device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const CUtens
   const bool active = j < g.ny - kGhost;
   if (tj == 0) {
     for (int s = 0; s < kRing2; ++s) mbar_init(&bar[s], 1);
+    if constexpr (kStream) for (int s = 0; s < 2; ++s) mbar_init(&pbar[s], 1);
     fence_barrier_init();
   }
   __syncthreads();
   constexpr uint32_t kBytes = R::kWide * 4;
-  if (tj == 0)
+  constexpr uint32_t kPBytes = (kV2StateF + kV2MapF + 1) * TY * 4;
+  auto issue_pw = [&](int slot, int x) {
+    if constexpr (kStream) {
+      mbar_arrive_expect_tx(&pbar[slot], kPBytes);
+      tma_load_3d_row(pst[slot], &tm->vst, &pbar[slot], y0, x, kState2V0);
+      tma_load_3d_row(pmp[slot], &tm->vmp, &pbar[slot], y0, x, kMapSlotVel);
+      tma_load_2d(pdc[slot], &tm->dc, &pbar[slot], y0, x);
+    }
+  };
+  if (tj == 0) {
     for (int s = 0; s < 3; ++s) {
       mbar_arrive_expect_tx(&bar[s], kBytes);
       tma_load_2d(ring[s], tm_p, &bar[s], y0 - 8, xb - 1 + s);
     }
+    issue_pw(0, xb);
+  }
   const int64_t sx = g.sx;
   const float* __restrict__ p = A.f.p;
   float q[16];  // q[t] = p[x - 7 + t]
@@ -81,20 +118,43 @@ __device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const CUtens
     const int it = x - xb;
     const int64_t c = (int64_t)x * sx + j;
     CV cv;
-    if (active) cv.load(A, c);
+    if constexpr (!kStream) {
+      if (active) cv.load(A, c);
+    }
     const float qn = (active && x + 9 < g.nx) ? __ldg(p + (int64_t)(x + 9) * sx + j) : 0.f;
-    __syncthreads();
+    __syncthreads();  // the halo slot of row x-2 and the point-wise slot of row x-1 are free
     if (tj == 0 && x + 1 < xe) {
       const int s = (it + 3) % kRing2;
       fence_proxy_async_smem();
       mbar_arrive_expect_tx(&bar[s], kBytes);
       tma_load_2d(ring[s], tm_p, &bar[s], y0 - 8, x + 2);
+      issue_pw((it + 1) & 1, x + 1);
     }
     if (it == 0) {
       mbar_wait_bounded(&bar[0], 0, status);
       mbar_wait_bounded(&bar[1], 0, status);
     }
     mbar_wait_bounded(&bar[(it + 2) % kRing2], ((it + 2) / kRing2) & 1, status);
+    if constexpr (kStream) {
+      const int ps = it & 1;
+      mbar_wait_bounded(&pbar[ps], (it >> 1) & 1, status);
+      if (active) {
+        static_assert(!kStream || CV::NA == 1, "streaming bodies: isotropic engine only");
+        cv.dc = pdc[ps][tj];
+        cv.rr = pmp[ps][0][tj];
+        cv.iku[0] = pmp[ps][1][tj];
+        cv.a1[0] = pmp[ps][2][tj];
+        cv.b1[0] = pmp[ps][3][tj];
+        cv.a2[0] = pmp[ps][4][tj];
+        cv.b2[0] = pmp[ps][5][tj];
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+          cv.v[a] = pst[ps][a][tj];
+          cv.s1[a] = pst[ps][2 + 2 * a][tj];
+          cv.s2[a] = pst[ps][3 + 2 * a][tj];
+        }
+      }
+    }
     const float* Rm = ring[it % kRing2];
     const float* R0 = ring[(it + 1) % kRing2];
     const float* R1 = ring[(it + 2) % kRing2];
@@ -118,14 +178,23 @@ __device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const CUtens
   }
 }
 
-template <int TY, int XC, class CP>
-__device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const CUtensorMap* tm_vx,
-                                                 const CUtensorMap* tm_vy, int by, int bx) {
+template <int TY, int XC, class CP, bool kStream = false, bool kBeta = false,
+          int kMapSlotPrs = 0>
+__device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const March2Maps* tm,
+                                                 int by, int bx) {
   static_assert(TY % kD2TY == 0 && XC % kD2TX == 0, "a march block must own whole list tiles");
   using R = Row2<TY>;
+  constexpr int kMapF = kV2MapF + (kBeta ? 1 : 0);
+  const CUtensorMap* tm_vx = &tm->vx;
+  const CUtensorMap* tm_vy = &tm->vy;
   __shared__ alignas(128) float rx[kRing2][R::kNarrowSlot];
   __shared__ alignas(128) float ry[kRing2][R::kWideSlot];
   __shared__ alignas(8) uint64_t bar[kRing2];
+  __shared__ alignas(128) float ppp[kStream ? 2 : 1][kStream ? TY : 1];
+  __shared__ alignas(128) float pph[kStream ? 2 : 1][kStream ? kP2PhiF : 1][kStream ? TY : 1];
+  __shared__ alignas(128) float pmp[kStream ? 2 : 1][kStream ? kMapF : 1][kStream ? TY : 1];
+  __shared__ alignas(128) int pdc[kStream ? 2 : 1][kStream ? TY : 1];
+  __shared__ alignas(8) uint64_t pbar[2];
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tj = threadIdx.x;
@@ -136,17 +205,30 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const CUtens
   const bool active = j < g.ny - kGhost;
   if (tj == 0) {
     for (int s = 0; s < kRing2; ++s) mbar_init(&bar[s], 1);
+    if constexpr (kStream) for (int s = 0; s < 2; ++s) mbar_init(&pbar[s], 1);
     fence_barrier_init();
   }
   __syncthreads();
   constexpr uint32_t kBytes = (R::kNarrow + R::kWide) * 4;
+  constexpr uint32_t kPBytes = (1 + kP2PhiF + kMapF + 1) * TY * 4;
   auto issue = [&](int s, int x) {
     mbar_arrive_expect_tx(&bar[s], kBytes);
     tma_load_2d(rx[s], tm_vx, &bar[s], y0 - 4, x);
     tma_load_2d(ry[s], tm_vy, &bar[s], y0 - 8, x);
   };
-  if (tj == 0)
+  auto issue_pw = [&](int slot, int x) {
+    if constexpr (kStream) {
+      mbar_arrive_expect_tx(&pbar[slot], kPBytes);
+      tma_load_3d_row(ppp[slot], &tm->pp, &pbar[slot], y0, x, 0);
+      tma_load_3d_row(pph[slot], &tm->phi, &pbar[slot], y0, x, kState2Phi0);
+      tma_load_3d_row(pmp[slot], kBeta ? &tm->pmp7 : &tm->pmp6, &pbar[slot], y0, x, kMapSlotPrs);
+      tma_load_2d(pdc[slot], &tm->dc, &pbar[slot], y0, x);
+    }
+  };
+  if (tj == 0) {
     for (int s = 0; s < 3; ++s) issue(s, xb - 1 + s);
+    issue_pw(0, xb);
+  }
   const int64_t sx = g.sx;
   const float* __restrict__ vx = A.f.v[0];
   float* p = A.f.p;
@@ -158,18 +240,42 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const CUtens
     const int it = x - xb;
     const int64_t c = (int64_t)x * sx + j;
     CP cp;
-    if (active) cp.load(A, c);
+    if constexpr (!kStream) {
+      if (active) cp.load(A, c);
+    }
     const float rn = active ? __ldg(vx + (int64_t)(x + 8) * sx + j) : 0.f;
     __syncthreads();
     if (tj == 0 && x + 1 < xe) {
       fence_proxy_async_smem();
       issue((it + 3) % kRing2, x + 2);
+      issue_pw((it + 1) & 1, x + 1);
     }
     if (it == 0) {
       mbar_wait_bounded(&bar[0], 0, status);
       mbar_wait_bounded(&bar[1], 0, status);
     }
     mbar_wait_bounded(&bar[(it + 2) % kRing2], ((it + 2) / kRing2) & 1, status);
+    if constexpr (kStream) {
+      const int ps = it & 1;
+      mbar_wait_bounded(&pbar[ps], (it >> 1) & 1, status);
+      if (active) {
+        static_assert(!kStream || CP::NA == 1, "streaming bodies: isotropic engine only");
+        cp.dc = pdc[ps][tj];
+        cp.dtk = pmp[ps][0][tj];
+        cp.ikx[0] = pmp[ps][1][tj];
+        cp.a1[0] = pmp[ps][2][tj];
+        cp.b1[0] = pmp[ps][3][tj];
+        cp.a2[0] = pmp[ps][4][tj];
+        cp.b2[0] = pmp[ps][5][tj];
+        cp.b2dt = kBeta ? pmp[ps][kMapF - 1][tj] : 0.f;
+        cp.pc = ppp[ps][tj];
+#pragma unroll
+        for (int a = 0; a < 2; ++a) {
+          cp.f1[a] = pph[ps][2 * a][tj];
+          cp.f2[a] = pph[ps][2 * a + 1][tj];
+        }
+      }
+    }
     const float* Xm = rx[it % kRing2];
     const float* X0 = rx[(it + 1) % kRing2];
     const float* Ym = ry[it % kRing2];
@@ -201,27 +307,26 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const CUtens
                 tj, TY);
 }
 
-// Single simulation: grid (y blocks, x chunks).
-template <int TY, int XC, class CV>
-__global__ void __launch_bounds__(TY)
-vel2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
+// Single simulation: grid (y blocks, x chunks); the tensor maps travel as one kernel parameter.
+template <int TY, int XC, class CV, bool kStream = false, int kMapSlotVel = 0>
+__global__ void __launch_bounds__(TY, 1024 / TY)
+vel2d_march(const StepArgs A, const __grid_constant__ March2Maps tm) {
   pdl_entry();
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *A.step += 1;
-  vel2d_march_body<TY, XC, CV>(A, &tm_p, blockIdx.x, blockIdx.y);
+  vel2d_march_body<TY, XC, CV, kStream, kMapSlotVel>(A, &tm, blockIdx.x, blockIdx.y);
 }
 
-template <int TY, int XC, class CP>
-__global__ void __launch_bounds__(TY)
-prs2d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
-            const __grid_constant__ CUtensorMap tm_vy) {
+template <int TY, int XC, class CP, bool kStream = false, bool kBeta = false, int kMapSlotPrs = 0>
+__global__ void __launch_bounds__(TY, 1024 / TY)
+prs2d_march(const StepArgs A, const __grid_constant__ March2Maps tm) {
   pdl_entry();
-  prs2d_march_body<TY, XC, CP>(A, &tm_vx, &tm_vy, blockIdx.x, blockIdx.y);
+  prs2d_march_body<TY, XC, CP, kStream, kBeta, kMapSlotPrs>(A, &tm, blockIdx.x, blockIdx.y);
 }
 
 // Group (batched) kernels: block b works on work[b] = {simulation, y block, x chunk, 1 if the
 // block advances that simulation's step counter}. `sims` holds one argument block per simulation
-// and `maps` three row tensor maps (p, vx, vy) per simulation, in global memory. The argument
-// block is copied to shared memory first: stores to the fields then cannot alias it.
+// and `maps` one March2Maps per simulation, in global memory. The argument block is copied to
+// shared memory first: stores to the fields then cannot alias it.
 __device__ __forceinline__ void stage_args(StepArgs& dst, const StepArgs& src) {
   static_assert(sizeof(StepArgs) % 4 == 0, "word copy");
   const int* s = reinterpret_cast<const int*>(&src);
@@ -230,28 +335,28 @@ __device__ __forceinline__ void stage_args(StepArgs& dst, const StepArgs& src) {
   __syncthreads();
 }
 
-template <int TY, int XC>
-__global__ void __launch_bounds__(TY)
-vel2d_march_group(const StepArgs* __restrict__ sims, const CUtensorMap* __restrict__ maps,
+template <int TY, int XC, bool kStream = false, int kMapSlotVel = 0>
+__global__ void __launch_bounds__(TY, 1024 / TY)
+vel2d_march_group(const StepArgs* __restrict__ sims, const March2Maps* __restrict__ maps,
                   const int4* __restrict__ work) {
   __shared__ alignas(16) StepArgs A;
   pdl_entry();
   const int4 t = work[blockIdx.x];
   stage_args(A, sims[t.x]);
   if (t.w && threadIdx.x == 0) *A.step += 1;
-  vel2d_march_body<TY, XC, CellVelT<2, false>>(A, maps + 3 * t.x, t.y, t.z);
+  vel2d_march_body<TY, XC, CellVelT<2, false>, kStream, kMapSlotVel>(A, maps + t.x, t.y, t.z);
 }
 
-template <int TY, int XC, bool kBeta>
-__global__ void __launch_bounds__(TY)
-prs2d_march_group(const StepArgs* __restrict__ sims, const CUtensorMap* __restrict__ maps,
+template <int TY, int XC, bool kBeta, bool kStream = false, int kMapSlotPrs = 0>
+__global__ void __launch_bounds__(TY, 1024 / TY)
+prs2d_march_group(const StepArgs* __restrict__ sims, const March2Maps* __restrict__ maps,
                   const int4* __restrict__ work) {
   __shared__ alignas(16) StepArgs A;
   pdl_entry();
   const int4 t = work[blockIdx.x];
   stage_args(A, sims[t.x]);
-  prs2d_march_body<TY, XC, CellPrsT<2, kBeta, false>>(A, maps + 3 * t.x + 1, maps + 3 * t.x + 2,
-                                                       t.y, t.z);
+  prs2d_march_body<TY, XC, CellPrsT<2, kBeta, false>, kStream, kBeta, kMapSlotPrs>(
+      A, maps + t.x, t.y, t.z);
 }
 
 }  // namespace fwgb

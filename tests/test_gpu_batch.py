@@ -64,7 +64,7 @@ def _group(engines, **env):
 
     from fullwave25_gb300.engine import EngineGroup
 
-    keys = ("FWGB_VARIANT", "FWGB_SHAPE2D", "FWGB_AUTOTUNE")
+    keys = ("FWGB_VARIANT", "FWGB_SHAPE2D", "FWGB_AUTOTUNE", "FWGB_STREAM2D")
     old = {k: os.environ.get(k) for k in keys}
     for k in keys:
         os.environ.pop(k, None)
@@ -95,6 +95,17 @@ def test_group_every_kernel_shape_equals_alone(engine_lib, cuda, instances, shap
     alone = [e.run() for e in engines]
     with _group(engines, FWGB_SHAPE2D=shape) as grp:
         assert grp.block_tile == SHAPE_TILES[shape]
+        grp.run()
+        for a, t in zip(alone, grp.traces()):
+            np.testing.assert_array_equal(a, t)
+    for e in engines:
+        e.close()
+
+
+def test_group_register_loads_equal_streaming(engine_lib, cuda, instances):
+    engines = [d.make_engine() for d in instances[:4]]
+    alone = [e.run() for e in engines]
+    with _group(engines, FWGB_SHAPE2D=1, FWGB_STREAM2D=0) as grp:
         grp.run()
         for a, t in zip(alone, grp.traces()):
             np.testing.assert_array_equal(a, t)

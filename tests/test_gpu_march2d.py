@@ -23,7 +23,7 @@ VARIANT = {1: "march", 2: "march", 3: "march", 4: "march", 5: "march", 6: "persi
 def _engine(inp, **env):
     from fullwave25_gb300.engine import Engine
 
-    keys = ("FWGB_VARIANT", "FWGB_SHAPE2D", "FWGB_AUTOTUNE")
+    keys = ("FWGB_VARIANT", "FWGB_SHAPE2D", "FWGB_AUTOTUNE", "FWGB_STREAM2D")
     old = {k: os.environ.get(k) for k in keys}
     for k in keys:
         os.environ.pop(k, None)
@@ -87,6 +87,16 @@ def test_scattered_sources_air_sensors_every_shape(engine_lib, cuda, ragged_2d):
         # air cells are zero after the final step
         z = ragged_2d.icczero
         assert not pf[z[:, 0], z[:, 1]].any()
+
+
+@pytest.mark.parametrize("case", ["ragged", "2d_air_beta"])
+def test_register_and_streaming_row_march_equal(engine_lib, cuda, case, ragged_2d):
+    """Row march with point-wise operands loaded by the threads (FWGB_STREAM2D=0) and staged by
+    TMA (default for the isotropic engine): bitwise equal, every march shape."""
+    inp = ragged_2d if case == "ragged" else load_case_inputs(case)
+    for k in (1, 2, 3, 4, 5):
+        with _engine(inp, FWGB_SHAPE2D=k) as es, _engine(inp, FWGB_SHAPE2D=k, FWGB_STREAM2D=0) as er:
+            np.testing.assert_array_equal(es.run(), er.run(), err_msg=f"{case}: shape {k}")
 
 
 def test_persistent_kernel_in_uneven_advances(engine_lib, cuda, ragged_2d):
