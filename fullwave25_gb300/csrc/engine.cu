@@ -1444,9 +1444,14 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     A.g32[q] = h->adj_lam + (size_t)(15 + q) * fs;
   }
   A.ndmap = h->d.ndmap;
-  // the tap table goes to shared memory when it fits the default 48 KB of dynamic shared memory
+  // the tap table goes to shared memory when it fits next to the tiled kernels' static tiles
+  // (11 KB) within the default 48 KB per block (up to 682 tap sets)
   const size_t tap_bytes = (size_t)h->d.ndmap * kTapStride * sizeof(float);
-  const bool smem_taps = tap_bytes <= 48 * 1024;
+  const bool smem_taps = tap_bytes <= 32 * 1024;
+  // FWGB_ADJ_FUSED=0: the five-launch reverse step (assemble, record, projections, pressure,
+  // velocity) instead of the two tiled launches
+  const char* fenv = std::getenv("FWGB_ADJ_FUSED");
+  const bool fused = !(fenv && std::strcmp(fenv, "0") == 0);
   const size_t sm = smem_taps ? tap_bytes : 0;
   // FWGB_ADJ_F64_STEPS=1: form and add every step's contributions in FP64 (slow on GB300's FP64
   // pipe; kept to validate the default segmented FP32-partial / FP64-total accumulation)
@@ -1481,6 +1486,22 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     for (int n = n1 - 1; n >= n0; --n) {
       A.Sn = h->adj_store + state_elems * (n - n0);
       A.Sn1 = h->adj_store + state_elems * (n - n0 + 1);
+      if (fused) {
+        if (f64_steps && smem_taps) {
+          adj2d_prs_fused<true, true><<<grid, block, sm, s>>>(A, L, residual, n);
+          adj2d_vel_tiled<true, true><<<grid, block, sm, s>>>(A);
+        } else if (f64_steps) {
+          adj2d_prs_fused<true, false><<<grid, block, 0, s>>>(A, L, residual, n);
+          adj2d_vel_tiled<true, false><<<grid, block, 0, s>>>(A);
+        } else if (smem_taps) {
+          adj2d_prs_fused<false, true><<<grid, block, sm, s>>>(A, L, residual, n);
+          adj2d_vel_tiled<false, true><<<grid, block, sm, s>>>(A);
+        } else {
+          adj2d_prs_fused<false, false><<<grid, block, 0, s>>>(A, L, residual, n);
+          adj2d_vel_tiled<false, false><<<grid, block, 0, s>>>(A);
+        }
+        continue;
+      }
       if (!first) {
         if (smem_taps) adj2d_assemble<true><<<grid, block, sm, s>>>(A);
         else adj2d_assemble<false><<<grid, block, 0, s>>>(A);

@@ -195,16 +195,13 @@ __global__ void adj2d_zero(const AdjArgs A, const Lists L, int n, int n_src, int
 // pipe is the bottleneck then); otherwise contributions are formed in FP32 (the precision of the
 // adjoint fields themselves) and summed per checkpoint segment in FP32 partials, which
 // adj2d_merge adds into the FP64 time sums at the end of every segment.
+// Pressure adjoint of body cell c, given its assembled lam_p.
 template <bool kF64, bool kS>
-__global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
+__device__ __forceinline__ void adj_prs_cell(const AdjArgs& A, const TapSrc<kS>& T, int64_t c,
+                                             const float lp) {
   using acc_t = typename std::conditional<kF64, double, float>::type;
-  extern __shared__ float s_taps[];
-  const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
-  int64_t c;
-  if (!adj_cell(A.g, &c)) return;
   const Grid& g = A.g;
   const int64_t fs = A.fs;
-  const float lp = A.lam_p[c];
   const float k = __ldg(A.m.dt_k + c), ikx = __ldg(A.m.inv_kx[0] + c);
   const float ax[2] = {__ldg(A.m.ax[0][0] + c), __ldg(A.m.ax[0][1] + c)};
   const float bx[2] = {__ldg(A.m.bx[0][0] + c), __ldg(A.m.bx[0][1] + c)};
@@ -247,12 +244,19 @@ __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
 }
 
 template <bool kF64, bool kS>
-__global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
-  using acc_t = typename std::conditional<kF64, double, float>::type;
+__global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
   extern __shared__ float s_taps[];
   const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
   int64_t c;
   if (!adj_cell(A.g, &c)) return;
+  adj_prs_cell<kF64, kS>(A, T, c, A.lam_p[c]);
+}
+
+// Velocity adjoint of body cell c, given (D'_a^T lam_d_a)(c) for both axes.
+template <bool kF64, bool kS>
+__device__ __forceinline__ void adj_vel_cell(const AdjArgs& A, const TapSrc<kS>& T, int64_t c,
+                                             const float (&dT)[2]) {
+  using acc_t = typename std::conditional<kF64, double, float>::type;
   const Grid& g = A.g;
   const int64_t fs = A.fs;
   const float r = __ldg(A.m.rdt_rho + c), iku = __ldg(A.m.inv_ku[0] + c);
@@ -262,7 +266,7 @@ __global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
   const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
 #pragma unroll
   for (int a = 0; a < 2; ++a) {
-    const float lv = A.lam_v[a][c] + div_T_at(A.m, T, A.lam_d[a], c, se[a], sf[a], g.inv_h[a]);
+    const float lv = A.lam_v[a][c] + dT[a];
     const float gr = grad_at(A.m, T, S_p(A.Sn, fs), c, se[a], sf[a], g.inv_h[a]);
     const float p1 = __ldg(S_psi(A.Sn1, fs, a, 0) + c), p2 = __ldg(S_psi(A.Sn1, fs, a, 1) + c);
     float lam_g = -r * iku * lv;
@@ -294,6 +298,166 @@ __global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
     A.g32[kGBu1][c] += g_bu[0];
     A.g32[kGBu2][c] += g_bu[1];
   }
+}
+
+template <bool kF64, bool kS>
+__global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
+  extern __shared__ float s_taps[];
+  const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
+  int64_t c;
+  if (!adj_cell(A.g, &c)) return;
+  const Grid& g = A.g;
+  const float dT[2] = {div_T_at(A.m, T, A.lam_d[0], c, g.sx, 1, g.inv_h[0]),
+                       div_T_at(A.m, T, A.lam_d[1], c, 1, g.sx, g.inv_h[1])};
+  adj_vel_cell<kF64, kS>(A, T, c, dT);
+}
+
+// ---- tiled reverse step: the transposed stencils read shared-memory tiles ----------------------
+// Block = one 32 (y) x 8 (x) tile of body cells (the list tiles), origin (i0, j0). Fields are
+// staged with the halo the transposed stencils need (zero / tap index 0 outside the array: the
+// adjoint fields are zero there, so those terms vanish).
+template <int R, int C, class Tv>
+__device__ __forceinline__ void stage_tile(Tv (&dst)[R][C], const Tv* src, const Grid& g,
+                                           int row0, int col0, int tid) {
+  for (int e = tid; e < R * C; e += kD2TY * kD2TX) {
+    const int r = e / C, cc = e % C;
+    const int gr = row0 + r, gc = col0 + cc;
+    dst[r][cc] = (gr >= 0 && gr < g.nx && gc >= 0 && gc < (int)g.sx) ? src[(int64_t)gr * g.sx + gc]
+                                                                      : Tv(0);
+  }
+}
+
+// Assemble + record adjoint + projections + pressure adjoint in one launch: lam_p of the tile's
+// cells is assembled from the staged lam_g tiles (same operation order as adj2d_assemble), the
+// tile's sensor residuals are added and its air / source cells zeroed in shared memory (same
+// order as adj2d_io, adj2d_zero), then the pressure adjoint runs on it. Ghost-cell list entries
+// (sensors or sources placed in the ghost layer) are skipped: their lam_p is never read.
+template <bool kF64, bool kS>
+__global__ void __launch_bounds__(256) adj2d_prs_fused(const AdjArgs A, const Lists L,
+                                                       const float* residual, int n) {
+  extern __shared__ float s_taps[];
+  __shared__ float GX[23][34], GY[10][47], LP[kD2TX][kD2TY];
+  __shared__ int DC[23][47];
+  const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
+  const Grid& g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kD2TY + tx;
+  const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
+  stage_tile(GX, A.lam_g[0], g, i0 - 8, j0 - 1, tid);
+  stage_tile(GY, A.lam_g[1], g, i0 - 1, j0 - 8, tid);
+  stage_tile(DC, A.m.dcmap, g, i0 - 8, j0 - 8, tid);
+  __syncthreads();
+  const int i = i0 + ty, j = j0 + tx;
+  const bool active = i < g.nx - kGhost && j < g.ny - kGhost;
+  const int64_t c = (int64_t)i * g.sx + j;
+  if (active) {
+    // (D_x^T lam_g_x)(c): se = one row, sf = one column (grad_T_at)
+    float ax = 0.f;
+#pragma unroll
+    for (int k = 1; k <= 8; ++k) {
+      const int r1 = ty - k + 8, r2 = ty + k - 1 + 8, cu = tx + 1, cd = tx + 8;
+      ax += T.tap(DC[r1][cd], k - 1) * GX[r1][cu] - T.tap(DC[r2][cd], k - 1) * GX[r2][cu];
+    }
+#pragma unroll
+    for (int s = -1; s <= 1; s += 2) {
+      ax += T.tap(DC[ty + 7][tx + 8 - s], 8) * GX[ty + 7][tx + 1 - s] -
+            T.tap(DC[ty + 8][tx + 8 - s], 8) * GX[ty + 8][tx + 1 - s];
+    }
+    ax *= g.inv_h[0];
+    // (D_y^T lam_g_y)(c): se = one column, sf = one row
+    float ay = 0.f;
+#pragma unroll
+    for (int k = 1; k <= 8; ++k) {
+      ay += T.tap(DC[ty + 8][tx + 8 - k], k - 1) * GY[ty + 1][tx + 8 - k] -
+            T.tap(DC[ty + 8][tx + 7 + k], k - 1) * GY[ty + 1][tx + 7 + k];
+    }
+#pragma unroll
+    for (int s = -1; s <= 1; s += 2) {
+      ay += T.tap(DC[ty + 8 - s][tx + 7], 8) * GY[ty + 1 - s][tx + 7] -
+            T.tap(DC[ty + 8 - s][tx + 8], 8) * GY[ty + 1 - s][tx + 8];
+    }
+    ay *= g.inv_h[1];
+    const float add = ax + ay;
+    LP[ty][tx] = A.lam_p[c] + add;
+  }
+  __syncthreads();
+  const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+  auto local = [&](int64_t cell, int* li, int* lj) {
+    const int ci = (int)(cell / g.sx), cj = (int)(cell % g.sx);
+    *li = ci - i0;
+    *lj = cj - j0;
+    return ci >= kGhost && ci < g.nx - kGhost && cj >= kGhost && cj < g.ny - kGhost &&
+           *li >= 0 && *li < kD2TX && *lj >= 0 && *lj < kD2TY;
+  };
+  if (n % L.mod_t == 0) {
+    const float* row = residual + (size_t)(n / L.mod_t) * L.ncoordsout;
+    for (int e = L.rec_ptr[tile] + tid; e < L.rec_ptr[tile + 1]; e += kD2TY * kD2TX) {
+      int li, lj;
+      if (local(L.rec_cell[e], &li, &lj)) atomicAdd(&LP[li][lj], row[L.rec_k[e]]);
+    }
+  }
+  __syncthreads();
+  for (int e = L.zero_ptr[tile] + tid; e < L.zero_ptr[tile + 1]; e += kD2TY * kD2TX) {
+    int li, lj;
+    if (local(L.zero_cell[e], &li, &lj)) LP[li][lj] = 0.f;
+  }
+  if (n < L.nt_ic) {
+    for (int e = L.src_ptr[tile] + tid; e < L.src_ptr[tile + 1]; e += kD2TY * kD2TX) {
+      int li, lj;
+      if (local(L.src_cell[e], &li, &lj)) LP[li][lj] = 0.f;
+    }
+  }
+  __syncthreads();
+  if (!active) return;
+  const float lp = LP[ty][tx];
+  A.lam_p[c] = lp;
+  adj_prs_cell<kF64, kS>(A, T, c, lp);
+}
+
+// Velocity adjoint with the transposed divergence read from staged lam_d tiles (div_T_at order).
+template <bool kF64, bool kS>
+__global__ void __launch_bounds__(256) adj2d_vel_tiled(const AdjArgs A) {
+  extern __shared__ float s_taps[];
+  __shared__ float DX[23][34], DY[10][47];
+  __shared__ int DC[23][47];
+  const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
+  const Grid& g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kD2TY + tx;
+  const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
+  stage_tile(DX, A.lam_d[0], g, i0 - 7, j0 - 1, tid);
+  stage_tile(DY, A.lam_d[1], g, i0 - 1, j0 - 7, tid);
+  stage_tile(DC, A.m.dcmap, g, i0 - 7, j0 - 7, tid);
+  __syncthreads();
+  const int i = i0 + ty, j = j0 + tx;
+  if (i >= g.nx - kGhost || j >= g.ny - kGhost) return;
+  const int64_t c = (int64_t)i * g.sx + j;
+  // (D'_x^T lam_d_x)(c): se = one row, sf = one column
+  float dx = 0.f;
+#pragma unroll
+  for (int k = 1; k <= 8; ++k) {
+    const int r1 = ty - k + 8, r2 = ty + k + 7;
+    dx += T.tap(DC[r1][tx + 7], k - 1) * DX[r1][tx + 1] - T.tap(DC[r2][tx + 7], k - 1) * DX[r2][tx + 1];
+  }
+#pragma unroll
+  for (int s = -1; s <= 1; s += 2) {
+    dx += T.tap(DC[ty + 7][tx + 7 - s], 8) * DX[ty + 7][tx + 1 - s] -
+          T.tap(DC[ty + 8][tx + 7 - s], 8) * DX[ty + 8][tx + 1 - s];
+  }
+  dx *= g.inv_h[0];
+  // (D'_y^T lam_d_y)(c): se = one column, sf = one row
+  float dy = 0.f;
+#pragma unroll
+  for (int k = 1; k <= 8; ++k) {
+    dy += T.tap(DC[ty + 7][tx + 8 - k], k - 1) * DY[ty + 1][tx + 8 - k] -
+          T.tap(DC[ty + 7][tx + 7 + k], k - 1) * DY[ty + 1][tx + 7 + k];
+  }
+#pragma unroll
+  for (int s = -1; s <= 1; s += 2) {
+    dy += T.tap(DC[ty + 7 - s][tx + 7], 8) * DY[ty + 1 - s][tx + 7] -
+          T.tap(DC[ty + 7 - s][tx + 8], 8) * DY[ty + 1 - s][tx + 8];
+  }
+  dy *= g.inv_h[1];
+  const float dT[2] = {dx, dy};
+  adj_vel_cell<kF64, kS>(A, T, c, dT);
 }
 
 // End of a segment: FP64 time sums += FP32 segment partials; partials reset (body cells).
