@@ -1345,6 +1345,27 @@ int fw_launches_per_step(const fw_handle* h, int32_t* n) {
   return FW_OK;
 }
 
+int fw_copy_state_rows(fw_handle* dst, int32_t dst_row0, const fw_handle* src, int32_t src_row0,
+                       int32_t n_rows, void* stream) {
+  if (!dst || !src) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  if (dst->ndim != src->ndim || dst->ny != src->ny || dst->nz != src->nz ||
+      dst->pitch != src->pitch)
+    return fail(dst, FW_ERR_ARGUMENT, "state rows copy between grids of different cross-section");
+  if (n_rows < 0 || dst_row0 < 0 || src_row0 < 0 || dst_row0 + n_rows > dst->nx ||
+      src_row0 + n_rows > src->nx)
+    return fail(dst, FW_ERR_ARGUMENT, "rows [%d, %d) <- [%d, %d) outside the grids (%lld, %lld)",
+                dst_row0, dst_row0 + n_rows, src_row0, src_row0 + n_rows, (long long)dst->nx,
+                (long long)src->nx);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const size_t row = (size_t)(dst->ndim == 2 ? dst->pitch : dst->ny * dst->pitch);
+  for (int f = 0; f < n_state(dst->ndim); ++f) {
+    float* d = state_field(dst, f) + row * dst_row0;
+    const float* sp = src->state + (size_t)f * src->ncells_padded + row * src_row0;
+    FW_CUDA(dst, cudaMemcpyAsync(d, sp, row * n_rows * sizeof(float), cudaMemcpyDeviceToDevice, s));
+  }
+  return FW_OK;
+}
+
 int fw_selftest_waits(int32_t status_out[2]) {
   if (!status_out) return fail(nullptr, FW_ERR_ARGUMENT, "status_out is NULL");
   int* st = nullptr;

@@ -24,7 +24,7 @@ EXPORTED = ("fw_abi_version", "fw_create", "fw_set_fields", "fw_set_fields_aniso
             "fw_set_source_signal",
             "fw_set_source_columns", "fw_set_sensor_groups", "fw_run",
             "fw_reset", "fw_advance", "fw_read_traces", "fw_trace_buffer", "fw_get_field",
-            "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_block_tile", "fw_selftest_waits",
+            "fw_current_step", "fw_device_bytes", "fw_kernel_variant", "fw_block_tile", "fw_selftest_waits", "fw_copy_state_rows",
             "fw_launches_per_step",
             "fw_destroy", "fw_adjoint_forward", "fw_adjoint_backward", "fw_group_create", "fw_group_run", "fw_group_set_members",
             "fw_group_advance", "fw_group_block_tile", "fw_group_destroy",
@@ -110,6 +110,7 @@ def load_library(path: Path | None = None) -> C.CDLL:
         "fw_kernel_variant": (C.c_int, [H, _IP]),
         "fw_block_tile": (C.c_int, [H, _IP]),
         "fw_selftest_waits": (C.c_int, [_IP]),
+        "fw_copy_state_rows": (C.c_int, [H, C.c_int32, H, C.c_int32, C.c_int32, vp]),
         "fw_launches_per_step": (C.c_int, [H, _IP]),
         "fw_destroy": (C.c_int, [H]),
         "fw_adjoint_forward": (C.c_int, [H, vp, C.c_int32]),
@@ -347,6 +348,13 @@ class Engine:
         v = C.c_int32()
         self._call("fw_kernel_variant", C.byref(v))
         return {0: "direct", 1: "march", 2: "persistent", 3: "stream"}[v.value]
+
+    def copy_state_rows_from(self, src: "Engine", src_row0: int, dst_row0: int, n_rows: int,
+                             stream: int | None = None) -> None:
+        """Copy ``n_rows`` depth rows of every state field from ``src`` (same cross-section)."""
+        st = self.lib.fw_copy_state_rows(self._h, int(dst_row0), src.handle, int(src_row0),
+                                         int(n_rows), C.c_void_p(stream or 0))
+        self._check("fw_copy_state_rows", st, self._h)
 
     @property
     def block_tile(self) -> tuple:

@@ -184,6 +184,15 @@ FWGB_API int fw_kernel_variant(const fw_handle *h, int32_t *variant);
  * reference. */
 FWGB_API int fw_block_tile(const fw_handle *h, int32_t tile[3]);
 
+/* Copy n_rows x-rows (depth rows) of every state field (p, velocities, memory variables) from
+ * src rows [src_row0, src_row0 + n_rows) to dst rows [dst_row0, ...), asynchronously on stream.
+ * The two grids must have the same cross-section (ny, nz). This is the halo exchange of a depth
+ * slab decomposition (fullwave25_gb300.slabs): the reference splits depth into per-GPU slabs
+ * inside its executables (README.md:249-261); here slabs of one simulation exchange their
+ * overlap rows every step through this call. */
+FWGB_API int fw_copy_state_rows(fw_handle *dst, int32_t dst_row0, const fw_handle *src,
+                                int32_t src_row0, int32_t n_rows, void *stream);
+
 /* Failure-detection self-test: runs a kernel that waits on an mbarrier nothing completes and a
  * one-block kernel at a grid barrier that counts two blocks; each wait gives up after its limit
  * (0.5 s, 1 s) and records it in a status word instead of hanging. status_out[0] = the mbarrier
