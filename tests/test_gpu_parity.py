@@ -207,3 +207,32 @@ def test_solver_whole_domain_recording_movie(engine_lib, cuda):
         eng.advance((n_out - 1) * mod + 1)   # the last recorded step is (n_out - 1) * mod
         np.testing.assert_array_equal(movie[-1], eng.get_field(0))
     assert np.abs(movie[-1]).max() > 0
+
+
+def test_plain_3d_full_size_determinism_scaling_shift(engine_lib, cuda):
+    """At the full plain 3D size (512^3 + PML = 656^3 cells), over the first 120 steps: bitwise
+    determinism, linearity in the source (x2 within 1e-6 relative L2) and exact time-shift
+    invariance (source delayed by 7 steps -> traces delayed by 7 steps, bitwise)."""
+    from fullwave25_gb300.workloads3d import plain_3d_device_inputs
+
+    d = plain_3d_device_inputs()
+    n = 120
+    icmat = d.icmat.cpu().numpy()
+    with d.make_engine() as eng:
+        def solve():
+            eng.reset()
+            eng.advance(n)
+            return eng.read_traces(0, n)
+
+        a = solve()
+        np.testing.assert_array_equal(solve(), a)
+        assert np.isfinite(a).all() and np.abs(a).max() > 0
+        eng.set_source_signal((icmat * np.float32(2.0)).astype(np.float32))
+        assert rel_l2(solve(), 2.0 * a) < 1e-6
+        shift = 7
+        sh = np.zeros_like(icmat)
+        sh[:, shift:] = icmat[:, :-shift]
+        eng.set_source_signal(sh)
+        b = solve()
+    np.testing.assert_array_equal(b[shift:], a[:-shift])
+    assert not b[:shift].any()
