@@ -16,7 +16,9 @@ from pathlib import Path
 PKG = Path(__file__).resolve().parent
 ROOT = PKG.parent
 LIB = PKG / "libfwgb.so"
-SOURCES = [PKG / "csrc" / "engine.cu", PKG / "csrc" / "noalloc.cu"]
+SOURCES = [PKG / "csrc" / f for f in ("engine.cu", "launch.cu", "group.cu", "adjoint.cu",
+                                       "noalloc.cu")]
+OBJDIR = PKG / "_build"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 
 
@@ -36,16 +38,28 @@ def needs_build() -> bool:
 
 
 def build(force: bool = False, verbose: bool = False) -> Path:
+    """Compile every translation unit in parallel (one nvcc process each), then link."""
     if not force and not needs_build():
         return LIB
-    cmd = [nvcc_path(), *ARCH, "-O3", "-lineinfo", "-std=c++17", "--shared",
-           "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
-           "-I", str(ROOT / "include"), "-o", str(LIB) + ".tmp",
-           *[str(s) for s in SOURCES]]
+    OBJDIR.mkdir(exist_ok=True)
+    common = [nvcc_path(), *ARCH, "-O3", "-lineinfo", "-std=c++17",
+              "-Xcompiler", "-fPIC", "-Xcompiler", "-fvisibility=hidden",
+              "-I", str(ROOT / "include")]
     if verbose:
-        cmd.insert(1, "-Xptxas=-v")
-        print(" ".join(cmd), file=sys.stderr)
-    subprocess.run(cmd, check=True)
+        common.insert(1, "-Xptxas=-v")
+    procs, objs = [], []
+    for src in SOURCES:
+        obj = OBJDIR / (src.stem + ".o")
+        cmd = [*common, "-c", str(src), "-o", str(obj)]
+        if verbose:
+            print(" ".join(cmd), file=sys.stderr)
+        procs.append((src, subprocess.Popen(cmd)))
+        objs.append(obj)
+    failed = [str(src) for src, p in procs if p.wait() != 0]
+    if failed:
+        raise subprocess.CalledProcessError(1, "nvcc " + " ".join(failed))
+    subprocess.run([nvcc_path(), *ARCH, "--shared", "-Xcompiler", "-fPIC", "-o",
+                    str(LIB) + ".tmp", *[str(o) for o in objs]], check=True)
     os.replace(str(LIB) + ".tmp", LIB)
     return LIB
 

@@ -1,0 +1,173 @@
+// Host side of the discrete adjoint (2D): checkpointed forward pass and the reverse pass with
+// per-segment recomputation (the C ABI's fw_adjoint_forward / fw_adjoint_backward).
+#include "engine_host.cuh"
+
+using namespace fwgbh;
+
+extern "C" {
+
+int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  if (h->ndim != 2) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint is implemented for 2D grids");
+  if (h->has_beta) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs beta = 0 everywhere");
+  if (h->aniso || h->exp)
+    return fail(h, FW_ERR_UNSUPPORTED, "the adjoint covers the isotropic relaxation engine");
+  if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called first");
+  if (checkpoint_every < 1) return fail(h, FW_ERR_ARGUMENT, "checkpoint_every must be >= 1");
+  const size_t state_elems = (size_t)h->ncells_padded * n_state(h->ndim);
+  const int nckpt = (h->d.nt + checkpoint_every - 1) / checkpoint_every;
+  if (checkpoint_every != h->adj_every || nckpt != h->adj_nckpt) {
+    void* bufs[] = {h->adj_ckpt, h->adj_store, h->adj_lam, h->adj_grad};
+    for (void* b : bufs)
+      if (b) cudaFree(b);
+    h->bytes -= h->adj_bytes;
+    h->adj_ckpt = h->adj_store = h->adj_lam = nullptr;
+    h->adj_grad = nullptr;
+    const size_t b_ckpt = state_elems * std::max(nckpt, 1) * sizeof(float);
+    const size_t b_store = state_elems * (checkpoint_every + 1) * sizeof(float);
+    // 15 adjoint fields and temporaries, then the FP32 per-segment gradient partials
+    const size_t b_lam = (size_t)h->ncells_padded * (15 + kNumGrad) * sizeof(float);
+    const size_t b_grad = (size_t)h->ncells_padded * kNumGrad * sizeof(double);
+    FW_CUDA(h, cudaMalloc(&h->adj_ckpt, b_ckpt));
+    FW_CUDA(h, cudaMalloc(&h->adj_store, b_store));
+    FW_CUDA(h, cudaMalloc(&h->adj_lam, b_lam));
+    FW_CUDA(h, cudaMalloc(&h->adj_grad, b_grad));
+    h->adj_bytes = b_ckpt + b_store + b_lam + b_grad;
+    h->bytes += h->adj_bytes;
+    h->adj_every = checkpoint_every;
+    h->adj_nckpt = nckpt;
+  }
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int st = fw_reset(h, stream);
+  if (st) return st;
+  for (int seg = 0; seg < nckpt; ++seg) {
+    FW_CUDA(h, cudaMemcpyAsync(h->adj_ckpt + state_elems * seg, h->state, state_elems * sizeof(float),
+                               cudaMemcpyDeviceToDevice, s));
+    const int n = std::min(checkpoint_every, h->d.nt - seg * checkpoint_every);
+    if ((st = fw_advance(h, stream, n))) return st;
+  }
+  return FW_OK;
+}
+
+int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, double* grad_out) {
+  if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
+  if (!h->adj_ckpt || h->host_step != h->d.nt)
+    return fail(h, FW_ERR_STATE, "fw_adjoint_forward must run (to nt) before fw_adjoint_backward");
+  if (!residual && h->d.ncoordsout) return fail(h, FW_ERR_ARGUMENT, "residual is NULL");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int64_t fs = h->ncells_padded;
+  const size_t state_elems = (size_t)fs * n_state(h->ndim);
+  FW_CUDA(h, cudaMemsetAsync(h->adj_lam, 0, (size_t)fs * (15 + kNumGrad) * sizeof(float), s));
+  FW_CUDA(h, cudaMemsetAsync(h->adj_grad, 0, (size_t)fs * kNumGrad * sizeof(double), s));
+  AdjArgs A{};
+  A.g = h->args.g;
+  A.m = h->args.m;
+  A.fs = fs;
+  A.lam_p = h->adj_lam;
+  for (int a = 0; a < 2; ++a) {
+    A.lam_v[a] = h->adj_lam + (1 + a) * fs;
+    for (int nu = 0; nu < 2; ++nu) {
+      A.lam_psi[a][nu] = h->adj_lam + (3 + 2 * a + nu) * fs;
+      A.lam_phi[a][nu] = h->adj_lam + (7 + 2 * a + nu) * fs;
+    }
+    A.lam_d[a] = h->adj_lam + (11 + a) * fs;
+    A.lam_g[a] = h->adj_lam + (13 + a) * fs;
+  }
+  for (int q = 0; q < kNumGrad; ++q) {
+    A.grad[q] = h->adj_grad + (size_t)q * fs;
+    A.g32[q] = h->adj_lam + (size_t)(15 + q) * fs;
+  }
+  A.ndmap = h->d.ndmap;
+  // the tap table goes to shared memory when it fits next to the tiled kernels' static tiles
+  // (11 KB) within the default 48 KB per block (up to 682 tap sets)
+  const size_t tap_bytes = (size_t)h->d.ndmap * kTapStride * sizeof(float);
+  const bool smem_taps = tap_bytes <= 32 * 1024;
+  // FWGB_ADJ_FUSED=0: the five-launch reverse step (assemble, record, projections, pressure,
+  // velocity) instead of the two tiled launches
+  const char* fenv = std::getenv("FWGB_ADJ_FUSED");
+  const bool fused = !(fenv && std::strcmp(fenv, "0") == 0);
+  const size_t sm = smem_taps ? tap_bytes : 0;
+  // FWGB_ADJ_F64_STEPS=1: form and add every step's contributions in FP64 (slow on GB300's FP64
+  // pipe; kept to validate the default segmented FP32-partial / FP64-total accumulation)
+  const char* f64env = std::getenv("FWGB_ADJ_F64_STEPS");
+  const bool f64_steps = f64env && std::strcmp(f64env, "1") == 0;
+  const Lists& L = h->args.l;
+  // list lengths: sources after de-duplication, air cells, sensors
+  int32_t counts[3] = {0, 0, 0};
+  {
+    const int nt_tiles = h->tiling.count();
+    FW_CUDA(h, cudaMemcpy(&counts[0], L.src_ptr + nt_tiles, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    FW_CUDA(h, cudaMemcpy(&counts[1], L.zero_ptr + nt_tiles, sizeof(int32_t), cudaMemcpyDeviceToHost));
+    FW_CUDA(h, cudaMemcpy(&counts[2], L.rec_ptr + nt_tiles, sizeof(int32_t), cudaMemcpyDeviceToHost));
+  }
+  const dim3 block(32, 8), grid((unsigned)((h->ny - 2 * kGhost + 31) / 32),
+                                (unsigned)((h->nx - 2 * kGhost + 7) / 8));
+  const int K = h->adj_every;
+  bool first = true;
+  for (int seg = h->adj_nckpt - 1; seg >= 0; --seg) {
+    const int n0 = seg * K, n1 = std::min(n0 + K, (int)h->d.nt);
+    // recompute the segment from its checkpoint, keeping every state
+    FW_CUDA(h, cudaMemcpyAsync(h->state, h->adj_ckpt + state_elems * seg, state_elems * sizeof(float),
+                               cudaMemcpyDeviceToDevice, s));
+    set_step_counter<<<1, 1, 0, s>>>(h->step, n0);
+    for (int n = n0; n < n1; ++n) {
+      FW_CUDA(h, cudaMemcpyAsync(h->adj_store + state_elems * (n - n0), h->state,
+                                 state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      launch_step(h, s);
+    }
+    FW_CUDA(h, cudaMemcpyAsync(h->adj_store + state_elems * (n1 - n0), h->state,
+                               state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    for (int n = n1 - 1; n >= n0; --n) {
+      A.Sn = h->adj_store + state_elems * (n - n0);
+      A.Sn1 = h->adj_store + state_elems * (n - n0 + 1);
+      if (fused) {
+        if (f64_steps && smem_taps) {
+          adj2d_prs_fused<true, true><<<grid, block, sm, s>>>(A, L, residual, n);
+          adj2d_vel_tiled<true, true><<<grid, block, sm, s>>>(A);
+        } else if (f64_steps) {
+          adj2d_prs_fused<true, false><<<grid, block, 0, s>>>(A, L, residual, n);
+          adj2d_vel_tiled<true, false><<<grid, block, 0, s>>>(A);
+        } else if (smem_taps) {
+          adj2d_prs_fused<false, true><<<grid, block, sm, s>>>(A, L, residual, n);
+          adj2d_vel_tiled<false, true><<<grid, block, sm, s>>>(A);
+        } else {
+          adj2d_prs_fused<false, false><<<grid, block, 0, s>>>(A, L, residual, n);
+          adj2d_vel_tiled<false, false><<<grid, block, 0, s>>>(A);
+        }
+        continue;
+      }
+      if (!first) {
+        if (smem_taps) adj2d_assemble<true><<<grid, block, sm, s>>>(A);
+        else adj2d_assemble<false><<<grid, block, 0, s>>>(A);
+      }
+      first = false;
+      if (counts[2]) adj2d_io<<<(counts[2] + 255) / 256, 256, 0, s>>>(A, L, residual, n, 0, 0, counts[2]);
+      if (counts[0] || counts[1])
+        adj2d_zero<<<(std::max(counts[0], counts[1]) + 255) / 256, 256, 0, s>>>(A, L, n, counts[0], counts[1]);
+      if (f64_steps && smem_taps) {
+        adj2d_prs<true, true><<<grid, block, sm, s>>>(A);
+        adj2d_vel<true, true><<<grid, block, sm, s>>>(A);
+      } else if (f64_steps) {
+        adj2d_prs<true, false><<<grid, block, 0, s>>>(A);
+        adj2d_vel<true, false><<<grid, block, 0, s>>>(A);
+      } else if (smem_taps) {
+        adj2d_prs<false, true><<<grid, block, sm, s>>>(A);
+        adj2d_vel<false, true><<<grid, block, sm, s>>>(A);
+      } else {
+        adj2d_prs<false, false><<<grid, block, 0, s>>>(A);
+        adj2d_vel<false, false><<<grid, block, 0, s>>>(A);
+      }
+    }
+    if (!f64_steps) adj2d_merge<<<grid, block, 0, s>>>(A);
+    FW_CUDA(h, cudaGetLastError());
+  }
+  if (grad_out) {
+    for (int q = 0; q < kNumGrad; ++q)
+      FW_CUDA(h, cudaMemcpy2DAsync(grad_out + (size_t)q * h->nx * h->ny, h->ny * sizeof(double),
+                                   A.grad[q], h->pitch * sizeof(double), h->ny * sizeof(double),
+                                   h->nx, cudaMemcpyDeviceToDevice, s));
+  }
+  return FW_OK;
+}
+
+}  // extern "C"

@@ -14,6 +14,7 @@
 #pragma once
 #include <type_traits>
 #include "engine_common.cuh"
+#include "kernels_direct.cuh"
 
 namespace fwgb {
 
@@ -173,7 +174,7 @@ __global__ void __launch_bounds__(256) adj2d_assemble(const AdjArgs A) {
 }
 
 // record adjoint and projections for step n
-__global__ void adj2d_io(const AdjArgs A, const Lists L, const float* residual, int n,
+static __global__ void adj2d_io(const AdjArgs A, const Lists L, const float* residual, int n,
                          int n_src, int n_zero, int n_rec) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
@@ -183,7 +184,7 @@ __global__ void adj2d_io(const AdjArgs A, const Lists L, const float* residual, 
   }
 }
 
-__global__ void adj2d_zero(const AdjArgs A, const Lists L, int n, int n_src, int n_zero) {
+static __global__ void adj2d_zero(const AdjArgs A, const Lists L, int n, int n_src, int n_zero) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   const int stride = gridDim.x * blockDim.x;
   for (int e = t; e < n_zero; e += stride) A.lam_p[L.zero_cell[e]] = 0.f;
@@ -461,7 +462,7 @@ __global__ void __launch_bounds__(256) adj2d_vel_tiled(const AdjArgs A) {
 }
 
 // End of a segment: FP64 time sums += FP32 segment partials; partials reset (body cells).
-__global__ void __launch_bounds__(256) adj2d_merge(const AdjArgs A) {
+static __global__ void __launch_bounds__(256) adj2d_merge(const AdjArgs A) {
   int64_t c;
   if (!adj_cell(A.g, &c)) return;
 #pragma unroll
@@ -471,6 +472,6 @@ __global__ void __launch_bounds__(256) adj2d_merge(const AdjArgs A) {
   }
 }
 
-__global__ void set_step_counter(int* step, int value) { *step = value; }
+static __global__ void set_step_counter(int* step, int value) { *step = value; }
 
 }  // namespace fwgb

@@ -101,7 +101,7 @@ __global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
 // within that simulation}; `sims` holds one argument block per simulation, each with its own step
 // counter, advanced by the block that owns the simulation's tile 0. One launch per phase advances
 // every listed simulation by one step; simulations may be at different steps.
-__global__ void __launch_bounds__(256) vel2d_group(const StepArgs* __restrict__ sims,
+static __global__ void __launch_bounds__(256) vel2d_group(const StepArgs* __restrict__ sims,
                                                    const int4* __restrict__ tiles) {
   pdl_entry();
   const int4 t = tiles[blockIdx.x];
