@@ -620,7 +620,8 @@ def run_adjoint(args):
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
     n = args.grid or 1024
-    nt = 6000 if n == 1024 else int(6000 * n / 1024)
+    nt = args.nt or (6000 if n == 1024 else int(6000 * n / 1024))
+    every = args.checkpoint_every
     dx = 1540 / 3e6 / 12
     c, rho, a0, gam = ellipse_medium_2d((n, n), dx, seed=0)
     sig = 2e-3 / dx
@@ -635,7 +636,7 @@ def run_adjoint(args):
 
     def evaluate():
         cc, rr, aa = [x.clone().requires_grad_(True) for x in start[:3]]
-        J = prob.misfit(cc, rr, aa, start[3], observed, checkpoint_every=200)
+        J = prob.misfit(cc, rr, aa, start[3], observed, checkpoint_every=every)
         J.backward()
         return float(J.detach()), cc.grad, rr.grad, aa.grad
 
@@ -657,7 +658,7 @@ def run_adjoint(args):
             "config": {"workload": f"adjoint gradient, {n}x{n} + PML 40 + transition 40 "
                                    f"({ext[0]}x{ext[1]}), nt {nt}, {observed.shape[1]}-sensor "
                                    "row, true medium vs Gaussian-blurred (sigma 2 mm) start, "
-                                   "gradient w.r.t. c, rho, alpha0, checkpoints every 200 steps",
+                                   f"gradient w.r.t. c, rho, alpha0, checkpoints every {every} steps",
                        "misfit": J,
                        "time_steps_per_evaluation": "3 nt (forward, recompute, adjoint)"},
             "equivalent_Gcell_updates_per_s": 3 * nt * cells / el / 1e9,
@@ -686,7 +687,12 @@ def main():
                     help="batch2d: instances also run one by one through the host-side API")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=0,
-                    help="3D workload edge in cells (default 512; smaller for profiling)")
+                    help="3D workload edge in cells (default 512; smaller for profiling); "
+                         "adjoint2d: grid edge (default 1024)")
+    ap.add_argument("--nt", type=int, default=0,
+                    help="adjoint2d: time steps (default 6000 at 1024, scaled with the grid)")
+    ap.add_argument("--checkpoint-every", type=int, default=200,
+                    help="adjoint2d: steps between wavefield checkpoints")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps requested; using 3", file=sys.stderr)

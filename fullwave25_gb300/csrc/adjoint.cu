@@ -4,6 +4,50 @@
 
 using namespace fwgbh;
 
+namespace {
+
+static_assert(kAdjMapVel == kMRdtRho && kAdjMapPrs == kMDtK, "map runs of the adjoint kernels");
+
+// Field of each gradient partial (AdjGrad order) in the adjoint allocation: coefficient-map order
+// after the adjoint fields, so each TMA kernel reads its six partials as one run.
+constexpr int kGradSlot[kNumGrad] = {kMRdtRho, kMDtK, kMInvKu, kMInvKx, kMAu1, kMBu1,
+                                     kMAu2,    kMBu2, kMAx1,   kMBx1,   kMAx2, kMBx2};
+
+// Tensor maps of the TMA reverse-step kernels over this handle's adjoint fields, coefficient
+// maps, state store (K + 1 slots) and tap-index map.
+int encode_adj_maps(fw_handle* h, AdjMaps* M) {
+  const cuuint64_t row = (cuuint64_t)h->pitch * 4, field = (cuuint64_t)h->ncells_padded * 4;
+  const cuuint64_t pitch = (cuuint64_t)h->pitch, nx = (cuuint64_t)h->nx;
+  const cuuint64_t d_lam[3] = {pitch, nx, (cuuint64_t)kAdjStack};
+  const cuuint64_t d_map[3] = {pitch, nx, (cuuint64_t)n_maps(h)};
+  const cuuint64_t s3[2] = {row, field};
+  const int ns = n_state(h->ndim);
+  const cuuint64_t d_st[4] = {pitch, nx, (cuuint64_t)ns, (cuuint64_t)h->adj_every + 1};
+  const cuuint64_t s4[3] = {row, field, field * ns};
+  const cuuint64_t d_dc[2] = {pitch, nx};
+  const cuuint32_t b1[3] = {kD2TY, kD2TX, 1}, b4[3] = {kD2TY, kD2TX, 4}, b6[3] = {kD2TY, kD2TX, 6};
+  const cuuint32_t bhx[3] = {kHXW, kHXR, 1}, bhy[3] = {kHYW, kHYR, 1};
+  const cuuint32_t bs4[4] = {kD2TY, kD2TX, 4, 1}, bsx[4] = {kHXW, kHXR, 1, 1};
+  const cuuint32_t bsy[4] = {kHYW, kHYR, 1, 1}, bsp[4] = {kHFW, kHFR, 1, 1};
+  const cuuint32_t bdc[2] = {kHFW, kHFR};
+  int st;
+  if ((st = encode_map(h, &M->lam1, h->adj_lam, 3, d_lam, s3, b1)) ||
+      (st = encode_map(h, &M->lam4, h->adj_lam, 3, d_lam, s3, b4)) ||
+      (st = encode_map(h, &M->lam6, h->adj_lam, 3, d_lam, s3, b6)) ||
+      (st = encode_map(h, &M->halo_x, h->adj_lam, 3, d_lam, s3, bhx)) ||
+      (st = encode_map(h, &M->halo_y, h->adj_lam, 3, d_lam, s3, bhy)) ||
+      (st = encode_map(h, &M->maps6, h->maps, 3, d_map, s3, b6)) ||
+      (st = encode_map(h, &M->st4, h->adj_store, 4, d_st, s4, bs4)) ||
+      (st = encode_map(h, &M->st_vx, h->adj_store, 4, d_st, s4, bsx)) ||
+      (st = encode_map(h, &M->st_vy, h->adj_store, 4, d_st, s4, bsy)) ||
+      (st = encode_map(h, &M->st_p, h->adj_store, 4, d_st, s4, bsp)) ||
+      (st = encode_map(h, &M->dc, h->dcmap, 2, d_dc, s3, bdc, CU_TENSOR_MAP_DATA_TYPE_INT32)))
+    return st;
+  return FW_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
@@ -26,10 +70,12 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
     const size_t b_ckpt = state_elems * std::max(nckpt, 1) * sizeof(float);
     const size_t b_store = state_elems * (checkpoint_every + 1) * sizeof(float);
     // 15 adjoint fields and temporaries, then the FP32 per-segment gradient partials
-    const size_t b_lam = (size_t)h->ncells_padded * (15 + kNumGrad) * sizeof(float);
+    const size_t b_lam = (size_t)h->ncells_padded * kAdjStack * sizeof(float);
     const size_t b_grad = (size_t)h->ncells_padded * kNumGrad * sizeof(double);
     FW_CUDA(h, cudaMalloc(&h->adj_ckpt, b_ckpt));
     FW_CUDA(h, cudaMalloc(&h->adj_store, b_store));
+    // the out-of-place recomputation never writes the ghost layer of a stored state: keep it zero
+    FW_CUDA(h, cudaMemset(h->adj_store, 0, b_store));
     FW_CUDA(h, cudaMalloc(&h->adj_lam, b_lam));
     FW_CUDA(h, cudaMalloc(&h->adj_grad, b_grad));
     h->adj_bytes = b_ckpt + b_store + b_lam + b_grad;
@@ -57,7 +103,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int64_t fs = h->ncells_padded;
   const size_t state_elems = (size_t)fs * n_state(h->ndim);
-  FW_CUDA(h, cudaMemsetAsync(h->adj_lam, 0, (size_t)fs * (15 + kNumGrad) * sizeof(float), s));
+  FW_CUDA(h, cudaMemsetAsync(h->adj_lam, 0, (size_t)fs * kAdjStack * sizeof(float), s));
   FW_CUDA(h, cudaMemsetAsync(h->adj_grad, 0, (size_t)fs * kNumGrad * sizeof(double), s));
   AdjArgs A{};
   A.g = h->args.g;
@@ -65,19 +111,20 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   A.fs = fs;
   A.lam_p = h->adj_lam;
   for (int a = 0; a < 2; ++a) {
-    A.lam_v[a] = h->adj_lam + (1 + a) * fs;
+    A.lam_v[a] = h->adj_lam + (kAdjLamV + a) * fs;
     for (int nu = 0; nu < 2; ++nu) {
-      A.lam_psi[a][nu] = h->adj_lam + (3 + 2 * a + nu) * fs;
-      A.lam_phi[a][nu] = h->adj_lam + (7 + 2 * a + nu) * fs;
+      A.lam_psi[a][nu] = h->adj_lam + (kAdjLamPsi + 2 * a + nu) * fs;
+      A.lam_phi[a][nu] = h->adj_lam + (kAdjLamPhi + 2 * a + nu) * fs;
     }
-    A.lam_d[a] = h->adj_lam + (11 + a) * fs;
-    A.lam_g[a] = h->adj_lam + (13 + a) * fs;
+    A.lam_d[a] = h->adj_lam + (kAdjLamD + a) * fs;
+    A.lam_g[a] = h->adj_lam + (kAdjLamG + a) * fs;
   }
   for (int q = 0; q < kNumGrad; ++q) {
     A.grad[q] = h->adj_grad + (size_t)q * fs;
-    A.g32[q] = h->adj_lam + (size_t)(15 + q) * fs;
+    A.g32[q] = h->adj_lam + (size_t)(kAdjFields + kGradSlot[q]) * fs;
   }
   A.ndmap = h->d.ndmap;
+  A.status = h->step + 1;
   // the tap table goes to shared memory when it fits next to the tiled kernels' static tiles
   // (11 KB) within the default 48 KB per block (up to 682 tap sets)
   const size_t tap_bytes = (size_t)h->d.ndmap * kTapStride * sizeof(float);
@@ -91,6 +138,30 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   // pipe; kept to validate the default segmented FP32-partial / FP64-total accumulation)
   const char* f64env = std::getenv("FWGB_ADJ_F64_STEPS");
   const bool f64_steps = f64env && std::strcmp(f64env, "1") == 0;
+  // Default reverse step: the TMA-staged kernels (FP32 partials; the tap table goes to shared
+  // memory with the tiles when it fits the per-block limit). FWGB_ADJ_TMA=0: the tiled kernels.
+  const char* tenv = std::getenv("FWGB_ADJ_TMA");
+  int dev = 0, smem_optin = 0;
+  FW_CUDA(h, cudaGetDevice(&dev));
+  FW_CUDA(h, cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+  const size_t smem_prs = adj_prs_tma_smem(h->d.ndmap), smem_vel = adj_vel_tma_smem(h->d.ndmap);
+  const bool tma = fused && !f64_steps && !(tenv && std::strcmp(tenv, "0") == 0) &&
+                   std::max(smem_prs, smem_vel) <= (size_t)smem_optin;
+  // Recomputation: out of place from one stored state into the next (the direct step kernels
+  // reading slot n and writing slot n + 1), unless pressure is written in the ghost layer (it
+  // persists there in place) or FWGB_ADJ_OOP=0: then a copy of the state into the store before
+  // each in-place step.
+  const char* oenv = std::getenv("FWGB_ADJ_OOP");
+  const bool oop = !h->ghost_writes && !(oenv && std::strcmp(oenv, "0") == 0);
+  AdjMaps M{};
+  if (tma) {
+    int st = encode_adj_maps(h, &M);
+    if (st) return st;
+    FW_CUDA(h, cudaFuncSetAttribute(adj2d_prs_tma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem_prs));
+    FW_CUDA(h, cudaFuncSetAttribute(adj2d_vel_tma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smem_vel));
+  }
   const Lists& L = h->args.l;
   // list lengths: sources after de-duplication, air cells, sensors
   int32_t counts[3] = {0, 0, 0};
@@ -107,19 +178,39 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   for (int seg = h->adj_nckpt - 1; seg >= 0; --seg) {
     const int n0 = seg * K, n1 = std::min(n0 + K, (int)h->d.nt);
     // recompute the segment from its checkpoint, keeping every state
-    FW_CUDA(h, cudaMemcpyAsync(h->state, h->adj_ckpt + state_elems * seg, state_elems * sizeof(float),
-                               cudaMemcpyDeviceToDevice, s));
     set_step_counter<<<1, 1, 0, s>>>(h->step, n0);
-    for (int n = n0; n < n1; ++n) {
-      FW_CUDA(h, cudaMemcpyAsync(h->adj_store + state_elems * (n - n0), h->state,
+    if (oop) {
+      FW_CUDA(h, cudaMemcpyAsync(h->adj_store, h->adj_ckpt + state_elems * seg,
                                  state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
-      launch_step(h, s);
+      StepArgs in = h->args, out = h->args;
+      for (int n = n0; n < n1; ++n) {
+        set_state_pointers(h, &in, h->adj_store + state_elems * (n - n0));
+        set_state_pointers(h, &out, h->adj_store + state_elems * (n - n0 + 1));
+        vel2d_direct_oop<CellVelT<2, false>><<<grid, block, 0, s>>>(in, out);
+        prs2d_direct_oop<CellPrsT<2, false>><<<grid, block, 0, s>>>(in, out);
+      }
+      if (seg == 0)   // leave the first segment's recomputation in the handle, as in place
+        FW_CUDA(h, cudaMemcpyAsync(h->state, h->adj_store + state_elems * (n1 - n0),
+                                   state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    } else {
+      FW_CUDA(h, cudaMemcpyAsync(h->state, h->adj_ckpt + state_elems * seg,
+                                 state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      for (int n = n0; n < n1; ++n) {
+        FW_CUDA(h, cudaMemcpyAsync(h->adj_store + state_elems * (n - n0), h->state,
+                                   state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
+        launch_step(h, s);
+      }
+      FW_CUDA(h, cudaMemcpyAsync(h->adj_store + state_elems * (n1 - n0), h->state,
+                                 state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
     }
-    FW_CUDA(h, cudaMemcpyAsync(h->adj_store + state_elems * (n1 - n0), h->state,
-                               state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
     for (int n = n1 - 1; n >= n0; --n) {
       A.Sn = h->adj_store + state_elems * (n - n0);
       A.Sn1 = h->adj_store + state_elems * (n - n0 + 1);
+      if (tma) {
+        adj2d_prs_tma<0><<<grid, block, smem_prs, s>>>(A, L, residual, n, n - n0, M);
+        adj2d_vel_tma<0><<<grid, block, smem_vel, s>>>(A, n - n0, M);
+        continue;
+      }
       if (fused) {
         if (f64_steps && smem_taps) {
           adj2d_prs_fused<true, true><<<grid, block, sm, s>>>(A, L, residual, n);
@@ -167,7 +258,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
                                    A.grad[q], h->pitch * sizeof(double), h->ny * sizeof(double),
                                    h->nx, cudaMemcpyDeviceToDevice, s));
   }
-  return FW_OK;
+  return check_device_status(h, s);
 }
 
 }  // extern "C"

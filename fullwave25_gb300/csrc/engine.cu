@@ -257,13 +257,7 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   A.g.inv_h[0] = 1.f / desc->dx;
   A.g.inv_h[1] = 1.f / desc->dy;
   A.g.inv_h[2] = h->ndim == 3 ? 1.f / desc->dz : 0.f;
-  int s = 0;
-  A.f.p = state_field(h, s++);
-  for (int a = 0; a < 3; ++a) A.f.v[a] = a < h->ndim ? state_field(h, s++) : nullptr;
-  for (int a = 0; a < 3; ++a)
-    for (int nu = 0; nu < 2; ++nu) A.f.psi[a][nu] = a < h->ndim ? state_field(h, s++) : nullptr;
-  for (int a = 0; a < 3; ++a)
-    for (int nu = 0; nu < 2; ++nu) A.f.phi[a][nu] = a < h->ndim ? state_field(h, s++) : nullptr;
+  set_state_pointers(h, &A, h->state);
   A.m.rdt_rho = map_field(h, kMRdtRho);
   A.m.dt_k = map_field(h, kMDtK);
   A.m.beta2dt = map_field(h, kMBeta2dt);
@@ -432,6 +426,15 @@ int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an,
       (st = build(zero, d.ncoordszero, "icczero", true, ez)) ||
       (st = build(outc, d.ncoordsout, "outc", false, eo)))
     return st;
+  // pressure written in the ghost layer (sources or air cells there): it then persists across
+  // steps, which the out-of-place adjoint recomputation does not carry over
+  auto in_ghost = [&](const std::vector<int32_t>& v, int n) {
+    for (int e = 0; e < n; ++e)
+      for (int a = 0; a < nd; ++a)
+        if (v[(size_t)e * nd + a] < kGhost || v[(size_t)e * nd + a] >= ext[a] - kGhost) return true;
+    return false;
+  };
+  h->ghost_writes = in_ghost(icc, d.ncoords) || in_ghost(zero, d.ncoordszero);
   // layout: src_ptr, zero_ptr, rec_ptr (int32, ntiles+1 each), src_k, rec_k (int32),
   //         then src_cell, zero_cell, rec_cell (int64, 8-byte aligned)
   const size_t n_i32 = 3 * (size_t)(ntiles + 1) + es.size() + eo.size();
@@ -706,6 +709,7 @@ int autotune_2d(fw_handle* h, cudaStream_t s) {
   int st = FW_OK, best = 0;
   float best_ms = 0.f;
   for (int k = 0; k < kNumShapes2D && st == FW_OK; ++k) {
+    if (kShapes2D[k].tile && (h->aniso || h->exp)) continue;   // runs the direct kernels
     float ms = 0.f;
     if ((st = set_shape2d(h, k))) break;
     if (kShapes2D[k].persistent) {

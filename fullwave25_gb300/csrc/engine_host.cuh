@@ -26,6 +26,7 @@
 #include "kernels_march3d.cuh"
 #include "kernels_persistent2d.cuh"
 #include "kernels_stream3d.cuh"
+#include "kernels_tile2d.cuh"
 
 using namespace fwgb;
 
@@ -37,16 +38,20 @@ constexpr int kStreamXC = 32;  // x planes per block of the streaming 3D march (
 // 2D kernel shapes the autotuner chooses from: 0 = direct kernels (one block per 32 y x 8 x tile),
 // 1-5 = row-march kernels with TY threads (y columns) walking XC rows (TY + 16 <= 256, the TMA box
 // limit; TY a multiple of 32 and XC of 8, whole list tiles per block), 6 = the persistent kernel
-// (direct bodies, one cooperative launch per block of steps, grid barriers between phases).
-struct Shape2D { int ty, xc; bool persistent; };
-constexpr Shape2D kShapes2D[] = {{0, 0, false},   {64, 16, false},  {64, 32, false},
-                                 {128, 16, false}, {128, 32, false}, {128, 64, false},
-                                 {0, 0, true}};
+// (direct bodies, one cooperative launch per block of steps, grid barriers between phases),
+// 7 = the TMA tile kernels (isotropic engine; one 32 x 8 tile per block, every operand staged by
+// TMA; the other engines run the direct kernels for it).
+struct Shape2D { int ty, xc; bool persistent, tile; };
+constexpr Shape2D kShapes2D[] = {{0, 0, false, false},   {64, 16, false, false},
+                                 {64, 32, false, false},  {128, 16, false, false},
+                                 {128, 32, false, false}, {128, 64, false, false},
+                                 {0, 0, true, false},     {0, 0, false, true}};
 constexpr int kPersistentShape = 6;
+constexpr int kTileShape = 7;
 constexpr int kNumShapes2D = sizeof(kShapes2D) / sizeof(kShapes2D[0]);
 constexpr int kTuneSteps = 64;   // time steps per autotuning trial (one graph)
 
-enum Variant { kDirect = 0, kMarch = 1, kPersistent = 2, kStream = 3 };
+enum Variant { kDirect = 0, kMarch = 1, kPersistent = 2, kStream = 3, kTile = 4 };
 
 struct Tiling {
   int t[3];   // tile extent along x, y, z (z unused in 2D)
@@ -78,6 +83,7 @@ struct fw_handle {
   int32_t n_cols = 0;          // trace row length: ncoordsout, or n_groups with sensor groups
   size_t bytes = 0;
   bool has_beta = false, fields_set = false;
+  bool ghost_writes = false;   // a source or air cell lies in the ghost layer (p written there)
   bool aniso = false;          // per-axis relaxation maps (the anisotropic engine)
   bool exp = false;            // exponential-attenuation engine (n_relax = 0, map a_exp)
   int n_out = 0;
@@ -92,6 +98,7 @@ struct fw_handle {
   bool shape_fixed = false;    // 2D shape forced (FWGB_SHAPE2D / FWGB_VARIANT) or already tuned
   fwgb::MarchMaps tmaps{};
   fwgb::March2Maps tmaps2{};
+  fwgb::Tile2Maps tmaps_t{};   // TMA tile kernels (2D isotropic)
   bool stream2d = false;       // 2D isotropic row march: point-wise operands staged by TMA too
   fwgb::StreamMaps smaps{};
   bool stream3d = false;       // 3D isotropic: point-wise operands staged by TMA too
@@ -139,6 +146,17 @@ constexpr int kMaps = 13;
 inline int n_maps(const fw_handle* h) { return kMaps + (h->aniso ? 10 * (h->ndim - 1) : 0); }
 inline int axis_map(int a, int k) { return kMaps + 10 * (a - 1) + k; }
 inline float* state_field(fw_handle* h, int idx) { return h->state + (size_t)idx * h->ncells_padded; }
+// Point the state-field pointers of A at a state laid out like h->state (state order) at base.
+inline void set_state_pointers(const fw_handle* h, fwgb::StepArgs* A, float* base) {
+  int s = 0;
+  auto field = [&]() { return base + (size_t)(s++) * h->ncells_padded; };
+  A->f.p = field();
+  for (int a = 0; a < 3; ++a) A->f.v[a] = a < h->ndim ? field() : nullptr;
+  for (int a = 0; a < 3; ++a)
+    for (int nu = 0; nu < 2; ++nu) A->f.psi[a][nu] = a < h->ndim ? field() : nullptr;
+  for (int a = 0; a < 3; ++a)
+    for (int nu = 0; nu < 2; ++nu) A->f.phi[a][nu] = a < h->ndim ? field() : nullptr;
+}
 inline float* map_field(fw_handle* h, int idx) { return h->maps + (size_t)idx * h->ncells_padded; }
 
 // Time-step kernels are launched with programmatic dependent launch (FWGB_PDL=0 turns it off):
@@ -169,6 +187,10 @@ void launch_k(void (*kernel)(KArgs...), dim3 grid, dim3 block, size_t smem, cuda
 }
 
 // launch.cu
+// Tiled tensor map of `rank` dimensions (innermost first; strides in bytes of dims 1..rank-1).
+int encode_map(fw_handle* h, CUtensorMap* map, void* base, cuuint32_t rank,
+               const cuuint64_t* dims, const cuuint64_t* strides, const cuuint32_t* box,
+               CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_FLOAT32);
 void launch_step(fw_handle* h, cudaStream_t s);
 int launch_persistent(fw_handle* h, cudaStream_t s, int n0, int n_steps);
 int build_graph(fw_handle* h, int steps);

@@ -44,7 +44,7 @@ void group_launch_march(fw_group* g, int n_blocks, cudaStream_t s) {
 }
 
 void group_launch_step(fw_group* g, int n_tiles, cudaStream_t s) {
-  static_assert(kNumShapes2D == 7, "one case per 2D kernel shape");
+  static_assert(kNumShapes2D == 8, "one case per 2D kernel shape");
   switch (g->shape) {
     case 0: {
       const dim3 block(kD2TY, kD2TX);
@@ -60,7 +60,7 @@ void group_launch_step(fw_group* g, int n_tiles, cudaStream_t s) {
     case 3: group_launch_march<128, 16>(g, n_tiles, s); break;
     case 4: group_launch_march<128, 32>(g, n_tiles, s); break;
     case 5: group_launch_march<128, 64>(g, n_tiles, s); break;
-    default: break;  // no persistent group kernel: group shapes are 0-5
+    default: break;  // no persistent or tile group kernels: group shapes are 0-5
   }
 }
 
@@ -182,7 +182,7 @@ int group_autotune(fw_group* g, cudaStream_t s) {
   int st = FW_OK, best = 0;
   float best_ms = 0.f;
   for (int k = 0; k < kNumShapes2D && st == FW_OK; ++k) {
-    if (kShapes2D[k].persistent) continue;  // single-simulation kernel only
+    if (kShapes2D[k].persistent || kShapes2D[k].tile) continue;  // single-simulation kernels
     float ms = 0.f;
     if ((st = group_set_shape(g, k)) || (st = group_advance(g, s, kTuneSteps))) break;
     if (cudaEventRecord(e0, s) != cudaSuccess) { st = fail(nullptr, FW_ERR_CUDA, "event record failed"); break; }
@@ -265,7 +265,7 @@ int fw_group_create(fw_handle* const* handles, int32_t n, fw_group** out) {
         delete g;
         return fail(nullptr, FW_ERR_ARGUMENT, "FWGB_SHAPE2D=%s outside [0, %d)", sh, kNumShapes2D);
       }
-      g->shape = kShapes2D[k].persistent ? 0 : k;
+      g->shape = kShapes2D[k].persistent || kShapes2D[k].tile ? 0 : k;
       g->shape_fixed = true;
     } else if (a && std::strcmp(a, "0") == 0) {
       g->shape_fixed = true;

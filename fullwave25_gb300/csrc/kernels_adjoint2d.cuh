@@ -15,6 +15,7 @@
 #include <type_traits>
 #include "engine_common.cuh"
 #include "kernels_direct.cuh"
+#include "tma.cuh"
 
 namespace fwgb {
 
@@ -38,6 +39,7 @@ struct AdjArgs {
   int ndmap;                 // tap sets in m.taps
   double* grad[kNumGrad];    // FP64 time sums
   float* g32[kNumGrad];      // FP32 partial sums of the current segment (segmented mode)
+  int* status;               // device status word (bounded waits, alignment)
 };
 
 // state field indices (2D): p, vx, vy, psi[a][nu] = 3 + 2a + nu, phi[a][nu] = 7 + 2a + nu
@@ -473,5 +475,354 @@ static __global__ void __launch_bounds__(256) adj2d_merge(const AdjArgs A) {
 }
 
 static __global__ void set_step_counter(int* step, int value) { *step = value; }
+
+// ---- TMA-staged reverse step ------------------------------------------------------------------
+// Every operand of a block's 32 (y) x 8 (x) tile is brought into shared memory at block start by
+// one thread: TMA boxes over the adjoint-field stack, the coefficient-map stack, the two stored
+// states and the tap-index map, and a bulk copy of the tap table, all completing on one mbarrier
+// (bounded wait). A block thus has its whole input (about 42 KB) in flight at once instead of a
+// few dependent loads per thread, which is what limits the tiled kernels above (long-scoreboard
+// stalls at full occupancy, a fifth of the DRAM bandwidth). The arithmetic is that of
+// adj2d_prs_fused / adj2d_vel_tiled, term for term in the same order.
+//
+// The adjoint-field allocation holds, per padded cell array: lam_p, lam_v (2), lam_psi (4),
+// lam_phi (4), lam_d (2), lam_g (2), then the FP32 gradient partials in coefficient-map order
+// (velocity maps rdt_rho inv_ku au1 bu1 au2 bu2, pressure maps dt_k inv_kx ax1 bx1 ax2 bx2), so
+// that each kernel's point-wise operands are runs of consecutive fields.
+constexpr int kAdjFields = 15;                 // adjoint fields before the gradient partials
+constexpr int kAdjStack = kAdjFields + kNumGrad;
+constexpr int kAdjLamP = 0, kAdjLamV = 1, kAdjLamPsi = 3, kAdjLamPhi = 7, kAdjLamD = 11,
+              kAdjLamG = 13;
+constexpr int kAdjMapVel = 0, kAdjMapPrs = 6;  // first coefficient map of each kernel's run of 6
+constexpr int kStPsi = 3, kStPhi = 7;          // first psi / phi field of a stored 2D state
+
+struct AdjMaps {
+  CUtensorMap lam1, lam4, lam6;     // adjoint stack (pitch, nx, kAdjStack): boxes {32, 8, f}
+  CUtensorMap halo_x, halo_y;       // adjoint stack: boxes {40, 24, 1} and {48, 10, 1}
+  CUtensorMap maps6;                // coefficient-map stack: box {32, 8, 6}
+  CUtensorMap st4, st_vx, st_vy, st_p;  // stored states (pitch, nx, 11, slots): {32, 8, 4, 1},
+                                        // {40, 24, 1, 1}, {48, 10, 1, 1}, {48, 24, 1, 1}
+  CUtensorMap dc;                   // tap-index map (pitch, nx): box {48, 24}
+};
+
+// Halo tiles: x-halo boxes start at (i0 - 8, j0 - 4) (40 wide, 24 rows), y-halo boxes at
+// (i0 - 1, j0 - 8) (48 wide, 10 rows), full boxes at (i0 - 8, j0 - 8) (48 x 24). Box starts
+// along y are multiples of 4 floats (16 bytes): j0 = 8 + 32 blockIdx.x.
+constexpr int kHXW = 40, kHXR = 24, kHYW = 48, kHYR = 10, kHFW = 48, kHFR = 24;
+constexpr int kPrsPW = 25, kVelPW = 26;    // point-wise planes of each kernel
+
+struct AdjPrsSmem {
+  float gx[kHXR][kHXW];                 // lam_g_x
+  float gy[kHYR][kHYW];                 // lam_g_y
+  float vx[kHXR][kHXW];                 // v_x of S_{n+1}
+  float vy[kHYR][kHYW];                 // v_y of S_{n+1}
+  int dc[kHFR][kHFW];
+  // point-wise: 0 lam_p | 1-4 lam_phi | 5-10 dt_k inv_kx ax1 bx1 ax2 bx2 | 11-14 phi of S_n |
+  // 15-18 phi of S_{n+1} | 19-24 gradient partials of the pressure maps
+  float pw[kPrsPW][kD2TX][kD2TY];
+  float lp[kD2TX][kD2TY];
+  uint64_t bar;
+};
+struct AdjVelSmem {
+  float dx[kHXR][kHXW];                 // lam_d_x
+  float dy[kHYR][kHYW];                 // lam_d_y
+  float p[kHFR][kHFW];                  // p of S_n
+  int dc[kHFR][kHFW];
+  // point-wise: 0-1 lam_v | 2-5 lam_psi | 6-11 rdt_rho inv_ku au1 bu1 au2 bu2 | 12-15 psi of
+  // S_n | 16-19 psi of S_{n+1} | 20-25 gradient partials of the velocity maps
+  float pw[kVelPW][kD2TX][kD2TY];
+  uint64_t bar;
+};
+constexpr uint32_t kPrsTx = sizeof(float) * (2 * kHXR * kHXW + 2 * kHYR * kHYW + kHFR * kHFW +
+                                             kPrsPW * kD2TX * kD2TY);
+constexpr uint32_t kVelTx = sizeof(float) * (kHXR * kHXW + kHYR * kHYW + 2 * kHFR * kHFW +
+                                             kVelPW * kD2TX * kD2TY);
+__host__ __device__ constexpr size_t adj_tap_offset(size_t smem_struct) {
+  return (smem_struct + 127) / 128 * 128;
+}
+static_assert(offsetof(AdjPrsSmem, gy) % 128 == 0 && offsetof(AdjPrsSmem, vx) % 128 == 0 &&
+                  offsetof(AdjPrsSmem, vy) % 128 == 0 && offsetof(AdjPrsSmem, dc) % 128 == 0 &&
+                  offsetof(AdjPrsSmem, pw) % 128 == 0,
+              "TMA destinations must be 128-byte aligned");
+static_assert(offsetof(AdjVelSmem, dy) % 128 == 0 && offsetof(AdjVelSmem, p) % 128 == 0 &&
+                  offsetof(AdjVelSmem, dc) % 128 == 0 && offsetof(AdjVelSmem, pw) % 128 == 0,
+              "TMA destinations must be 128-byte aligned");
+
+// Shared-memory bytes of the TMA reverse-step kernels for a tap table of ndmap sets.
+inline size_t adj_prs_tma_smem(int ndmap) {
+  return adj_tap_offset(sizeof(AdjPrsSmem)) + (size_t)ndmap * kTapStride * sizeof(float);
+}
+inline size_t adj_vel_tma_smem(int ndmap) {
+  return adj_tap_offset(sizeof(AdjVelSmem)) + (size_t)ndmap * kTapStride * sizeof(float);
+}
+
+// Block prologue: alignment guard, barrier init, one thread issues the loads. Returns false when
+// the block must stop (misaligned shared memory: reported, nothing issued).
+template <class SmemT>
+__device__ __forceinline__ bool adj_tma_begin(SmemT& S, const unsigned char* base, int* status,
+                                              int tid, uint32_t tx_bytes) {
+  if (smem_u32(base) & 127u) {
+    if (tid == 0) atomicOr(status, kStatusAlign);
+    return false;
+  }
+  if (tid == 0) {
+    mbar_init(&S.bar, 1);
+    fence_barrier_init();
+    mbar_arrive_expect_tx(&S.bar, tx_bytes);
+  }
+  return true;
+}
+
+// Reverse step, launch 1 (adj2d_prs_fused with TMA-staged operands). `slot` = store slot of S_n.
+template <int kUnused = 0>
+__global__ void __launch_bounds__(256, 4) adj2d_prs_tma(const AdjArgs A, const Lists L,
+                                                        const float* residual, int n, int slot,
+                                                        const __grid_constant__ AdjMaps M) {
+  extern __shared__ __align__(128) unsigned char adj_smem[];
+  AdjPrsSmem& S = *reinterpret_cast<AdjPrsSmem*>(adj_smem);
+  float* taps = reinterpret_cast<float*>(adj_smem + adj_tap_offset(sizeof(AdjPrsSmem)));
+  const Grid& g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kD2TY + tx;
+  const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
+  const uint32_t tap_bytes = (uint32_t)A.ndmap * kTapStride * sizeof(float);
+  if (!adj_tma_begin(S, adj_smem, A.status, tid, kPrsTx + tap_bytes)) return;
+  if (tid == 0) {
+    tma_load_3d(S.gx, &M.halo_x, &S.bar, j0 - 4, i0 - 8, kAdjLamG);
+    tma_load_3d(S.gy, &M.halo_y, &S.bar, j0 - 8, i0 - 1, kAdjLamG + 1);
+    tma_load_4d(S.vx, &M.st_vx, &S.bar, j0 - 4, i0 - 8, 1, slot + 1);
+    tma_load_4d(S.vy, &M.st_vy, &S.bar, j0 - 8, i0 - 1, 2, slot + 1);
+    tma_load_2d(S.dc, &M.dc, &S.bar, j0 - 8, i0 - 8);
+    tma_load_3d(S.pw[0], &M.lam1, &S.bar, j0, i0, kAdjLamP);
+    tma_load_3d(S.pw[1], &M.lam4, &S.bar, j0, i0, kAdjLamPhi);
+    tma_load_3d(S.pw[5], &M.maps6, &S.bar, j0, i0, kAdjMapPrs);
+    tma_load_4d(S.pw[11], &M.st4, &S.bar, j0, i0, kStPhi, slot);
+    tma_load_4d(S.pw[15], &M.st4, &S.bar, j0, i0, kStPhi, slot + 1);
+    tma_load_3d(S.pw[19], &M.lam6, &S.bar, j0, i0, kAdjFields + kAdjMapPrs);
+    bulk_load(taps, A.m.taps, tap_bytes, &S.bar);
+  }
+  __syncthreads();   // barrier initialised before anyone polls it
+  mbar_wait_bounded(&S.bar, 0, A.status);
+  const TapSrc<true> T{taps};
+  const int i = i0 + ty, j = j0 + tx;
+  const bool active = i < g.nx - kGhost && j < g.ny - kGhost;
+  const int64_t c = (int64_t)i * g.sx + j;
+  if (active) {
+    // (D_x^T lam_g_x)(c)
+    float ax = 0.f;
+#pragma unroll
+    for (int k = 1; k <= 8; ++k) {
+      const int r1 = ty - k + 8, r2 = ty + k - 1 + 8, cu = tx + 4, cd = tx + 8;
+      ax += T.tap(S.dc[r1][cd], k - 1) * S.gx[r1][cu] - T.tap(S.dc[r2][cd], k - 1) * S.gx[r2][cu];
+    }
+#pragma unroll
+    for (int s = -1; s <= 1; s += 2) {
+      ax += T.tap(S.dc[ty + 7][tx + 8 - s], 8) * S.gx[ty + 7][tx + 4 - s] -
+            T.tap(S.dc[ty + 8][tx + 8 - s], 8) * S.gx[ty + 8][tx + 4 - s];
+    }
+    ax *= g.inv_h[0];
+    // (D_y^T lam_g_y)(c)
+    float ay = 0.f;
+#pragma unroll
+    for (int k = 1; k <= 8; ++k) {
+      ay += T.tap(S.dc[ty + 8][tx + 8 - k], k - 1) * S.gy[ty + 1][tx + 8 - k] -
+            T.tap(S.dc[ty + 8][tx + 7 + k], k - 1) * S.gy[ty + 1][tx + 7 + k];
+    }
+#pragma unroll
+    for (int s = -1; s <= 1; s += 2) {
+      ay += T.tap(S.dc[ty + 8 - s][tx + 7], 8) * S.gy[ty + 1 - s][tx + 7] -
+            T.tap(S.dc[ty + 8 - s][tx + 8], 8) * S.gy[ty + 1 - s][tx + 8];
+    }
+    ay *= g.inv_h[1];
+    const float add = ax + ay;
+    S.lp[ty][tx] = S.pw[0][ty][tx] + add;
+  }
+  __syncthreads();
+  const int tile = blockIdx.y * gridDim.x + blockIdx.x;
+  auto local = [&](int64_t cell, int* li, int* lj) {
+    const int ci = (int)(cell / g.sx), cj = (int)(cell % g.sx);
+    *li = ci - i0;
+    *lj = cj - j0;
+    return ci >= kGhost && ci < g.nx - kGhost && cj >= kGhost && cj < g.ny - kGhost &&
+           *li >= 0 && *li < kD2TX && *lj >= 0 && *lj < kD2TY;
+  };
+  if (n % L.mod_t == 0) {
+    const float* row = residual + (size_t)(n / L.mod_t) * L.ncoordsout;
+    for (int e = L.rec_ptr[tile] + tid; e < L.rec_ptr[tile + 1]; e += kD2TY * kD2TX) {
+      int li, lj;
+      if (local(L.rec_cell[e], &li, &lj)) atomicAdd(&S.lp[li][lj], row[L.rec_k[e]]);
+    }
+  }
+  __syncthreads();
+  for (int e = L.zero_ptr[tile] + tid; e < L.zero_ptr[tile + 1]; e += kD2TY * kD2TX) {
+    int li, lj;
+    if (local(L.zero_cell[e], &li, &lj)) S.lp[li][lj] = 0.f;
+  }
+  if (n < L.nt_ic) {
+    for (int e = L.src_ptr[tile] + tid; e < L.src_ptr[tile + 1]; e += kD2TY * kD2TX) {
+      int li, lj;
+      if (local(L.src_cell[e], &li, &lj)) S.lp[li][lj] = 0.f;
+    }
+  }
+  __syncthreads();
+  if (!active) return;
+  const float lp = S.lp[ty][tx];
+  A.lam_p[c] = lp;
+  // pressure adjoint (adj_prs_cell, FP32 contributions)
+  auto P = [&](int q) { return S.pw[q][ty][tx]; };
+  const float k = P(5), ikx = P(6);
+  const float axm[2] = {P(7), P(9)};
+  const float bxm[2] = {P(8), P(10)};
+  float g_dtk = 0, g_ikx = 0, g_ax[2] = {0, 0}, g_bx[2] = {0, 0};
+  float div = 0.f;
+  float cm[8], co;
+  T.load(S.dc[ty + 8][tx + 8], cm, co);
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    // D'_a v^{n+1/2} at c (div_at order)
+    float d = 0.f;
+    if (a == 0) {
+#pragma unroll
+      for (int kk = 1; kk <= 8; ++kk)
+        d = fmaf(cm[kk - 1], S.vx[ty + 8 + kk - 1][tx + 4] - S.vx[ty + 8 - kk][tx + 4], d);
+      d = fmaf(co, (S.vx[ty + 8][tx + 5] - S.vx[ty + 7][tx + 5]) +
+                       (S.vx[ty + 8][tx + 3] - S.vx[ty + 7][tx + 3]), d);
+    } else {
+#pragma unroll
+      for (int kk = 1; kk <= 8; ++kk)
+        d = fmaf(cm[kk - 1], S.vy[ty + 1][tx + 8 + kk - 1] - S.vy[ty + 1][tx + 8 - kk], d);
+      d = fmaf(co, (S.vy[ty + 2][tx + 8] - S.vy[ty + 2][tx + 7]) +
+                       (S.vy[ty][tx + 8] - S.vy[ty][tx + 7]), d);
+    }
+    d = d * g.inv_h[a];
+    const float n1 = P(15 + 2 * a), n2 = P(16 + 2 * a);
+    div += fmaf(d, ikx, n1) + n2;
+    float lam_d = -k * ikx * lp;
+#pragma unroll
+    for (int nu = 0; nu < 2; ++nu) {
+      const float Lv = P(1 + 2 * a + nu) - k * lp;
+      lam_d = fmaf(axm[nu], Lv, lam_d);
+      g_ax[nu] += Lv * d;
+      g_bx[nu] += Lv * P(11 + 2 * a + nu);
+      A.lam_phi[a][nu][c] = bxm[nu] * Lv;
+    }
+    g_ikx -= k * lp * d;
+    A.lam_d[a][c] = lam_d;
+  }
+  g_dtk -= div * lp;
+  A.g32[kGDtK][c] = P(19) + g_dtk;
+  A.g32[kGInvKx][c] = P(20) + g_ikx;
+  A.g32[kGAx1][c] = P(21) + g_ax[0];
+  A.g32[kGBx1][c] = P(22) + g_bx[0];
+  A.g32[kGAx2][c] = P(23) + g_ax[1];
+  A.g32[kGBx2][c] = P(24) + g_bx[1];
+}
+
+// Reverse step, launch 2 (adj2d_vel_tiled with TMA-staged operands).
+template <int kUnused = 0>
+__global__ void __launch_bounds__(256, 4) adj2d_vel_tma(const AdjArgs A, int slot,
+                                                        const __grid_constant__ AdjMaps M) {
+  extern __shared__ __align__(128) unsigned char adj_smem[];
+  AdjVelSmem& S = *reinterpret_cast<AdjVelSmem*>(adj_smem);
+  float* taps = reinterpret_cast<float*>(adj_smem + adj_tap_offset(sizeof(AdjVelSmem)));
+  const Grid& g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kD2TY + tx;
+  const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
+  const uint32_t tap_bytes = (uint32_t)A.ndmap * kTapStride * sizeof(float);
+  if (!adj_tma_begin(S, adj_smem, A.status, tid, kVelTx + tap_bytes)) return;
+  if (tid == 0) {
+    tma_load_3d(S.dx, &M.halo_x, &S.bar, j0 - 4, i0 - 8, kAdjLamD);
+    tma_load_3d(S.dy, &M.halo_y, &S.bar, j0 - 8, i0 - 1, kAdjLamD + 1);
+    tma_load_4d(S.p, &M.st_p, &S.bar, j0 - 8, i0 - 8, 0, slot);
+    tma_load_2d(S.dc, &M.dc, &S.bar, j0 - 8, i0 - 8);
+    tma_load_3d(S.pw[0], &M.lam6, &S.bar, j0, i0, kAdjLamV);
+    tma_load_3d(S.pw[6], &M.maps6, &S.bar, j0, i0, kAdjMapVel);
+    tma_load_4d(S.pw[12], &M.st4, &S.bar, j0, i0, kStPsi, slot);
+    tma_load_4d(S.pw[16], &M.st4, &S.bar, j0, i0, kStPsi, slot + 1);
+    tma_load_3d(S.pw[20], &M.lam6, &S.bar, j0, i0, kAdjFields + kAdjMapVel);
+    bulk_load(taps, A.m.taps, tap_bytes, &S.bar);
+  }
+  __syncthreads();
+  mbar_wait_bounded(&S.bar, 0, A.status);
+  const int i = i0 + ty, j = j0 + tx;
+  if (i >= g.nx - kGhost || j >= g.ny - kGhost) return;
+  const int64_t c = (int64_t)i * g.sx + j;
+  const TapSrc<true> T{taps};
+  // (D'_x^T lam_d_x)(c)
+  float dx = 0.f;
+#pragma unroll
+  for (int k = 1; k <= 8; ++k) {
+    const int r1 = ty - k + 9, r2 = ty + k + 8;
+    dx += T.tap(S.dc[r1][tx + 8], k - 1) * S.dx[r1][tx + 4] -
+          T.tap(S.dc[r2][tx + 8], k - 1) * S.dx[r2][tx + 4];
+  }
+#pragma unroll
+  for (int s = -1; s <= 1; s += 2) {
+    dx += T.tap(S.dc[ty + 8][tx + 8 - s], 8) * S.dx[ty + 8][tx + 4 - s] -
+          T.tap(S.dc[ty + 9][tx + 8 - s], 8) * S.dx[ty + 9][tx + 4 - s];
+  }
+  dx *= g.inv_h[0];
+  // (D'_y^T lam_d_y)(c)
+  float dy = 0.f;
+#pragma unroll
+  for (int k = 1; k <= 8; ++k) {
+    dy += T.tap(S.dc[ty + 8][tx + 9 - k], k - 1) * S.dy[ty + 1][tx + 9 - k] -
+          T.tap(S.dc[ty + 8][tx + 8 + k], k - 1) * S.dy[ty + 1][tx + 8 + k];
+  }
+#pragma unroll
+  for (int s = -1; s <= 1; s += 2) {
+    dy += T.tap(S.dc[ty + 8 - s][tx + 8], 8) * S.dy[ty + 1 - s][tx + 8] -
+          T.tap(S.dc[ty + 8 - s][tx + 9], 8) * S.dy[ty + 1 - s][tx + 9];
+  }
+  dy *= g.inv_h[1];
+  const float dT[2] = {dx, dy};
+  // velocity adjoint (adj_vel_cell, FP32 contributions)
+  auto P = [&](int q) { return S.pw[q][ty][tx]; };
+  const float r = P(6), iku = P(7);
+  const float aum[2] = {P(8), P(10)};
+  const float bum[2] = {P(9), P(11)};
+  float g_r = 0, g_iku = 0, g_au[2] = {0, 0}, g_bu[2] = {0, 0};
+  float cm[8], co;
+  T.load(S.dc[ty + 8][tx + 8], cm, co);
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    const float lv = P(a) + dT[a];
+    // D_a p^n at c (grad_at order)
+    float gr = 0.f;
+    if (a == 0) {
+#pragma unroll
+      for (int kk = 1; kk <= 8; ++kk)
+        gr = fmaf(cm[kk - 1], S.p[ty + 8 + kk][tx + 8] - S.p[ty + 9 - kk][tx + 8], gr);
+      gr = fmaf(co, (S.p[ty + 9][tx + 9] - S.p[ty + 8][tx + 9]) +
+                        (S.p[ty + 9][tx + 7] - S.p[ty + 8][tx + 7]), gr);
+    } else {
+#pragma unroll
+      for (int kk = 1; kk <= 8; ++kk)
+        gr = fmaf(cm[kk - 1], S.p[ty + 8][tx + 8 + kk] - S.p[ty + 8][tx + 9 - kk], gr);
+      gr = fmaf(co, (S.p[ty + 9][tx + 9] - S.p[ty + 9][tx + 8]) +
+                        (S.p[ty + 7][tx + 9] - S.p[ty + 7][tx + 8]), gr);
+    }
+    gr = gr * g.inv_h[a];
+    const float p1 = P(16 + 2 * a), p2 = P(17 + 2 * a);
+    float lam_g = -r * iku * lv;
+#pragma unroll
+    for (int nu = 0; nu < 2; ++nu) {
+      const float Mv = P(2 + 2 * a + nu) - r * lv;
+      lam_g = fmaf(aum[nu], Mv, lam_g);
+      g_au[nu] += Mv * gr;
+      g_bu[nu] += Mv * P(12 + 2 * a + nu);
+      A.lam_psi[a][nu][c] = bum[nu] * Mv;
+    }
+    g_r -= lv * (fmaf(gr, iku, p1) + p2);
+    g_iku -= r * gr * lv;
+    A.lam_v[a][c] = lv;
+    A.lam_g[a][c] = lam_g;
+  }
+  A.g32[kGRdtRho][c] = P(20) + g_r;
+  A.g32[kGInvKu][c] = P(21) + g_iku;
+  A.g32[kGAu1][c] = P(22) + g_au[0];
+  A.g32[kGBu1][c] = P(23) + g_bu[0];
+  A.g32[kGAu2][c] = P(24) + g_au[1];
+  A.g32[kGBu2][c] = P(25) + g_bu[1];
+}
 
 }  // namespace fwgb

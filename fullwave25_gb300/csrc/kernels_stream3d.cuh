@@ -26,7 +26,6 @@ constexpr int kCell = kMThreads;                  // cells per plane of a block 
 constexpr int kVelStateF = 9, kVelMapF = 6;       // field counts of the velocity boxes
 constexpr int kPrsPhiF = 6;
 constexpr int kStateV0 = 1, kStatePhi0 = 10;      // first field of v and of phi in the state
-constexpr int kStatusAlign = 8;                   // device status bit: bad shared-memory alignment
 
 template <int kPS>
 constexpr size_t vel_stream_smem() {

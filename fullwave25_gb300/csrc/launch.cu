@@ -26,6 +26,15 @@ void launch_stream2d_shape(fw_handle* h, cudaStream_t s) {
            s, h->args, h->tmaps2);
 }
 
+// TMA tile kernels (2D isotropic): one 32 x 8 tile per block, operands staged by TMA.
+template <bool kBeta>
+void launch_tile2d(fw_handle* h, cudaStream_t s) {
+  const Tiling& t = h->tiling;
+  dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
+  launch_k(vel2d_tile<kMRdtRho>, grid, block, sizeof(VelTileSmem), s, h->args, h->tmaps_t);
+  launch_k(prs2d_tile<kBeta, kMDtK>, grid, block, sizeof(PrsTileSmem), s, h->args, h->tmaps_t);
+}
+
 template <bool kBeta>
 void launch_stream2d(fw_handle* h, cudaStream_t s) {
   switch (h->shape2d) {
@@ -42,9 +51,10 @@ template <int ND, class CV, class CP, int kMin>
 void launch_typed(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
   if constexpr (ND == 2) {
-    static_assert(kNumShapes2D == 7, "one case per 2D kernel shape");
+    static_assert(kNumShapes2D == 8, "one case per 2D kernel shape");
     switch (h->shape2d) {
       case 0:
+      case kTileShape:          // tile kernels exist for the isotropic engine only (launch_nd)
       case kPersistentShape: {  // the persistent shape issues the direct kernels when captured
         dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
         launch_k(vel2d_direct<CV>, grid, block, 0, s, h->args);
@@ -104,6 +114,10 @@ void launch_nd(fw_handle* h, cudaStream_t s) {
         return;
       }
     } else {
+      if (kShapes2D[h->shape2d].tile) {
+        launch_tile2d<kBeta>(h, s);
+        return;
+      }
       if (h->stream2d && kShapes2D[h->shape2d].ty > 0) {
         launch_stream2d<kBeta>(h, s);
         return;
@@ -184,7 +198,7 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t
 
 int encode_map(fw_handle* h, CUtensorMap* map, void* base, cuuint32_t rank,
                const cuuint64_t* dims, const cuuint64_t* strides, const cuuint32_t* box,
-               CUtensorMapDataType type = CU_TENSOR_MAP_DATA_TYPE_FLOAT32) {
+               CUtensorMapDataType type) {
   static EncodeTiledFn encode = nullptr;
   if (!encode) {
     void* fn = nullptr;
@@ -284,13 +298,45 @@ int encode_march2_maps(fw_handle* h, uint32_t ty, March2Maps* m) {
 }
 
 // Select 2D kernel shape k: encode the row tensor maps for its width, drop the step graph.
+// Tensor maps of the TMA tile kernels: the state stack (pitch, nx, 11), the coefficient-map
+// stack and the tap-index map.
+int encode_tile2_maps(fw_handle* h, Tile2Maps* m) {
+  const cuuint64_t row = (cuuint64_t)h->pitch * 4, field = (cuuint64_t)h->ncells_padded * 4;
+  const cuuint64_t pitch = (cuuint64_t)h->pitch, nx = (cuuint64_t)h->nx;
+  const cuuint64_t d_st[3] = {pitch, nx, (cuuint64_t)n_state(h->ndim)};
+  const cuuint64_t d_mp[3] = {pitch, nx, (cuuint64_t)n_maps(h)};
+  const cuuint64_t str[2] = {row, field};
+  const cuuint64_t d_dc[2] = {pitch, nx};
+  const cuuint32_t bp[3] = {48, 24, 1}, bx[3] = {40, 24, 1}, by[3] = {48, 10, 1};
+  const cuuint32_t b1[3] = {kD2TY, kD2TX, 1}, b4[3] = {kD2TY, kD2TX, 4}, b6[3] = {kD2TY, kD2TX, 6};
+  const cuuint32_t b7[3] = {kD2TY, kD2TX, 7}, bdc[2] = {kD2TY, kD2TX};
+  int st;
+  if ((st = encode_map(h, &m->p_halo, h->state, 3, d_st, str, bp)) ||
+      (st = encode_map(h, &m->vx_halo, h->state, 3, d_st, str, bx)) ||
+      (st = encode_map(h, &m->vy_halo, h->state, 3, d_st, str, by)) ||
+      (st = encode_map(h, &m->st1, h->state, 3, d_st, str, b1)) ||
+      (st = encode_map(h, &m->st4, h->state, 3, d_st, str, b4)) ||
+      (st = encode_map(h, &m->st6, h->state, 3, d_st, str, b6)) ||
+      (st = encode_map(h, &m->maps6, h->maps, 3, d_mp, str, b6)) ||
+      (st = encode_map(h, &m->maps7, h->maps, 3, d_mp, str, b7)) ||
+      (st = encode_map(h, &m->dc, h->dcmap, 2, d_dc, str, bdc, CU_TENSOR_MAP_DATA_TYPE_INT32)))
+    return st;
+  return FW_OK;
+}
+
 int set_shape2d(fw_handle* h, int k) {
   if (kShapes2D[k].ty > 0) {
     int st = encode_march2_maps(h, (uint32_t)kShapes2D[k].ty, &h->tmaps2);
     if (st) return st;
   }
+  const bool tile = kShapes2D[k].tile && !h->aniso && !h->exp;
+  if (tile) {
+    int st = encode_tile2_maps(h, &h->tmaps_t);
+    if (st) return st;
+  }
   h->shape2d = k;
-  h->variant = kShapes2D[k].persistent ? kPersistent : kShapes2D[k].ty > 0 ? kMarch : kDirect;
+  h->variant = kShapes2D[k].persistent ? kPersistent : kShapes2D[k].ty > 0 ? kMarch
+               : tile ? kTile : kDirect;
   h->graph_steps = 0;   // the next advance captures a graph with the new kernels
   return FW_OK;
 }

@@ -29,6 +29,26 @@ __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, uint32_t by
                : "memory");
 }
 
+// 2D tiled TMA load of one box (innermost coordinate first; same alignment rule as below).
+__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1)
+      : "memory");
+}
+
+// Untiled bulk copy of `bytes` contiguous bytes (both addresses 16-byte aligned, bytes a multiple
+// of 16) into shared memory; completion is signalled on `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, uint32_t bytes, uint64_t* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+          smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(src)), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+
 // 3D tiled TMA load of one box into shared memory; completion is signalled on `bar`.
 // Coordinates are element indices, innermost first; the innermost coordinate times 4 bytes must
 // be a multiple of 16 (callers pass multiples of 4).
@@ -69,6 +89,7 @@ __device__ __forceinline__ uint64_t global_timer_ns() {
 }
 
 constexpr int kStatusWaitTimeout = 1;   // device status bit: an mbarrier wait gave up
+constexpr int kStatusAlign = 8;         // device status bit: bad shared-memory alignment
 constexpr uint64_t kWaitLimitNs = 500ull * 1000 * 1000;
 
 // Wait for phase `parity` of `bar`, giving up after kWaitLimitNs: then the status bit is set in

@@ -347,7 +347,7 @@ class Engine:
     def kernel_variant(self) -> str:
         v = C.c_int32()
         self._call("fw_kernel_variant", C.byref(v))
-        return {0: "direct", 1: "march", 2: "persistent", 3: "stream"}[v.value]
+        return {0: "direct", 1: "march", 2: "persistent", 3: "stream", 4: "tile"}[v.value]
 
     def copy_state_rows_from(self, src: "Engine", src_row0: int, dst_row0: int, n_rows: int,
                              stream: int | None = None) -> None:

@@ -169,14 +169,18 @@ FWGB_API int fw_device_bytes(const fw_handle *h, uint64_t *bytes);
 /* Kernel family in use: 0 = direct-addressed kernels, 1 = plane/row-march kernels (TMA-staged
  * halo planes in 3D, halo rows in 2D), 2 = the persistent 2D kernel (one cooperative launch per
  * fw_advance, grid barriers between the velocity and pressure phases), 3 = the 3D plane march
- * with the point-wise state and maps staged by TMA as well (isotropic engine). 3D handles use 3
+ * with the point-wise state and maps staged by TMA as well (isotropic engine), 4 = the 2D tile
+ * kernels (one 32 x 8 tile per block, every operand staged by TMA; isotropic engine). 3D handles
+ * use 3
  * (isotropic; 1 with FWGB_STREAM3D=0) or 1 (anisotropic, exponential) unless the environment
  * variable FWGB_VARIANT=direct was set when the handle was created. 2D handles
  * start on 0 and the first fw_advance from step 0 autotunes the kernel shape (direct, a march
- * block of TY columns x XC rows, or persistent), timing each shape for a few dozen steps on the
+ * block of TY columns x XC rows, persistent, or TMA tiles), timing each shape for a few dozen
+ * steps on the
  * handle itself and resetting it after each trial; the choice is cached per device, grid size and
  * physics. FWGB_AUTOTUNE=0 disables the trials, FWGB_VARIANT=direct|march or
- * FWGB_SHAPE2D=<index 0-6> fixes the shape at creation. Every shape gives bit-identical results.
+ * FWGB_SHAPE2D=<index 0-7> fixes the shape at creation (groups: 0-5; the single-simulation shapes
+ * 6-7 give a group the direct kernels). Every shape gives bit-identical results.
  * No counterpart in the reference (one CUDA kernel family). */
 FWGB_API int fw_kernel_variant(const fw_handle *h, int32_t *variant);
 
@@ -217,10 +221,14 @@ FWGB_API int fw_adjoint_forward(fw_handle *h, void *stream, int32_t checkpoint_e
 /* Reverse pass: recompute each segment from its checkpoint and run the adjoint step backwards,
  * accumulating the gradient: each step's contributions are formed in FP32 (the precision of the
  * adjoint fields) into per-segment FP32 partial sums that are added into FP64 time sums at the
- * end of every segment (FWGB_ADJ_F64_STEPS=1: every step's contributions in FP64 instead). `residual` = traces - observed, device float32
- * [n_out][ncoordsout]. `grad_out`: device FP64 [12][nx][ny] in the order dt/rho, dt*K, 1/kappau,
- * 1/kappax, au1, bu1, au2, bu2, ax1, bx1, ax2, bx2 (ghost cells zero). The wavefield left in the
- * handle afterwards is the first segment's recomputation. */
+ * end of every segment (FWGB_ADJ_F64_STEPS=1: every step's contributions in FP64 instead).
+ * Each reverse step is two launches whose operands are staged in shared memory by TMA
+ * (FWGB_ADJ_TMA=0: the same arithmetic with the operands loaded by the threads).
+ * `residual` = traces - observed, device float32 [n_out][ncoordsout]. `grad_out`: device FP64
+ * [12][nx][ny] in the order dt/rho, dt*K, 1/kappau, 1/kappax, au1, bu1, au2, bu2, ax1, bx1, ax2,
+ * bx2 (ghost cells zero). The wavefield left in the handle afterwards is the first segment's
+ * recomputation. Returns after the stream has finished the pass (FW_ERR_DEVICE if a kernel
+ * reported a timed-out wait). */
 FWGB_API int fw_adjoint_backward(fw_handle *h, void *stream, const float *residual,
                                  double *grad_out);
 

@@ -91,10 +91,10 @@ def test_segmented_accumulation_matches_fp64_steps(engine_lib, cuda):
 
 
 @pytest.mark.parametrize("name", ["2d_small", "2d_air_beta_free"])
-def test_tiled_reverse_step_equals_unfused(engine_lib, cuda, name):
-    """Two tiled launches per reverse step (assemble + record + projections + pressure adjoint
-    fused; velocity adjoint from staged lam_d tiles) against the five-launch reverse step
-    (FWGB_ADJ_FUSED=0): bitwise equal map gradients, also with air cells and sources."""
+def test_reverse_step_forms_are_bitwise_equal(engine_lib, cuda, name):
+    """The three forms of the reverse step give bitwise equal map gradients, also with air cells
+    and sources: TMA-staged operands (default), two tiled launches with thread loads
+    (FWGB_ADJ_TMA=0), and the five-launch form (FWGB_ADJ_FUSED=0)."""
     import os
 
     torch = cuda
@@ -110,9 +110,9 @@ def test_tiled_reverse_step_equals_unfused(engine_lib, cuda, name):
     obs.maps["K"] = (obs.maps["K"] * np.float32(1.01)).astype(np.float32)
     observed = Oracle(obs).run().astype(np.float32)
     out = {}
-    for mode in ("tiled", "unfused"):
-        if mode == "unfused":
-            os.environ["FWGB_ADJ_FUSED"] = "0"
+    modes = {"tma": {}, "tiled": {"FWGB_ADJ_TMA": "0"}, "unfused": {"FWGB_ADJ_FUSED": "0"}}
+    for mode, env in modes.items():
+        os.environ.update(env)
         try:
             with Engine(inp) as eng:
                 eng.adjoint_forward(25)
@@ -122,9 +122,58 @@ def test_tiled_reverse_step_equals_unfused(engine_lib, cuda, name):
                 torch.cuda.synchronize()
                 out[mode] = g.cpu().numpy()
         finally:
-            os.environ.pop("FWGB_ADJ_FUSED", None)
+            for k in env:
+                os.environ.pop(k, None)
     assert np.abs(out["unfused"]).max() > 0
     np.testing.assert_array_equal(out["tiled"], out["unfused"])
+    np.testing.assert_array_equal(out["tma"], out["tiled"])
+
+
+@pytest.mark.parametrize("shape,every,ghost_src", [((61, 83), 7, False), ((45, 120), 40, False),
+                                                   ((45, 120), 40, True)])
+def test_reverse_pass_variants_ragged(engine_lib, cuda, shape, every, ghost_src):
+    """Reverse pass on grids whose body is not a whole number of 32 x 8 tiles (TMA boxes running
+    past the array edge read zeros) and with checkpoint intervals that do not divide nt: TMA
+    reverse step with out-of-place recomputation (default), tiled reverse step
+    (FWGB_ADJ_TMA=0) and recomputation by state copies (FWGB_ADJ_OOP=0) give bitwise equal
+    gradients. With a source in the ghost layer (pressure written there persists across steps)
+    the engine recomputes by copies by itself, so the default matches too."""
+    import os
+
+    torch = cuda
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.workloads import plain_2d_inputs
+
+    def problem(scale):
+        inp = plain_2d_inputs(shape=shape, nt=60, n_pml=6, n_transition=6)
+        inp.maps = dict(inp.maps)
+        inp.maps["rho"] = (inp.maps["rho"] * np.float32(scale)).astype(np.float32)
+        if ghost_src:   # one more source row inside the ghost layer
+            extra = np.stack([np.full(20, 3), np.arange(30, 50)], 1).astype(np.int32)
+            inp.icc = np.concatenate([inp.icc, extra])
+            inp.icmat = np.concatenate([inp.icmat, inp.icmat[:20]])
+        return inp
+
+    inp = problem(1.0)
+    observed = Oracle(problem(1.03)).run().astype(np.float32)
+    out = {}
+    modes = {"default": {}, "tiled": {"FWGB_ADJ_TMA": "0"}, "copies": {"FWGB_ADJ_OOP": "0"}}
+    for mode, env in modes.items():
+        os.environ.update(env)
+        try:
+            with Engine(inp) as eng:
+                eng.adjoint_forward(every)
+                res = torch.as_tensor(eng.read_traces() - observed, device="cuda").contiguous()
+                g = torch.zeros((12,) + tuple(inp.shape), dtype=torch.float64, device="cuda")
+                eng.adjoint_backward(res.data_ptr(), g.data_ptr())
+                torch.cuda.synchronize()
+                out[mode] = g.cpu().numpy()
+        finally:
+            for k in env:
+                os.environ.pop(k, None)
+    assert np.abs(out["copies"]).max() > 0
+    np.testing.assert_array_equal(out["default"], out["copies"])
+    np.testing.assert_array_equal(out["tiled"], out["copies"])
 
 
 @pytest.fixture(scope="module")

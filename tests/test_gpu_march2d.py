@@ -16,8 +16,9 @@ from golden_io import load_case_inputs
 
 pytestmark = pytest.mark.gpu
 TOL = 1e-4
-MARCH_SHAPES = (1, 2, 3, 4, 5, 6)   # march shapes 1-5, persistent kernel 6; 0 = direct kernels
-VARIANT = {1: "march", 2: "march", 3: "march", 4: "march", 5: "march", 6: "persistent"}
+MARCH_SHAPES = (1, 2, 3, 4, 5, 6, 7)   # march 1-5, persistent 6, TMA tiles 7; 0 = direct kernels
+VARIANT = {1: "march", 2: "march", 3: "march", 4: "march", 5: "march", 6: "persistent",
+           7: "tile"}
 
 
 def _engine(inp, **env):
@@ -69,7 +70,9 @@ def test_every_march_shape_equals_direct_bitwise(engine_lib, cuda, case):
     for k in MARCH_SHAPES:
         with _engine(inp, FWGB_SHAPE2D=k) as em:
             got = em.run()
-            assert em.kernel_variant == VARIANT[k]
+            # the tile kernels cover the isotropic engine; the others run the direct kernels
+            tile_direct = k == 7 and case in ("2d_aniso", "2d_exp")
+            assert em.kernel_variant == ("direct" if tile_direct else VARIANT[k])
         np.testing.assert_array_equal(got, ref, err_msg=f"{case}: shape {k}")
 
 
@@ -135,9 +138,17 @@ def test_autotuned_engine_matches_direct_and_oracle(engine_lib, cuda, ragged_2d)
     assert err < TOL, f"rel-L2 {err:.3e}"
 
 
-def test_autotune_disabled_and_short_runs_stay_direct(engine_lib, cuda):
+def test_autotune_disabled_and_short_runs_stay_direct(engine_lib, cuda, monkeypatch):
     inp = load_case_inputs("2d_small")
+    monkeypatch.setenv("FWGB_AUTOTUNE", "0")   # read at the first advance
     with _engine(inp, FWGB_AUTOTUNE=0) as e:
+        e.run()
+        assert e.kernel_variant == "direct"
+    monkeypatch.delenv("FWGB_AUTOTUNE")
+    short = load_case_inputs("2d_small")          # fewer steps than two tuning trials
+    short.nt = 100
+    short.icmat = np.ascontiguousarray(short.icmat[:, :100])
+    with _engine(short) as e:
         e.run()
         assert e.kernel_variant == "direct"
 
