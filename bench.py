@@ -574,6 +574,7 @@ def run_serve(args):
             r = Request(rid=i, arrival=float(t), build=lambda i=i: batch_instance(i, scale=scale))
             d = r.build()  # memory need from the instance geometry (built once to measure)
             r.bytes_needed = engine_bytes(d.shape, d.nt, d.outc.shape[0])
+            r.cells = int(np.prod(d.shape))
             del d
             reqs.append(r)
     torch.cuda.synchronize()
@@ -583,8 +584,10 @@ def run_serve(args):
     for r in warm:
         r.admitted = r.finished = -1.0
         r.traces = r.result = None
+    cap = int(args.max_active_mcells * 1e6) if args.max_active_mcells > 0 else None
     with ClockSampler(0) as clocks:
-        cont = serve_continuous(reqs, budget_bytes=args.budget_gb << 30, chunk_steps=256)
+        cont = serve_continuous(reqs, budget_bytes=args.budget_gb << 30, chunk_steps=256,
+                                max_active_cells=cap)
     for r in reqs:
         r.result = None
     fifo = serve_fifo(reqs)
@@ -601,7 +604,8 @@ def run_serve(args):
                                    f"grids, nt 6000 at 1024), sizes scaled by {scale}; device "
                                    f"budget {args.budget_gb} GB, blocks of 256 steps, "
                                    "2 gradient worker streams",
-                       "requests": len(reqs), "gradient_requests": n_grad},
+                       "requests": len(reqs), "gradient_requests": n_grad,
+                       "max_active_cells": cap},
             "continuous": cont, "fifo_one_at_a_time": fifo,
             "sims_per_s_ratio": cont["sims_per_s"] / fifo["sims_per_s"],
             "clocks": clocks.summary()}
@@ -680,6 +684,9 @@ def main():
     ap.add_argument("--duration", type=float, default=10.0, help="serve2d: stream length [s]")
     ap.add_argument("--scale", type=float, default=0.5, help="serve2d: instance size scale")
     ap.add_argument("--budget-gb", type=int, default=150, help="serve2d: device memory budget")
+    ap.add_argument("--max-active-mcells", type=float, default=16.0,
+                    help="serve2d: cap on the grid cells (millions) of the forward requests "
+                         "stepping together (0: memory budget only)")
     ap.add_argument("--grad-frac", type=float, default=0.2,
                     help="serve2d: fraction of gradient requests")
     ap.add_argument("--batch", type=int, default=64, help="simulations per rank (batch2d)")

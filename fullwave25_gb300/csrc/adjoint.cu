@@ -46,6 +46,23 @@ int encode_adj_maps(fw_handle* h, AdjMaps* M) {
   return FW_OK;
 }
 
+// Allow the TMA reverse-step kernels the device's whole opt-in shared memory, once per device.
+// Handles with different tap-table sizes run concurrently (gradient workers on their own
+// streams), so the limit is not set per call: a smaller per-call value set by one thread would
+// make another thread's larger launch invalid.
+int prepare_adjoint_kernels(fw_handle* h, int dev, int smem_optin) {
+  static std::mutex mu;
+  static std::vector<int> done;
+  std::lock_guard<std::mutex> lk(mu);
+  if (std::find(done.begin(), done.end(), dev) != done.end()) return FW_OK;
+  FW_CUDA(h, cudaFuncSetAttribute(adj2d_prs_tma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem_optin));
+  FW_CUDA(h, cudaFuncSetAttribute(adj2d_vel_tma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem_optin));
+  done.push_back(dev);
+  return FW_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -147,20 +164,21 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   const size_t smem_prs = adj_prs_tma_smem(h->d.ndmap), smem_vel = adj_vel_tma_smem(h->d.ndmap);
   const bool tma = fused && !f64_steps && !(tenv && std::strcmp(tenv, "0") == 0) &&
                    std::max(smem_prs, smem_vel) <= (size_t)smem_optin;
-  // Recomputation: out of place from one stored state into the next (the direct step kernels
+  // Recomputation: out of place from one stored state into the next (the TMA tile step kernels
   // reading slot n and writing slot n + 1), unless pressure is written in the ghost layer (it
   // persists there in place) or FWGB_ADJ_OOP=0: then a copy of the state into the store before
   // each in-place step.
   const char* oenv = std::getenv("FWGB_ADJ_OOP");
   const bool oop = !h->ghost_writes && !(oenv && std::strcmp(oenv, "0") == 0);
+  Tile2Maps MT{};
+  if (oop) {
+    int st = encode_tile2_maps(h, &MT, h->adj_store, h->adj_every + 1);
+    if (st) return st;
+  }
   AdjMaps M{};
   if (tma) {
     int st = encode_adj_maps(h, &M);
-    if (st) return st;
-    FW_CUDA(h, cudaFuncSetAttribute(adj2d_prs_tma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem_prs));
-    FW_CUDA(h, cudaFuncSetAttribute(adj2d_vel_tma<0>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smem_vel));
+    if (st || (st = prepare_adjoint_kernels(h, dev, smem_optin))) return st;
   }
   const Lists& L = h->args.l;
   // list lengths: sources after de-duplication, air cells, sensors
@@ -182,12 +200,11 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     if (oop) {
       FW_CUDA(h, cudaMemcpyAsync(h->adj_store, h->adj_ckpt + state_elems * seg,
                                  state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
-      StepArgs in = h->args, out = h->args;
+      StepArgs out = h->args;
       for (int n = n0; n < n1; ++n) {
-        set_state_pointers(h, &in, h->adj_store + state_elems * (n - n0));
         set_state_pointers(h, &out, h->adj_store + state_elems * (n - n0 + 1));
-        vel2d_direct_oop<CellVelT<2, false>><<<grid, block, 0, s>>>(in, out);
-        prs2d_direct_oop<CellPrsT<2, false>><<<grid, block, 0, s>>>(in, out);
+        vel2d_tile<kMRdtRho, true><<<grid, block, sizeof(VelTileSmem), s>>>(out, MT, n - n0);
+        prs2d_tile<false, kMDtK, true><<<grid, block, sizeof(PrsTileSmem), s>>>(out, MT, n - n0);
       }
       if (seg == 0)   // leave the first segment's recomputation in the handle, as in place
         FW_CUDA(h, cudaMemcpyAsync(h->state, h->adj_store + state_elems * (n1 - n0),

@@ -198,6 +198,7 @@ int encode_field_map(fw_handle* h, CUtensorMap* map, float* base, uint32_t bz, u
 int encode_stream_maps(fw_handle* h);
 int encode_march2_maps(fw_handle* h, uint32_t ty, March2Maps* m);
 int set_shape2d(fw_handle* h, int k);
+int encode_tile2_maps(fw_handle* h, fwgb::Tile2Maps* m, float* store, int slots);
 int prepare_stream3d(fw_handle* h);
 
 // engine.cu

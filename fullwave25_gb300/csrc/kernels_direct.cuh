@@ -25,10 +25,8 @@ __device__ __forceinline__ float ld_field(const float* q) {
   else return __ldg(q);
 }
 
-// A: the fields read (p, v, psi at step n); O: the fields written (v, psi). O = A in place.
 template <class CV, bool kCoherent = false>
-__device__ __forceinline__ void vel2d_body_io(const StepArgs& A, const StepArgs& O, int tile_y,
-                                              int tile_x) {
+__device__ __forceinline__ void vel2d_body(const StepArgs& A, int tile_y, int tile_x) {
   const Grid& g = A.g;
   const int j = kGhost + tile_y * kD2TY + threadIdx.x;
   const int i = kGhost + tile_x * kD2TX + threadIdx.y;
@@ -50,29 +48,22 @@ __device__ __forceinline__ void vel2d_body_io(const StepArgs& A, const StepArgs&
   gx = fmaf(co, (P(sx + 1) - P(1)) + (P(sx - 1) - P(-1)), gx);
   gy = fmaf(co, (P(1 + sx) - P(sx)) + (P(1 - sx) - P(-sx)), gy);
   const float gg[2] = {gx * g.inv_h[0], gy * g.inv_h[1]};
-  cv.update_store(O, c, gg);
+  cv.update_store(A, c, gg);
 }
 
-template <class CV, bool kCoherent = false>
-__device__ __forceinline__ void vel2d_body(const StepArgs& A, int tile_y, int tile_x) {
-  vel2d_body_io<CV, kCoherent>(A, A, tile_y, tile_x);
-}
-
-// A: the fields read (p, phi at step n); O: the fields written (p, phi) and the new velocity the
-// divergence is taken of. O = A in place. `n`: the time step being completed (-1: read the device
-// step counter in the epilogue).
+// `n`: the time step being completed (-1: read the device step counter in the epilogue).
 template <class CP, bool kCoherent = false>
-__device__ __forceinline__ void prs2d_body_io(const StepArgs& A, const StepArgs& O, int tile_y,
-                                              int tile_x, int tile, int n = -1) {
+__device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int tile_x, int tile,
+                                           int n = -1) {
   const Grid& g = A.g;
   const int j = kGhost + tile_y * kD2TY + threadIdx.x;
   const int i = kGhost + tile_x * kD2TX + threadIdx.y;
-  float* p = O.f.p;
+  float* p = A.f.p;
   if (i < g.nx - kGhost && j < g.ny - kGhost) {
     const int64_t sx = g.sx;
     const int64_t c = i * sx + j;
-    const float* vx = O.f.v[0];
-    const float* vy = O.f.v[1];
+    const float* vx = A.f.v[0];
+    const float* vy = A.f.v[1];
     auto X = [&](int64_t o) { return ld_field<kCoherent>(vx + c + o); };
     auto Y = [&](int64_t o) { return ld_field<kCoherent>(vy + c + o); };
     CP cp;
@@ -88,15 +79,9 @@ __device__ __forceinline__ void prs2d_body_io(const StepArgs& A, const StepArgs&
     dx = fmaf(co, (X(1) - X(-sx + 1)) + (X(-1) - X(-sx - 1)), dx);
     dy = fmaf(co, (Y(sx) - Y(sx - 1)) + (Y(-sx) - Y(-sx - 1)), dy);
     const float dd[2] = {dx * g.inv_h[0], dy * g.inv_h[1]};
-    cp.update_store(O, c, dd);
+    cp.update_store(A, c, dd);
   }
-  tile_epilogue(O, p, tile, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y, n);
-}
-
-template <class CP, bool kCoherent = false>
-__device__ __forceinline__ void prs2d_body(const StepArgs& A, int tile_y, int tile_x, int tile,
-                                           int n = -1) {
-  prs2d_body_io<CP, kCoherent>(A, A, tile_y, tile_x, tile, n);
+  tile_epilogue(A, p, tile, threadIdx.y * blockDim.x + threadIdx.x, blockDim.x * blockDim.y, n);
 }
 
 template <class CV>
@@ -110,20 +95,6 @@ template <class CP>
 __global__ void __launch_bounds__(256) prs2d_direct(const StepArgs A) {
   pdl_entry();
   prs2d_body<CP>(A, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x);
-}
-
-// Out-of-place time step (the discrete adjoint's recomputation into its store of states): fields
-// read from In (state n), written to Out (state n + 1). Every body cell of every field of Out is
-// written; its ghost layer is not (callers keep it zero). Same arithmetic as the in-place step.
-template <class CV>
-__global__ void __launch_bounds__(256) vel2d_direct_oop(const StepArgs In, const StepArgs Out) {
-  if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0 && threadIdx.y == 0) *In.step += 1;
-  vel2d_body_io<CV>(In, Out, blockIdx.x, blockIdx.y);
-}
-
-template <class CP>
-__global__ void __launch_bounds__(256) prs2d_direct_oop(const StepArgs In, const StepArgs Out) {
-  prs2d_body_io<CP>(In, Out, blockIdx.x, blockIdx.y, blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 // Group (batched) kernels: block b works on tiles[b] = {simulation, tile_y, tile_x, tile index

@@ -9,6 +9,12 @@
 // is in flight at once, with up to eight such blocks per SM. The arithmetic is that of
 // vel2d_body / prs2d_body (same cell classes, same operation order), so the results are bitwise
 // equal to the direct kernels'; the pressure kernel ends with the same tile epilogue.
+//
+// kStore: the step runs out of place over a store of states (the discrete adjoint's
+// recomputation): the boxes are read from store slot `slot` (state n; the pressure kernel's
+// velocity halos from slot + 1) through 4D tensor maps (pitch, nx, field, slot), and the results
+// are written through the field pointers of A, which point at slot + 1. Every body cell of every
+// field of slot + 1 is written; its ghost layer is not (the caller keeps it zero).
 #pragma once
 #include "engine_common.cuh"
 #include "kernels_direct.cuh"
@@ -16,6 +22,8 @@
 
 namespace fwgb {
 
+// State boxes are 3D over the state (pitch, nx, field), or 4D over a state store (pitch, nx,
+// field, slot) with one more unit box dimension.
 struct Tile2Maps {
   CUtensorMap p_halo;    // state stack: box {48, 24, 1} (p: rows i0 - 8.., columns j0 - 8..)
   CUtensorMap vx_halo;   // state stack: box {40, 24, 1} (v_x: rows i0 - 8.., columns j0 - 4..)
@@ -24,8 +32,6 @@ struct Tile2Maps {
   CUtensorMap maps6, maps7;    // coefficient-map stack: boxes {32, 8, 6} and {32, 8, 7}
   CUtensorMap dc;              // tap-index map: box {32, 8}
 };
-
-constexpr int kTileState = 11;   // fields of a 2D state: p, v (2), psi (4), phi (4)
 
 struct VelTileSmem {
   float p[24][48];
@@ -56,6 +62,14 @@ __host__ __device__ constexpr uint32_t prs_tile_tx(bool beta) {
          4 * kD2TX * kD2TY;
 }
 
+// One box of state fields: from the state (3D map) or from a slot of a state store (4D map).
+template <bool kStore>
+__device__ __forceinline__ void tma_state(void* dst, const CUtensorMap* map, uint64_t* bar, int x,
+                                          int y, int field, int slot) {
+  if constexpr (kStore) tma_load_4d(dst, map, bar, x, y, field, slot);
+  else tma_load_3d(dst, map, bar, x, y, field);
+}
+
 // Block prologue of the tile kernels: alignment guard and barrier init (one thread).
 template <class SmemT>
 __device__ __forceinline__ bool tile_begin(SmemT& S, const unsigned char* base, int* status,
@@ -72,9 +86,9 @@ __device__ __forceinline__ bool tile_begin(SmemT& S, const unsigned char* base, 
   return true;
 }
 
-template <int kMapVel>
+template <int kMapVel, bool kStore = false>
 __global__ void __launch_bounds__(256) vel2d_tile(const StepArgs A,
-                                                  const __grid_constant__ Tile2Maps M) {
+                                                  const __grid_constant__ Tile2Maps M, int slot) {
   pdl_entry();
   extern __shared__ __align__(128) unsigned char tile_smem[];
   VelTileSmem& S = *reinterpret_cast<VelTileSmem*>(tile_smem);
@@ -85,8 +99,8 @@ __global__ void __launch_bounds__(256) vel2d_tile(const StepArgs A,
   if (!tile_begin(S, tile_smem, status, tid, kVelTileTx)) return;
   if (blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) *A.step += 1;
   if (tid == 0) {
-    tma_load_3d(S.p, &M.p_halo, &S.bar, j0 - 8, i0 - 8, 0);
-    tma_load_3d(S.st, &M.st6, &S.bar, j0, i0, 1);
+    tma_state<kStore>(S.p, &M.p_halo, &S.bar, j0 - 8, i0 - 8, 0, slot);
+    tma_state<kStore>(S.st, &M.st6, &S.bar, j0, i0, 1, slot);
     tma_load_3d(S.mp, &M.maps6, &S.bar, j0, i0, kMapVel);
     tma_load_2d(S.dc, &M.dc, &S.bar, j0, i0);
   }
@@ -124,9 +138,9 @@ __global__ void __launch_bounds__(256) vel2d_tile(const StepArgs A,
   cv.update_store(A, c, gg);
 }
 
-template <bool kBeta, int kMapPrs>
+template <bool kBeta, int kMapPrs, bool kStore = false>
 __global__ void __launch_bounds__(256) prs2d_tile(const StepArgs A,
-                                                  const __grid_constant__ Tile2Maps M) {
+                                                  const __grid_constant__ Tile2Maps M, int slot) {
   pdl_entry();
   extern __shared__ __align__(128) unsigned char tile_smem[];
   PrsTileSmem& S = *reinterpret_cast<PrsTileSmem*>(tile_smem);
@@ -136,10 +150,10 @@ __global__ void __launch_bounds__(256) prs2d_tile(const StepArgs A,
   const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
   if (!tile_begin(S, tile_smem, status, tid, prs_tile_tx(kBeta))) return;
   if (tid == 0) {
-    tma_load_3d(S.vx, &M.vx_halo, &S.bar, j0 - 4, i0 - 8, 1);
-    tma_load_3d(S.vy, &M.vy_halo, &S.bar, j0 - 8, i0 - 1, 2);
-    tma_load_3d(S.p, &M.st1, &S.bar, j0, i0, 0);
-    tma_load_3d(S.phi, &M.st4, &S.bar, j0, i0, 7);
+    tma_state<kStore>(S.vx, &M.vx_halo, &S.bar, j0 - 4, i0 - 8, 1, slot + 1);
+    tma_state<kStore>(S.vy, &M.vy_halo, &S.bar, j0 - 8, i0 - 1, 2, slot + 1);
+    tma_state<kStore>(S.p, &M.st1, &S.bar, j0, i0, 0, slot);
+    tma_state<kStore>(S.phi, &M.st4, &S.bar, j0, i0, 7, slot);
     tma_load_3d(S.mp, kBeta ? &M.maps7 : &M.maps6, &S.bar, j0, i0, kMapPrs);
     tma_load_2d(S.dc, &M.dc, &S.bar, j0, i0);
   }

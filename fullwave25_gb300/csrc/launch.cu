@@ -31,8 +31,8 @@ template <bool kBeta>
 void launch_tile2d(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
   dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
-  launch_k(vel2d_tile<kMRdtRho>, grid, block, sizeof(VelTileSmem), s, h->args, h->tmaps_t);
-  launch_k(prs2d_tile<kBeta, kMDtK>, grid, block, sizeof(PrsTileSmem), s, h->args, h->tmaps_t);
+  launch_k(vel2d_tile<kMRdtRho>, grid, block, sizeof(VelTileSmem), s, h->args, h->tmaps_t, 0);
+  launch_k(prs2d_tile<kBeta, kMDtK>, grid, block, sizeof(PrsTileSmem), s, h->args, h->tmaps_t, 0);
 }
 
 template <bool kBeta>
@@ -298,25 +298,30 @@ int encode_march2_maps(fw_handle* h, uint32_t ty, March2Maps* m) {
 }
 
 // Select 2D kernel shape k: encode the row tensor maps for its width, drop the step graph.
-// Tensor maps of the TMA tile kernels: the state stack (pitch, nx, 11), the coefficient-map
-// stack and the tap-index map.
-int encode_tile2_maps(fw_handle* h, Tile2Maps* m) {
+// Tensor maps of the TMA tile kernels: the state stack (pitch, nx, 11) -- or, with slots > 0, a
+// store of `slots` states at `store` (pitch, nx, 11, slots) --, the coefficient-map stack and the
+// tap-index map.
+int encode_tile2_maps(fw_handle* h, Tile2Maps* m, float* store, int slots) {
   const cuuint64_t row = (cuuint64_t)h->pitch * 4, field = (cuuint64_t)h->ncells_padded * 4;
   const cuuint64_t pitch = (cuuint64_t)h->pitch, nx = (cuuint64_t)h->nx;
-  const cuuint64_t d_st[3] = {pitch, nx, (cuuint64_t)n_state(h->ndim)};
+  const int ns = n_state(h->ndim);
+  const cuuint64_t d_st[4] = {pitch, nx, (cuuint64_t)ns, (cuuint64_t)slots};
   const cuuint64_t d_mp[3] = {pitch, nx, (cuuint64_t)n_maps(h)};
-  const cuuint64_t str[2] = {row, field};
+  const cuuint64_t str[3] = {row, field, field * ns};
   const cuuint64_t d_dc[2] = {pitch, nx};
-  const cuuint32_t bp[3] = {48, 24, 1}, bx[3] = {40, 24, 1}, by[3] = {48, 10, 1};
-  const cuuint32_t b1[3] = {kD2TY, kD2TX, 1}, b4[3] = {kD2TY, kD2TX, 4}, b6[3] = {kD2TY, kD2TX, 6};
-  const cuuint32_t b7[3] = {kD2TY, kD2TX, 7}, bdc[2] = {kD2TY, kD2TX};
+  const cuuint32_t bp[4] = {48, 24, 1, 1}, bx[4] = {40, 24, 1, 1}, by[4] = {48, 10, 1, 1};
+  const cuuint32_t b1[4] = {kD2TY, kD2TX, 1, 1}, b4[4] = {kD2TY, kD2TX, 4, 1};
+  const cuuint32_t b6[4] = {kD2TY, kD2TX, 6, 1}, b7[3] = {kD2TY, kD2TX, 7};
+  const cuuint32_t bdc[2] = {kD2TY, kD2TX};
+  float* base = slots > 0 ? store : h->state;
+  const cuuint32_t r = slots > 0 ? 4 : 3;
   int st;
-  if ((st = encode_map(h, &m->p_halo, h->state, 3, d_st, str, bp)) ||
-      (st = encode_map(h, &m->vx_halo, h->state, 3, d_st, str, bx)) ||
-      (st = encode_map(h, &m->vy_halo, h->state, 3, d_st, str, by)) ||
-      (st = encode_map(h, &m->st1, h->state, 3, d_st, str, b1)) ||
-      (st = encode_map(h, &m->st4, h->state, 3, d_st, str, b4)) ||
-      (st = encode_map(h, &m->st6, h->state, 3, d_st, str, b6)) ||
+  if ((st = encode_map(h, &m->p_halo, base, r, d_st, str, bp)) ||
+      (st = encode_map(h, &m->vx_halo, base, r, d_st, str, bx)) ||
+      (st = encode_map(h, &m->vy_halo, base, r, d_st, str, by)) ||
+      (st = encode_map(h, &m->st1, base, r, d_st, str, b1)) ||
+      (st = encode_map(h, &m->st4, base, r, d_st, str, b4)) ||
+      (st = encode_map(h, &m->st6, base, r, d_st, str, b6)) ||
       (st = encode_map(h, &m->maps6, h->maps, 3, d_mp, str, b6)) ||
       (st = encode_map(h, &m->maps7, h->maps, 3, d_mp, str, b7)) ||
       (st = encode_map(h, &m->dc, h->dcmap, 2, d_dc, str, bdc, CU_TENSOR_MAP_DATA_TYPE_INT32)))
@@ -331,7 +336,7 @@ int set_shape2d(fw_handle* h, int k) {
   }
   const bool tile = kShapes2D[k].tile && !h->aniso && !h->exp;
   if (tile) {
-    int st = encode_tile2_maps(h, &h->tmaps_t);
+    int st = encode_tile2_maps(h, &h->tmaps_t, nullptr, 0);
     if (st) return st;
   }
   h->shape2d = k;

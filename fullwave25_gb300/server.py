@@ -65,6 +65,7 @@ class Request:
     build: object                      # callable -> DeviceInputs (forward) or GradientJob
     bytes_needed: int = 0
     kind: str = "forward"              # "forward" or "gradient"
+    cells: int = 0                     # grid cells (forward requests; 0 = not counted)
     # filled by the server
     admitted: float = -1.0
     finished: float = -1.0
@@ -95,13 +96,17 @@ def poisson_arrivals(rate_hz: float, duration_s: float, seed: int = 0) -> np.nda
 
 
 def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, stream=None,
-                     clock=time.perf_counter, gradient_workers: int = 2) -> dict:
+                     clock=time.perf_counter, gradient_workers: int = 2,
+                     max_active_cells: int | None = None) -> dict:
     """Run ``requests`` with continuous batching; returns summary stats.
 
     Forward requests join the group engine between blocks of ``chunk_steps`` steps; gradient
     requests run on up to ``gradient_workers`` threads with a CUDA stream each. Admission is FIFO
     by arrival while the device-memory budget allows (a request larger than the budget runs
-    alone)."""
+    alone) and, with ``max_active_cells``, while the group's forward requests hold at most that
+    many grid cells: enough to keep the GPU's bandwidth busy, few enough that an overloaded
+    stream does not share the GPU among every waiting request (which delays them all alike) but
+    finishes the earlier arrivals first."""
     import torch  # noqa: PLC0415
 
     pending = sorted(requests, key=lambda r: r.arrival)
@@ -109,6 +114,7 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
     running: dict = {}           # future -> request, admitted gradient requests
     lock = threading.Lock()
     used = 0
+    cells_active = 0
     group = None
     main = stream or torch.cuda.Stream()
     streams = [torch.cuda.Stream() for _ in range(max(1, gradient_workers))]
@@ -138,7 +144,11 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
                 s = free_streams.pop()
                 running[pool.submit(gradient, r, s)] = (r, s)
             else:
+                if (max_active_cells is not None and active
+                        and cells_active + r.cells > max_active_cells):
+                    break
                 pending.pop(0)
+                cells_active += r.cells
                 with torch.cuda.stream(main):
                     eng = Engine(r.build(), validate=False)
                 r.admitted = clock() - t0
@@ -170,6 +180,7 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
                 r.traces = e.read_traces(stream=main.cuda_stream)
                 r.finished = clock() - t0
                 used -= r.bytes_needed
+                cells_active -= r.cells
                 e.close()
             else:
                 still.append((r, e))

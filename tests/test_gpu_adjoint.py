@@ -176,6 +176,41 @@ def test_reverse_pass_variants_ragged(engine_lib, cuda, shape, every, ghost_src)
     np.testing.assert_array_equal(out["tiled"], out["copies"])
 
 
+def test_concurrent_gradients_with_different_tap_tables(engine_lib, cuda):
+    """Gradient evaluations of handles whose tap tables differ in size (the reverse-step kernels'
+    shared-memory needs differ) running at once, each on its own thread and stream: every result
+    equals the same evaluation run alone."""
+    import threading
+
+    torch = cuda
+    from fullwave25_gb300.workloads_batch import gradient_job
+
+    jobs = [gradient_job(i, scale=0.12) for i in range(4)]
+    sizes = {int(j.problem.build(*j.start).dmap.shape[-1]) for j in jobs}
+    assert len(sizes) > 1
+    alone = [j.run() for j in jobs]
+    out = [None] * len(jobs)
+    gate = threading.Barrier(len(jobs))
+
+    def work(k):
+        s = torch.cuda.Stream()
+        gate.wait()
+        for _ in range(2):
+            out[k] = jobs[k].run(s)
+
+    threads = [threading.Thread(target=work, args=(k,)) for k in range(len(jobs))]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for k, (a, b) in enumerate(zip(alone, out)):
+        assert b is not None, f"job {k} raised"
+        assert a["J"] == b["J"] and a["J"] > 0
+        for key, g in a["grads"].items():
+            np.testing.assert_array_equal(b["grads"][key].cpu().numpy(), g.cpu().numpy(),
+                                          err_msg=f"job {k} {key}")
+
+
 @pytest.fixture(scope="module")
 def problem(cuda):
     torch = cuda

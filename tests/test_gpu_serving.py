@@ -46,6 +46,29 @@ def test_budget_limits_concurrency(engine_lib, cuda):
         assert b.admitted >= a.finished - 1e-9
 
 
+def test_cell_cap_limits_the_group(engine_lib, cuda):
+    """With max_active_cells, the forward requests stepping together never hold more grid cells
+    than the cap (unless one request alone exceeds it), and results still equal the alone runs."""
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.server import serve_continuous
+
+    reqs = _requests(8, 0.12, rate_hz=1000.0)
+    for r in reqs:
+        r.cells = int(np.prod(r.build().shape))
+    cap = 2 * int(np.median([r.cells for r in reqs]))
+    stats = serve_continuous(reqs, budget_bytes=8 << 30, chunk_steps=64, max_active_cells=cap)
+    assert stats["requests"] == 8
+    most = 0
+    for r in reqs:
+        live = [q for q in reqs if q.admitted <= r.admitted < q.finished]
+        most = max(most, len(live))
+        assert len(live) == 1 or sum(q.cells for q in live) <= cap
+    assert most >= 2   # the cap still lets requests share the group
+    for r in reqs:
+        with Engine(r.build(), validate=False) as e:
+            np.testing.assert_array_equal(r.traces, e.run())
+
+
 def test_forward_and_gradient_mix_equal_alone(engine_lib, cuda):
     """Gradient requests run on worker streams while forward requests step in the group: every
     forward result and every gradient equals the one computed alone."""
