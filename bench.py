@@ -118,45 +118,57 @@ def traffic_from_profiles(workload: str):
 
 
 # --------------------------------------------------------------------------------- workloads
-def workload_desc(name: str, grid: int = 0) -> dict:
+PHYSICS_TEXT = {
+    "isotropic": "2 relaxation mechanisms (isotropic relaxation engine)",
+    "aniso": "2 relaxation mechanisms, one map set per derivative direction (anisotropic "
+             "relaxation engine)",
+    "exp": "exponential attenuation from alpha0 (exponential-attenuation engine)",
+}
+
+
+def workload_desc(name: str, grid: int = 0, physics: str = "isotropic") -> dict:
     """The ``config`` description of a workload (shared by the GPU arm and the reference arm)."""
     if name == "plain2d":
-        return {"workload": "plain 2D forward, 768x512 + PML 40 + transition 40 (944x688), "
-                            "nt 4000, 8 random ellipses, 2 relaxation mechanisms",
-                "grid": [944, 688], "nt": 4000, "steps_per_bench_step": 4000,
+        pad = "PML 40 (864x608)" if physics == "exp" else "PML 40 + transition 40 (944x688)"
+        return {"workload": f"plain 2D forward, 768x512 + {pad}, nt 4000, 8 random ellipses, "
+                            + PHYSICS_TEXT[physics],
+                "grid": [864, 608] if physics == "exp" else [944, 688], "nt": 4000,
+                "physics": physics, "steps_per_bench_step": 4000,
                 "l2": "flushed (256 MB write) before every bench step; working set 60 MB"}
     if name == "plain3d":
         edge = grid or 512
         return {"workload": f"plain 3D forward, {edge}^3 + PML 32 + transition 32 "
                             f"({edge + 144}^3), nt 3000, "
                             "layered fat/muscle/liver with perturbed interfaces and 0.5% scatterers,"
-                            " 64-element plane-wave source, 256x256 sensor plane",
-                "grid": [edge + 144] * 3, "nt": 3000, "steps_per_bench_step": 100,
+                            " 64-element plane-wave source, 256x256 sensor plane, "
+                            + PHYSICS_TEXT[physics],
+                "grid": [edge + 144] * 3, "nt": 3000, "physics": physics,
+                "steps_per_bench_step": 100,
                 "l2": "inputs larger than L2 (working set ~30 GB)"}
     raise ValueError(f"unknown workload {name}")
 
 
-def make_workload(name: str, rank: int, grid: int = 0):
+def make_workload(name: str, rank: int, grid: int = 0, physics: str = "isotropic"):
     """Return (inputs-or-builder, steps_per_bench_step, description dict).
 
     ``grid`` > 0 replaces the 3D workload's 512^3 cells by grid^3 (small profiling cases)."""
-    desc = workload_desc(name, grid)
+    desc = workload_desc(name, grid, physics)
     if name == "plain2d":
         from fullwave25_gb300.workloads import plain_2d_inputs
 
-        inp = plain_2d_inputs(seed=rank)
+        inp = plain_2d_inputs(physics=physics, seed=rank)
         assert list(inp.shape) == desc["grid"] and inp.nt == desc["nt"]
         return inp, inp.nt, desc
     from fullwave25_gb300.workloads3d import plain_3d_device_inputs
 
     edge = grid or 512
-    dinp = plain_3d_device_inputs(seed=rank, shape=(edge, edge, edge))
+    dinp = plain_3d_device_inputs(seed=rank, shape=(edge, edge, edge), physics=physics)
     assert list(dinp.shape) == desc["grid"] and dinp.nt == desc["nt"]
     return dinp, 100, desc
 
 
 # --------------------------------------------------------------------------------- CPU baseline
-def time_oracle(workload: str, budget_s: float):
+def time_oracle(workload: str, budget_s: float, physics: str = "isotropic"):
     """FP64 C oracle (OpenMP, all host cores) on a bounded sample of the workload: the 2D grid,
     or a 96^3 block of the 3D medium, for as many time steps as fit in ``budget_s``."""
     sys.path.insert(0, str(ROOT / "oracle"))
@@ -165,12 +177,12 @@ def time_oracle(workload: str, budget_s: float):
     if workload == "plain2d":
         from fullwave25_gb300.workloads import plain_2d_inputs
 
-        inp = plain_2d_inputs()
-        label = "plain 2D grid 944x688"
+        inp = plain_2d_inputs(physics=physics)
+        label = f"plain 2D grid {inp.shape[0]}x{inp.shape[1]}"
     else:
         from fullwave25_gb300.workloads3d import plain_3d_host_sample
 
-        inp = plain_3d_host_sample()
+        inp = plain_3d_host_sample(physics=physics)
         label = f"plain 3D medium, {inp.shape[0]}x{inp.shape[1]}x{inp.shape[2]} sub-block"
     o = OracleC(inp)
     o.run(1)  # warm-up
@@ -232,14 +244,14 @@ def run_reference(args):
     per_step_budget = float(os.environ.get("FWGB_REF_SAMPLE_S", "8"))
     vals = []
     for i in range(args.warmup + args.steps):
-        r = time_oracle(args.workload, per_step_budget)
+        r = time_oracle(args.workload, per_step_budget, args.physics)
         if i >= args.warmup:
             vals.append(r["value"])
     v = statistics.mean(vals)
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": {**workload_desc(args.workload, args.grid),
+            "config": {**workload_desc(args.workload, args.grid, args.physics),
                        "parallelism": "single GPU" if world == 1 else f"replicas x{world}",
                        "engine": "FP64 C oracle restatement on the host cores (the reference "
                                  "engine is a closed x86-64 CUDA executable; it has no CPU "
@@ -264,7 +276,7 @@ def run_gpu(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    inputs, chunk, desc = make_workload(args.workload, rank, args.grid)
+    inputs, chunk, desc = make_workload(args.workload, rank, args.grid, args.physics)
     engine = Engine(inputs) if args.workload == "plain2d" else inputs.make_engine()
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
@@ -313,12 +325,13 @@ def run_gpu(args):
 
     # roofline: one time step (velocity + pressure kernels) over the whole grid
     step_s = (dev_ms / 1e3) / (chunk * args.steps)
-    alg_bytes = algorithmic_bytes_per_cell(len(inputs.shape)) * cells
+    bpc = algorithmic_bytes_per_cell(len(inputs.shape), physics=args.physics)
+    alg_bytes = bpc * cells
     achieved = alg_bytes / step_s / 1e9
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (
         ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    tr = traffic_from_profiles(args.workload)
+    tr = traffic_from_profiles(args.workload) if args.physics == "isotropic" else None
 
     # e2e through the C ABI with host buffers
     e2e = run_e2e(args, engine, inputs, chunk, sptr, dev, world)
@@ -326,8 +339,8 @@ def run_gpu(args):
     if rank != 0:
         engine.close()
         return
-    cpu = time_oracle(args.workload, float(os.environ.get("FWGB_CPU_SAMPLE_S", "15"))) if (
-        world == 1 and not args.no_cpu_baseline) else None
+    cpu = time_oracle(args.workload, float(os.environ.get("FWGB_CPU_SAMPLE_S", "15")),
+                      args.physics) if (world == 1 and not args.no_cpu_baseline) else None
     parity = parity_vs_oracle() if cpu is not None else None
     cpu_numpy = (time_numpy_oracle(args.workload, float(os.environ.get("FWGB_NUMPY_SAMPLE_S", "5")))
                  if cpu is not None else None)
@@ -342,8 +355,7 @@ def run_gpu(args):
                      "frac": achieved / peak,
                      "traffic": (tr * cells if tr is not None else None),
                      "kernel": "time step = velocity + pressure kernels",
-                     "algorithmic_bytes_per_cell_update":
-                         algorithmic_bytes_per_cell(len(inputs.shape)),
+                     "algorithmic_bytes_per_cell_update": bpc,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
                      else "fallback 6800 GB/s"},
         "cpu_baseline": cpu,
@@ -680,6 +692,9 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=os.environ.get("FWGB_WORKLOAD", "plain3d"),
                     choices=["plain2d", "plain3d", "batch2d", "serve2d", "adjoint2d"])
+    ap.add_argument("--physics", default="isotropic", choices=["isotropic", "aniso", "exp"],
+                    help="plain2d/plain3d: cell physics (relaxation engine, anisotropic "
+                         "relaxation, exponential attenuation)")
     ap.add_argument("--rate", type=float, default=20.0, help="serve2d: arrivals per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serve2d: stream length [s]")
     ap.add_argument("--scale", type=float, default=0.5, help="serve2d: instance size scale")

@@ -203,8 +203,10 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
       StepArgs out = h->args;
       for (int n = n0; n < n1; ++n) {
         set_state_pointers(h, &out, h->adj_store + state_elems * (n - n0 + 1));
-        vel2d_tile<kMRdtRho, true><<<grid, block, sizeof(VelTileSmem), s>>>(out, MT, n - n0);
-        prs2d_tile<false, kMDtK, true><<<grid, block, sizeof(PrsTileSmem), s>>>(out, MT, n - n0);
+        vel2d_tile<kTileIso, true><<<grid, block, sizeof(VelTileSmem<kTileIso>), s>>>(
+            out, MT, n - n0);
+        prs2d_tile<kTileIso, false, true><<<grid, block, sizeof(PrsTileSmem<kTileIso, false>),
+                                            s>>>(out, MT, n - n0);
       }
       if (seg == 0)   // leave the first segment's recomputation in the handle, as in place
         FW_CUDA(h, cudaMemcpyAsync(h->state, h->adj_store + state_elems * (n1 - n0),

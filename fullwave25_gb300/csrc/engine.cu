@@ -709,7 +709,6 @@ int autotune_2d(fw_handle* h, cudaStream_t s) {
   int st = FW_OK, best = 0;
   float best_ms = 0.f;
   for (int k = 0; k < kNumShapes2D && st == FW_OK; ++k) {
-    if (kShapes2D[k].tile && (h->aniso || h->exp)) continue;   // runs the direct kernels
     float ms = 0.f;
     if ((st = set_shape2d(h, k))) break;
     if (kShapes2D[k].persistent) {

@@ -39,8 +39,8 @@ constexpr int kStreamXC = 32;  // x planes per block of the streaming 3D march (
 // 1-5 = row-march kernels with TY threads (y columns) walking XC rows (TY + 16 <= 256, the TMA box
 // limit; TY a multiple of 32 and XC of 8, whole list tiles per block), 6 = the persistent kernel
 // (direct bodies, one cooperative launch per block of steps, grid barriers between phases),
-// 7 = the TMA tile kernels (isotropic engine; one 32 x 8 tile per block, every operand staged by
-// TMA; the other engines run the direct kernels for it).
+// 7 = the TMA tile kernels (one 32 x 8 tile per block, every operand staged by TMA; every cell
+// physics).
 struct Shape2D { int ty, xc; bool persistent, tile; };
 constexpr Shape2D kShapes2D[] = {{0, 0, false, false},   {64, 16, false, false},
                                  {64, 32, false, false},  {128, 16, false, false},

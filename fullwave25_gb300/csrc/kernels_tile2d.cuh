@@ -1,11 +1,12 @@
 // 2D step kernels over one 32 (y) x 8 (x) tile per block with every operand staged in shared
-// memory by TMA (isotropic relaxation engine).
+// memory by TMA, for every cell physics (isotropic and anisotropic relaxation, exponential
+// attenuation).
 //
 // The direct kernels load each operand with a thread load when it is needed, so a warp has only
 // a few loads in flight and the kernels are latency-bound (long-scoreboard stalls) on grids that
 // are too small for the row-march shapes to fill the GPU. Here one thread issues, at block start,
 // TMA boxes for the stencil field with its halo, the point-wise state, the coefficient maps and
-// the tap-index map, all completing on one mbarrier (bounded wait): the whole tile input (18-20 KB)
+// the tap-index map, all completing on one mbarrier (bounded wait): the whole tile input (10-25 KB)
 // is in flight at once, with up to eight such blocks per SM. The arithmetic is that of
 // vel2d_body / prs2d_body (same cell classes, same operation order), so the results are bitwise
 // equal to the direct kernels'; the pressure kernel ends with the same tile epilogue.
@@ -16,6 +17,7 @@
 // are written through the field pointers of A, which point at slot + 1. Every body cell of every
 // field of slot + 1 is written; its ghost layer is not (the caller keeps it zero).
 #pragma once
+#include <type_traits>
 #include "engine_common.cuh"
 #include "kernels_direct.cuh"
 #include "tma.cuh"
@@ -23,44 +25,65 @@
 namespace fwgb {
 
 // State boxes are 3D over the state (pitch, nx, field), or 4D over a state store (pitch, nx,
-// field, slot) with one more unit box dimension.
+// field, slot) with one more unit box dimension. Map boxes are 3D over the coefficient-map stack.
 struct Tile2Maps {
-  CUtensorMap p_halo;    // state stack: box {48, 24, 1} (p: rows i0 - 8.., columns j0 - 8..)
-  CUtensorMap vx_halo;   // state stack: box {40, 24, 1} (v_x: rows i0 - 8.., columns j0 - 4..)
-  CUtensorMap vy_halo;   // state stack: box {48, 10, 1} (v_y: rows i0 - 1.., columns j0 - 8..)
-  CUtensorMap st1, st4, st6;   // state stack: boxes {32, 8, f}
-  CUtensorMap maps6, maps7;    // coefficient-map stack: boxes {32, 8, 6} and {32, 8, 7}
-  CUtensorMap dc;              // tap-index map: box {32, 8}
+  CUtensorMap p_halo;    // state: box {48, 24, 1} (p: rows i0 - 8.., columns j0 - 8..)
+  CUtensorMap vx_halo;   // state: box {40, 24, 1} (v_x: rows i0 - 8.., columns j0 - 4..)
+  CUtensorMap vy_halo;   // state: box {48, 10, 1} (v_y: rows i0 - 1.., columns j0 - 8..)
+  CUtensorMap st1, st2, st4, st6;          // state: boxes {32, 8, f}
+  CUtensorMap mp1, mp3, mp5, mp6;          // coefficient maps: boxes {32, 8, f}
+  CUtensorMap dc;                          // tap-index map: box {32, 8}
 };
 
+enum TilePhysics { kTileIso = 0, kTileAniso = 1, kTileExp = 2 };
+
+// Map-stack slots the tile kernels read (the engine's map order): velocity maps 0-5 (rdt_rho and
+// the x-gradient set inv_ku au1 bu1 au2 bu2), pressure maps 6-11 (dt_k and the x-divergence
+// set), beta 2 dt at 12; anisotropic y sets at 13-17 (gradient) and 18-22 (divergence); the
+// exponential engine's a_exp in slot 2.
+constexpr int kTileMapVel = 0, kTileMapPrs = 6, kTileMapBeta = 12, kTileMapGradY = 13,
+              kTileMapDivY = 18, kTileMapAexp = 2;
+
+// Planes of each kernel's point-wise boxes, per physics.
+template <int P> struct TileVelPlanes {
+  static constexpr int kSt = P == kTileExp ? 2 : 6;                           // v (+ psi)
+  static constexpr int kMp = P == kTileExp ? 3 : P == kTileAniso ? 11 : 6;    // maps
+};
+template <int P, bool kBeta> struct TilePrsPlanes {
+  static constexpr int kPhi = P == kTileExp ? 0 : 4;
+  static constexpr int kMp = (P == kTileExp ? 2 : P == kTileAniso ? 11 : 6) + (kBeta ? 1 : 0);
+};
+
+template <int P>
 struct VelTileSmem {
   float p[24][48];
-  float st[6][kD2TX][kD2TY];   // v_x v_y psi_x1 psi_x2 psi_y1 psi_y2
-  float mp[6][kD2TX][kD2TY];   // rdt_rho inv_ku au1 bu1 au2 bu2
+  float st[TileVelPlanes<P>::kSt][kD2TX][kD2TY];
+  float mp[TileVelPlanes<P>::kMp][kD2TX][kD2TY];
   int dc[kD2TX][kD2TY];
   uint64_t bar;
+  static constexpr uint32_t kTx =
+      sizeof(float) * (24 * 48 + (TileVelPlanes<P>::kSt + TileVelPlanes<P>::kMp) * kD2TX * kD2TY) +
+      4 * kD2TX * kD2TY;
 };
+template <int P, bool kBeta>
 struct PrsTileSmem {
+  static constexpr int kPhi = TilePrsPlanes<P, kBeta>::kPhi;
+  static constexpr int kMp = TilePrsPlanes<P, kBeta>::kMp;
   float vx[24][40];
   float vy[10][48];
   float p[kD2TX][kD2TY];
-  float phi[4][kD2TX][kD2TY];  // phi_x1 phi_x2 phi_y1 phi_y2
-  float mp[7][kD2TX][kD2TY];   // dt_k inv_kx ax1 bx1 ax2 bx2 [beta2dt]
+  float phi[kPhi > 0 ? kPhi : 1][kD2TX][kD2TY];
+  float mp[kMp][kD2TX][kD2TY];
   int dc[kD2TX][kD2TY];
   uint64_t bar;
+  static constexpr uint32_t kTx =
+      sizeof(float) * (24 * 40 + 10 * 48 + (1 + kPhi + kMp) * kD2TX * kD2TY) + 4 * kD2TX * kD2TY;
 };
-static_assert(offsetof(VelTileSmem, st) % 128 == 0 && offsetof(VelTileSmem, mp) % 128 == 0 &&
-                  offsetof(VelTileSmem, dc) % 128 == 0,
+// Every TMA destination starts on a 128-byte boundary: the halo boxes are 4608, 3840 and 1920
+// bytes and every plane 1024 bytes.
+static_assert(sizeof(float) * 24 * 48 % 128 == 0 && sizeof(float) * 24 * 40 % 128 == 0 &&
+                  sizeof(float) * 10 * 48 % 128 == 0 && sizeof(float) * kD2TX * kD2TY % 128 == 0,
               "TMA destinations must be 128-byte aligned");
-static_assert(offsetof(PrsTileSmem, vy) % 128 == 0 && offsetof(PrsTileSmem, p) % 128 == 0 &&
-                  offsetof(PrsTileSmem, phi) % 128 == 0 && offsetof(PrsTileSmem, mp) % 128 == 0 &&
-                  offsetof(PrsTileSmem, dc) % 128 == 0,
-              "TMA destinations must be 128-byte aligned");
-constexpr uint32_t kVelTileTx = sizeof(float) * (24 * 48 + 12 * kD2TX * kD2TY) + 4 * kD2TX * kD2TY;
-__host__ __device__ constexpr uint32_t prs_tile_tx(bool beta) {
-  return sizeof(float) * (24 * 40 + 10 * 48 + (beta ? 12 : 11) * kD2TX * kD2TY) +
-         4 * kD2TX * kD2TY;
-}
 
 // One box of state fields: from the state (3D map) or from a slot of a state store (4D map).
 template <bool kStore>
@@ -86,22 +109,29 @@ __device__ __forceinline__ bool tile_begin(SmemT& S, const unsigned char* base, 
   return true;
 }
 
-template <int kMapVel, bool kStore = false>
+template <int P, bool kStore = false>
 __global__ void __launch_bounds__(256) vel2d_tile(const StepArgs A,
                                                   const __grid_constant__ Tile2Maps M, int slot) {
   pdl_entry();
   extern __shared__ __align__(128) unsigned char tile_smem[];
-  VelTileSmem& S = *reinterpret_cast<VelTileSmem*>(tile_smem);
+  using Smem = VelTileSmem<P>;
+  Smem& S = *reinterpret_cast<Smem*>(tile_smem);
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kD2TY + tx;
   const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
-  if (!tile_begin(S, tile_smem, status, tid, kVelTileTx)) return;
+  if (!tile_begin(S, tile_smem, status, tid, Smem::kTx)) return;
   if (blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) *A.step += 1;
   if (tid == 0) {
     tma_state<kStore>(S.p, &M.p_halo, &S.bar, j0 - 8, i0 - 8, 0, slot);
-    tma_state<kStore>(S.st, &M.st6, &S.bar, j0, i0, 1, slot);
-    tma_load_3d(S.mp, &M.maps6, &S.bar, j0, i0, kMapVel);
+    if constexpr (P == kTileExp) {
+      tma_state<kStore>(S.st, &M.st2, &S.bar, j0, i0, 1, slot);
+      tma_load_3d(S.mp, &M.mp3, &S.bar, j0, i0, kTileMapVel);
+    } else {
+      tma_state<kStore>(S.st, &M.st6, &S.bar, j0, i0, 1, slot);
+      tma_load_3d(S.mp, &M.mp6, &S.bar, j0, i0, kTileMapVel);
+      if constexpr (P == kTileAniso) tma_load_3d(S.mp[6], &M.mp5, &S.bar, j0, i0, kTileMapGradY);
+    }
     tma_load_2d(S.dc, &M.dc, &S.bar, j0, i0);
   }
   __syncthreads();   // barrier initialised before anyone polls it
@@ -109,52 +139,73 @@ __global__ void __launch_bounds__(256) vel2d_tile(const StepArgs A,
   const int i = i0 + ty, j = j0 + tx;
   if (i >= g.nx - kGhost || j >= g.ny - kGhost) return;
   const int64_t c = (int64_t)i * g.sx + j;
-  CellVelT<2, false> cv;
+  auto Q = [&](int q) { return S.mp[q][ty][tx]; };
+  using CV = typename std::conditional<P == kTileExp, CellVelExpT<2>,
+                                       CellVelT<2, P == kTileAniso>>::type;
+  CV cv;
   cv.dc = S.dc[ty][tx];
-  cv.rr = S.mp[0][ty][tx];
-  cv.iku[0] = S.mp[1][ty][tx];
-  cv.a1[0] = S.mp[2][ty][tx];
-  cv.b1[0] = S.mp[3][ty][tx];
-  cv.a2[0] = S.mp[4][ty][tx];
-  cv.b2[0] = S.mp[5][ty][tx];
+  cv.rr = Q(0);
+  if constexpr (P == kTileExp) {
+    cv.ae = Q(2);
 #pragma unroll
-  for (int a = 0; a < 2; ++a) {
-    cv.v[a] = S.st[a][ty][tx];
-    cv.s1[a] = S.st[2 + 2 * a][ty][tx];
-    cv.s2[a] = S.st[3 + 2 * a][ty][tx];
+    for (int a = 0; a < 2; ++a) cv.v[a] = S.st[a][ty][tx];
+  } else {
+#pragma unroll
+    for (int q = 0; q < CV::NA; ++q) {   // x set in maps 1-5, y set (anisotropic) in 6-10
+      cv.iku[q] = Q(1 + 5 * q);
+      cv.a1[q] = Q(2 + 5 * q);
+      cv.b1[q] = Q(3 + 5 * q);
+      cv.a2[q] = Q(4 + 5 * q);
+      cv.b2[q] = Q(5 + 5 * q);
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      cv.v[a] = S.st[a][ty][tx];
+      cv.s1[a] = S.st[2 + 2 * a][ty][tx];
+      cv.s2[a] = S.st[3 + 2 * a][ty][tx];
+    }
   }
   float cm[8], co;
   load_taps(A.m.taps, cv.dc, cm, co);
-  auto P = [&](int di, int dj) { return S.p[ty + 8 + di][tx + 8 + dj]; };
+  auto Pp = [&](int di, int dj) { return S.p[ty + 8 + di][tx + 8 + dj]; };
   float gx = 0.f, gy = 0.f;
 #pragma unroll
   for (int m = 1; m <= 8; ++m) {
-    gx = fmaf(cm[m - 1], P(m, 0) - P(-(m - 1), 0), gx);
-    gy = fmaf(cm[m - 1], P(0, m) - P(0, -(m - 1)), gy);
+    gx = fmaf(cm[m - 1], Pp(m, 0) - Pp(-(m - 1), 0), gx);
+    gy = fmaf(cm[m - 1], Pp(0, m) - Pp(0, -(m - 1)), gy);
   }
-  gx = fmaf(co, (P(1, 1) - P(0, 1)) + (P(1, -1) - P(0, -1)), gx);
-  gy = fmaf(co, (P(1, 1) - P(1, 0)) + (P(-1, 1) - P(-1, 0)), gy);
+  gx = fmaf(co, (Pp(1, 1) - Pp(0, 1)) + (Pp(1, -1) - Pp(0, -1)), gx);
+  gy = fmaf(co, (Pp(1, 1) - Pp(1, 0)) + (Pp(-1, 1) - Pp(-1, 0)), gy);
   const float gg[2] = {gx * g.inv_h[0], gy * g.inv_h[1]};
   cv.update_store(A, c, gg);
 }
 
-template <bool kBeta, int kMapPrs, bool kStore = false>
+template <int P, bool kBeta, bool kStore = false>
 __global__ void __launch_bounds__(256) prs2d_tile(const StepArgs A,
                                                   const __grid_constant__ Tile2Maps M, int slot) {
   pdl_entry();
   extern __shared__ __align__(128) unsigned char tile_smem[];
-  PrsTileSmem& S = *reinterpret_cast<PrsTileSmem*>(tile_smem);
+  using Smem = PrsTileSmem<P, kBeta>;
+  Smem& S = *reinterpret_cast<Smem*>(tile_smem);
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kD2TY + tx;
   const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
-  if (!tile_begin(S, tile_smem, status, tid, prs_tile_tx(kBeta))) return;
+  if (!tile_begin(S, tile_smem, status, tid, Smem::kTx)) return;
+  constexpr int kBetaPlane = Smem::kMp - 1;   // beta 2 dt, when present, is the last map plane
   if (tid == 0) {
     tma_state<kStore>(S.vx, &M.vx_halo, &S.bar, j0 - 4, i0 - 8, 1, slot + 1);
     tma_state<kStore>(S.vy, &M.vy_halo, &S.bar, j0 - 8, i0 - 1, 2, slot + 1);
     tma_state<kStore>(S.p, &M.st1, &S.bar, j0, i0, 0, slot);
-    tma_state<kStore>(S.phi, &M.st4, &S.bar, j0, i0, 7, slot);
-    tma_load_3d(S.mp, kBeta ? &M.maps7 : &M.maps6, &S.bar, j0, i0, kMapPrs);
+    if constexpr (P == kTileExp) {
+      tma_load_3d(S.mp[0], &M.mp1, &S.bar, j0, i0, kTileMapPrs);
+      tma_load_3d(S.mp[1], &M.mp1, &S.bar, j0, i0, kTileMapAexp);
+    } else {
+      tma_state<kStore>(S.phi, &M.st4, &S.bar, j0, i0, 7, slot);
+      tma_load_3d(S.mp, &M.mp6, &S.bar, j0, i0, kTileMapPrs);
+      if constexpr (P == kTileAniso) tma_load_3d(S.mp[6], &M.mp5, &S.bar, j0, i0, kTileMapDivY);
+    }
+    if constexpr (kBeta) tma_load_3d(S.mp[kBetaPlane], &M.mp1, &S.bar, j0, i0, kTileMapBeta);
     tma_load_2d(S.dc, &M.dc, &S.bar, j0, i0);
   }
   __syncthreads();
@@ -162,20 +213,30 @@ __global__ void __launch_bounds__(256) prs2d_tile(const StepArgs A,
   const int i = i0 + ty, j = j0 + tx;
   if (i < g.nx - kGhost && j < g.ny - kGhost) {
     const int64_t c = (int64_t)i * g.sx + j;
-    CellPrsT<2, kBeta, false> cp;
+    auto Q = [&](int q) { return S.mp[q][ty][tx]; };
+    using CP = typename std::conditional<P == kTileExp, CellPrsExpT<2, kBeta>,
+                                         CellPrsT<2, kBeta, P == kTileAniso>>::type;
+    CP cp;
     cp.dc = S.dc[ty][tx];
-    cp.dtk = S.mp[0][ty][tx];
-    cp.b2dt = kBeta ? S.mp[6][ty][tx] : 0.f;
-    cp.ikx[0] = S.mp[1][ty][tx];
-    cp.a1[0] = S.mp[2][ty][tx];
-    cp.b1[0] = S.mp[3][ty][tx];
-    cp.a2[0] = S.mp[4][ty][tx];
-    cp.b2[0] = S.mp[5][ty][tx];
+    cp.dtk = Q(0);
+    cp.b2dt = kBeta ? Q(kBetaPlane) : 0.f;
     cp.pc = S.p[ty][tx];
+    if constexpr (P == kTileExp) {
+      cp.ae = Q(1);
+    } else {
 #pragma unroll
-    for (int a = 0; a < 2; ++a) {
-      cp.f1[a] = S.phi[2 * a][ty][tx];
-      cp.f2[a] = S.phi[2 * a + 1][ty][tx];
+      for (int q = 0; q < CP::NA; ++q) {   // x set in maps 1-5, y set (anisotropic) in 6-10
+        cp.ikx[q] = Q(1 + 5 * q);
+        cp.a1[q] = Q(2 + 5 * q);
+        cp.b1[q] = Q(3 + 5 * q);
+        cp.a2[q] = Q(4 + 5 * q);
+        cp.b2[q] = Q(5 + 5 * q);
+      }
+#pragma unroll
+      for (int a = 0; a < 2; ++a) {
+        cp.f1[a] = S.phi[2 * a][ty][tx];
+        cp.f2[a] = S.phi[2 * a + 1][ty][tx];
+      }
     }
     float cm[8], co;
     load_taps(A.m.taps, cp.dc, cm, co);

@@ -26,13 +26,18 @@ void launch_stream2d_shape(fw_handle* h, cudaStream_t s) {
            s, h->args, h->tmaps2);
 }
 
-// TMA tile kernels (2D isotropic): one 32 x 8 tile per block, operands staged by TMA.
-template <bool kBeta>
+static_assert(kTileMapVel == kMRdtRho && kTileMapPrs == kMDtK && kTileMapBeta == kMBeta2dt &&
+                  kTileMapAexp == kMAu1 && kTileMapGradY == kMaps && kTileMapDivY == kMaps + 5,
+              "map slots read by the tile kernels");
+
+// TMA tile kernels (2D, cell physics P): one 32 x 8 tile per block, operands staged by TMA.
+template <int P, bool kBeta>
 void launch_tile2d(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
   dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
-  launch_k(vel2d_tile<kMRdtRho>, grid, block, sizeof(VelTileSmem), s, h->args, h->tmaps_t, 0);
-  launch_k(prs2d_tile<kBeta, kMDtK>, grid, block, sizeof(PrsTileSmem), s, h->args, h->tmaps_t, 0);
+  launch_k(vel2d_tile<P>, grid, block, sizeof(VelTileSmem<P>), s, h->args, h->tmaps_t, 0);
+  launch_k(prs2d_tile<P, kBeta>, grid, block, sizeof(PrsTileSmem<P, kBeta>), s, h->args,
+           h->tmaps_t, 0);
 }
 
 template <bool kBeta>
@@ -54,7 +59,6 @@ void launch_typed(fw_handle* h, cudaStream_t s) {
     static_assert(kNumShapes2D == 8, "one case per 2D kernel shape");
     switch (h->shape2d) {
       case 0:
-      case kTileShape:          // tile kernels exist for the isotropic engine only (launch_nd)
       case kPersistentShape: {  // the persistent shape issues the direct kernels when captured
         dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
         launch_k(vel2d_direct<CV>, grid, block, 0, s, h->args);
@@ -103,6 +107,14 @@ void launch_stream3d(fw_handle* h, cudaStream_t s) {
 
 template <int ND, bool kBeta>
 void launch_nd(fw_handle* h, cudaStream_t s) {
+  if constexpr (ND == 2) {
+    if (kShapes2D[h->shape2d].tile) {
+      if (h->exp) launch_tile2d<kTileExp, kBeta>(h, s);
+      else if (h->aniso) launch_tile2d<kTileAniso, kBeta>(h, s);
+      else launch_tile2d<kTileIso, kBeta>(h, s);
+      return;
+    }
+  }
   if (h->exp) {
     launch_typed<ND, CellVelExpT<ND>, CellPrsExpT<ND, kBeta>, 3>(h, s);
   } else if (h->aniso) {
@@ -114,10 +126,6 @@ void launch_nd(fw_handle* h, cudaStream_t s) {
         return;
       }
     } else {
-      if (kShapes2D[h->shape2d].tile) {
-        launch_tile2d<kBeta>(h, s);
-        return;
-      }
       if (h->stream2d && kShapes2D[h->shape2d].ty > 0) {
         launch_stream2d<kBeta>(h, s);
         return;
@@ -310,8 +318,9 @@ int encode_tile2_maps(fw_handle* h, Tile2Maps* m, float* store, int slots) {
   const cuuint64_t str[3] = {row, field, field * ns};
   const cuuint64_t d_dc[2] = {pitch, nx};
   const cuuint32_t bp[4] = {48, 24, 1, 1}, bx[4] = {40, 24, 1, 1}, by[4] = {48, 10, 1, 1};
-  const cuuint32_t b1[4] = {kD2TY, kD2TX, 1, 1}, b4[4] = {kD2TY, kD2TX, 4, 1};
-  const cuuint32_t b6[4] = {kD2TY, kD2TX, 6, 1}, b7[3] = {kD2TY, kD2TX, 7};
+  const cuuint32_t b1[4] = {kD2TY, kD2TX, 1, 1}, b2[4] = {kD2TY, kD2TX, 2, 1};
+  const cuuint32_t b3[4] = {kD2TY, kD2TX, 3, 1}, b4[4] = {kD2TY, kD2TX, 4, 1};
+  const cuuint32_t b5[4] = {kD2TY, kD2TX, 5, 1}, b6[4] = {kD2TY, kD2TX, 6, 1};
   const cuuint32_t bdc[2] = {kD2TY, kD2TX};
   float* base = slots > 0 ? store : h->state;
   const cuuint32_t r = slots > 0 ? 4 : 3;
@@ -320,10 +329,13 @@ int encode_tile2_maps(fw_handle* h, Tile2Maps* m, float* store, int slots) {
       (st = encode_map(h, &m->vx_halo, base, r, d_st, str, bx)) ||
       (st = encode_map(h, &m->vy_halo, base, r, d_st, str, by)) ||
       (st = encode_map(h, &m->st1, base, r, d_st, str, b1)) ||
+      (st = encode_map(h, &m->st2, base, r, d_st, str, b2)) ||
       (st = encode_map(h, &m->st4, base, r, d_st, str, b4)) ||
       (st = encode_map(h, &m->st6, base, r, d_st, str, b6)) ||
-      (st = encode_map(h, &m->maps6, h->maps, 3, d_mp, str, b6)) ||
-      (st = encode_map(h, &m->maps7, h->maps, 3, d_mp, str, b7)) ||
+      (st = encode_map(h, &m->mp1, h->maps, 3, d_mp, str, b1)) ||
+      (st = encode_map(h, &m->mp3, h->maps, 3, d_mp, str, b3)) ||
+      (st = encode_map(h, &m->mp5, h->maps, 3, d_mp, str, b5)) ||
+      (st = encode_map(h, &m->mp6, h->maps, 3, d_mp, str, b6)) ||
       (st = encode_map(h, &m->dc, h->dcmap, 2, d_dc, str, bdc, CU_TENSOR_MAP_DATA_TYPE_INT32)))
     return st;
   return FW_OK;
@@ -334,7 +346,7 @@ int set_shape2d(fw_handle* h, int k) {
     int st = encode_march2_maps(h, (uint32_t)kShapes2D[k].ty, &h->tmaps2);
     if (st) return st;
   }
-  const bool tile = kShapes2D[k].tile && !h->aniso && !h->exp;
+  const bool tile = kShapes2D[k].tile;
   if (tile) {
     int st = encode_tile2_maps(h, &h->tmaps_t, nullptr, 0);
     if (st) return st;

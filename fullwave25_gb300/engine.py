@@ -229,17 +229,21 @@ class Engine:
         fptr = lambda t: C.cast(C.c_void_p(t.data_ptr()), _FP) if t.numel() else None  # noqa: E731
         iptr = lambda t: C.cast(C.c_void_p(t.data_ptr()), _IP) if t.numel() else None  # noqa: E731
         m = inp.maps
-        for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS):
+        exp = "a_exp" in m   # exponential-attenuation engine: no relaxation maps
+        names = ("c", "rho", "K", "beta", *(("a_exp",) if exp else ISOTROPIC_MAPS))
+        for k in names:
             assert m[k].dtype == torch.float32 and m[k].is_contiguous() and m[k].is_cuda, k
         fields = FwFields(
             d=fptr(keep["d"]), dmap=fptr(keep["dmap"]), dcmap=iptr(inp.dcmap),
             icc=iptr(inp.icc), outc=iptr(inp.outc), icczero=iptr(inp.icczero),
             icmat=fptr(inp.icmat), on_device=1,
-            **{k: fptr(m[k]) for k in ("c", "rho", "K", "beta", *ISOTROPIC_MAPS)})
+            **{k: fptr(m[k]) for k in names if k != "a_exp"})
         # the tensors were produced on the caller's current stream: wait for that stream only,
         # so that work on other streams (other simulations) keeps running
         torch.cuda.current_stream(dev).synchronize()
-        if "kappay" in m:
+        if exp:
+            self._call("fw_set_fields_exp", C.byref(fields), fptr(m["a_exp"]))
+        elif "kappay" in m:
             for k in anisotropic_extra_maps(inp.ndim):
                 assert m[k].dtype == torch.float32 and m[k].is_contiguous() and m[k].is_cuda, k
             an = FwFieldsAniso(**{k: fptr(m[k]) for k in anisotropic_extra_maps(inp.ndim)})

@@ -69,21 +69,48 @@ def plain_2d_problem(shape=(768, 512), nt: int = 4000, f0: float = 3e6, ppw: int
     return grid, medium, source, sensor, (n_pml, n_transition)
 
 
-def plain_2d_inputs(**kw) -> EngineInputs:
-    """Engine inputs (PML-extended, 944 x 688 by default) of the plain 2D forward workload."""
+PHYSICS = ("isotropic", "aniso", "exp")
+
+
+def plain_2d_inputs(physics: str = "isotropic", **kw) -> EngineInputs:
+    """Engine inputs (PML-extended, 944 x 688 by default) of the plain 2D forward workload.
+
+    ``physics``: "isotropic" (the two-mechanism relaxation engine), "aniso" (the same medium
+    through the anisotropic-relaxation PML builder, one set of maps per derivative direction, as
+    ``Solver(use_isotropic_relaxation=False)``), or "exp" (the exponential-attenuation engine
+    with alpha0 of the same medium; its builder pads by PML + 8 cells only: 864 x 608)."""
     grid, medium, source, sensor, (n_pml, n_tr) = plain_2d_problem(**kw)
-    b = PMLBuilder(grid, medium, source, sensor, n_pml_layer=n_pml, n_transition_layer=n_tr)
+    if physics == "exp":
+        from .exponential import PMLBuilderExponentialAttenuation  # noqa: PLC0415
+        from .inputs import build_inputs_exponential  # noqa: PLC0415
+
+        c, rho, a0, _ = ellipse_medium_2d(grid.shape, grid.dx, seed=kw.get("seed", 0))
+        b = PMLBuilderExponentialAttenuation(grid, c, rho, a0, np.zeros(grid.shape), source,
+                                             sensor, n_pml_layer=n_pml)
+        return build_inputs_exponential(b.extended_grid, b.run(), b.extended_source,
+                                        b.extended_sensor)
+    if physics not in PHYSICS:
+        raise ValueError(f"unknown physics {physics!r}")
+    iso = physics == "isotropic"
+    medium.use_isotropic_relaxation = iso   # as the solver sets it before building
+    b = PMLBuilder(grid, medium, source, sensor, n_pml_layer=n_pml, n_transition_layer=n_tr,
+                   use_isotropic_relaxation=iso)
     return build_inputs(b.extended_grid, b.run(), b.extended_source, b.extended_sensor)
 
 
-def algorithmic_bytes_per_cell(ndim: int, beta: bool = False) -> int:
+def algorithmic_bytes_per_cell(ndim: int, beta: bool = False, physics: str = "isotropic") -> int:
     """Algorithmic HBM bytes of one cell-update: 4 * (2 S + M).
 
-    S state fields read and written once per step (p, ndim velocities, 2 ndim gradient and
-    2 ndim divergence memory variables) and M read-only maps read once per step (rho, K,
-    kappau, kappax, four a/b pairs, dcmap = 12, plus beta when it is not zero):
-    136 B in 2D, 176 B in 3D.
+    Isotropic engine: S state fields read and written once per step (p, ndim velocities, 2 ndim
+    gradient and 2 ndim divergence memory variables) and M = 12 read-only maps read once per
+    step, the figure of the workload definition (rho, K, kappau, kappax, four a/b pairs and the
+    tap index; plus beta when it is not zero): 136 B in 2D, 176 B in 3D. Anisotropic engine: 10
+    more maps per further axis (kappa, two a/b pairs for each derivative direction): 176 B in
+    2D, 256 B in 3D. Exponential engine: S = p and the velocities, M = rho, K, a_exp and the tap
+    index: 40 B in 2D, 48 B in 3D.
     """
+    if physics == "exp":
+        return 4 * (2 * (1 + ndim) + 4 + (1 if beta else 0))
     s = 1 + ndim + 4 * ndim
-    m = 12 + (1 if beta else 0)
+    m = 12 + (1 if beta else 0) + (10 * (ndim - 1) if physics == "aniso" else 0)
     return 4 * (2 * s + m)

@@ -240,10 +240,36 @@ def layered_medium_3d(shape, dx, seed, device, n_boundary=0):
     return c, rho, layer
 
 
+def exp_attenuation_t(alpha0, grid, n_body: int):
+    """``a_exp`` of the exponential-attenuation engine on the device: the amplitude fraction
+    kept per update, ``exp(-dt * alpha0 / 2 * f0[MHz] * c0 / (1e-2 * 8.686))``
+    (medium.py:1068-1090), scaled by ``1 - r`` inside the ``n_body``-cell padding, ``r`` the
+    normalised distance into it (pml_builder.py:1800-1935; :func:`exponential.body_mask`)."""
+    torch = _torch()
+    np_factor = -10 * np.log10(np.exp(-1))
+    texp = alpha0 / 2.0 * (grid.f0 / 1e6) * grid.c0 / (1e-2 * np_factor)
+    a = torch.exp(-grid.dt * texp)
+    r2 = torch.zeros((), dtype=torch.float64, device=alpha0.device)
+    for ax, n in enumerate(a.shape):
+        idx = torch.arange(1, n + 1, dtype=torch.float64, device=alpha0.device)
+        r = torch.where(idx <= n_body, n_body - idx + 1,
+                        torch.where(idx > n - n_body, idx - (n - n_body), torch.zeros_like(idx)))
+        r2 = r2 + (r ** 2).reshape([-1 if b == ax else 1 for b in range(a.ndim)])
+    mask = torch.sqrt(r2)
+    if float(mask.max()) > 0:
+        mask = mask / mask.max()
+    return a * (1 - mask)
+
+
 def plain_3d_device_inputs(seed: int = 0, shape=(512, 512, 512), nt: int = 3000,
                            f0: float = 2e6, ppw: int = 10, cfl: float = 0.2, n_pml: int = 32,
                            n_transition: int = 32, device=None, sensor_plane: int = 256,
-                           element_height: int = 32) -> DeviceInputs:
+                           element_height: int = 32, physics: str = "isotropic") -> DeviceInputs:
+    """The plain 3D forward workload built on the device. ``physics``: "isotropic", "aniso"
+    (one map set per derivative direction; the reference's anisotropic PML builder gives every
+    direction the ramps of every axis, so the sets equal the isotropic ones,
+    pml_builder.py:130-170), or "exp" (exponential attenuation from each layer's alpha0, on the
+    same extended grid, ``a_exp`` ramped to zero over the boundary cells)."""
     torch = _torch()
     t_start = time.perf_counter()
     device = device or torch.device("cuda", torch.cuda.current_device())
@@ -258,6 +284,9 @@ def plain_3d_device_inputs(seed: int = 0, shape=(512, 512, 512), nt: int = 3000,
                                     for k in keys]) for l in LAYERS])
     plt = torch.as_tensor(per_layer, dtype=torch.float64, device=device)
     lid = layer.long()
+    if physics == "exp":
+        a0_tab = torch.tensor([l[3] for l in LAYERS], dtype=torch.float64, device=device)
+        a_exp = exp_attenuation_t(a0_tab[lid], grid, nb).to(torch.float32)
     params = {k: plt[:, i][lid] for i, k in enumerate(keys)}
     # mechanism sort by time constant d/kappa + alpha (fullwave/medium.py:121-209)
     for op in ("x1", "x2"):
@@ -279,6 +308,18 @@ def plain_3d_device_inputs(seed: int = 0, shape=(512, 512, 512), nt: int = 3000,
             names[f"bpml{ax}{nu}"] = f"b_pml_{ax}{nu}"
     maps = {k: fw2[v].to(torch.float32).contiguous() for k, v in names.items()}
     del fw2
+    if physics == "aniso":
+        from .inputs import DIV_AXIS_LETTER, GRAD_AXIS_LETTER, axis_maps  # noqa: PLC0415
+
+        for a in (1, 2):
+            for src, dst in ((GRAD_AXIS_LETTER[0], GRAD_AXIS_LETTER[a]),
+                             (DIV_AXIS_LETTER[0], DIV_AXIS_LETTER[a])):
+                for ks, kd in zip(axis_maps(src), axis_maps(dst)):
+                    maps[kd] = maps[ks].clone()
+    elif physics == "exp":
+        maps = {"a_exp": a_exp}
+    elif physics != "isotropic":
+        raise ValueError(f"unknown physics {physics!r}")
     maps["K"] = (c * c * rho).to(torch.float32)
     maps["rho"] = rho.to(torch.float32)
     maps["beta"] = torch.zeros(ext, dtype=torch.float32, device=device)
@@ -325,11 +366,11 @@ def to_host_inputs(dinp: DeviceInputs):
                         outc=dinp.outc.cpu().numpy(), icczero=dinp.icczero.cpu().numpy())
 
 
-def plain_3d_host_sample(edge: int = 48, nt: int = 3000):
+def plain_3d_host_sample(edge: int = 48, nt: int = 3000, physics: str = "isotropic"):
     """A small block of the plain 3D medium (same layers, PML 8 + transition 8) as numpy inputs,
     used to time the FP64 oracle on the host."""
     torch = _torch()
     d = plain_3d_device_inputs(shape=(edge, edge, edge), nt=nt, n_pml=8, n_transition=8,
                                device=torch.device("cpu") if not torch.cuda.is_available()
-                               else None, sensor_plane=16, element_height=8)
+                               else None, sensor_plane=16, element_height=8, physics=physics)
     return to_host_inputs(d)

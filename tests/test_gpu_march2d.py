@@ -70,9 +70,7 @@ def test_every_march_shape_equals_direct_bitwise(engine_lib, cuda, case):
     for k in MARCH_SHAPES:
         with _engine(inp, FWGB_SHAPE2D=k) as em:
             got = em.run()
-            # the tile kernels cover the isotropic engine; the others run the direct kernels
-            tile_direct = k == 7 and case in ("2d_aniso", "2d_exp")
-            assert em.kernel_variant == ("direct" if tile_direct else VARIANT[k])
+            assert em.kernel_variant == VARIANT[k]
         np.testing.assert_array_equal(got, ref, err_msg=f"{case}: shape {k}")
 
 

@@ -92,3 +92,28 @@ def test_relaxation_coefficients_formula():
     eb = np.exp(-(d / k + al) * dt)
     np.testing.assert_allclose(b, eb, rtol=1e-12)
     np.testing.assert_allclose(a, d / (k * (d + k * al) + 1e-10) * (eb - 1), rtol=1e-12)
+
+
+def test_plain_2d_workload_physics_variants():
+    """The plain 2D workload through the anisotropic-relaxation builder (every direction's map set
+    equals the isotropic set, the reference builder's structure) and through the
+    exponential-attenuation builder (PML 40 + 8 ghost cells, a_exp in [0, 1))."""
+    from fullwave25_gb300.inputs import anisotropic_extra_maps
+    from fullwave25_gb300.workloads import algorithmic_bytes_per_cell, plain_2d_inputs
+
+    iso = plain_2d_inputs()
+    an = plain_2d_inputs(physics="aniso")
+    an.validate()
+    assert not an.isotropic and set(an.maps) == set(iso.maps) | set(anisotropic_extra_maps(2))
+    for k in iso.maps:
+        np.testing.assert_array_equal(an.maps[k], iso.maps[k])
+    np.testing.assert_array_equal(an.maps["apmly1"], iso.maps["apmlx1"])
+    ex = plain_2d_inputs(physics="exp")
+    ex.validate()
+    assert ex.exponential and ex.shape == (864, 608)
+    assert 0 <= ex.maps["a_exp"].min() and ex.maps["a_exp"].max() < 1
+    np.testing.assert_array_equal(ex.icmat, iso.icmat)
+    assert [algorithmic_bytes_per_cell(2, physics=p) for p in ("isotropic", "aniso", "exp")] == \
+        [136, 176, 40]
+    assert [algorithmic_bytes_per_cell(3, physics=p) for p in ("isotropic", "aniso", "exp")] == \
+        [176, 256, 48]

@@ -58,3 +58,55 @@ def test_small_plain_3d_workload_on_cpu():
     assert inp.icc.shape[0] == 24 * 8 and inp.outc.shape[0] == 16 * 16
     assert np.isfinite(np.stack([v for v in inp.maps.values()])).all()
     assert inp.dcmap.min() == 0 and inp.dcmap.max() == inp.dmap.shape[2] - 1
+
+
+def test_anisotropic_host_builder_gives_every_direction_the_same_maps():
+    """The anisotropic PML builder ramps every direction's maps along every axis from the same
+    gradient / divergence parameters, so the per-direction sets equal the first direction's:
+    what the device-side anisotropic workload replicates."""
+    from fullwave25_gb300.grid import Grid
+    from fullwave25_gb300.medium import MediumRelaxationMaps
+    from fullwave25_gb300.pml import PMLBuilder
+    from fullwave25_gb300.source import Sensor, Source
+    from golden_io import load_case
+
+    z = load_case("3d_small")
+    shape = tuple(int(v) for v in z["shape"])
+    g = Grid.from_cells(shape, f0=float(z["f0"]), nt=int(z["nt"]), ppw=int(z["ppw"]),
+                        cfl=float(z["cfl"]))
+    relax = {k[6:]: z[k] for k in z.files if k.startswith("relax/")}
+    med = MediumRelaxationMaps(g, z["c"], z["rho"], z["beta"], relax)
+    med.use_isotropic_relaxation = False
+    b = PMLBuilder(g, med, Source(z["p0"], z["src_mask"]), Sensor(z["sens_mask"]),
+                   n_pml_layer=int(z["n_pml"]), n_transition_layer=int(z["n_transition"]),
+                   use_isotropic_relaxation=False)
+    out = b.run().relaxation_param_dict_for_fw2
+    for first, others in (("u", ("w", "v")), ("x", ("y", "z"))):
+        for o in others:
+            for key in ("kappa_{}", "a_pml_{}1", "b_pml_{}1", "a_pml_{}2", "b_pml_{}2"):
+                np.testing.assert_array_equal(out[key.format(o)], out[key.format(first)])
+
+
+def test_physics_variants_of_the_3d_workload():
+    from fullwave25_gb300.exponential import body_mask, db_mhz_cm_to_a_exp
+    from fullwave25_gb300.grid import Grid
+    from fullwave25_gb300.inputs import anisotropic_extra_maps
+    from fullwave25_gb300.workloads3d import exp_attenuation_t, plain_3d_host_sample
+
+    iso = plain_3d_host_sample(edge=24, nt=50)
+    an = plain_3d_host_sample(edge=24, nt=50, physics="aniso")
+    an.validate()
+    assert set(an.maps) == set(iso.maps) | set(anisotropic_extra_maps(3))
+    np.testing.assert_array_equal(an.maps["kappav"], iso.maps["kappau"])
+    np.testing.assert_array_equal(an.maps["bpmlz2"], iso.maps["bpmlx2"])
+    ex = plain_3d_host_sample(edge=24, nt=50, physics="exp")
+    ex.validate()
+    assert set(ex.maps) == {"c", "rho", "K", "beta", "a_exp"}
+    a = ex.maps["a_exp"]
+    assert a.shape == ex.shape and 0 <= a.min() and a.max() < 1 and a[36, 36, 36] > 0.99
+    # the device formula against the host builder's
+    g = Grid.from_cells((20, 18, 16), f0=2e6, nt=10, ppw=10, cfl=0.2)
+    alpha = np.random.default_rng(0).uniform(0.2, 1.2, size=(20, 18, 16))
+    ref = db_mhz_cm_to_a_exp(alpha, g) * (1 - body_mask(alpha.shape, 5))
+    got = exp_attenuation_t(torch.as_tensor(alpha), g, 5).numpy()
+    np.testing.assert_allclose(got, ref, rtol=1e-14, atol=1e-300)
