@@ -605,6 +605,28 @@ def run_serve(args):
     fifo = serve_fifo(reqs)
     for r in reqs:
         r.result = None
+    # one at a time through the host-side API (the reference's call sequence: NumPy
+    # pre-processing, engine creation and upload, solve, traces back) on the stream's first
+    # forward requests; gradient requests have no host-side path and are left out, so the ratio
+    # against the whole mixed stream understates the served advantage
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.workloads_batch import batch_inputs_host
+
+    host_reqs = [r for r in reqs if r.kind == "forward"][:args.host_sample]
+    host_s, host_err = [], []
+    for r in host_reqs:
+        t0 = time.perf_counter()
+        with Engine(batch_inputs_host(r.rid, scale=scale), validate=False) as e:
+            tr = e.run()
+        host_s.append(time.perf_counter() - t0)
+        host_err.append(float(np.linalg.norm(tr - r.traces) / max(np.linalg.norm(r.traces), 1e-30)))
+    host_api = ({"requests": [r.rid for r in host_reqs],
+                 "sims_per_s": len(host_s) / sum(host_s),
+                 "continuous_over_host_api": cont["sims_per_s"] / (len(host_s) / sum(host_s)),
+                 "rel_l2_vs_served_traces_max": max(host_err),
+                 "api": "NumPy pre-processing (relaxation lookup, PML builder) + Engine "
+                        "(fw_create, fw_set_fields host) + fw_run with host traces, per request"}
+                if host_s else None)
     n_grad = int((kinds == "gradient").sum())
     line = {"metric": "simulations/s (serving stream)", "value": cont["sims_per_s"],
             "unit": "sims/s", "n_gpus": 1, "steps": 1, "warmup": 1,
@@ -619,6 +641,7 @@ def run_serve(args):
                        "requests": len(reqs), "gradient_requests": n_grad,
                        "max_active_cells": cap},
             "continuous": cont, "fifo_one_at_a_time": fifo,
+            "one_by_one_host_api_forward_sample": host_api,
             "sims_per_s_ratio": cont["sims_per_s"] / fifo["sims_per_s"],
             "clocks": clocks.summary()}
     print(json.dumps(line), flush=True)
@@ -706,7 +729,8 @@ def main():
                     help="serve2d: fraction of gradient requests")
     ap.add_argument("--batch", type=int, default=64, help="simulations per rank (batch2d)")
     ap.add_argument("--host-sample", type=int, default=8,
-                    help="batch2d: instances also run one by one through the host-side API")
+                    help="batch2d / serve2d: instances (forward requests) also run one by one "
+                         "through the host-side API")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--grid", type=int, default=0,
                     help="3D workload edge in cells (default 512; smaller for profiling); "
