@@ -432,6 +432,9 @@ def run_batch(args):
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     ids = rank_instances(rank, world, args.batch)
     torch.zeros(1, device=dev)  # context creation outside the timed build
+    # process warm-up outside the timed build: the first use of every builder and engine kernel
+    # (module loading), on a small instance that is not part of the batch
+    batch_instance(ids[0], scale=0.1).make_engine().close()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     insts = [batch_instance(i) for i in ids]

@@ -136,15 +136,16 @@ def batch_instance(i: int, device=None, n_pml: int = 40, n_transition: int = 40,
     cmin, cmax = float(c.min()), float(c.max())
     dmap = coefficients.d_map(np.array([cmin, cmax]), grid.dt, grid.dx, is_3d=False)
     dcmap = (torch.round(c + 1e-9) - round(cmin + 1e-9)).to(torch.int32).contiguous()
-    # transmit: element e covers lateral cells [e*w, (e+1)*w) of depth row 0
+    # transmit: element e covers lateral cells [e*w, (e+1)*w) of depth row 0; the element
+    # signals (all delays at once) go to the device, which repeats them over the element's cells
     w = ny // N_ELEMENTS
     delays = transmit_delays(spec, grid.dx)
-    sig = np.stack([gaussian_modulated_sinusoidal_signal(
+    sig = gaussian_modulated_sinusoidal_signal(
         nt=nt, duration=grid.duration, ncycles=2, drop_off=2, f0=spec["f0"], p0=1e6,
-        delay_sec=float(d)) for d in delays]).astype(np.float32)
+        delay_sec=delays[:, None]).astype(np.float32)
     cols = np.arange(N_ELEMENTS * w)
     icc = np.stack([np.zeros_like(cols), cols], axis=1) + nb
-    icmat = torch.as_tensor(np.repeat(sig, w, axis=0), device=device)
+    icmat = torch.as_tensor(sig, device=device).repeat_interleave(w, dim=0)
     outc = np.stack([np.ones(ny, dtype=np.int64), np.arange(ny)], axis=1) + nb
     i32 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.int32), device=device)  # noqa: E731
     d = DeviceInputs(shape=(nx + 2 * nb, ny + 2 * nb), nt=nt, spacing=(grid.dx, grid.dy),
