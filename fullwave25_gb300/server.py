@@ -100,7 +100,8 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
                      max_active_cells: int | None = None) -> dict:
     """Run ``requests`` with continuous batching; returns summary stats.
 
-    Forward requests join the group engine between blocks of ``chunk_steps`` steps; gradient
+    Forward requests are built on their own stream while the group runs a block and join the
+    group engine between blocks of ``chunk_steps`` steps; gradient
     requests run on up to ``gradient_workers`` threads with a CUDA stream each. Admission is FIFO
     by arrival while the device-memory budget allows (a request larger than the budget runs
     alone) and, with ``max_active_cells``, while the group's forward requests hold at most that
@@ -130,11 +131,17 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
         finally:
             r.finished = clock() - t0
 
-    while pending or active or running:
+    build = torch.cuda.Stream()   # forward requests are built here, overlapping the group's steps
+    joining: list = []            # built forward requests that join the group at the next block
+
+    def admit():
+        """Admit arrived requests in FIFO order while the memory budget (and the cell cap)
+        allow: gradient requests start on a worker stream, forward requests are built."""
+        nonlocal used, cells_active
         now = clock() - t0
-        # admit arrived requests in FIFO order while the memory budget allows
         while pending and pending[0].arrival <= now and (
-                used + pending[0].bytes_needed <= budget_bytes or not (active or running)):
+                used + pending[0].bytes_needed <= budget_bytes
+                or not (active or joining or running)):
             r = pending[0]
             if r.kind == "gradient":
                 if not free_streams:
@@ -144,22 +151,27 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
                 s = free_streams.pop()
                 running[pool.submit(gradient, r, s)] = (r, s)
             else:
-                if (max_active_cells is not None and active
+                if (max_active_cells is not None and (active or joining)
                         and cells_active + r.cells > max_active_cells):
                     break
                 pending.pop(0)
                 cells_active += r.cells
-                with torch.cuda.stream(main):
+                with torch.cuda.stream(build):
                     eng = Engine(r.build(), validate=False)
                 r.admitted = clock() - t0
-                active.append((r, eng))
+                joining.append((r, eng))
             used += r.bytes_needed
+
+    while pending or active or joining or running:
+        admit()
         # retire finished gradient requests
         for fut in [f for f in running if f.done()]:
             r, s = running.pop(fut)
             fut.result()  # re-raise a worker's error here
             free_streams.append(s)
             used -= r.bytes_needed
+        active += joining
+        joining = []
         if not active:
             # idle until the next arrival or a gradient finishes
             wait = (pending[0].arrival - (clock() - t0)) if pending else 0.01
@@ -172,6 +184,7 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
         else:
             group.set_members(engines)
         group.advance(chunk_steps, main.cuda_stream)
+        admit()            # requests arriving meanwhile are built while the block runs
         main.synchronize()
         n_chunks += 1
         still = []
@@ -185,7 +198,7 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
             else:
                 still.append((r, e))
         active = still
-        if not active and group is not None:
+        if not active and not joining and group is not None:
             group.set_members([])
     pool.shutdown()
     if group is not None:
