@@ -170,7 +170,7 @@ FWGB_API int fw_device_bytes(const fw_handle *h, uint64_t *bytes);
  * halo planes in 3D, halo rows in 2D), 2 = the persistent 2D kernel (one cooperative launch per
  * fw_advance, grid barriers between the velocity and pressure phases), 3 = the 3D plane march
  * with the point-wise state and maps staged by TMA as well (isotropic engine), 4 = the 2D tile
- * kernels (one 32 x 8 tile per block, every operand staged by TMA; isotropic engine). 3D handles
+ * kernels (one 32 x 8 tile per block, every operand staged by TMA; every cell physics). 3D handles
  * use 3
  * (isotropic; 1 with FWGB_STREAM3D=0) or 1 (anisotropic, exponential) unless the environment
  * variable FWGB_VARIANT=direct was set when the handle was created. 2D handles
