@@ -25,6 +25,7 @@ int encode_adj_maps(fw_handle* h, AdjMaps* M) {
   const cuuint64_t d_st[4] = {pitch, nx, (cuuint64_t)ns, (cuuint64_t)h->adj_every + 1};
   const cuuint64_t s4[3] = {row, field, field * ns};
   const cuuint64_t d_dc[2] = {pitch, nx};
+  const cuuint64_t s_dc[1] = {(cuuint64_t)h->pitch * 2};
   const cuuint32_t b1[3] = {kD2TY, kD2TX, 1}, b4[3] = {kD2TY, kD2TX, 4}, b6[3] = {kD2TY, kD2TX, 6};
   const cuuint32_t bhx[3] = {kHXW, kHXR, 1}, bhy[3] = {kHYW, kHYR, 1};
   const cuuint32_t bs4[4] = {kD2TY, kD2TX, 4, 1}, bsx[4] = {kHXW, kHXR, 1, 1};
@@ -41,7 +42,7 @@ int encode_adj_maps(fw_handle* h, AdjMaps* M) {
       (st = encode_map(h, &M->st_vx, h->adj_store, 4, d_st, s4, bsx)) ||
       (st = encode_map(h, &M->st_vy, h->adj_store, 4, d_st, s4, bsy)) ||
       (st = encode_map(h, &M->st_p, h->adj_store, 4, d_st, s4, bsp)) ||
-      (st = encode_map(h, &M->dc, h->dcmap, 2, d_dc, s3, bdc, CU_TENSOR_MAP_DATA_TYPE_INT32)))
+      (st = encode_map(h, &M->dc, h->dcmap, 2, d_dc, s_dc, bdc, CU_TENSOR_MAP_DATA_TYPE_UINT16)))
     return st;
   return FW_OK;
 }

@@ -158,6 +158,8 @@ int check_desc(const fw_desc* d) {
   if (d->nt < 0 || d->nt_ic < 0 || d->mod_t < 1 || d->ncoords < 0 || d->ncoordsout < 0 ||
       d->ncoordszero < 0 || d->ndmap < 1)
     return fail(nullptr, FW_ERR_ARGUMENT, "negative count or modT/ndmap < 1");
+  if (d->ndmap > 65535)   // the engine keeps the tap-set index of a cell in 16 bits
+    return fail(nullptr, FW_ERR_ARGUMENT, "ndmap = %d: at most 65535 tap sets", d->ndmap);
   if (!(d->dt > 0.f) || !(d->dx > 0.f) || !(d->dy > 0.f) || (d->ndim == 3 && !(d->dz > 0.f)))
     return fail(nullptr, FW_ERR_ARGUMENT, "grid spacing and time step must be positive");
   if (d->isotropic != 0 && d->isotropic != 1)
@@ -229,7 +231,7 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   const size_t cells = (size_t)h->ncells_padded;
   if ((st = alloc((void**)&h->state, cells * n_state(h->ndim) * sizeof(float))) ||
       (st = alloc((void**)&h->maps, cells * n_maps(h) * sizeof(float))) ||
-      (st = alloc((void**)&h->dcmap, cells * sizeof(int32_t))) ||
+      (st = alloc((void**)&h->dcmap, cells * sizeof(uint16_t))) ||
       (st = alloc((void**)&h->taps, (size_t)desc->ndmap * kTapStride * sizeof(float))) ||
       (st = alloc((void**)&h->icmat_t, (size_t)desc->ncoords * desc->nt_ic * sizeof(float))) ||
       (st = alloc((void**)&h->traces, (size_t)h->n_out * desc->ncoordsout * sizeof(float))) ||
@@ -244,7 +246,7 @@ int fw_create(const fw_desc* desc, fw_handle** out) {
   // zero everything once: ghost cells, padding and memory variables start at zero
   if (cudaMemset(h->state, 0, cells * n_state(h->ndim) * sizeof(float)) != cudaSuccess ||
       cudaMemset(h->maps, 0, cells * n_maps(h) * sizeof(float)) != cudaSuccess ||
-      cudaMemset(h->dcmap, 0, cells * sizeof(int32_t)) != cudaSuccess ||
+      cudaMemset(h->dcmap, 0, cells * sizeof(uint16_t)) != cudaSuccess ||
       cudaMemset(h->step, 0, sizeof(int) * 4) != cudaSuccess) {
     fw_destroy(h);
     return fail(nullptr, FW_ERR_CUDA, "initial cudaMemset failed");
@@ -525,7 +527,11 @@ int set_fields_impl(fw_handle* h, const fw_fields* f, const fw_fields_aniso* an,
       kappa_maps.push_back(axis_map(a, 5));
     }
   }
-  if ((st = upload_grid(h, h->dcmap, dcm.data(), sizeof(int32_t), false, s))) return st;
+  {  // 16-bit tap-set indices (validated above: 0 <= dcmap < ndmap <= 65535)
+    std::vector<uint16_t> dc16(dcm.begin(), dcm.end());
+    if ((st = upload_grid(h, h->dcmap, dc16.data(), sizeof(uint16_t), false, s))) return st;
+    FW_CUDA(h, cudaStreamSynchronize(s));   // the host copy is freed on return
+  }
   transform_maps<<<1024, 256, 0, s>>>(map_field(h, kMRdtRho), map_field(h, kMDtK),
                                       map_field(h, kMBeta2dt), h->ncells_padded, d.dt);
   for (int idx : kappa_maps) invert_map<<<1024, 256, 0, s>>>(map_field(h, idx), h->ncells_padded);

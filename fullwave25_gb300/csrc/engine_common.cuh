@@ -1,9 +1,10 @@
 // Shared definitions of the FDTD engine: device-side parameter blocks and small helpers.
 //
 // Memory layout in HBM (one handle = one simulation):
-//   every field and map is a separate float32 (dcmap: int32) array in C order with the last
-//   axis padded to a multiple of 32 elements (128 bytes), so that every row of the contiguous
-//   axis starts on a 128-byte boundary; padding and the 8-cell ghost layer hold zeros and are
+//   every field and map is a separate float32 array in C order (the tap-set index map dcmap:
+//   uint16, at most 65535 tap sets) with the last axis padded to a multiple of 32 elements, so
+//   that every float row of the contiguous axis starts on a 128-byte boundary (a uint16 row on a
+//   64-byte one); padding and the 8-cell ghost layer hold zeros and are
 //   never updated. Cell (i, j[, k]) lives at ((i * ny + j) * pitch + k) in 3D and
 //   (i * pitch + j) in 2D.
 //   state  (read + written every step): p, v[ndim], psi[ndim][2] (pressure-gradient memory
@@ -63,7 +64,7 @@ struct Maps {
   const float* ax[3][2];
   const float* bx[3][2];
   const float* a_exp;        // exponential-attenuation engine: amplitude kept per field update
-  const int32_t* dcmap;
+  const uint16_t* dcmap;     // tap-set index per cell (16-bit: at most 65535 tap sets)
   const float* taps;         // [ndmap][12]
 };
 

@@ -71,7 +71,7 @@ struct fw_handle {
   // device memory
   float* state = nullptr;      // n_state padded arrays
   float* maps = nullptr;       // n_maps padded arrays
-  int32_t* dcmap = nullptr;
+  uint16_t* dcmap = nullptr;   // tap-set index per cell, 16-bit (ndmap <= 65535)
   float* taps = nullptr;
   float* icmat_t = nullptr;    // [nt_ic][ncoords]
   float* traces = nullptr;     // [n_out][ncoordsout]

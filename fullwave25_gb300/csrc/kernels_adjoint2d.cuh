@@ -319,8 +319,8 @@ __global__ void __launch_bounds__(256) adj2d_vel(const AdjArgs A) {
 // Block = one 32 (y) x 8 (x) tile of body cells (the list tiles), origin (i0, j0). Fields are
 // staged with the halo the transposed stencils need (zero / tap index 0 outside the array: the
 // adjoint fields are zero there, so those terms vanish).
-template <int R, int C, class Tv>
-__device__ __forceinline__ void stage_tile(Tv (&dst)[R][C], const Tv* src, const Grid& g,
+template <int R, int C, class Tv, class Ts>
+__device__ __forceinline__ void stage_tile(Tv (&dst)[R][C], const Ts* src, const Grid& g,
                                            int row0, int col0, int tid) {
   for (int e = tid; e < R * C; e += kD2TY * kD2TX) {
     const int r = e / C, cc = e % C;
@@ -516,7 +516,7 @@ struct AdjPrsSmem {
   float gy[kHYR][kHYW];                 // lam_g_y
   float vx[kHXR][kHXW];                 // v_x of S_{n+1}
   float vy[kHYR][kHYW];                 // v_y of S_{n+1}
-  int dc[kHFR][kHFW];
+  uint16_t dc[kHFR][kHFW];
   // point-wise: 0 lam_p | 1-4 lam_phi | 5-10 dt_k inv_kx ax1 bx1 ax2 bx2 | 11-14 phi of S_n |
   // 15-18 phi of S_{n+1} | 19-24 gradient partials of the pressure maps
   float pw[kPrsPW][kD2TX][kD2TY];
@@ -527,16 +527,18 @@ struct AdjVelSmem {
   float dx[kHXR][kHXW];                 // lam_d_x
   float dy[kHYR][kHYW];                 // lam_d_y
   float p[kHFR][kHFW];                  // p of S_n
-  int dc[kHFR][kHFW];
+  uint16_t dc[kHFR][kHFW];
   // point-wise: 0-1 lam_v | 2-5 lam_psi | 6-11 rdt_rho inv_ku au1 bu1 au2 bu2 | 12-15 psi of
   // S_n | 16-19 psi of S_{n+1} | 20-25 gradient partials of the velocity maps
   float pw[kVelPW][kD2TX][kD2TY];
   uint64_t bar;
 };
-constexpr uint32_t kPrsTx = sizeof(float) * (2 * kHXR * kHXW + 2 * kHYR * kHYW + kHFR * kHFW +
-                                             kPrsPW * kD2TX * kD2TY);
-constexpr uint32_t kVelTx = sizeof(float) * (kHXR * kHXW + kHYR * kHYW + 2 * kHFR * kHFW +
-                                             kVelPW * kD2TX * kD2TY);
+constexpr uint32_t kPrsTx = sizeof(float) * (2 * kHXR * kHXW + 2 * kHYR * kHYW +
+                                             kPrsPW * kD2TX * kD2TY) +
+                            sizeof(uint16_t) * kHFR * kHFW;
+constexpr uint32_t kVelTx = sizeof(float) * (kHXR * kHXW + kHYR * kHYW + kHFR * kHFW +
+                                             kVelPW * kD2TX * kD2TY) +
+                            sizeof(uint16_t) * kHFR * kHFW;
 __host__ __device__ constexpr size_t adj_tap_offset(size_t smem_struct) {
   return (smem_struct + 127) / 128 * 128;
 }

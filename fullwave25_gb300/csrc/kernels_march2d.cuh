@@ -66,7 +66,7 @@ __device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const March2
   __shared__ alignas(8) uint64_t bar[kRing2];
   __shared__ alignas(128) float pst[kStream ? 2 : 1][kStream ? kV2StateF : 1][kStream ? TY : 1];
   __shared__ alignas(128) float pmp[kStream ? 2 : 1][kStream ? kV2MapF : 1][kStream ? TY : 1];
-  __shared__ alignas(128) int pdc[kStream ? 2 : 1][kStream ? TY : 1];
+  __shared__ alignas(128) uint16_t pdc[kStream ? 2 : 1][kStream ? TY : 1];
   __shared__ alignas(8) uint64_t pbar[2];
   const Grid& g = A.g;
   int* status = A.step + 1;
@@ -83,7 +83,8 @@ __device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const March2
   }
   __syncthreads();
   constexpr uint32_t kBytes = R::kWide * 4;
-  constexpr uint32_t kPBytes = (kV2StateF + kV2MapF + 1) * TY * 4;
+  constexpr uint32_t kPBytes = (kV2StateF + kV2MapF) * TY * 4 + TY * sizeof(uint16_t);
+  static_assert(!kStream || (TY * sizeof(uint16_t)) % 128 == 0, "tap-index row slots: 128 B");
   auto issue_pw = [&](int slot, int x) {
     if constexpr (kStream) {
       mbar_arrive_expect_tx(&pbar[slot], kPBytes);
@@ -184,7 +185,7 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const March2
   __shared__ alignas(128) float ppp[kStream ? 2 : 1][kStream ? TY : 1];
   __shared__ alignas(128) float pph[kStream ? 2 : 1][kStream ? kP2PhiF : 1][kStream ? TY : 1];
   __shared__ alignas(128) float pmp[kStream ? 2 : 1][kStream ? kMapF : 1][kStream ? TY : 1];
-  __shared__ alignas(128) int pdc[kStream ? 2 : 1][kStream ? TY : 1];
+  __shared__ alignas(128) uint16_t pdc[kStream ? 2 : 1][kStream ? TY : 1];
   __shared__ alignas(8) uint64_t pbar[2];
   const Grid& g = A.g;
   int* status = A.step + 1;
@@ -201,7 +202,8 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const March2
   }
   __syncthreads();
   constexpr uint32_t kBytes = (R::kNarrow + R::kWide) * 4;
-  constexpr uint32_t kPBytes = (1 + kP2PhiF + kMapF + 1) * TY * 4;
+  constexpr uint32_t kPBytes = (1 + kP2PhiF + kMapF) * TY * 4 + TY * sizeof(uint16_t);
+  static_assert(!kStream || (TY * sizeof(uint16_t)) % 128 == 0, "tap-index row slots: 128 B");
   auto issue = [&](int s, int x) {
     mbar_arrive_expect_tx(&bar[s], kBytes);
     tma_load_2d(rx[s], tm_vx, &bar[s], y0 - 4, x);

@@ -29,11 +29,12 @@ constexpr int kStateV0 = 1, kStatePhi0 = 10;      // first field of v and of phi
 
 template <int kPS>
 constexpr size_t vel_stream_smem() {
-  return (size_t)kPS * ((kVelStateF + kVelMapF) * kCell * 4 + kCell * 4);
+  return (size_t)kPS * ((kVelStateF + kVelMapF) * kCell * 4 + kCell * sizeof(uint16_t));
 }
 template <int kPS, bool kBeta>
 constexpr size_t prs_stream_smem() {
-  return (size_t)kPS * ((1 + kPrsPhiF + kVelMapF + (kBeta ? 1 : 0)) * kCell * 4 + kCell * 4);
+  return (size_t)kPS *
+         ((1 + kPrsPhiF + kVelMapF + (kBeta ? 1 : 0)) * kCell * 4 + kCell * sizeof(uint16_t));
 }
 
 struct StreamMaps {
@@ -43,7 +44,7 @@ struct StreamMaps {
   CUtensorMap phi;      // state, box {32, 8, 1, 6} (phi)
   CUtensorMap pmaps6;   // maps,  box {32, 8, 1, 6} (pressure maps)
   CUtensorMap pmaps7;   // maps,  box {32, 8, 1, 7} (pressure maps + beta2dt)
-  CUtensorMap dcmap;    // int32 tap index, box {32, 8, 1}
+  CUtensorMap dcmap;    // 16-bit tap index, box {32, 8, 1}
 };
 
 template <int XC, int kPS, int kMapSlotVel>
@@ -58,7 +59,7 @@ vel3d_stream(const StepArgs A, const __grid_constant__ CUtensorMap tm_p,
   extern __shared__ __align__(128) float dyn[];
   float* pst = dyn;                                             // [kPS][9][256]
   float* pmp = pst + kPS * kVelStateF * kCell;                  // [kPS][6][256]
-  int* pdc = reinterpret_cast<int*>(pmp + kPS * kVelMapF * kCell);  // [kPS][256]
+  uint16_t* pdc = reinterpret_cast<uint16_t*>(pmp + kPS * kVelMapF * kCell);  // [kPS][256]
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * kMTZ + tz;
@@ -79,7 +80,7 @@ vel3d_stream(const StepArgs A, const __grid_constant__ CUtensorMap tm_p,
   }
   __syncthreads();
   constexpr uint32_t kBytes = kPSlot * 4;
-  constexpr uint32_t kPBytes = (kVelStateF + kVelMapF + 1) * kCell * 4;
+  constexpr uint32_t kPBytes = (kVelStateF + kVelMapF) * kCell * 4 + kCell * sizeof(uint16_t);
   auto issue_pw = [&](int slot, int x) {
     mbar_arrive_expect_tx(&pbar[slot], kPBytes);
     tma_load_4d(pst + slot * kVelStateF * kCell, &tm_st, &pbar[slot], z0, y0, x, kStateV0);
@@ -182,7 +183,7 @@ prs3d_stream(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
   float* ppp = dyn;                                            // [kPS][256]
   float* pph = ppp + kPS * kCell;                              // [kPS][6][256]
   float* pmp = pph + kPS * kPrsPhiF * kCell;                   // [kPS][kMapF][256]
-  int* pdc = reinterpret_cast<int*>(pmp + kPS * kMapF * kCell);  // [kPS][256]
+  uint16_t* pdc = reinterpret_cast<uint16_t*>(pmp + kPS * kMapF * kCell);  // [kPS][256]
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tz = threadIdx.x, ty = threadIdx.y, tid = ty * kMTZ + tz;
@@ -202,7 +203,7 @@ prs3d_stream(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
   }
   __syncthreads();
   constexpr uint32_t kBytes = (kXW * kXH + kYSlot + kZSlot) * 4;
-  constexpr uint32_t kPBytes = (1 + kPrsPhiF + kMapF + 1) * kCell * 4;
+  constexpr uint32_t kPBytes = (1 + kPrsPhiF + kMapF) * kCell * 4 + kCell * sizeof(uint16_t);
   auto issue = [&](int s, int x) {
     mbar_arrive_expect_tx(&bar[s], kBytes);
     tma_load_3d(rx[s], &tm_vx, &bar[s], z0 - 4, y0 - 1, x);

@@ -59,11 +59,11 @@ struct VelTileSmem {
   float p[24][48];
   float st[TileVelPlanes<P>::kSt][kD2TX][kD2TY];
   float mp[TileVelPlanes<P>::kMp][kD2TX][kD2TY];
-  int dc[kD2TX][kD2TY];
+  uint16_t dc[kD2TX][kD2TY];
   uint64_t bar;
   static constexpr uint32_t kTx =
       sizeof(float) * (24 * 48 + (TileVelPlanes<P>::kSt + TileVelPlanes<P>::kMp) * kD2TX * kD2TY) +
-      4 * kD2TX * kD2TY;
+      sizeof(uint16_t) * kD2TX * kD2TY;
 };
 template <int P, bool kBeta>
 struct PrsTileSmem {
@@ -74,13 +74,14 @@ struct PrsTileSmem {
   float p[kD2TX][kD2TY];
   float phi[kPhi > 0 ? kPhi : 1][kD2TX][kD2TY];
   float mp[kMp][kD2TX][kD2TY];
-  int dc[kD2TX][kD2TY];
+  uint16_t dc[kD2TX][kD2TY];
   uint64_t bar;
   static constexpr uint32_t kTx =
-      sizeof(float) * (24 * 40 + 10 * 48 + (1 + kPhi + kMp) * kD2TX * kD2TY) + 4 * kD2TX * kD2TY;
+      sizeof(float) * (24 * 40 + 10 * 48 + (1 + kPhi + kMp) * kD2TX * kD2TY) +
+      sizeof(uint16_t) * kD2TX * kD2TY;
 };
 // Every TMA destination starts on a 128-byte boundary: the halo boxes are 4608, 3840 and 1920
-// bytes and every plane 1024 bytes.
+// bytes, every float plane 1024 bytes and the 16-bit tap-index plane 512 bytes.
 static_assert(sizeof(float) * 24 * 48 % 128 == 0 && sizeof(float) * 24 * 40 % 128 == 0 &&
                   sizeof(float) * 10 * 48 % 128 == 0 && sizeof(float) * kD2TX * kD2TY % 128 == 0,
               "TMA destinations must be 128-byte aligned");

@@ -241,7 +241,7 @@ int encode_stream_maps(fw_handle* h) {
   StreamMaps& m = h->smaps;
   const int ns = n_state(h->ndim), nm = n_maps(h);
   const cuuint64_t dims[3] = {(cuuint64_t)h->pitch, (cuuint64_t)h->ny, (cuuint64_t)h->nx};
-  const cuuint64_t strides[2] = {(cuuint64_t)h->pitch * 4, (cuuint64_t)(h->pitch * h->ny) * 4};
+  const cuuint64_t dc_strides[2] = {(cuuint64_t)h->pitch * 2, (cuuint64_t)(h->pitch * h->ny) * 2};
   const cuuint32_t box[3] = {(cuuint32_t)kMTZ, (cuuint32_t)kMTY, 1};
   int st;
   if ((st = encode_stack_map(h, &m.vstate, h->state, ns, kVelStateF)) ||
@@ -250,7 +250,8 @@ int encode_stream_maps(fw_handle* h) {
       (st = encode_stack_map(h, &m.phi, h->state, ns, kPrsPhiF)) ||
       (st = encode_stack_map(h, &m.pmaps6, h->maps, nm, kVelMapF)) ||
       (st = encode_stack_map(h, &m.pmaps7, h->maps, nm, kVelMapF + 1)) ||
-      (st = encode_map(h, &m.dcmap, h->dcmap, 3, dims, strides, box, CU_TENSOR_MAP_DATA_TYPE_INT32)))
+      (st = encode_map(h, &m.dcmap, h->dcmap, 3, dims, dc_strides, box,
+                       CU_TENSOR_MAP_DATA_TYPE_UINT16)))
     return st;
   return FW_OK;
 }
@@ -292,7 +293,7 @@ int encode_march2_maps(fw_handle* h, uint32_t ty, March2Maps* m) {
   if (h->aniso || h->exp) return FW_OK;
   const int ns = n_state(h->ndim), nm = n_maps(h);
   const cuuint64_t dims[2] = {(cuuint64_t)h->pitch, (cuuint64_t)h->nx};
-  const cuuint64_t strides[1] = {(cuuint64_t)h->pitch * 4};
+  const cuuint64_t dc_strides[1] = {(cuuint64_t)h->pitch * 2};
   const cuuint32_t box[2] = {ty, 1};
   if ((st = encode_row_stack_map(h, &m->vst, h->state, ns, ty, kV2StateF)) ||
       (st = encode_row_stack_map(h, &m->vmp, h->maps, nm, ty, kV2MapF)) ||
@@ -300,7 +301,8 @@ int encode_march2_maps(fw_handle* h, uint32_t ty, March2Maps* m) {
       (st = encode_row_stack_map(h, &m->phi, h->state, ns, ty, kP2PhiF)) ||
       (st = encode_row_stack_map(h, &m->pmp6, h->maps, nm, ty, kV2MapF)) ||
       (st = encode_row_stack_map(h, &m->pmp7, h->maps, nm, ty, kV2MapF + 1)) ||
-      (st = encode_map(h, &m->dc, h->dcmap, 2, dims, strides, box, CU_TENSOR_MAP_DATA_TYPE_INT32)))
+      (st = encode_map(h, &m->dc, h->dcmap, 2, dims, dc_strides, box,
+                       CU_TENSOR_MAP_DATA_TYPE_UINT16)))
     return st;
   return FW_OK;
 }
@@ -317,6 +319,7 @@ int encode_tile2_maps(fw_handle* h, Tile2Maps* m, float* store, int slots) {
   const cuuint64_t d_mp[3] = {pitch, nx, (cuuint64_t)n_maps(h)};
   const cuuint64_t str[3] = {row, field, field * ns};
   const cuuint64_t d_dc[2] = {pitch, nx};
+  const cuuint64_t dc_str[1] = {(cuuint64_t)h->pitch * 2};
   const cuuint32_t bp[4] = {48, 24, 1, 1}, bx[4] = {40, 24, 1, 1}, by[4] = {48, 10, 1, 1};
   const cuuint32_t b1[4] = {kD2TY, kD2TX, 1, 1}, b2[4] = {kD2TY, kD2TX, 2, 1};
   const cuuint32_t b3[4] = {kD2TY, kD2TX, 3, 1}, b4[4] = {kD2TY, kD2TX, 4, 1};
@@ -336,7 +339,7 @@ int encode_tile2_maps(fw_handle* h, Tile2Maps* m, float* store, int slots) {
       (st = encode_map(h, &m->mp3, h->maps, 3, d_mp, str, b3)) ||
       (st = encode_map(h, &m->mp5, h->maps, 3, d_mp, str, b5)) ||
       (st = encode_map(h, &m->mp6, h->maps, 3, d_mp, str, b6)) ||
-      (st = encode_map(h, &m->dc, h->dcmap, 2, d_dc, str, bdc, CU_TENSOR_MAP_DATA_TYPE_INT32)))
+      (st = encode_map(h, &m->dc, h->dcmap, 2, d_dc, dc_str, bdc, CU_TENSOR_MAP_DATA_TYPE_UINT16)))
     return st;
   return FW_OK;
 }
