@@ -280,3 +280,45 @@ def test_adjoint_rejects_3d_and_beta(engine_lib, cuda):
     with Engine(load_case_inputs("2d_air_beta")) as e:
         with pytest.raises(EngineError, match="FW_ERR_UNSUPPORTED"):
             e.adjoint_forward(10)
+
+
+def test_reverse_step_with_wide_tap_table(engine_lib, cuda):
+    """2001 tap sets (sound speeds 1000-3000 m/s): the TMA reverse step copies a 96 KB tap table
+    next to its tiles, the thread-load form reads the table from global memory; bitwise equal."""
+    import os
+
+    torch = cuda
+    from fullwave25_gb300 import coefficients
+    from fullwave25_gb300.engine import Engine
+    from fullwave25_gb300.workloads import plain_2d_inputs
+
+    def problem(scale):
+        inp = plain_2d_inputs(shape=(50, 70), nt=60, n_pml=6, n_transition=6)
+        c = np.random.default_rng(4).uniform(1000.0, 3000.0, size=inp.shape)
+        c[0, 0], c[-1, -1] = 1000.0, 3000.0
+        inp.maps = dict(inp.maps)
+        inp.maps["c"] = c.astype(np.float32)
+        inp.maps["K"] = (inp.maps["K"] * np.float32(scale)).astype(np.float32)
+        inp.dmap = coefficients.d_map(c, inp.dt, inp.spacing[0], is_3d=False)
+        inp.dcmap = coefficients.dc_map(c)
+        return inp
+
+    inp = problem(1.0)
+    assert inp.dmap.shape[2] == 2001
+    observed = Oracle(problem(1.02)).run().astype(np.float32)
+    out = {}
+    for mode, env in {"tma": {}, "tiled": {"FWGB_ADJ_TMA": "0"}}.items():
+        os.environ.update(env)
+        try:
+            with Engine(inp) as eng:
+                eng.adjoint_forward(20)
+                res = torch.as_tensor(eng.read_traces() - observed, device="cuda").contiguous()
+                g = torch.zeros((12,) + tuple(inp.shape), dtype=torch.float64, device="cuda")
+                eng.adjoint_backward(res.data_ptr(), g.data_ptr())
+                torch.cuda.synchronize()
+                out[mode] = g.cpu().numpy()
+        finally:
+            for k in env:
+                os.environ.pop(k, None)
+    assert np.abs(out["tiled"]).max() > 0
+    np.testing.assert_array_equal(out["tma"], out["tiled"])

@@ -156,3 +156,29 @@ def test_invalid_shape_index_is_an_argument_error(engine_lib, cuda):
 
     with pytest.raises(EngineError, match="FWGB_SHAPE2D"):
         _engine(load_case_inputs("2d_small"), FWGB_SHAPE2D=17)
+
+
+def test_wide_tap_table_every_shape(engine_lib, cuda):
+    """Sound speeds spanning 1000-3000 m/s: 2001 tap sets, tap-set indices above 8 bits in the
+    16-bit device map; every kernel shape equals the direct kernels and the FP64 oracle."""
+    from fdtd_oracle_c import run_oracle_c
+    from fullwave25_gb300 import coefficients
+    from fullwave25_gb300.workloads import plain_2d_inputs
+
+    inp = plain_2d_inputs(shape=(60, 70), nt=160, n_pml=8, n_transition=8)
+    rng = np.random.default_rng(2)
+    c = rng.uniform(1000.0, 3000.0, size=inp.shape).astype(np.float32)
+    c[0, 0], c[-1, -1] = 1000.0, 3000.0
+    inp.maps = dict(inp.maps)
+    inp.maps["c"] = c
+    inp.dmap = coefficients.d_map(c.astype(np.float64), inp.dt, inp.spacing[0], is_3d=False)
+    inp.dcmap = coefficients.dc_map(c.astype(np.float64))
+    assert inp.dmap.shape[2] == 2001 and inp.dcmap.max() == 2000
+    with _engine(inp, FWGB_VARIANT="direct") as ed:
+        ref = ed.run()
+    assert np.abs(ref).max() > 0
+    err = rel_l2(ref, run_oracle_c(inp))
+    assert err < TOL, f"rel-L2 {err:.3e}"
+    for k in MARCH_SHAPES:
+        with _engine(inp, FWGB_SHAPE2D=k) as em:
+            np.testing.assert_array_equal(em.run(), ref, err_msg=f"shape {k}")

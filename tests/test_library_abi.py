@@ -29,7 +29,7 @@ def test_library_exports_every_declared_symbol(engine_lib):
 
 @pytest.mark.parametrize("field,value,code", [
     ("ndim", 4, 1), ("nx", 10, 1), ("mod_t", 0, 1), ("isotropic", 2, 1), ("n_relax", 3, 6),
-    ("dt", 0.0, 1),
+    ("dt", 0.0, 1), ("ndmap", 65536, 1),   # the device keeps a cell's tap-set index in 16 bits
 ])
 def test_create_rejects_bad_descriptor(engine_lib, field, value, code):
     d = engine.FwDesc(ndim=2, nx=64, ny=64, nz=1, nt=10, nt_ic=10, mod_t=1, dx=1e-4, dy=1e-4,
