@@ -605,6 +605,21 @@ def run_serve(args):
                                 max_active_cells=cap)
     for r in reqs:
         r.result = None
+    # the FIFO baseline runs every request on its own handle: tune the kernel shape of each
+    # forward grid size first (untimed; cached per size, as in a long-running server), so that
+    # the baseline does not pay autotuning trials inside its timed stream
+    from fullwave25_gb300.engine import Engine
+
+    tuned = set()
+    for r in reqs:
+        if r.kind == "forward":
+            d = r.build()
+            if tuple(d.shape) not in tuned:
+                tuned.add(tuple(d.shape))
+                with Engine(d, validate=False) as e:
+                    e.advance(1)   # the first advance from step 0 runs the trials
+            del d
+    torch.cuda.synchronize()
     fifo = serve_fifo(reqs)
     for r in reqs:
         r.result = None
@@ -612,7 +627,6 @@ def run_serve(args):
     # pre-processing, engine creation and upload, solve, traces back) on the stream's first
     # forward requests; gradient requests have no host-side path and are left out, so the ratio
     # against the whole mixed stream understates the served advantage
-    from fullwave25_gb300.engine import Engine
     from fullwave25_gb300.workloads_batch import batch_inputs_host
 
     host_reqs = [r for r in reqs if r.kind == "forward"][:args.host_sample]
@@ -640,7 +654,8 @@ def run_serve(args):
                                    f"{args.grad_frac:.0%} gradient solves (512-1024 square "
                                    f"grids, nt 6000 at 1024), sizes scaled by {scale}; device "
                                    f"budget {args.budget_gb} GB, blocks of 256 steps, "
-                                   "2 gradient worker streams",
+                                   "2 gradient worker streams; FIFO after the kernel shape of "
+                                   "every forward grid size was tuned (untimed)",
                        "requests": len(reqs), "gradient_requests": n_grad,
                        "max_active_cells": cap},
             "continuous": cont, "fifo_one_at_a_time": fifo,
