@@ -98,7 +98,7 @@ struct fw_handle {
   bool shape_fixed = false;    // 2D shape forced (FWGB_SHAPE2D / FWGB_VARIANT) or already tuned
   fwgb::MarchMaps tmaps{};
   fwgb::March2Maps tmaps2{};
-  fwgb::Tile2Maps tmaps_t{};   // TMA tile kernels (2D isotropic)
+  fwgb::Tile2Maps tmaps_t{};   // TMA tile kernels (2D)
   bool stream2d = false;       // 2D isotropic row march: point-wise operands staged by TMA too
   fwgb::StreamMaps smaps{};
   bool stream3d = false;       // 3D isotropic: point-wise operands staged by TMA too

@@ -94,49 +94,49 @@ __device__ __forceinline__ void tma_state(void* dst, const CUtensorMap* map, uin
   else tma_load_3d(dst, map, bar, x, y, field);
 }
 
-// Block prologue of the tile kernels: alignment guard and barrier init (one thread).
-template <class SmemT>
-__device__ __forceinline__ bool tile_begin(SmemT& S, const unsigned char* base, int* status,
-                                           int tid, uint32_t tx_bytes) {
-  if (smem_u32(base) & 127u) {
-    if (tid == 0) atomicOr(status, kStatusAlign);
-    return false;
+// The loads of one tile (one thread issues them; completion on S.bar).
+template <int P, bool kStore>
+__device__ __forceinline__ void vel_tile_issue(VelTileSmem<P>& S, const Tile2Maps& M, int i0,
+                                               int j0, int slot) {
+  mbar_arrive_expect_tx(&S.bar, VelTileSmem<P>::kTx);
+  tma_state<kStore>(S.p, &M.p_halo, &S.bar, j0 - 8, i0 - 8, 0, slot);
+  if constexpr (P == kTileExp) {
+    tma_state<kStore>(S.st, &M.st2, &S.bar, j0, i0, 1, slot);
+    tma_load_3d(S.mp, &M.mp3, &S.bar, j0, i0, kTileMapVel);
+  } else {
+    tma_state<kStore>(S.st, &M.st6, &S.bar, j0, i0, 1, slot);
+    tma_load_3d(S.mp, &M.mp6, &S.bar, j0, i0, kTileMapVel);
+    if constexpr (P == kTileAniso) tma_load_3d(S.mp[6], &M.mp5, &S.bar, j0, i0, kTileMapGradY);
   }
-  if (tid == 0) {
-    mbar_init(&S.bar, 1);
-    fence_barrier_init();
-    mbar_arrive_expect_tx(&S.bar, tx_bytes);
-  }
-  return true;
+  tma_load_2d(S.dc, &M.dc, &S.bar, j0, i0);
 }
 
-template <int P, bool kStore = false>
-__global__ void __launch_bounds__(256) vel2d_tile(const StepArgs A,
-                                                  const __grid_constant__ Tile2Maps M, int slot) {
-  pdl_entry();
-  extern __shared__ __align__(128) unsigned char tile_smem[];
-  using Smem = VelTileSmem<P>;
-  Smem& S = *reinterpret_cast<Smem*>(tile_smem);
-  const Grid& g = A.g;
-  int* status = A.step + 1;
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kD2TY + tx;
-  const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
-  if (!tile_begin(S, tile_smem, status, tid, Smem::kTx)) return;
-  if (blockIdx.x == 0 && blockIdx.y == 0 && tid == 0) *A.step += 1;
-  if (tid == 0) {
-    tma_state<kStore>(S.p, &M.p_halo, &S.bar, j0 - 8, i0 - 8, 0, slot);
-    if constexpr (P == kTileExp) {
-      tma_state<kStore>(S.st, &M.st2, &S.bar, j0, i0, 1, slot);
-      tma_load_3d(S.mp, &M.mp3, &S.bar, j0, i0, kTileMapVel);
-    } else {
-      tma_state<kStore>(S.st, &M.st6, &S.bar, j0, i0, 1, slot);
-      tma_load_3d(S.mp, &M.mp6, &S.bar, j0, i0, kTileMapVel);
-      if constexpr (P == kTileAniso) tma_load_3d(S.mp[6], &M.mp5, &S.bar, j0, i0, kTileMapGradY);
-    }
-    tma_load_2d(S.dc, &M.dc, &S.bar, j0, i0);
+template <int P, bool kBeta, bool kStore>
+__device__ __forceinline__ void prs_tile_issue(PrsTileSmem<P, kBeta>& S, const Tile2Maps& M,
+                                               int i0, int j0, int slot) {
+  using Smem = PrsTileSmem<P, kBeta>;
+  mbar_arrive_expect_tx(&S.bar, Smem::kTx);
+  tma_state<kStore>(S.vx, &M.vx_halo, &S.bar, j0 - 4, i0 - 8, 1, slot + 1);
+  tma_state<kStore>(S.vy, &M.vy_halo, &S.bar, j0 - 8, i0 - 1, 2, slot + 1);
+  tma_state<kStore>(S.p, &M.st1, &S.bar, j0, i0, 0, slot);
+  if constexpr (P == kTileExp) {
+    tma_load_3d(S.mp[0], &M.mp1, &S.bar, j0, i0, kTileMapPrs);
+    tma_load_3d(S.mp[1], &M.mp1, &S.bar, j0, i0, kTileMapAexp);
+  } else {
+    tma_state<kStore>(S.phi, &M.st4, &S.bar, j0, i0, 7, slot);
+    tma_load_3d(S.mp, &M.mp6, &S.bar, j0, i0, kTileMapPrs);
+    if constexpr (P == kTileAniso) tma_load_3d(S.mp[6], &M.mp5, &S.bar, j0, i0, kTileMapDivY);
   }
-  __syncthreads();   // barrier initialised before anyone polls it
-  mbar_wait_bounded(&S.bar, 0, status);
+  if constexpr (kBeta) tma_load_3d(S.mp[Smem::kMp - 1], &M.mp1, &S.bar, j0, i0, kTileMapBeta);
+  tma_load_2d(S.dc, &M.dc, &S.bar, j0, i0);
+}
+
+// Velocity update of the calling thread's cell of the staged tile at (i0, j0).
+template <int P>
+__device__ __forceinline__ void vel_tile_compute(const StepArgs& A, const VelTileSmem<P>& S,
+                                                 int i0, int j0) {
+  const Grid& g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y;
   const int i = i0 + ty, j = j0 + tx;
   if (i >= g.nx - kGhost || j >= g.ny - kGhost) return;
   const int64_t c = (int64_t)i * g.sx + j;
@@ -181,36 +181,16 @@ __global__ void __launch_bounds__(256) vel2d_tile(const StepArgs A,
   cv.update_store(A, c, gg);
 }
 
-template <int P, bool kBeta, bool kStore = false>
-__global__ void __launch_bounds__(256) prs2d_tile(const StepArgs A,
-                                                  const __grid_constant__ Tile2Maps M, int slot) {
-  pdl_entry();
-  extern __shared__ __align__(128) unsigned char tile_smem[];
+// Pressure update of the calling thread's cell of the staged tile, then the tile's epilogue
+// (every thread of the block calls it).
+template <int P, bool kBeta>
+__device__ __forceinline__ void prs_tile_compute(const StepArgs& A,
+                                                 const PrsTileSmem<P, kBeta>& S, int i0, int j0,
+                                                 int tile) {
   using Smem = PrsTileSmem<P, kBeta>;
-  Smem& S = *reinterpret_cast<Smem*>(tile_smem);
-  const Grid& g = A.g;
-  int* status = A.step + 1;
-  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kD2TY + tx;
-  const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
-  if (!tile_begin(S, tile_smem, status, tid, Smem::kTx)) return;
   constexpr int kBetaPlane = Smem::kMp - 1;   // beta 2 dt, when present, is the last map plane
-  if (tid == 0) {
-    tma_state<kStore>(S.vx, &M.vx_halo, &S.bar, j0 - 4, i0 - 8, 1, slot + 1);
-    tma_state<kStore>(S.vy, &M.vy_halo, &S.bar, j0 - 8, i0 - 1, 2, slot + 1);
-    tma_state<kStore>(S.p, &M.st1, &S.bar, j0, i0, 0, slot);
-    if constexpr (P == kTileExp) {
-      tma_load_3d(S.mp[0], &M.mp1, &S.bar, j0, i0, kTileMapPrs);
-      tma_load_3d(S.mp[1], &M.mp1, &S.bar, j0, i0, kTileMapAexp);
-    } else {
-      tma_state<kStore>(S.phi, &M.st4, &S.bar, j0, i0, 7, slot);
-      tma_load_3d(S.mp, &M.mp6, &S.bar, j0, i0, kTileMapPrs);
-      if constexpr (P == kTileAniso) tma_load_3d(S.mp[6], &M.mp5, &S.bar, j0, i0, kTileMapDivY);
-    }
-    if constexpr (kBeta) tma_load_3d(S.mp[kBetaPlane], &M.mp1, &S.bar, j0, i0, kTileMapBeta);
-    tma_load_2d(S.dc, &M.dc, &S.bar, j0, i0);
-  }
-  __syncthreads();
-  mbar_wait_bounded(&S.bar, 0, status);
+  const Grid& g = A.g;
+  const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * kD2TY + tx;
   const int i = i0 + ty, j = j0 + tx;
   if (i < g.nx - kGhost && j < g.ny - kGhost) {
     const int64_t c = (int64_t)i * g.sx + j;
@@ -254,7 +234,55 @@ __global__ void __launch_bounds__(256) prs2d_tile(const StepArgs A,
     const float dd[2] = {dx * g.inv_h[0], dy * g.inv_h[1]};
     cp.update_store(A, c, dd);
   }
-  tile_epilogue(A, A.f.p, blockIdx.y * gridDim.x + blockIdx.x, tid, kD2TY * kD2TX);
+  tile_epilogue(A, A.f.p, tile, tid, kD2TY * kD2TX);
+}
+
+// ---- one tile per block ----------------------------------------------------------------------
+template <int P, bool kStore = false>
+__global__ void __launch_bounds__(256) vel2d_tile(const StepArgs A,
+                                                  const __grid_constant__ Tile2Maps M, int slot) {
+  pdl_entry();
+  extern __shared__ __align__(128) unsigned char tile_smem[];
+  VelTileSmem<P>& S = *reinterpret_cast<VelTileSmem<P>*>(tile_smem);
+  int* status = A.step + 1;
+  const int tid = threadIdx.y * kD2TY + threadIdx.x;
+  const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
+  if (smem_u32(tile_smem) & 127u) {   // TMA destinations need 128-byte alignment: refuse
+    if (tid == 0) atomicOr(status, kStatusAlign);
+    return;
+  }
+  if (tid == 0) {
+    mbar_init(&S.bar, 1);
+    fence_barrier_init();
+    vel_tile_issue<P, kStore>(S, M, i0, j0, slot);
+    if (blockIdx.x == 0 && blockIdx.y == 0) *A.step += 1;
+  }
+  __syncthreads();   // barrier initialised before anyone polls it
+  mbar_wait_bounded(&S.bar, 0, status);
+  vel_tile_compute<P>(A, S, i0, j0);
+}
+
+template <int P, bool kBeta, bool kStore = false>
+__global__ void __launch_bounds__(256) prs2d_tile(const StepArgs A,
+                                                  const __grid_constant__ Tile2Maps M, int slot) {
+  pdl_entry();
+  extern __shared__ __align__(128) unsigned char tile_smem[];
+  PrsTileSmem<P, kBeta>& S = *reinterpret_cast<PrsTileSmem<P, kBeta>*>(tile_smem);
+  int* status = A.step + 1;
+  const int tid = threadIdx.y * kD2TY + threadIdx.x;
+  const int i0 = kGhost + blockIdx.y * kD2TX, j0 = kGhost + blockIdx.x * kD2TY;
+  if (smem_u32(tile_smem) & 127u) {
+    if (tid == 0) atomicOr(status, kStatusAlign);
+    return;
+  }
+  if (tid == 0) {
+    mbar_init(&S.bar, 1);
+    fence_barrier_init();
+    prs_tile_issue<P, kBeta, kStore>(S, M, i0, j0, slot);
+  }
+  __syncthreads();
+  mbar_wait_bounded(&S.bar, 0, status);
+  prs_tile_compute<P, kBeta>(A, S, i0, j0, blockIdx.y * gridDim.x + blockIdx.x);
 }
 
 }  // namespace fwgb

@@ -34,7 +34,8 @@ static_assert(kTileMapVel == kMRdtRho && kTileMapPrs == kMDtK && kTileMapBeta ==
 template <int P, bool kBeta>
 void launch_tile2d(fw_handle* h, cudaStream_t s) {
   const Tiling& t = h->tiling;
-  dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
+  const dim3 block(kD2TY, kD2TX);
+  dim3 grid(t.n[1], t.n[0]);
   launch_k(vel2d_tile<P>, grid, block, sizeof(VelTileSmem<P>), s, h->args, h->tmaps_t, 0);
   launch_k(prs2d_tile<P, kBeta>, grid, block, sizeof(PrsTileSmem<P, kBeta>), s, h->args,
            h->tmaps_t, 0);
@@ -59,6 +60,7 @@ void launch_typed(fw_handle* h, cudaStream_t s) {
     static_assert(kNumShapes2D == 8, "one case per 2D kernel shape");
     switch (h->shape2d) {
       case 0:
+      case kTileShape:      // the tile shape is launched by launch_nd for every physics
       case kPersistentShape: {  // the persistent shape issues the direct kernels when captured
         dim3 grid(t.n[1], t.n[0]), block(kD2TY, kD2TX);
         launch_k(vel2d_direct<CV>, grid, block, 0, s, h->args);
