@@ -64,6 +64,18 @@ int prepare_adjoint_kernels(fw_handle* h, int dev, int smem_optin) {
   return FW_OK;
 }
 
+// Free the adjoint buffers of h (checkpoints, state store, adjoint fields, gradient sums).
+void release_adjoint(fw_handle* h) {
+  void* bufs[] = {h->adj_ckpt, h->adj_store, h->adj_lam, h->adj_grad};
+  for (void* b : bufs)
+    if (b) cudaFree(b);
+  h->adj_ckpt = h->adj_store = h->adj_lam = nullptr;
+  h->adj_grad = nullptr;
+  h->bytes -= h->adj_bytes;
+  h->adj_bytes = 0;
+  h->adj_every = h->adj_nckpt = 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -79,23 +91,24 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
   const size_t state_elems = (size_t)h->ncells_padded * n_state(h->ndim);
   const int nckpt = (h->d.nt + checkpoint_every - 1) / checkpoint_every;
   if (checkpoint_every != h->adj_every || nckpt != h->adj_nckpt) {
-    void* bufs[] = {h->adj_ckpt, h->adj_store, h->adj_lam, h->adj_grad};
-    for (void* b : bufs)
-      if (b) cudaFree(b);
-    h->bytes -= h->adj_bytes;
-    h->adj_ckpt = h->adj_store = h->adj_lam = nullptr;
-    h->adj_grad = nullptr;
+    release_adjoint(h);
     const size_t b_ckpt = state_elems * std::max(nckpt, 1) * sizeof(float);
     const size_t b_store = state_elems * (checkpoint_every + 1) * sizeof(float);
     // 15 adjoint fields and temporaries, then the FP32 per-segment gradient partials
     const size_t b_lam = (size_t)h->ncells_padded * kAdjStack * sizeof(float);
     const size_t b_grad = (size_t)h->ncells_padded * kNumGrad * sizeof(double);
-    FW_CUDA(h, cudaMalloc(&h->adj_ckpt, b_ckpt));
-    FW_CUDA(h, cudaMalloc(&h->adj_store, b_store));
+    cudaError_t e = cudaMalloc(&h->adj_ckpt, b_ckpt);
+    if (e == cudaSuccess) e = cudaMalloc(&h->adj_store, b_store);
     // the out-of-place recomputation never writes the ghost layer of a stored state: keep it zero
-    FW_CUDA(h, cudaMemset(h->adj_store, 0, b_store));
-    FW_CUDA(h, cudaMalloc(&h->adj_lam, b_lam));
-    FW_CUDA(h, cudaMalloc(&h->adj_grad, b_grad));
+    if (e == cudaSuccess) e = cudaMemset(h->adj_store, 0, b_store);
+    if (e == cudaSuccess) e = cudaMalloc(&h->adj_lam, b_lam);
+    if (e == cudaSuccess) e = cudaMalloc(&h->adj_grad, b_grad);
+    if (e != cudaSuccess) {   // leave no partial allocation behind
+      release_adjoint(h);
+      return fail(h, e == cudaErrorMemoryAllocation ? FW_ERR_OOM : FW_ERR_CUDA,
+                  "adjoint buffers (%zu bytes): %s", b_ckpt + b_store + b_lam + b_grad,
+                  cudaGetErrorString(e));
+    }
     h->adj_bytes = b_ckpt + b_store + b_lam + b_grad;
     h->bytes += h->adj_bytes;
     h->adj_every = checkpoint_every;

@@ -162,47 +162,53 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
                 joining.append((r, eng))
             used += r.bytes_needed
 
-    while pending or active or joining or running:
-        admit()
-        # retire finished gradient requests
-        for fut in [f for f in running if f.done()]:
-            r, s = running.pop(fut)
-            fut.result()  # re-raise a worker's error here
-            free_streams.append(s)
-            used -= r.bytes_needed
-        active += joining
-        joining = []
-        if not active:
-            # idle until the next arrival or a gradient finishes
-            wait = (pending[0].arrival - (clock() - t0)) if pending else 0.01
-            if wait > 0:
-                time.sleep(min(wait, 0.01))
-            continue
-        engines = [e for _, e in active]
-        if group is None:
-            group = EngineGroup(engines)
-        else:
-            group.set_members(engines)
-        group.advance(chunk_steps, main.cuda_stream)
-        admit()            # requests arriving meanwhile are built while the block runs
-        main.synchronize()
-        n_chunks += 1
-        still = []
-        for r, e in active:
-            if e.current_step >= e.inputs.nt:
-                r.traces = e.read_traces(stream=main.cuda_stream)
-                r.finished = clock() - t0
+    try:
+        while pending or active or joining or running:
+            admit()
+            # retire finished gradient requests
+            for fut in [f for f in running if f.done()]:
+                r, s = running.pop(fut)
+                fut.result()  # re-raise a worker's error here
+                free_streams.append(s)
                 used -= r.bytes_needed
-                cells_active -= r.cells
-                e.close()
+            active += joining
+            joining = []
+            if not active:
+                # idle until the next arrival or a gradient finishes
+                wait = (pending[0].arrival - (clock() - t0)) if pending else 0.01
+                if wait > 0:
+                    time.sleep(min(wait, 0.01))
+                continue
+            engines = [e for _, e in active]
+            if group is None:
+                group = EngineGroup(engines)
             else:
-                still.append((r, e))
-        active = still
-        if not active and not joining and group is not None:
-            group.set_members([])
-    pool.shutdown()
-    if group is not None:
-        group.close()
+                group.set_members(engines)
+            group.advance(chunk_steps, main.cuda_stream)
+            admit()            # requests arriving meanwhile are built while the block runs
+            main.synchronize()
+            n_chunks += 1
+            still = []
+            for r, e in active:
+                if e.current_step >= e.inputs.nt:
+                    r.traces = e.read_traces(stream=main.cuda_stream)
+                    r.finished = clock() - t0
+                    used -= r.bytes_needed
+                    cells_active -= r.cells
+                    e.close()
+                else:
+                    still.append((r, e))
+            active = still
+            if not active and not joining and group is not None:
+                group.set_members([])
+    finally:
+        # on an error (a worker's exception re-raised above, a failed build) release every
+        # engine still held; on success all of them are closed already
+        pool.shutdown(wait=True)
+        if group is not None:
+            group.close()
+        for _, e in active + joining:
+            e.close()
     del lock
     return summarize(requests, clock() - t0, extra={"chunks": n_chunks})
 
