@@ -131,10 +131,27 @@ __device__ __forceinline__ void prs_tile_issue(PrsTileSmem<P, kBeta>& S, const T
   tma_load_2d(S.dc, &M.dc, &S.bar, j0, i0);
 }
 
-// Velocity update of the calling thread's cell of the staged tile at (i0, j0).
+// Tap set of the calling thread's cell (zeros outside the body), read from global memory before
+// the block waits for its tile, so that its latency overlaps the TMA transfer.
+__device__ __forceinline__ void tile_taps(const StepArgs& A, int i0, int j0, float (&cm)[8],
+                                          float& co) {
+  const Grid& g = A.g;
+  const int i = i0 + threadIdx.y, j = j0 + threadIdx.x;
+  if (i < g.nx - kGhost && j < g.ny - kGhost) {
+    load_taps(A.m.taps, __ldg(A.m.dcmap + (int64_t)i * g.sx + j), cm, co);
+  } else {
+#pragma unroll
+    for (int m = 0; m < 8; ++m) cm[m] = 0.f;
+    co = 0.f;
+  }
+}
+
+// Velocity update of the calling thread's cell of the staged tile at (i0, j0); cm / co: the
+// cell's tap set (tile_taps).
 template <int P>
 __device__ __forceinline__ void vel_tile_compute(const StepArgs& A, const VelTileSmem<P>& S,
-                                                 int i0, int j0) {
+                                                 int i0, int j0, const float (&cm)[8],
+                                                 float co) {
   const Grid& g = A.g;
   const int tx = threadIdx.x, ty = threadIdx.y;
   const int i = i0 + ty, j = j0 + tx;
@@ -166,8 +183,6 @@ __device__ __forceinline__ void vel_tile_compute(const StepArgs& A, const VelTil
       cv.s2[a] = S.st[3 + 2 * a][ty][tx];
     }
   }
-  float cm[8], co;
-  load_taps(A.m.taps, cv.dc, cm, co);
   auto Pp = [&](int di, int dj) { return S.p[ty + 8 + di][tx + 8 + dj]; };
   float gx = 0.f, gy = 0.f;
 #pragma unroll
@@ -186,7 +201,7 @@ __device__ __forceinline__ void vel_tile_compute(const StepArgs& A, const VelTil
 template <int P, bool kBeta>
 __device__ __forceinline__ void prs_tile_compute(const StepArgs& A,
                                                  const PrsTileSmem<P, kBeta>& S, int i0, int j0,
-                                                 int tile) {
+                                                 int tile, const float (&cm)[8], float co) {
   using Smem = PrsTileSmem<P, kBeta>;
   constexpr int kBetaPlane = Smem::kMp - 1;   // beta 2 dt, when present, is the last map plane
   const Grid& g = A.g;
@@ -219,8 +234,6 @@ __device__ __forceinline__ void prs_tile_compute(const StepArgs& A,
         cp.f2[a] = S.phi[2 * a + 1][ty][tx];
       }
     }
-    float cm[8], co;
-    load_taps(A.m.taps, cp.dc, cm, co);
     auto X = [&](int di, int dj) { return S.vx[ty + 8 + di][tx + 4 + dj]; };
     auto Y = [&](int di, int dj) { return S.vy[ty + 1 + di][tx + 8 + dj]; };
     float dx = 0.f, dy = 0.f;
@@ -257,9 +270,11 @@ __global__ void __launch_bounds__(256) vel2d_tile(const StepArgs A,
     vel_tile_issue<P, kStore>(S, M, i0, j0, slot);
     if (blockIdx.x == 0 && blockIdx.y == 0) *A.step += 1;
   }
+  float cm[8], co;
+  tile_taps(A, i0, j0, cm, co);
   __syncthreads();   // barrier initialised before anyone polls it
   mbar_wait_bounded(&S.bar, 0, status);
-  vel_tile_compute<P>(A, S, i0, j0);
+  vel_tile_compute<P>(A, S, i0, j0, cm, co);
 }
 
 template <int P, bool kBeta, bool kStore = false>
@@ -280,9 +295,11 @@ __global__ void __launch_bounds__(256) prs2d_tile(const StepArgs A,
     fence_barrier_init();
     prs_tile_issue<P, kBeta, kStore>(S, M, i0, j0, slot);
   }
+  float cm[8], co;
+  tile_taps(A, i0, j0, cm, co);
   __syncthreads();
   mbar_wait_bounded(&S.bar, 0, status);
-  prs_tile_compute<P, kBeta>(A, S, i0, j0, blockIdx.y * gridDim.x + blockIdx.x);
+  prs_tile_compute<P, kBeta>(A, S, i0, j0, blockIdx.y * gridDim.x + blockIdx.x, cm, co);
 }
 
 }  // namespace fwgb
