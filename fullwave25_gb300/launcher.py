@@ -21,8 +21,6 @@ import logging
 import time
 from pathlib import Path
 
-import numpy as np
-
 from .inputs import load_dat_data, read_simulation_dir
 
 logger = logging.getLogger("__main__." + __name__)

@@ -17,7 +17,6 @@ implementations agree on a small grid.
 
 from __future__ import annotations
 
-import copy
 import time
 from dataclasses import dataclass, field
 
