@@ -95,6 +95,22 @@ def poisson_arrivals(rate_hz: float, duration_s: float, seed: int = 0) -> np.nda
         out.append(t)
 
 
+def admissible(r, *, used: int, budget_bytes: int, busy: bool, free_workers: int,
+               cells_active: int, forward_active: bool, max_active_cells: int | None) -> bool:
+    """Whether arrived request ``r`` (the head of the FIFO queue) may start now.
+
+    ``used``: device bytes held by admitted requests; ``busy``: anything admitted and unfinished
+    (a request larger than the whole budget runs only when nothing else does);
+    ``free_workers``: idle gradient worker streams; ``cells_active`` / ``forward_active``: grid
+    cells and presence of forward requests in (or joining) the group."""
+    if used + r.bytes_needed > budget_bytes and busy:
+        return False
+    if r.kind == "gradient":
+        return free_workers > 0
+    return not (max_active_cells is not None and forward_active
+                and cells_active + r.cells > max_active_cells)
+
+
 def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, stream=None,
                      clock=time.perf_counter, gradient_workers: int = 2,
                      max_active_cells: int | None = None) -> dict:
@@ -139,22 +155,17 @@ def serve_continuous(requests, *, budget_bytes: int, chunk_steps: int = 256, str
         allow: gradient requests start on a worker stream, forward requests are built."""
         nonlocal used, cells_active
         now = clock() - t0
-        while pending and pending[0].arrival <= now and (
-                used + pending[0].bytes_needed <= budget_bytes
-                or not (active or joining or running)):
-            r = pending[0]
+        while pending and pending[0].arrival <= now and admissible(
+                pending[0], used=used, budget_bytes=budget_bytes,
+                busy=bool(active or joining or running), free_workers=len(free_streams),
+                cells_active=cells_active, forward_active=bool(active or joining),
+                max_active_cells=max_active_cells):
+            r = pending.pop(0)
             if r.kind == "gradient":
-                if not free_streams:
-                    break
-                pending.pop(0)
                 r.admitted = clock() - t0
                 s = free_streams.pop()
                 running[pool.submit(gradient, r, s)] = (r, s)
             else:
-                if (max_active_cells is not None and (active or joining)
-                        and cells_active + r.cells > max_active_cells):
-                    break
-                pending.pop(0)
                 cells_active += r.cells
                 with torch.cuda.stream(build):
                     eng = Engine(r.build(), validate=False)

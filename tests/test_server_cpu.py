@@ -48,3 +48,26 @@ def test_gradient_memory_estimate_grows_with_grid_and_checkpoints():
     assert b25 < b10 < small.bytes_needed()
     nb = small.problem.nb
     assert small.bytes_needed() > engine_bytes((128 + 2 * nb, 128 + 2 * nb), 600, 64)
+
+
+def test_admission_rule():
+    """FIFO head admission: memory budget (an oversized request only when nothing else runs),
+    idle worker streams for gradient requests, and the cap on grid cells stepping together
+    (the first forward request is always admitted)."""
+    from fullwave25_gb300.server import Request, admissible
+
+    fwd = Request(rid=0, arrival=0.0, build=None, bytes_needed=4, cells=10)
+    grad = Request(rid=1, arrival=0.0, build=None, bytes_needed=4, kind="gradient")
+    big = Request(rid=2, arrival=0.0, build=None, bytes_needed=100, cells=10)
+    kw = dict(used=0, budget_bytes=10, busy=False, free_workers=1, cells_active=0,
+              forward_active=False, max_active_cells=None)
+    assert admissible(fwd, **kw) and admissible(grad, **kw)
+    assert not admissible(fwd, **{**kw, "used": 8, "busy": True})        # over the budget
+    assert admissible(big, **kw)                                          # alone: runs anyway
+    assert not admissible(big, **{**kw, "busy": True})
+    assert not admissible(grad, **{**kw, "free_workers": 0})              # no idle worker
+    capped = {**kw, "max_active_cells": 15, "busy": True, "used": 4}
+    assert admissible(fwd, **capped)                                      # nothing stepping yet
+    assert not admissible(fwd, **{**capped, "cells_active": 10, "forward_active": True})
+    assert admissible(fwd, **{**capped, "cells_active": 5, "forward_active": True})
+    assert admissible(grad, **{**capped, "cells_active": 10, "forward_active": True})
