@@ -53,7 +53,7 @@ typedef struct fw_desc {
     int32_t ncoords;        /* source cells */
     int32_t ncoordsout;     /* sensor cells */
     int32_t ncoordszero;    /* air (zero-pressure) cells */
-    int32_t ndmap;          /* tap sets in dmap */
+    int32_t ndmap;          /* tap sets in dmap, 1..65535 (a cell's index is kept in 16 bits) */
     int32_t isotropic;      /* 1: isotropic relaxation maps (fw_set_fields); 0: one set of maps
                                per derivative axis (fw_set_fields_aniso) */
     int32_t n_relax;        /* 2: the relaxation engine; 0: the exponential-attenuation engine
