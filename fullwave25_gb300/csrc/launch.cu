@@ -206,19 +206,27 @@ using EncodeTiledFn = CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t
                                    const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
                                    CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
 
+// The driver's tensor-map encoder, looked up once per process (thread-safe static
+// initialisation: handles are created from several threads, e.g. serving and gradient workers).
+EncodeTiledFn tensor_map_encoder() {
+  static const EncodeTiledFn fn = [] {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    const cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                                           cudaEnableDefault, &q);
+    return (e == cudaSuccess && p && q == cudaDriverEntryPointSuccess)
+               ? reinterpret_cast<EncodeTiledFn>(p)
+               : nullptr;
+  }();
+  return fn;
+}
+
 int encode_map(fw_handle* h, CUtensorMap* map, void* base, cuuint32_t rank,
                const cuuint64_t* dims, const cuuint64_t* strides, const cuuint32_t* box,
                CUtensorMapDataType type) {
-  static EncodeTiledFn encode = nullptr;
-  if (!encode) {
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q{};
-    cudaError_t e = cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000,
-                                                     cudaEnableDefault, &q);
-    if (e != cudaSuccess || !fn || q != cudaDriverEntryPointSuccess)
-      return fail(h, FW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
-    encode = reinterpret_cast<EncodeTiledFn>(fn);
-  }
+  const EncodeTiledFn encode = tensor_map_encoder();
+  if (!encode)
+    return fail(h, FW_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
   const cuuint32_t estr[4] = {1, 1, 1, 1};
   CUresult r = encode(map, type, rank, base, dims, strides, box, estr,
                       CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
