@@ -133,3 +133,15 @@ def _lossless():
     if "run" not in _LOSSLESS:
         _LOSSLESS["run"] = _run(0.0, 1.1)
     return _LOSSLESS["run"]
+
+
+def test_pml_absorbs_the_outgoing_pulse():
+    """Lossless run: after the direct pulse has passed the deeper sensor (40 cells before the
+    far boundary's transition + PML of 20 + 20 cells), nothing returns above -40 dB of its peak
+    (measured: -52 dB); an unabsorbed reflection from the zero ghost layer would return at 0 dB."""
+    tr, _, _ = _lossless()
+    s = tr[:, 1]
+    ip = int(np.argmax(np.abs(s)))
+    late = np.abs(s[ip + 100:]).max()
+    assert ip + 400 < len(s)   # the window covers the round trip to the PML and back
+    assert 20 * np.log10(late / np.abs(s).max()) < -40
