@@ -189,3 +189,60 @@ def test_exponential_engine_attenuates_alpha0_f0_at_every_frequency(a0):
         excess = loss[a0] - loss[0.0]
         target = a0 * F0 / 1e6
         assert abs(excess - target) < 0.02 * target, f"{freq / 1e6} MHz: {excess:.4f} dB/cm"
+
+
+def _nonlinear_run(beta, xs, ppw=12, nx=480, ny=200, waist=60.0, ncyc=10):
+    from fullwave25_gb300.grid import Grid
+    from fullwave25_gb300.inputs import build_inputs
+    from fullwave25_gb300.medium import MediumRelaxationMaps
+    from fullwave25_gb300.pml import PMLBuilder
+    from fullwave25_gb300.pulse import gaussian_modulated_sinusoidal_signal
+    from fullwave25_gb300.relaxation import default_table
+    from fullwave25_gb300.source import Sensor, Source
+
+    g0 = Grid.from_cells((nx, ny), f0=F0, nt=1, ppw=ppw, cfl=0.2)
+    nt = int(1.1 * nx * g0.dx / 1540.0 / g0.dt) + int(ncyc * 1.6 * ppw * 5) + 300
+    g = Grid.from_cells((nx, ny), f0=F0, nt=nt, ppw=ppw, cfl=0.2)
+    relax = default_table().lookup(np.zeros((nx, ny)), np.full((nx, ny), 1.1))   # lossless
+    med = MediumRelaxationMaps(g, np.full((nx, ny), 1540.0), np.full((nx, ny), 1000.0),
+                               np.full((nx, ny), beta), relax)
+    mask = np.zeros((nx, ny), dtype=bool)
+    mask[0, :] = True
+    sig = gaussian_modulated_sinusoidal_signal(nt=nt, duration=g.duration, ncycles=ncyc,
+                                               drop_off=2, f0=F0, p0=1e6)
+    apod = np.exp(-((np.arange(ny) - (ny - 1) / 2) / waist) ** 2)
+    smask = np.zeros((nx, ny), dtype=bool)
+    for x in xs:
+        smask[x, ny // 2] = True
+    b = PMLBuilder(g, med, Source(apod[:, None] * sig[None, :], mask), Sensor(smask),
+                   n_pml_layer=20, n_transition_layer=20)
+    return run_oracle_c(build_inputs(b.extended_grid, b.run(), b.extended_source,
+                                     b.extended_sensor)), g
+
+
+def _band_envelope_peak(s, dt, fc, half_width=0.6e6):
+    """Peak of the analytic-signal envelope of s band-passed to fc +- half_width."""
+    spec = np.fft.fft(s)
+    f = np.fft.fftfreq(len(s), dt)
+    keep = np.where((f > fc - half_width) & (f < fc + half_width), 2.0, 0.0)
+    return np.abs(np.fft.ifft(spec * keep)).max()
+
+
+def test_nonlinearity_grows_the_second_harmonic_as_theory():
+    """beta = 4, a 1 MPa 10-cycle tone burst at 3 MHz in a lossless medium: the second harmonic
+    grows with distance x as the quasi-linear plane-wave solution of the model's nonlinear term
+    (p <- p - dt (K + 2 beta p) div v, i.e. local speed c + beta p / (rho c)):
+    A2 / A1^2 = beta w x / (2 rho c^3), within 10 % at 3.9, 10.7 and 18.0 mm (measured 4-7 %);
+    with beta = 0 no harmonic appears (A2 / A1 < 1e-3)."""
+    xs = (90, 250, 420)
+    w = 2 * np.pi * F0
+    tr, g = _nonlinear_run(4.0, xs)
+    for i, x in enumerate(xs):
+        a1 = _band_envelope_peak(tr[:, i], g.dt, F0)
+        a2 = _band_envelope_peak(tr[:, i], g.dt, 2 * F0)
+        theory = 4.0 * w * (x * g.dx) / (2 * 1000.0 * 1540.0 ** 3)
+        assert abs(a2 / a1**2 / theory - 1) < 0.10, f"x = {x}: {a2 / a1**2 / theory:.3f}"
+    tr0, g0 = _nonlinear_run(0.0, xs)
+    for i in range(len(xs)):
+        a1 = _band_envelope_peak(tr0[:, i], g0.dt, F0)
+        assert _band_envelope_peak(tr0[:, i], g0.dt, 2 * F0) / a1 < 1e-3
