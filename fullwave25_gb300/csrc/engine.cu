@@ -86,19 +86,16 @@ __global__ void transform_maps(float* rho_to_rdt, float* k_to_dtk, float* beta_t
                                int64_t n, float dt) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
        c += (int64_t)gridDim.x * blockDim.x) {
-    const float r = rho_to_rdt[c];
-    rho_to_rdt[c] = r != 0.f ? dt / r : 0.f;
-    k_to_dtk[c] = dt * k_to_dtk[c];
-    beta_to_2dt[c] = 2.f * dt * beta_to_2dt[c];
+    rho_to_rdt[c] = fwgb::derive_rdt_rho(dt, rho_to_rdt[c]);
+    k_to_dtk[c] = fwgb::derive_dt_k(dt, k_to_dtk[c]);
+    beta_to_2dt[c] = fwgb::derive_beta2dt(dt, beta_to_2dt[c]);
   }
 }
 
 __global__ void invert_map(float* kappa_to_inv, int64_t n) {
   for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n;
-       c += (int64_t)gridDim.x * blockDim.x) {
-    const float k = kappa_to_inv[c];
-    kappa_to_inv[c] = k != 0.f ? 1.f / k : 0.f;
-  }
+       c += (int64_t)gridDim.x * blockDim.x)
+    kappa_to_inv[c] = fwgb::derive_inverse(kappa_to_inv[c]);
 }
 
 __global__ void transpose_icmat(const float* src, float* dst, int ncoords, int nt_ic) {

@@ -86,6 +86,14 @@ __device__ __forceinline__ void pdl_entry() {
   asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
 }
 
+// Derived coefficient maps, formed once from the caller's maps (the same float32 operations for
+// every entry point that prepares them): dt/rho, dt*K, 2*dt*beta and 1/kappa, with a zero map
+// entry (ghost cells of a map the caller left at zero) kept at zero.
+__device__ __forceinline__ float derive_rdt_rho(float dt, float rho) { return rho != 0.f ? dt / rho : 0.f; }
+__device__ __forceinline__ float derive_dt_k(float dt, float k) { return dt * k; }
+__device__ __forceinline__ float derive_beta2dt(float dt, float beta) { return 2.f * dt * beta; }
+__device__ __forceinline__ float derive_inverse(float kappa) { return kappa != 0.f ? 1.f / kappa : 0.f; }
+
 __device__ __forceinline__ void load_taps(const float* taps, int dc, float (&c)[8], float& co) {
   const float4* t = reinterpret_cast<const float4*>(taps + (size_t)dc * kTapStride);
   float4 a = __ldg(t), b = __ldg(t + 1), e = __ldg(t + 2);

@@ -264,24 +264,33 @@ FWGB_API int fw_group_block_tile(const fw_group *g, int32_t tile[3]);
 
 FWGB_API int fw_group_destroy(fw_group *g);
 
-/* Bytes of the file-scope device array that fw_run_noalloc keeps its wavefield in (32 MiB):
- * 2D grids up to 762,600 cells (11 float32 fields per cell). */
-#define FWGB_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+/* Bytes of the file-scope device array in which fw_run_noalloc keeps everything it needs besides
+ * the caller's inputs and outputs (48 MiB): 66 bytes per grid cell (11 state fields, 5 derived
+ * coefficient maps, a 16-bit tap index) plus 48 bytes per tap set and one byte per source, so 2D
+ * grids up to about 760,000 cells (e.g. the 944 x 688 PML-extended plain 2D workload). */
+#define FWGB_NOALLOC_SCRATCH_BYTES (48u * 1024u * 1024u)
 
 /* Full 2D forward solve that allocates nothing. This entry point has no counterpart in the
  * reference; it exists for callers that cannot call cudaMalloc while they run: applications whose
  * device memory comes only from their own pool, processes that must not grow their device
  * footprint after start-up, or code that only holds device buffers handed to it. Inputs
- * (`f`, with on_device = 1: device pointers, source coordinates distinct) and the output traces
- * (device memory, [n_out][ncoordsout]) are the caller's; the wavefield and memory variables live in
- * one file-scope device array of FWGB_NOALLOC_SCRATCH_BYTES that every GPU which loads this library
- * holds until the process exits. Grids that need more than that are rejected with
- * FW_ERR_ARGUMENT; 3D grids with FW_ERR_UNSUPPORTED. Each call zeroes the part of the array it
- * uses; the array keeps the last call's contents afterwards. All calls share the one array, so
- * calls that overlap on the GPU (other streams, other host threads) race: serialise them. The first
- * call on a device looks the array's device address up (cudaGetSymbolAddress) with that device
- * current; make that first call before any stream capture. Asynchronous on `stream`; errors are
- * reported by fw_last_error(NULL). Same results as fw_create + fw_set_fields + fw_run. */
+ * (`f`, with on_device = 1: device pointers) and the output traces (device memory,
+ * [n_out][ncoordsout]) are the caller's; the wavefield, memory variables, derived maps and tap
+ * table live in one file-scope device array of FWGB_NOALLOC_SCRATCH_BYTES that every GPU which
+ * loads this library holds until the process exits. Grids that need more than that are rejected
+ * with FW_ERR_ARGUMENT; 3D grids with FW_ERR_UNSUPPORTED.
+ * Before stepping, every source, sensor and air coordinate and every dcmap entry is checked on the
+ * device against the grid; the call waits for that check (it synchronises `stream` once) and
+ * returns FW_ERR_ARGUMENT, naming the first offending entry, without running any time step and
+ * without writing `traces`, if one lies outside. A cell listed twice as a source is driven by its
+ * last entry. After the check the solve is queued asynchronously on `stream`; its traces equal
+ * those of fw_create + fw_set_fields + fw_run bit for bit.
+ * Each call clears the parts of the array it uses that must start at zero; the array keeps the
+ * last call's contents afterwards. All calls share the one array, so calls that overlap on the GPU
+ * (other streams, other host threads) race: serialise them. Each call looks the array's device
+ * address up (cudaGetSymbolAddress) with the calling thread's current device; the first call on a
+ * device also loads this library's device code there, so make that first call before any stream
+ * capture. Errors are reported by fw_last_error(NULL). */
 FWGB_API int fw_run_noalloc(const fw_desc *desc, const fw_fields *f, void *stream, float *traces);
 
 /* Description of the last failure on this handle (or of the last failed fw_create when
