@@ -1,8 +1,11 @@
 """Generate the golden fixtures in this folder from the reference's own Python pre-processing.
 
-Run in a container that has the reference checkout (read-only) at ``/root/reference``:
+Run where a checkout of the reference is available (it is only read):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py --reference <reference checkout> [--only NAME,...]
+
+(or set ``FULLWAVE_REFERENCE`` to the checkout instead of passing ``--reference``). ``--only``
+regenerates a subset: ``coeff``, ``cases``, ``exp_cases``, ``pulse``, ``transducer``.
 
 The reference imports matplotlib, cv2 and tqdm only for plotting and progress bars; this script
 puts empty stand-ins for them on ``sys.path`` (in a temporary folder) before importing it. Nothing
@@ -18,13 +21,15 @@ here runs the reference's engine executables. Outputs (committed):
 
 from __future__ import annotations
 
+import argparse
+import os
 import sys
 import tempfile
 from pathlib import Path
 
 import numpy as np
 
-REFERENCE = Path("/root/reference")
+REFERENCE: Path | None = None   # set from --reference / FULLWAVE_REFERENCE by main()
 HERE = Path(__file__).resolve().parent
 
 _STUB = '''
@@ -236,17 +241,100 @@ def coefficient_tables(fw, tmp: Path):
     print(f"coeff_tables: {len(out)} arrays")
 
 
+PULSE_PARAMS = [
+    # nt, duration factor (x nt dt), ncycles, drop_off, f0, p0, delay_sec, i_layer
+    (400, 1.0, 2, 2, 3e6, 1e6, 0.0, 0),
+    (600, 1.0, 3, 1, 2.5e6, 2e5, 1.5e-7, 0),
+    (500, 1.0, 2, 2, 5e6, 1e6, 0.0, 3),
+    (300, 1.0, 1, 3, 4e6, 1.0, -2e-8, 1),
+]
+
+
+def pulse_golden(fw):
+    from fullwave.utils.pulse import gaussian_modulated_sinusoidal_signal  # noqa: PLC0415
+
+    out = {}
+    for k, (nt, fac, ncyc, drop, f0, p0, delay, layer) in enumerate(PULSE_PARAMS):
+        dx = 1540.0 / f0 / 12
+        dt = 0.2 * dx / 1540.0
+        kw = dict(nt=nt, duration=fac * nt * dt, ncycles=ncyc, drop_off=drop, f0=f0, p0=p0,
+                  delay_sec=delay)
+        if layer:
+            kw.update(i_layer=layer, dt_for_layer_delay=dt, cfl_for_layer_delay=0.2)
+        out[f"signal_{k}"] = gaussian_modulated_sinusoidal_signal(**kw)
+        out[f"params_{k}"] = np.array([nt, fac * nt * dt, ncyc, drop, f0, p0, delay, layer, dt, 0.2])
+    np.savez_compressed(HERE / "pulse.npz", **out)
+    print(f"pulse: {len(PULSE_PARAMS)} signals")
+
+
+def transducer_golden(fw):
+    from fullwave.transducer import Transducer, TransducerGeometry  # noqa: PLC0415
+
+    f0, c0, ppw, cfl, nt = 3e6, 1540.0, 12, 0.2, 60
+    dx = c0 / f0 / ppw
+    out = {}
+    layouts = {
+        "linear": ((40, 60), dict(number_elements=8, element_width_px=4, element_spacing_px=2,
+                                  element_layer_px=2, position_px=(3, 5)),
+                   (True, False, True, True, True, False, True, True)),
+        # with this pixel layout the convex array's element 7 has no sensor on its surface (the
+        # reference's own geometry), so it is inactive here, like element 3
+        "convex": ((80, 120), dict(number_elements=12, element_width_px=5, element_spacing_px=1,
+                                   element_layer_px=2, position_px=(6, 20), radius=0.1),
+                   (True, True, False, True, True, True, False, True, True, True, True, True)),
+    }
+    rng = np.random.default_rng(7)
+    for name, (shape, geo, active) in layouts.items():
+        grid = fw.Grid(domain_size=(shape[0] * dx, shape[1] * dx), f0=f0,
+                       duration=nt * cfl * dx / c0, c0=c0, ppw=ppw, cfl=cfl)
+        geom = TransducerGeometry(grid, **geo)
+        tr = Transducer(geom, grid, active_sensor_elements=active)
+        oc = np.asarray(tr.sensor.outcoords)
+        surf = tr.element_id_to_element_surface
+        ids = np.concatenate([np.full(len(v), k) for k, v in sorted(surf.items())])
+        coords = np.concatenate([np.asarray(v).reshape(-1, 2) for _, v in sorted(surf.items())])
+        traces = rng.standard_normal((oc.shape[0], nt)).astype(np.float32)
+        out[f"{name}/outcoords"] = oc
+        out[f"{name}/surface_id"] = ids
+        out[f"{name}/surface_coords"] = coords
+        out[f"{name}/active"] = np.asarray(tr.active_sensor_elements, dtype=bool)
+        out[f"{name}/traces"] = traces
+        out[f"{name}/averaged"] = tr.post_process_sensor_output(traces)
+        out[f"{name}/centre"] = tr.post_process_sensor_output(traces,
+                                                              average_surface_signals=False)
+        print(f"transducer {name}: {oc.shape[0]} sensors, {int(out[f'{name}/active'].sum())} "
+              "active elements")
+    np.savez_compressed(HERE / "transducer_post.npz", **out)
+
+
 def main():
+    global REFERENCE
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--reference", default=os.environ.get("FULLWAVE_REFERENCE"),
+                    help="checkout of the reference package (or FULLWAVE_REFERENCE)")
+    ap.add_argument("--only", default="coeff,cases,exp_cases,pulse,transducer")
+    args = ap.parse_args()
+    if not args.reference:
+        ap.error("pass --reference <checkout> or set FULLWAVE_REFERENCE")
+    REFERENCE = Path(args.reference)
+    only = set(args.only.split(","))
     with tempfile.TemporaryDirectory() as td:
         tmp = Path(td)
         stub_dir = tmp / "stubs"
         stub_dir.mkdir()
         fw = _import_reference(stub_dir)
-        coefficient_tables(fw, tmp)
-        for name, spec in CASES.items():
-            build_case(fw, name, spec, tmp)
-        for name, spec in EXP_CASES.items():
-            build_exp_case(fw, name, spec, tmp)
+        if "coeff" in only:
+            coefficient_tables(fw, tmp)
+        if "cases" in only:
+            for name, spec in CASES.items():
+                build_case(fw, name, spec, tmp)
+        if "exp_cases" in only:
+            for name, spec in EXP_CASES.items():
+                build_exp_case(fw, name, spec, tmp)
+        if "pulse" in only:
+            pulse_golden(fw)
+        if "transducer" in only:
+            transducer_golden(fw)
 
 
 if __name__ == "__main__":
