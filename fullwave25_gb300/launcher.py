@@ -30,14 +30,39 @@ class SimulationError(Exception):
     """Exception raised for errors in the simulation."""
 
 
-def _first_device(cuda_device_id) -> int:
+def device_list(cuda_device_id) -> list:
+    """The device ids named by ``cuda_device_id`` (None, an int, "0,1,2" or a list), as the
+    reference reads them to set CUDA_VISIBLE_DEVICES (launcher.py:64-105, :206)."""
     if cuda_device_id is None:
-        return 0
+        return [0]
     if isinstance(cuda_device_id, (list, tuple)):
         if not cuda_device_id:
             raise ValueError("cuda_device_id list is empty")
-        return int(cuda_device_id[0])
-    return int(str(cuda_device_id).split(",")[0])
+        return [int(v) for v in cuda_device_id]
+    ids = [v.strip() for v in str(cuda_device_id).split(",") if v.strip()]
+    if not ids:
+        raise ValueError(f"cuda_device_id {cuda_device_id!r} names no device")
+    return [int(v) for v in ids]
+
+
+_WARNED_MULTI: set = set()
+
+
+def resolve_device(cuda_device_id) -> int:
+    """The device one simulation runs on: the first listed id. The reference splits one
+    simulation into depth slabs across every listed GPU inside its executables; this engine runs
+    a simulation on one GPU (depth slabs exist as a tested decomposition, ``slabs.py``, without a
+    peer-to-peer transport), so when several ids are listed it says so once and uses the first."""
+    ids = device_list(cuda_device_id)
+    if len(ids) > 1 and tuple(ids) not in _WARNED_MULTI:
+        _WARNED_MULTI.add(tuple(ids))
+        logger.warning("cuda_device_id lists %d GPUs %s: one simulation runs on one GPU here; "
+                       "using GPU %d (run independent simulations on the others)", len(ids), ids,
+                       ids[0])
+    return ids[0]
+
+
+_first_device = resolve_device
 
 
 class Launcher:
@@ -49,8 +74,9 @@ class Launcher:
         self._path_fullwave_simulation_bin = path_fullwave_simulation_bin
         self.is_3d = is_3d
         self.use_gpu = use_gpu
-        self.device_index = _first_device(cuda_device_id)
-        self.cuda_device_id = str(self.device_index)
+        self.device_ids = device_list(cuda_device_id)
+        self.device_index = resolve_device(cuda_device_id)
+        self.cuda_device_id = ",".join(str(v) for v in self.device_ids)
         self.last_timing: dict = {}
 
     def run(self, simulation_dir: Path, *, load_results: bool = True):

@@ -10,7 +10,7 @@ import pytest
 
 import fullwave25_gb300.engine as engine_mod
 from fullwave25_gb300 import Launcher, SimulationError
-from fullwave25_gb300.launcher import _first_device
+from fullwave25_gb300.launcher import device_list, resolve_device
 from golden_io import write_case_dir
 
 
@@ -92,7 +92,21 @@ def test_missing_inputs_are_a_simulation_error(no_cuda):
             Launcher().run(Path(td))
 
 
-@pytest.mark.parametrize("given,expected", [(None, 0), (2, 2), ("1", 1), ("3,4", 3), ([5, 6], 5)])
+@pytest.mark.parametrize("given,expected", [(None, [0]), (2, [2]), ("1", [1]), ("3,4", [3, 4]),
+                                            ([5, 6], [5, 6]), (" 7 , 2", [7, 2])])
 def test_device_selection(given, expected):
-    assert _first_device(given) == expected
-    assert Launcher(cuda_device_id=given).device_index == expected
+    assert device_list(given) == expected
+    assert resolve_device(given) == expected[0]
+    la = Launcher(cuda_device_id=given)
+    assert la.device_index == expected[0] and la.device_ids == expected
+    assert la.cuda_device_id == ",".join(map(str, expected))
+
+
+def test_several_devices_are_reported_not_silently_dropped(caplog):
+    import logging
+
+    with caplog.at_level(logging.WARNING):
+        assert resolve_device([3, 1, 2]) == 3
+    assert any("one simulation runs on one GPU" in r.getMessage() for r in caplog.records)
+    with pytest.raises(ValueError):
+        device_list([])
