@@ -17,6 +17,15 @@ step uploads that step's inputs from pinned host memory (plain2d: every map and 
 signals, i.e. a full ``fw_set_fields``; plain3d: the source-signal columns of the step's 100
 time steps) and reads the step's sensor traces back to host memory.
 
+The default line (plain3d, one GPU) also carries ``extra``: secondary workloads measured in the
+same run, each with its own CUDA-event timing and its own check against the FP64 oracle or the
+one-by-one path: ``plain2d`` (full solves, rel-L2 of a full solve against the FP64 C oracle,
+e2e), ``batched`` (64 simulations: group engine vs one by one on the device, vs one by one
+through ``Solver.run()`` on 16 instances and through the host-side NumPy pre-processing on 8),
+``serving_short`` (10 s of the Poisson stream at half size: continuous batching vs FIFO) and
+``solver_config0`` (host-to-host ``Solver.run()`` of the plain 2D problem, GPU and NumPy
+pre-processing). ``--no-extra`` (or FWGB_BENCH_EXTRA=0) leaves them out.
+
 Multi-GPU (torchrun): every rank runs an independent replica of the workload (the engine does
 not shard a single solve); ``value`` = cell-updates of all ranks / max rank time ("weak").
 ``--impl reference`` times the reference path's CPU implementation: the reference ships no
@@ -272,31 +281,30 @@ def run_reference(args):
 
 
 # --------------------------------------------------------------------------------- GPU arm
-def run_gpu(args):
+def measure_forward(workload, physics="isotropic", grid=0, steps=10, warmup=3, *,
+                    cpu_baseline=True, full_parity=False):
+    """The plain 2D / 3D forward workload on this rank's GPU; returns the bench line (rank 0) or
+    None (other ranks). ``full_parity``: rel-L2 of one full solve against the FP64 C oracle
+    (plain2d only) instead of the CPU-sample parity that comes with ``cpu_baseline``."""
     import torch
 
     from fullwave25_gb300.engine import Engine
     from fullwave25_gb300.workloads import algorithmic_bytes_per_cell
 
     rank, world, local = dist_info()
-    if world > 1:
-        import torch.distributed as dist
-
-        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    inputs, chunk, desc = make_workload(args.workload, rank, args.grid, args.physics)
-    engine = Engine(inputs) if args.workload == "plain2d" else inputs.make_engine()
+    inputs, chunk, desc = make_workload(workload, rank, grid, physics)
+    engine = Engine(inputs) if workload == "plain2d" else inputs.make_engine()
     stream = torch.cuda.current_stream(dev)
     sptr = stream.cuda_stream
     nt = inputs.nt
     cells = int(np.prod(inputs.shape))
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    do_flush = args.workload == "plain2d"
+    do_flush = workload == "plain2d"
 
     def bench_step(i):
         # plain2d: one full solve; plain3d: `chunk` steps continuing a solve
-        if args.workload == "plain2d":
+        if workload == "plain2d":
             engine.reset(sptr)
             engine.advance(nt, sptr)
         else:
@@ -309,15 +317,15 @@ def run_gpu(args):
         if world > 1:
             torch.distributed.barrier()
 
-    for i in range(args.warmup):
+    for i in range(warmup):
         bench_step(i)
     barrier()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
     with ClockSampler(local) as clocks:
         barrier()
         t0 = time.perf_counter()
-        for i in range(args.steps):
+        for i in range(steps):
             if do_flush:
                 flush.fill_(float(i))
             starts[i].record(stream)
@@ -328,38 +336,53 @@ def run_gpu(args):
     dev_ms = sum(s.elapsed_time(e) for s, e in zip(starts, ends))
     from fullwave25_gb300.replicas import aggregate_throughput
 
-    _, t_max, units_per_s = aggregate_throughput(cells * chunk * args.steps, dev_ms / 1e3)
+    _, t_max, units_per_s = aggregate_throughput(cells * chunk * steps, dev_ms / 1e3)
     value = units_per_s / 1e9
-    ms_per_step = t_max * 1e3 / args.steps
+    ms_per_step = t_max * 1e3 / steps
 
     # roofline: one time step (velocity + pressure kernels) over the whole grid
-    step_s = (dev_ms / 1e3) / (chunk * args.steps)
-    bpc = algorithmic_bytes_per_cell(len(inputs.shape), physics=args.physics)
+    step_s = (dev_ms / 1e3) / (chunk * steps)
+    bpc = algorithmic_bytes_per_cell(len(inputs.shape), physics=physics)
     alg_bytes = bpc * cells
     achieved = alg_bytes / step_s / 1e9
     peaks = json.loads((ROOT / "MEASURED_PEAKS.json").read_text()) if (
         ROOT / "MEASURED_PEAKS.json").exists() else {}
     peak = float(peaks.get("hbm_gbs", 6800.0))
-    tr = traffic_from_profiles(args.workload) if args.physics == "isotropic" else None
+    tr = traffic_from_profiles(workload) if physics == "isotropic" else None
 
     # e2e through the C ABI with host buffers
-    e2e = run_e2e(args, engine, inputs, chunk, sptr, dev, world)
+    e2e = run_e2e(workload, steps, engine, inputs, chunk, sptr, dev, world)
     clk = clocks.summary()
+    parity = None
+    if full_parity and rank == 0:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        from fdtd_oracle_c import run_oracle_c
+
+        engine.reset(sptr)
+        got = engine.run(sptr)
+        t0 = time.perf_counter()
+        ref = run_oracle_c(inputs)
+        parity = {"rel_l2_vs_fp64_oracle": float(np.linalg.norm(got - ref) / np.linalg.norm(ref)),
+                  "tolerance": 1e-4,
+                  "sample": f"one full solve ({inputs.shape[0]}x{inputs.shape[1]}, {nt} steps, "
+                            f"{inputs.outc.shape[0]} sensors) against the FP64 C oracle "
+                            f"({time.perf_counter() - t0:.1f} s on the host cores)"}
+    kernels, tile, launches = engine.kernel_variant, list(engine.block_tile), engine.launches_per_step
+    engine.close()
+    del engine, flush
     if rank != 0:
-        engine.close()
-        return
-    cpu = time_oracle(args.workload, float(os.environ.get("FWGB_CPU_SAMPLE_S", "15")),
-                      args.physics) if (world == 1 and not args.no_cpu_baseline) else None
-    parity = parity_vs_oracle() if cpu is not None else None
-    cpu_numpy = (time_numpy_oracle(args.workload, float(os.environ.get("FWGB_NUMPY_SAMPLE_S", "5")))
-                 if cpu is not None else None)
-    line = {
-        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
+        return None
+    cpu = cpu_numpy = None
+    if cpu_baseline and world == 1:
+        cpu = time_oracle(workload, float(os.environ.get("FWGB_CPU_SAMPLE_S", "15")), physics)
+        parity = parity_vs_oracle()
+        cpu_numpy = time_numpy_oracle(workload, float(os.environ.get("FWGB_NUMPY_SAMPLE_S", "5")))
+    return {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": world, "steps": steps,
+        "warmup": warmup, "ms_per_step": ms_per_step, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {**desc, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "wall_s_timed": wall, "kernels": engine.kernel_variant,
-                   "block_tile_xyz": list(engine.block_tile)},
+                   "wall_s_timed": wall, "kernels": kernels, "block_tile_xyz": tile},
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak,
                      "traffic": (tr * cells if tr is not None else None),
@@ -371,20 +394,109 @@ def run_gpu(args):
         "cpu_baseline_numpy": cpu_numpy,
         "parity": parity,
         "e2e": e2e,
-        "gpu_launches": int(engine.launches_per_step * chunk * args.steps),
+        "gpu_launches": int(launches * chunk * steps),
         "clocks": clk,
     }
-    print(json.dumps(line), flush=True)
-    engine.close()
 
 
-def run_e2e(args, engine, inputs, chunk, sptr, dev, world):
+def run_gpu(args):
     import torch
 
-    from fullwave25_gb300.engine import Engine
+    rank, world, local = dist_info()
+    if world > 1:
+        import torch.distributed as dist
 
-    n_e2e = max(1, min(args.steps, 5))
-    if args.workload == "plain2d":
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    line = measure_forward(args.workload, args.physics, args.grid, args.steps, args.warmup,
+                           cpu_baseline=not args.no_cpu_baseline)
+    if line is None:
+        return
+    if (world == 1 and args.workload == "plain3d" and args.physics == "isotropic" and not args.grid
+            and not args.no_extra and os.environ.get("FWGB_BENCH_EXTRA", "1") != "0"):
+        torch.cuda.empty_cache()
+        line["extra"] = collect_extras()
+        line["extra_keys"] = sorted(line["extra"])
+    print(json.dumps(line), flush=True)
+
+
+def collect_extras() -> dict:
+    """Secondary workloads of the default run (one GPU), each timed and checked on its own."""
+    import torch
+
+    out = {}
+    t0 = time.perf_counter()
+    p2 = measure_forward("plain2d", steps=3, warmup=3, cpu_baseline=False, full_parity=True)
+    out["plain2d"] = {k: p2[k] for k in ("value", "unit", "ms_per_step", "parity", "e2e", "clocks")}
+    out["plain2d"].update(workload=p2["config"]["workload"], kernels=p2["config"]["kernels"],
+                          l2=p2["config"]["l2"],
+                          roofline={k: p2["roofline"][k] for k in ("achieved", "peak", "frac",
+                                                                   "unit")})
+    torch.cuda.empty_cache()
+    b = measure_batch(64, steps=1, warmup=1, host_sample=8, solver_sample=16)
+    out["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "sims_per_s", "e2e",
+                                        "one_by_one_host_api", "one_by_one_solver_run",
+                                        "one_by_one_latency_ms", "batched_latency_ms", "parity",
+                                        "clocks")}
+    out["batched"]["workload"] = b["config"]["workload"]
+    out["batched"]["roofline"] = {k: b["roofline"][k] for k in ("achieved", "peak", "frac", "unit")}
+    torch.cuda.empty_cache()
+    sv = measure_serve(rate=20.0, duration=10.0, scale=0.5, budget_gb=150, max_active_mcells=16.0,
+                       grad_frac=0.2, host_sample=8)
+    out["serving_short"] = {"sims_per_s": sv["value"], "unit": "sims/s",
+                            "workload": sv["config"]["workload"],
+                            "continuous": sv["continuous"], "fifo_one_at_a_time": sv["fifo_one_at_a_time"],
+                            "continuous_over_fifo": sv["sims_per_s_ratio"],
+                            "one_by_one_host_api_forward_sample": sv["one_by_one_host_api_forward_sample"],
+                            "clocks": sv["clocks"]}
+    torch.cuda.empty_cache()
+    out["solver_config0"] = solver_host_to_host(engine_solve_ms=p2["ms_per_step"])
+    out["wall_s"] = time.perf_counter() - t0
+    return out
+
+
+def solver_host_to_host(engine_solve_ms=None) -> dict:
+    """``Solver.run()`` of the plain 2D problem (768 x 512 + PML 40 + transition 40, nt 4000),
+    host arrays in, traces [512, 4000] back on the host: GPU pre-processing (default) and the
+    NumPy pre-processing path; the medium arrays are built before the timed call."""
+    import tempfile
+
+    import torch
+
+    from fullwave25_gb300.solver import Solver
+    from fullwave25_gb300.workloads import plain_2d_problem
+
+    grid, medium, source, sensor, (n_pml, n_tr) = plain_2d_problem()
+    res = {"workload": "plain 2D problem through Solver.run(): 768x512 + PML 40 + transition 40 "
+                       "(944x688), nt 4000, 512 sources, 512 sensors"}
+    traces = {}
+    for on_device in (True, False):
+        kw = dict(pml_layer_thickness_px=n_pml, n_transition_layer=n_tr,
+                  preprocess_on_device=on_device)
+        Solver(tempfile.gettempdir(), grid, medium, source, sensor, **kw).run()   # warm-up
+        torch.cuda.synchronize()
+        runs = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            s = Solver(tempfile.gettempdir(), grid, medium, source, sensor, **kw)
+            traces[on_device] = s.run()
+            runs.append((time.perf_counter() - t0, dict(s.last_timing)))
+        best = min(runs, key=lambda r: r[0])
+        res["gpu_preprocessing" if on_device else "numpy_preprocessing"] = {
+            "host_to_host_s": best[0],
+            **{k: best[1][k] for k in ("preprocess_s", "upload_s", "engine_s")}}
+    a, b = traces[True], traces[False]
+    res["rel_l2_gpu_vs_numpy_preprocessing"] = float(np.linalg.norm(a - b) / np.linalg.norm(b))
+    if engine_solve_ms is not None:
+        res["engine_solve_ms_device_timed"] = engine_solve_ms
+    return res
+
+
+def run_e2e(workload, steps, engine, inputs, chunk, sptr, dev, world):
+    import torch
+
+    n_e2e = max(1, min(steps, 5))
+    if workload == "plain2d":
         # pinned host copies of every input array
         pinned = {}
 
@@ -427,19 +539,33 @@ def run_batch(args):
     """Batched 2D workload: the group engine vs the same simulations one by one."""
     import torch
 
-    from fullwave25_gb300.engine import EngineGroup
-    from fullwave25_gb300.workloads_batch import batch_instance
-
     rank, world, local = dist_info()
     torch.cuda.set_device(local)
-    dev = torch.device("cuda", local)
-    from fullwave25_gb300.replicas import rank_instances
-
     if world > 1:
         import torch.distributed as dist
 
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
-    ids = rank_instances(rank, world, args.batch)
+    line = measure_batch(args.batch, args.steps, args.warmup, args.host_sample, args.solver_sample)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+def measure_batch(n_batch, steps, warmup, host_sample, solver_sample):
+    """The group engine on this rank's share of the batched workload, against the same
+    simulations one by one: device-resident, through ``Solver.run()`` (GPU pre-processing) on
+    ``solver_sample`` instances, and through the host-side NumPy pre-processing on
+    ``host_sample`` instances; parity of the smallest member against the FP64 C oracle."""
+    import tempfile
+
+    import torch
+
+    from fullwave25_gb300.engine import EngineGroup
+    from fullwave25_gb300.replicas import rank_instances
+    from fullwave25_gb300.workloads_batch import batch_instance
+
+    rank, world, local = dist_info()
+    dev = torch.device("cuda", local)
+    ids = rank_instances(rank, world, n_batch)
     torch.zeros(1, device=dev)  # context creation outside the timed build
     # process warm-up outside the timed build: the first use of every builder and engine kernel
     # (module loading), on a small instance that is not part of the batch
@@ -454,17 +580,17 @@ def run_batch(args):
     sptr = stream.cuda_stream
     units = sum(int(np.prod(d.shape)) * d.nt for d in insts)
     grp = EngineGroup(engines)
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         grp.run(sptr)
     torch.cuda.synchronize(dev)
-    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * args.steps)]
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(2 * steps)]
     with ClockSampler(local) as clocks:
-        for i in range(args.steps):
+        for i in range(steps):
             ev[2 * i].record(stream)
             grp.run(sptr)
             ev[2 * i + 1].record(stream)
         torch.cuda.synchronize(dev)
-    group_ms = sum(ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(args.steps)) / args.steps
+    group_ms = sum(ev[2 * i].elapsed_time(ev[2 * i + 1]) for i in range(steps)) / steps
     # end to end, batched: device build (timed above) + group solve + every trace to the host
     t0 = time.perf_counter()
     traces = grp.traces()
@@ -486,12 +612,57 @@ def run_batch(args):
         lat.append(a.elapsed_time(b))
     serial_ms = sum(lat)
     batched_e2e_s = build_s + group_ms / 1e3 + readback_s
-    # end to end, one by one through the host-side API (the reference's call sequence: NumPy
-    # pre-processing, engine creation and upload, solve, traces back), on a sample of instances
+    # the smallest member against the FP64 C oracle (full nt)
+    parity = None
+    if rank == 0:
+        sys.path.insert(0, str(ROOT / "oracle"))
+        from fdtd_oracle_c import run_oracle_c
+
+        from fullwave25_gb300.workloads3d import to_host_inputs
+
+        k = int(np.argmin([np.prod(d.shape) * d.nt for d in insts]))
+        t0 = time.perf_counter()
+        ref = run_oracle_c(to_host_inputs(insts[k]))
+        parity = {"rel_l2_vs_fp64_oracle": float(np.linalg.norm(traces[k] - ref)
+                                                 / np.linalg.norm(ref)),
+                  "tolerance": 1e-4,
+                  "sample": f"batch member {ids[k]} ({insts[k].shape[0]}x{insts[k].shape[1]}, "
+                            f"nt {insts[k].nt}) from the group run, against the FP64 C oracle "
+                            f"({time.perf_counter() - t0:.1f} s on the host cores)"}
+    # one by one through the reference-facing API: Solver.run() (GPU pre-processing), on a
+    # sample of instances; the scenario objects (Grid, medium maps, Source, Sensor) are built
+    # before each timed call
+    from fullwave25_gb300.solver import Solver
+    from fullwave25_gb300.workloads_batch import batch_problem_host
+
+    solver_ids = list(ids[:solver_sample])
+    solver_s, solver_err, scenario_s = [], [], []
+    for n, i in enumerate(solver_ids):
+        t0 = time.perf_counter()
+        grid, medium, source, sensor, (n_pml, n_tr) = batch_problem_host(i)
+        t1 = time.perf_counter()
+        out = Solver(tempfile.gettempdir(), grid, medium, source, sensor,
+                     pml_layer_thickness_px=n_pml, n_transition_layer=n_tr).run()
+        solver_s.append(time.perf_counter() - t1)
+        scenario_s.append(t1 - t0)
+        ref = traces[n].T
+        solver_err.append(float(np.linalg.norm(out - ref) / max(np.linalg.norm(ref), 1e-30)))
+    grp_solver_s = None
+    if solver_ids:
+        with EngineGroup(engines[:len(solver_ids)]) as gs:
+            gs.run(sptr)  # untimed: shape autotuning of this group
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            gs.run(sptr)
+            b.record(stream)
+            torch.cuda.synchronize(dev)
+            grp_solver_s = a.elapsed_time(b) / 1e3
+    # end to end, one by one through the host-side NumPy pre-processing (the reference's call
+    # sequence: NumPy pre-processing, engine creation and upload, solve, traces back)
     from fullwave25_gb300.engine import Engine
     from fullwave25_gb300.workloads_batch import batch_inputs_host
 
-    sample = list(ids[:args.host_sample])
+    sample = list(ids[:host_sample])
     host_s, host_err = [], []
     for n, i in enumerate(sample):
         t0 = time.perf_counter()
@@ -521,7 +692,7 @@ def run_batch(args):
     tr = traffic_from_profiles("batch2d")
     cells_all = sum(int(np.prod(d.shape)) for d in insts)
     line = {"metric": METRIC, "value": units / (group_ms / 1e3) / 1e9, "unit": METRIC,
-            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "n_gpus": world, "steps": steps, "warmup": warmup,
             "ms_per_step": group_ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32", "data": "synthetic",
             "config": {"workload": f"batched 2D forward, {len(insts)} simulations of uneven "
@@ -534,12 +705,28 @@ def run_batch(args):
             "sims_per_s": {"batched": len(insts) / (group_ms / 1e3),
                            "one_by_one": len(insts) / (serial_ms / 1e3),
                            "batched_over_one_by_one": serial_ms / group_ms},
+            "batched_latency_ms": {"max": group_ms,
+                                   "note": "every member's traces are ready when the group run "
+                                           "ends, so each member's latency is at most this"},
+            "parity": parity,
             "e2e": {"value": units / batched_e2e_s / 1e9, "unit": METRIC,
                     "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": int(sum(t.nbytes for t in traces)),
                     "sims_per_s": len(insts) / batched_e2e_s,
                     "api": "device-side build of every instance + fw_group_run + "
                            "fw_read_traces of every member (media built on the GPU)"},
+            "one_by_one_solver_run": {
+                "sample_instances": solver_ids,
+                "sims_per_s": len(solver_ids) / sum(solver_s) if solver_ids else None,
+                "scenario_build_s_mean": float(np.mean(scenario_s)) if scenario_s else None,
+                "batched_sims_per_s_same_sample":
+                    len(solver_ids) / grp_solver_s if grp_solver_s else None,
+                "batched_over_solver_run_same_sample":
+                    sum(solver_s) / grp_solver_s if grp_solver_s else None,
+                "rel_l2_vs_batched_traces_max": max(solver_err) if solver_err else None,
+                "api": "Solver(grid, medium, source, sensor).run() per instance (GPU "
+                       "pre-processing, engine creation, solve, traces to the host); the "
+                       "scenario objects are built before the timed call"},
             "one_by_one_host_api": {
                 "sample_instances": sample,
                 "sims_per_s": len(sample) / sum(host_s) if sample else None,
@@ -563,13 +750,12 @@ def run_batch(args):
                          "algorithmic_bytes_per_cell_update": algorithmic_bytes_per_cell(2),
                          "peak_source": "MEASURED_PEAKS.json hbm_gbs (of measured)" if peaks
                          else "fallback 6800 GB/s"},
-            "gpu_launches": 2 * max(d.nt for d in insts) * args.steps,
+            "gpu_launches": 2 * max(d.nt for d in insts) * steps,
             "clocks": clocks.summary()}
-    if rank == 0:
-        print(json.dumps(line), flush=True)
     grp.close()
     for e in engines:
         e.close()
+    return line
 
 
 def run_serve(args):
@@ -577,14 +763,22 @@ def run_serve(args):
     FIFO one at a time."""
     import torch
 
+    torch.cuda.set_device(0)
+    line = measure_serve(args.rate, args.duration, args.scale, args.budget_gb,
+                         args.max_active_mcells, args.grad_frac, args.host_sample)
+    print(json.dumps(line), flush=True)
+
+
+def measure_serve(rate, duration, scale, budget_gb, max_active_mcells, grad_frac, host_sample):
+    """The serving stream on GPU 0; returns its line."""
+    import torch
+
     from fullwave25_gb300.server import (Request, engine_bytes, poisson_arrivals,
                                          serve_continuous, serve_fifo)
     from fullwave25_gb300.workloads_batch import batch_instance, gradient_job
 
-    torch.cuda.set_device(0)
-    arrivals = poisson_arrivals(args.rate, args.duration, seed=0)
-    scale = args.scale
-    kinds = np.where(np.random.default_rng(1).random(len(arrivals)) < args.grad_frac,
+    arrivals = poisson_arrivals(rate, duration, seed=0)
+    kinds = np.where(np.random.default_rng(1).random(len(arrivals)) < grad_frac,
                      "gradient", "forward")
 
     reqs = []
@@ -604,13 +798,13 @@ def run_serve(args):
     torch.cuda.synchronize()
     # warm-up: one small continuous run so that graphs and kernels are loaded
     warm = [r for r in reqs if r.kind == "forward"][:3] + [r for r in reqs if r.kind == "gradient"][:1]
-    serve_continuous(warm, budget_bytes=args.budget_gb << 30)
+    serve_continuous(warm, budget_bytes=budget_gb << 30)
     for r in warm:
         r.admitted = r.finished = -1.0
         r.traces = r.result = None
-    cap = int(args.max_active_mcells * 1e6) if args.max_active_mcells > 0 else None
+    cap = int(max_active_mcells * 1e6) if max_active_mcells > 0 else None
     with ClockSampler(0) as clocks:
-        cont = serve_continuous(reqs, budget_bytes=args.budget_gb << 30, chunk_steps=256,
+        cont = serve_continuous(reqs, budget_bytes=budget_gb << 30, chunk_steps=256,
                                 max_active_cells=cap)
     for r in reqs:
         r.result = None
@@ -638,7 +832,7 @@ def run_serve(args):
     # against the whole mixed stream understates the served advantage
     from fullwave25_gb300.workloads_batch import batch_inputs_host
 
-    host_reqs = [r for r in reqs if r.kind == "forward"][:args.host_sample]
+    host_reqs = [r for r in reqs if r.kind == "forward"][:host_sample]
     host_s, host_err = [], []
     for r in host_reqs:
         t0 = time.perf_counter()
@@ -658,11 +852,11 @@ def run_serve(args):
             "unit": "sims/s", "n_gpus": 1, "steps": 1, "warmup": 1,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic",
-            "config": {"workload": f"Poisson {args.rate} req/s for {args.duration} s: 2D forward "
+            "config": {"workload": f"Poisson {rate} req/s for {duration} s: 2D forward "
                                    f"solves (batched-workload instances) and "
-                                   f"{args.grad_frac:.0%} gradient solves (512-1024 square "
+                                   f"{grad_frac:.0%} gradient solves (512-1024 square "
                                    f"grids, nt 6000 at 1024), sizes scaled by {scale}; device "
-                                   f"budget {args.budget_gb} GB, blocks of 256 steps, "
+                                   f"budget {budget_gb} GB, blocks of 256 steps, "
                                    "2 gradient worker streams; FIFO after the kernel shape of "
                                    "every forward grid size was tuned (untimed)",
                        "requests": len(reqs), "gradient_requests": n_grad,
@@ -671,7 +865,7 @@ def run_serve(args):
             "one_by_one_host_api_forward_sample": host_api,
             "sims_per_s_ratio": cont["sims_per_s"] / fifo["sims_per_s"],
             "clocks": clocks.summary()}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def run_adjoint(args):
@@ -758,7 +952,11 @@ def main():
     ap.add_argument("--host-sample", type=int, default=8,
                     help="batch2d / serve2d: instances (forward requests) also run one by one "
                          "through the host-side API")
+    ap.add_argument("--solver-sample", type=int, default=16,
+                    help="batch2d: instances also run one by one through Solver.run()")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="plain3d: leave out the secondary workloads of the default line")
     ap.add_argument("--grid", type=int, default=0,
                     help="3D workload edge in cells (default 512; smaller for profiling); "
                          "adjoint2d: grid edge (default 1024)")
