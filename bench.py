@@ -24,7 +24,8 @@ e2e), ``batched`` (64 simulations: group engine vs one by one on the device, vs 
 through ``Solver.run()`` on 16 instances and through the host-side NumPy pre-processing on 8),
 ``serving_short`` (10 s of the Poisson stream at half size: continuous batching vs FIFO) and
 ``solver_config0`` (host-to-host ``Solver.run()`` of the plain 2D problem, GPU and NumPy
-pre-processing). ``--no-extra`` (or FWGB_BENCH_EXTRA=0) leaves them out.
+pre-processing) and ``adjoint`` (gradient evaluations of the 1024^2, nt 6000 misfit through the
+autograd API). ``--no-extra`` (or FWGB_BENCH_EXTRA=0) leaves them out.
 
 Multi-GPU (torchrun): every rank runs an independent replica of the workload (the engine does
 not shard a single solve); ``value`` = cell-updates of all ranks / max rank time ("weak").
@@ -451,6 +452,11 @@ def collect_extras() -> dict:
                             "clocks": sv["clocks"]}
     torch.cuda.empty_cache()
     out["solver_config0"] = solver_host_to_host(engine_solve_ms=p2["ms_per_step"])
+    torch.cuda.empty_cache()
+    ad = measure_adjoint(1024, 0, 200, steps=2, warmup=1)
+    out["adjoint"] = {k: ad[k] for k in ("value", "unit", "ms_per_step",
+                                         "equivalent_Gcell_updates_per_s", "grad_norms", "clocks")}
+    out["adjoint"]["workload"] = ad["config"]["workload"]
     out["wall_s"] = time.perf_counter() - t0
     return out
 
@@ -870,6 +876,13 @@ def measure_serve(rate, duration, scale, budget_gb, max_active_mcells, grad_frac
 
 def run_adjoint(args):
     """Adjoint gradient: 1024^2 grid, nt 6000, 512-sensor row, checkpoints every 200 steps."""
+    line = measure_adjoint(args.grid or 1024, args.nt, args.checkpoint_every, steps,
+                           warmup)
+    print(json.dumps(line), flush=True)
+
+
+def measure_adjoint(n=1024, nt=0, every=200, steps=3, warmup=3):
+    """Gradient evaluations through the public autograd API on GPU 0; returns the line."""
     import torch
     from scipy.ndimage import gaussian_filter
 
@@ -879,9 +892,7 @@ def run_adjoint(args):
 
     torch.cuda.set_device(0)
     dev = torch.device("cuda", 0)
-    n = args.grid or 1024
-    nt = args.nt or (6000 if n == 1024 else int(6000 * n / 1024))
-    every = args.checkpoint_every
+    nt = nt or (6000 if n == 1024 else int(6000 * n / 1024))
     dx = 1540 / 3e6 / 12
     c, rho, a0, gam = ellipse_medium_2d((n, n), dx, seed=0)
     sig = 2e-3 / dx
@@ -900,19 +911,19 @@ def run_adjoint(args):
         J.backward()
         return float(J.detach()), cc.grad, rr.grad, aa.grad
 
-    for _ in range(args.warmup):
+    for _ in range(warmup):
         evaluate()
     torch.cuda.synchronize(dev)
     t0 = time.perf_counter()
     with ClockSampler(0) as clocks:
-        for _ in range(args.steps):
+        for _ in range(steps):
             J, gc, gr, ga = evaluate()
         torch.cuda.synchronize(dev)
-    el = (time.perf_counter() - t0) / args.steps
+    el = (time.perf_counter() - t0) / steps
     ext = prob.build(*start).shape
     cells = int(np.prod(ext))
     line = {"metric": "gradient evaluations/s (adjoint)", "value": 1.0 / el, "unit": "grad/s",
-            "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": el * 1e3,
+            "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": el * 1e3,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32 wavefields, f64 gradient accumulation", "data": "synthetic",
             "config": {"workload": f"adjoint gradient, {n}x{n} + PML 40 + transition 40 "
@@ -925,7 +936,7 @@ def run_adjoint(args):
             "grad_norms": {"c": float(gc.norm()), "rho": float(gr.norm()),
                            "alpha0": float(ga.norm())},
             "clocks": clocks.summary()}
-    print(json.dumps(line), flush=True)
+    return line
 
 
 def main():
