@@ -61,11 +61,18 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
   const int64_t sx = g.sx;
   const int64_t col = (int64_t)j * g.sy + k;
   const float* __restrict__ p = A.f.p;
-  float q[16];  // q[t] = p[x - 7 + t]
+  // x-direction register queue, rotated instead of shifted: at plane x = xb + 16 m + u the
+  // sample p[x - 7 + t] is q[(u + t) & 15]; the plane loop is unrolled by 16 so that every index
+  // is a compile-time register
+  float q[16];
 #pragma unroll
   for (int t = 0; t < 16; ++t) q[t] = active ? __ldg(p + (int64_t)(xb - 7 + t) * sx + col) : 0.f;
   const int si = (ty + 8) * kPW + (tz + 8);
-  for (int x = xb; x < xe; ++x) {
+  for (int x0 = xb; x0 < xe; x0 += 16) {
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int x = x0 + u;
+    if (x >= xe) break;  // uniform over the block
     const int it = x - xb;
     const int64_t c = (int64_t)x * sx + col;
     // point-wise operands of this plane: issued before the block barrier and the TMA wait so
@@ -94,7 +101,7 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
       float gx = 0.f, gy = 0.f, gz = 0.f;
 #pragma unroll
       for (int m = 1; m <= 8; ++m) {
-        gx = fmaf(cm[m - 1], q[7 + m] - q[8 - m], gx);
+        gx = fmaf(cm[m - 1], q[(u + 7 + m) & 15] - q[(u + 8 - m) & 15], gx);
         gy = fmaf(cm[m - 1], P0[si + m * kPW] - P0[si - (m - 1) * kPW], gy);
         gz = fmaf(cm[m - 1], P0[si + m] - P0[si - (m - 1)], gz);
       }
@@ -107,9 +114,8 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
       const float gg[3] = {gx * g.inv_h[0], gy * g.inv_h[1], gz * g.inv_h[2]};
       cv.update_store(A, c, gg);
     }
-#pragma unroll
-    for (int t = 0; t < 15; ++t) q[t] = q[t + 1];
-    q[15] = qn;
+    q[u] = qn;  // p[x + 9]: the sample at t = 15 of plane x + 1
+  }
   }
 }
 
@@ -148,13 +154,19 @@ prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
   const int64_t col = (int64_t)j * g.sy + k;
   const float* __restrict__ vx = A.f.v[0];
   float* p = A.f.p;
-  float r[16];  // r[t] = vx[x - 8 + t]
+  // rotated register queue as in vel3d_march: at plane x = xb + 16 m + u, vx[x - 8 + t] is
+  // r[(u + t) & 15]
+  float r[16];
 #pragma unroll
   for (int t = 0; t < 16; ++t) r[t] = active ? __ldg(vx + (int64_t)(xb - 8 + t) * sx + col) : 0.f;
   const int xi = (ty + 1) * kXW + (tz + 4);
   const int yi = (ty + 8) * kYW + (tz + 4);
   const int zi = (ty + 1) * kZW + (tz + 8);
-  for (int x = xb; x < xe; ++x) {
+  for (int x0 = xb; x0 < xe; x0 += 16) {
+#pragma unroll
+  for (int u = 0; u < 16; ++u) {
+    const int x = x0 + u;
+    if (x >= xe) break;  // uniform over the block
     const int it = x - xb;
     const int64_t c = (int64_t)x * sx + col;
     CP cp;
@@ -184,7 +196,7 @@ prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
       float dx = 0.f, dy = 0.f, dz = 0.f;
 #pragma unroll
       for (int m = 1; m <= 8; ++m) {
-        dx = fmaf(cm[m - 1], r[7 + m] - r[8 - m], dx);
+        dx = fmaf(cm[m - 1], r[(u + 7 + m) & 15] - r[(u + 8 - m) & 15], dx);
         dy = fmaf(cm[m - 1], Y0[yi + (m - 1) * kYW] - Y0[yi - m * kYW], dy);
         dz = fmaf(cm[m - 1], Z0[zi + (m - 1)] - Z0[zi - m], dz);
       }
@@ -197,9 +209,8 @@ prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
       const float dd[3] = {dx * g.inv_h[0], dy * g.inv_h[1], dz * g.inv_h[2]};
       cp.update_store(A, c, dd);
     }
-#pragma unroll
-    for (int t = 0; t < 15; ++t) r[t] = r[t + 1];
-    r[15] = rn;
+    r[u] = rn;  // vx[x + 8]: the sample at t = 15 of plane x + 1
+  }
   }
   tile_epilogue(A, p, (blockIdx.z * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x, tid,
                 kMThreads);

@@ -118,7 +118,9 @@ void launch_nd(fw_handle* h, cudaStream_t s) {
     }
   }
   if (h->exp) {
-    launch_typed<ND, CellVelExpT<ND>, CellPrsExpT<ND, kBeta>, 3>(h, s);
+    // the exponential engine is issue- and latency-bound (few bytes per cell): 4 blocks per SM
+    // (64 registers) hide more latency than 3 (measured 58.7 vs 54.9 Gcell-updates/s, 656^3)
+    launch_typed<ND, CellVelExpT<ND>, CellPrsExpT<ND, kBeta>, 4>(h, s);
   } else if (h->aniso) {
     launch_typed<ND, CellVelT<ND, true>, CellPrsT<ND, kBeta, true>, 2>(h, s);
   } else {
