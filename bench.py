@@ -939,6 +939,114 @@ def measure_adjoint(n=1024, nt=0, every=200, steps=3, warmup=3):
     return line
 
 
+def plain_3d_problem(edge=512, seed=0, nt=3000, f0=2e6, ppw=10, cfl=0.2, element_height=32,
+                     sensor_plane=256):
+    """The plain 3D workload as a user of the reference API holds it: host arrays of the
+    original 512^3 grid (sound speed, density, beta, the per-cell relaxation parameters of each
+    layer's table entry) in a MediumRelaxationMaps, and Source / Sensor masks (64 x 1 element
+    plane wave on depth row 0, a 256 x 256 sensor plane on depth row 4). The arrays are generated
+    on the GPU (same seeded layers and scatterers as the device-built workload) and copied to
+    the host."""
+    import torch
+
+    from fullwave25_gb300.grid import Grid
+    from fullwave25_gb300.medium import MediumRelaxationMaps, relaxation_param_keys
+    from fullwave25_gb300.pulse import gaussian_modulated_sinusoidal_signal
+    from fullwave25_gb300.relaxation import default_table
+    from fullwave25_gb300.source import Sensor, Source
+    from fullwave25_gb300.workloads3d import LAYERS, layered_medium_3d
+
+    shape = (edge, edge, edge)
+    grid = Grid.from_cells(shape, f0=f0, nt=nt, ppw=ppw, cfl=cfl)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    c, rho, layer = layered_medium_3d(shape, grid.dx, seed, dev, n_boundary=0)
+    table = default_table()
+    keys = relaxation_param_keys(2)
+    per_layer = np.stack([np.array([table.lookup(np.array([[lay[3]]]), np.array([[lay[4]]]))[k][0, 0]
+                                    for k in keys]) for lay in LAYERS])
+    lid = layer.cpu().numpy().astype(np.intp)
+    relax = {k: per_layer[:, i][lid] for i, k in enumerate(keys)}
+    del lid, layer
+    medium = MediumRelaxationMaps(grid, c.cpu().numpy(), rho.cpu().numpy(), np.zeros(shape), relax)
+    del c, rho, relax
+    ny, nz = shape[1], shape[2]
+    z0 = nz // 2 - element_height // 2
+    mask = np.zeros(shape, dtype=bool)
+    mask[0, :, z0:z0 + element_height] = True
+    sig = gaussian_modulated_sinusoidal_signal(nt=nt, duration=grid.duration, ncycles=2,
+                                               drop_off=2, f0=f0, p0=1e6)
+    source = Source(np.broadcast_to(sig, (int(mask.sum()), nt)), mask)
+    smask = np.zeros(shape, dtype=bool)
+    y0, zs0 = ny // 2 - sensor_plane // 2, nz // 2 - sensor_plane // 2
+    smask[4, y0:y0 + sensor_plane, zs0:zs0 + sensor_plane] = True
+    return grid, medium, source, Sensor(smask)
+
+
+def measure_solver3d(edge=512, parity=True) -> dict:
+    """Host-to-host ``Solver.run()`` of the plain 3D workload (GPU pre-processing): host arrays
+    in, traces [65536, 3000] back on the host, against the engine's own device-timed solve of
+    the device-built workload (the same maps, built directly on the extended grid: the traces
+    must agree to rounding)."""
+    import tempfile
+
+    import torch
+
+    from fullwave25_gb300.solver import Solver
+    from fullwave25_gb300.workloads3d import plain_3d_device_inputs
+
+    sp, eh = min(256, edge // 2), min(32, edge // 2)
+    t0 = time.perf_counter()
+    grid, medium, source, sensor = plain_3d_problem(edge, element_height=eh, sensor_plane=sp)
+    scenario_s = time.perf_counter() - t0
+    torch.cuda.empty_cache()
+    solver = Solver(tempfile.gettempdir(), grid, medium, source, sensor, pml_layer_thickness_px=32,
+                    n_transition_layer=32)
+    t0 = time.perf_counter()
+    out = solver.run()
+    host_to_host_s = time.perf_counter() - t0
+    timing = dict(solver.last_timing)
+    del solver, medium
+    torch.cuda.empty_cache()
+    ext = [edge + 144] * 3
+    res = {"workload": f"plain 3D problem through Solver.run(): {edge}^3 + PML 32 + transition 32 "
+                       f"({ext[0]}^3), nt {grid.nt}, {source.n_sources} sources, "
+                       f"{sensor.n_sensors} sensors",
+           "host_to_host_s": host_to_host_s,
+           **{k: timing[k] for k in ("preprocess_s", "upload_s", "engine_s")},
+           "scenario_build_s": scenario_s,
+           "gcell_updates_per_s_host_to_host": float(np.prod(ext)) * grid.nt / host_to_host_s / 1e9,
+           "trace_shape": list(out.shape)}
+    if parity:
+        d = plain_3d_device_inputs(shape=(edge,) * 3, sensor_plane=sp, element_height=eh)
+        eng = d.make_engine()
+        stream = torch.cuda.current_stream()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        eng.reset(stream.cuda_stream)
+        a.record(stream)
+        eng.advance(d.nt, stream.cuda_stream)
+        b.record(stream)
+        torch.cuda.synchronize()
+        ref = eng.read_traces().T
+        eng.close()
+        res["engine_solve_s_device_timed"] = a.elapsed_time(b) / 1e3
+        res["rel_l2_vs_device_built_workload"] = float(np.linalg.norm(out - ref)
+                                                       / np.linalg.norm(ref))
+    return res
+
+
+def run_solver3d(args):
+    import torch
+
+    torch.cuda.set_device(0)
+    with ClockSampler(0) as clocks:
+        res = measure_solver3d(args.grid or 512)
+    line = {"metric": "host-to-host Solver.run() time", "value": res["host_to_host_s"], "unit": "s",
+            "n_gpus": 1, "steps": 1, "warmup": 0, "higher_is_better": False, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic", "config": res,
+            "clocks": clocks.summary()}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -946,7 +1054,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=os.environ.get("FWGB_WORKLOAD", "plain3d"),
-                    choices=["plain2d", "plain3d", "batch2d", "serve2d", "adjoint2d"])
+                    choices=["plain2d", "plain3d", "batch2d", "serve2d", "adjoint2d", "solver3d"])
     ap.add_argument("--physics", default="isotropic", choices=["isotropic", "aniso", "exp"],
                     help="plain2d/plain3d: cell physics (relaxation engine, anisotropic "
                          "relaxation, exponential attenuation)")
@@ -987,6 +1095,8 @@ def main():
         run_serve(args)
     elif args.workload == "adjoint2d":
         run_adjoint(args)
+    elif args.workload == "solver3d":
+        run_solver3d(args)
     else:
         run_gpu(args)
 

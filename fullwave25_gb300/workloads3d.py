@@ -228,14 +228,21 @@ def layered_medium_3d(shape, dx, seed, device, n_boundary=0):
     rho_tab = torch.tensor([l[2] for l in LAYERS], dtype=torch.float64, device=device)
     c = c_tab[layer.long()]
     rho = rho_tab[layer.long()]
-    # scatterers: 0.5 % of the original grid's cells, +-2 % sound speed
+    # scatterers: 0.5 % of the original grid's cells, +-2 % sound speed; a cell drawn twice takes
+    # its last draw. The factor lives on the original grid and is edge-replicated like every map,
+    # so the extended maps equal the padded original ones exactly.
     g = torch.Generator(device="cpu").manual_seed(seed * 7 + 100)
     n_scat = int(0.005 * nx * ny * nz)
-    lin = torch.randint(0, nx * ny * nz, (n_scat,), generator=g)
-    amp = (torch.rand(n_scat, generator=g, dtype=torch.float64) * 2 - 1) * 0.02
-    sx, sy, sz = lin // (ny * nz), (lin // nz) % ny, lin % nz
-    sx, sy, sz = (sx + nb).to(device), (sy + nb).to(device), (sz + nb).to(device)
-    c[sx, sy, sz] = c[sx, sy, sz] * (1 + amp.to(device))
+    lin = torch.randint(0, nx * ny * nz, (n_scat,), generator=g).numpy()
+    amp = ((torch.rand(n_scat, generator=g, dtype=torch.float64) * 2 - 1) * 0.02).numpy()
+    _, last = np.unique(lin[::-1], return_index=True)
+    keep = n_scat - 1 - last
+    factor = torch.ones(nx * ny * nz, dtype=torch.float64, device=device)
+    factor[torch.as_tensor(lin[keep], device=device)] = torch.as_tensor(1 + amp[keep], device=device)
+    factor = factor.reshape(nx, ny, nz)
+    if nb:
+        factor = factor[ix][:, iy][:, :, iz]
+    c = c * factor
     return c, rho, layer
 
 
