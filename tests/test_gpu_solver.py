@@ -59,6 +59,66 @@ def test_device_preprocessing_gives_host_preprocessing_traces(engine_lib, cuda, 
     assert rel_l2(out[True], run_oracle_c(host).T) < TOL
 
 
+def _problem_3d(shape=(26, 24, 22), nt=150, physics="isotropic", seed=5):
+    from fullwave25_gb300.grid import Grid
+    from fullwave25_gb300.medium import Medium, MediumRelaxationMaps
+    from fullwave25_gb300.pulse import gaussian_modulated_sinusoidal_signal
+    from fullwave25_gb300.relaxation import default_table
+    from fullwave25_gb300.source import Sensor, Source
+
+    rng = np.random.default_rng(seed)
+    grid = Grid.from_cells(shape, f0=3e6, nt=nt, ppw=12, cfl=0.2)
+    c = 1540 + 40 * rng.standard_normal(shape).clip(-2, 2)
+    rho = 1000 + 50 * rng.standard_normal(shape).clip(-2, 2)
+    a0 = rng.uniform(0.3, 1.0, shape)
+    gam = np.full(shape, 1.1)
+    if physics == "exp":
+        medium = Medium(grid, c, rho, a0, gam, np.zeros(shape))
+    else:
+        medium = MediumRelaxationMaps(grid, c, rho, np.zeros(shape),
+                                      default_table().lookup(a0, gam))
+    mask = np.zeros(shape, dtype=bool)
+    mask[0, 4:-4, 4:-4] = True
+    sig = gaussian_modulated_sinusoidal_signal(nt=nt, duration=grid.duration, ncycles=2,
+                                               drop_off=2, f0=3e6, p0=1e5)
+    smask = np.zeros(shape, dtype=bool)
+    smask[6, ::3, ::3] = True
+    return grid, medium, Source(np.tile(sig, (int(mask.sum()), 1)), mask), Sensor(smask)
+
+
+@pytest.mark.parametrize("physics", ["isotropic", "aniso", "exp"])
+def test_device_preprocessing_3d_gives_host_preprocessing_traces(engine_lib, cuda, physics):
+    """The 3D engines through Solver.run(): GPU and NumPy pre-processing give the same maps (to
+    the float32 ulp bound above) and traces, and the FP64 oracle's traces within 1e-4."""
+    from fullwave25_gb300 import Solver
+    from fullwave25_gb300.workloads3d import to_host_inputs
+
+    grid, medium, source, sensor = _problem_3d(physics=physics)
+    kw = dict(pml_layer_thickness_px=6, n_transition_layer=6,
+              use_isotropic_relaxation=physics != "aniso",
+              use_exponential_attenuation=physics == "exp")
+    out = {}
+    for on_device in (True, False):
+        s = Solver(Path(tempfile.gettempdir()), grid, medium, source, sensor,
+                   preprocess_on_device=on_device, **kw)
+        out[on_device] = s.run()
+    host, _ = s.build_engine_inputs()
+    dev = to_host_inputs(s.build_device_inputs()[0])
+    assert set(dev.maps) == set(host.maps)
+    n_diff = 0
+    for k in host.maps:
+        u = _ulp_diff(dev.maps[k], host.maps[k])
+        assert u.max() <= 1, k
+        n_diff += int((u > 0).sum())
+    assert n_diff <= 1e-4 * host.n_cells * len(host.maps)
+    if n_diff == 0:
+        np.testing.assert_array_equal(out[True], out[False])
+    else:
+        assert rel_l2(out[True], out[False]) < 1e-6
+    assert np.abs(out[True]).max() > 0
+    assert rel_l2(out[True], run_oracle_c(host).T) < TOL
+
+
 def test_static_map_sequence_keeps_the_medium_resident(engine_lib, cuda):
     from fullwave25_gb300 import Solver
     from fullwave25_gb300.solver import release_resident_media
