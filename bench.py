@@ -454,7 +454,7 @@ def collect_extras() -> dict:
     out["solver_config0"] = solver_host_to_host(engine_solve_ms=p2["ms_per_step"])
     torch.cuda.empty_cache()
     ad = measure_adjoint(1024, 0, 200, steps=2, warmup=1)
-    out["adjoint"] = {k: ad[k] for k in ("value", "unit", "ms_per_step",
+    out["adjoint"] = {k: ad[k] for k in ("value", "unit", "ms_per_step", "gradient_check",
                                          "equivalent_Gcell_updates_per_s", "grad_norms", "clocks")}
     out["adjoint"]["workload"] = ad["config"]["workload"]
     out["wall_s"] = time.perf_counter() - t0
@@ -876,9 +876,37 @@ def measure_serve(rate, duration, scale, budget_gb, max_active_mcells, grad_frac
 
 def run_adjoint(args):
     """Adjoint gradient: 1024^2 grid, nt 6000, 512-sensor row, checkpoints every 200 steps."""
-    line = measure_adjoint(args.grid or 1024, args.nt, args.checkpoint_every, steps,
-                           warmup)
+    line = measure_adjoint(args.grid or 1024, args.nt, args.checkpoint_every, args.steps,
+                           args.warmup)
     print(json.dumps(line), flush=True)
+
+
+def directional_gradient_check(prob, start, observed, grad_c, amplitude=1.0, sigma=20.0):
+    """The adjoint's derivative of J along a smooth perturbation of c against a central finite
+    difference of J itself: a Gaussian bump of ``amplitude`` m/s and ``sigma`` cells at the grid
+    centre, J(c +- bump) from plain forward solves (J = 1/2 sum (traces - observed)^2 in FP64)."""
+    import torch
+
+    from fullwave25_gb300.engine import Engine
+
+    nx, ny = prob.shape
+    dev = start[0].device
+    x = torch.arange(nx, dtype=torch.float64, device=dev)[:, None] - (nx - 1) / 2
+    y = torch.arange(ny, dtype=torch.float64, device=dev)[None, :] - (ny - 1) / 2
+    bump = amplitude * torch.exp(-(x * x + y * y) / (2 * sigma * sigma))
+    obs = observed.double()
+
+    def J(c):
+        with Engine(prob.build(c, *start[1:]), validate=False) as e:
+            tr = torch.as_tensor(e.run(), device=dev).double()
+        return 0.5 * float(((tr - obs) ** 2).sum())
+
+    fd = (J(start[0] + bump) - J(start[0] - bump)) / 2.0
+    ad = float((grad_c.double() * bump).sum())
+    return {"adjoint_directional_derivative": ad, "central_difference": fd,
+            "rel_diff": abs(ad - fd) / max(abs(fd), 1e-300),
+            "perturbation": f"Gaussian bump of {amplitude} m/s in c, sigma {sigma} cells, at the "
+                            "grid centre; J(c +- bump) from forward solves"}
 
 
 def measure_adjoint(n=1024, nt=0, every=200, steps=3, warmup=3):
@@ -921,6 +949,7 @@ def measure_adjoint(n=1024, nt=0, every=200, steps=3, warmup=3):
         torch.cuda.synchronize(dev)
     el = (time.perf_counter() - t0) / steps
     ext = prob.build(*start).shape
+    check = directional_gradient_check(prob, start, observed, gc)
     cells = int(np.prod(ext))
     line = {"metric": "gradient evaluations/s (adjoint)", "value": 1.0 / el, "unit": "grad/s",
             "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": el * 1e3,
@@ -935,6 +964,7 @@ def measure_adjoint(n=1024, nt=0, every=200, steps=3, warmup=3):
             "equivalent_Gcell_updates_per_s": 3 * nt * cells / el / 1e9,
             "grad_norms": {"c": float(gc.norm()), "rho": float(gr.norm()),
                            "alpha0": float(ga.norm())},
+            "gradient_check": check,
             "clocks": clocks.summary()}
     return line
 
