@@ -881,10 +881,12 @@ def run_adjoint(args):
     print(json.dumps(line), flush=True)
 
 
-def directional_gradient_check(prob, start, observed, grad_c, amplitude=1.0, sigma=20.0):
+def directional_gradient_check(prob, start, observed, grad_c, amplitude=2.0, sigma=60.0):
     """The adjoint's derivative of J along a smooth perturbation of c against a central finite
     difference of J itself: a Gaussian bump of ``amplitude`` m/s and ``sigma`` cells at the grid
-    centre, J(c +- bump) from plain forward solves (J = 1/2 sum (traces - observed)^2 in FP64)."""
+    centre, J(c +- bump) from plain forward solves (J = 1/2 sum (traces - observed)^2 in FP64).
+    The bump is wide enough that J's change dominates the float32 rounding of the perturbed maps
+    (narrow or weak bumps move K = c^2 rho by less than its float32 resolution in most cells)."""
     import torch
 
     from fullwave25_gb300.engine import Engine
