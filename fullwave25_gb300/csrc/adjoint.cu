@@ -15,7 +15,7 @@ constexpr int kGradSlot[kNumGrad] = {kMRdtRho, kMDtK, kMInvKu, kMInvKx, kMAu1, k
 
 // Tensor maps of the TMA reverse-step kernels over this handle's adjoint fields, coefficient
 // maps, state store (K + 1 slots) and tap-index map.
-int encode_adj_maps(fw_handle* h, AdjMaps* M) {
+int encode_adj_maps(fw_handle* h, AdjMaps* M, float* store) {
   const cuuint64_t row = (cuuint64_t)h->pitch * 4, field = (cuuint64_t)h->ncells_padded * 4;
   const cuuint64_t pitch = (cuuint64_t)h->pitch, nx = (cuuint64_t)h->nx;
   const cuuint64_t d_lam[3] = {pitch, nx, (cuuint64_t)kAdjStack};
@@ -38,10 +38,10 @@ int encode_adj_maps(fw_handle* h, AdjMaps* M) {
       (st = encode_map(h, &M->halo_x, h->adj_lam, 3, d_lam, s3, bhx)) ||
       (st = encode_map(h, &M->halo_y, h->adj_lam, 3, d_lam, s3, bhy)) ||
       (st = encode_map(h, &M->maps6, h->maps, 3, d_map, s3, b6)) ||
-      (st = encode_map(h, &M->st4, h->adj_store, 4, d_st, s4, bs4)) ||
-      (st = encode_map(h, &M->st_vx, h->adj_store, 4, d_st, s4, bsx)) ||
-      (st = encode_map(h, &M->st_vy, h->adj_store, 4, d_st, s4, bsy)) ||
-      (st = encode_map(h, &M->st_p, h->adj_store, 4, d_st, s4, bsp)) ||
+      (st = encode_map(h, &M->st4, store, 4, d_st, s4, bs4)) ||
+      (st = encode_map(h, &M->st_vx, store, 4, d_st, s4, bsx)) ||
+      (st = encode_map(h, &M->st_vy, store, 4, d_st, s4, bsy)) ||
+      (st = encode_map(h, &M->st_p, store, 4, d_st, s4, bsp)) ||
       (st = encode_map(h, &M->dc, h->dcmap, 2, d_dc, s_dc, bdc, CU_TENSOR_MAP_DATA_TYPE_UINT16)))
     return st;
   return FW_OK;
@@ -64,12 +64,22 @@ int prepare_adjoint_kernels(fw_handle* h, int dev, int smem_optin) {
   return FW_OK;
 }
 
+// The FP64 gradient sums of the 12 coefficient maps into the caller's dense [12][nx][ny] buffer.
+int copy_gradients(fw_handle* h, const AdjArgs& A, double* grad_out, cudaStream_t s) {
+  if (!grad_out) return FW_OK;
+  for (int q = 0; q < kNumGrad; ++q)
+    FW_CUDA(h, cudaMemcpy2DAsync(grad_out + (size_t)q * h->nx * h->ny, h->ny * sizeof(double),
+                                 A.grad[q], h->pitch * sizeof(double), h->ny * sizeof(double),
+                                 h->nx, cudaMemcpyDeviceToDevice, s));
+  return FW_OK;
+}
+
 // Free the adjoint buffers of h (checkpoints, state store, adjoint fields, gradient sums).
 void release_adjoint(fw_handle* h) {
-  void* bufs[] = {h->adj_ckpt, h->adj_store, h->adj_lam, h->adj_grad};
+  void* bufs[] = {h->adj_ckpt, h->adj_store, h->adj_store2, h->adj_lam, h->adj_grad};
   for (void* b : bufs)
     if (b) cudaFree(b);
-  h->adj_ckpt = h->adj_store = h->adj_lam = nullptr;
+  h->adj_ckpt = h->adj_store = h->adj_store2 = h->adj_lam = nullptr;
   h->adj_grad = nullptr;
   h->bytes -= h->adj_bytes;
   h->adj_bytes = 0;
@@ -97,19 +107,24 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
     // 15 adjoint fields and temporaries, then the FP32 per-segment gradient partials
     const size_t b_lam = (size_t)h->ncells_padded * kAdjStack * sizeof(float);
     const size_t b_grad = (size_t)h->ncells_padded * kNumGrad * sizeof(double);
+    // FWGB_ADJ_OVERLAP=0: one state store, segments recomputed and reversed one after another
+    const char* ov = std::getenv("FWGB_ADJ_OVERLAP");
+    const bool two = !(ov && std::strcmp(ov, "0") == 0);
     cudaError_t e = cudaMalloc(&h->adj_ckpt, b_ckpt);
     if (e == cudaSuccess) e = cudaMalloc(&h->adj_store, b_store);
+    if (e == cudaSuccess && two) e = cudaMalloc(&h->adj_store2, b_store);
     // the out-of-place recomputation never writes the ghost layer of a stored state: keep it zero
     if (e == cudaSuccess) e = cudaMemset(h->adj_store, 0, b_store);
+    if (e == cudaSuccess && two) e = cudaMemset(h->adj_store2, 0, b_store);
     if (e == cudaSuccess) e = cudaMalloc(&h->adj_lam, b_lam);
     if (e == cudaSuccess) e = cudaMalloc(&h->adj_grad, b_grad);
     if (e != cudaSuccess) {   // leave no partial allocation behind
       release_adjoint(h);
       return fail(h, e == cudaErrorMemoryAllocation ? FW_ERR_OOM : FW_ERR_CUDA,
-                  "adjoint buffers (%zu bytes): %s", b_ckpt + b_store + b_lam + b_grad,
+                  "adjoint buffers (%zu bytes): %s", b_ckpt + (two ? 2 : 1) * b_store + b_lam + b_grad,
                   cudaGetErrorString(e));
     }
-    h->adj_bytes = b_ckpt + b_store + b_lam + b_grad;
+    h->adj_bytes = b_ckpt + (two ? 2 : 1) * b_store + b_lam + b_grad;
     h->bytes += h->adj_bytes;
     h->adj_every = checkpoint_every;
     h->adj_nckpt = nckpt;
@@ -184,15 +199,23 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   // each in-place step.
   const char* oenv = std::getenv("FWGB_ADJ_OOP");
   const bool oop = !h->ghost_writes && !(oenv && std::strcmp(oenv, "0") == 0);
-  Tile2Maps MT{};
-  if (oop) {
-    int st = encode_tile2_maps(h, &MT, h->adj_store, h->adj_every + 1);
+  // Overlap (default when a second store exists, with out-of-place recomputation and the TMA
+  // reverse step): segment k-1 is recomputed on a second stream into the other store while
+  // segment k is reversed on `stream`; events order each store's reuse. Same kernels, same
+  // operands: the gradient is bitwise that of the sequential pass.
+  const bool overlap = oop && tma && h->adj_store2 != nullptr;
+  float* stores[2] = {h->adj_store, overlap ? h->adj_store2 : h->adj_store};
+  Tile2Maps MT[2] = {};
+  AdjMaps M[2] = {};
+  for (int b = 0; b < (overlap ? 2 : 1); ++b) {
+    int st = FW_OK;
+    if (oop) st = encode_tile2_maps(h, &MT[b], stores[b], h->adj_every + 1);
+    if (!st && tma) st = encode_adj_maps(h, &M[b], stores[b]);
     if (st) return st;
   }
-  AdjMaps M{};
   if (tma) {
-    int st = encode_adj_maps(h, &M);
-    if (st || (st = prepare_adjoint_kernels(h, dev, smem_optin))) return st;
+    int st = prepare_adjoint_kernels(h, dev, smem_optin);
+    if (st) return st;
   }
   const Lists& L = h->args.l;
   // list lengths: sources after de-duplication, air cells, sensors
@@ -206,26 +229,90 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   const dim3 block(32, 8), grid((unsigned)((h->ny - 2 * kGhost + 31) / 32),
                                 (unsigned)((h->nx - 2 * kGhost + 7) / 8));
   const int K = h->adj_every;
+  // recompute segment seg from its checkpoint into store b, keeping every state (out of place)
+  auto recompute_oop = [&](int seg, int b, cudaStream_t rs) -> int {
+    const int n0 = seg * K, n1 = std::min(n0 + K, (int)h->d.nt);
+    set_step_counter<<<1, 1, 0, rs>>>(h->step, n0);
+    FW_CUDA(h, cudaMemcpyAsync(stores[b], h->adj_ckpt + state_elems * seg,
+                               state_elems * sizeof(float), cudaMemcpyDeviceToDevice, rs));
+    StepArgs out = h->args;
+    for (int n = n0; n < n1; ++n) {
+      set_state_pointers(h, &out, stores[b] + state_elems * (n - n0 + 1));
+      vel2d_tile<kTileIso, true><<<grid, block, sizeof(VelTileSmem<kTileIso>), rs>>>(
+          out, MT[b], n - n0);
+      prs2d_tile<kTileIso, false, true><<<grid, block, sizeof(PrsTileSmem<kTileIso, false>),
+                                          rs>>>(out, MT[b], n - n0);
+    }
+    if (seg == 0)   // leave the first segment's recomputation in the handle, as in place
+      FW_CUDA(h, cudaMemcpyAsync(h->state, stores[b] + state_elems * (n1 - n0),
+                                 state_elems * sizeof(float), cudaMemcpyDeviceToDevice, rs));
+    FW_CUDA(h, cudaGetLastError());
+    return FW_OK;
+  };
+  if (overlap) {
+    // i-th segment from the end -> store i % 2; the recomputation of segment i + 1 runs on the
+    // second stream while segment i is reversed on `stream`
+    cudaStream_t rs = nullptr;
+    cudaEvent_t ev[5] = {};   // start, recomputed[2], reversed[2]
+    auto cleanup = [&]() {
+      for (cudaEvent_t e : ev)
+        if (e) cudaEventDestroy(e);
+      if (rs) cudaStreamDestroy(rs);
+    };
+    auto run = [&]() -> int {
+      FW_CUDA(h, cudaStreamCreateWithFlags(&rs, cudaStreamNonBlocking));
+      for (cudaEvent_t& e : ev) FW_CUDA(h, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+      cudaEvent_t ev_start = ev[0], *rec = ev + 1, *rev = ev + 3;
+      FW_CUDA(h, cudaEventRecord(ev_start, s));
+      FW_CUDA(h, cudaStreamWaitEvent(rs, ev_start, 0));
+      const int nseg = h->adj_nckpt;
+      int st;
+      if ((st = recompute_oop(nseg - 1, 0, rs))) return st;
+      FW_CUDA(h, cudaEventRecord(rec[0], rs));
+      for (int i = 0; i < nseg; ++i) {
+        const int seg = nseg - 1 - i, b = i % 2;
+        if (i + 1 < nseg) {
+          if (i >= 1) FW_CUDA(h, cudaStreamWaitEvent(rs, rev[(i + 1) % 2], 0));
+          if ((st = recompute_oop(seg - 1, (i + 1) % 2, rs))) return st;
+          FW_CUDA(h, cudaEventRecord(rec[(i + 1) % 2], rs));
+        }
+        FW_CUDA(h, cudaStreamWaitEvent(s, rec[b], 0));
+        const int n0 = seg * K, n1 = std::min(n0 + K, (int)h->d.nt);
+        for (int n = n1 - 1; n >= n0; --n) {
+          A.Sn = stores[b] + state_elems * (n - n0);
+          A.Sn1 = stores[b] + state_elems * (n - n0 + 1);
+          adj2d_prs_tma<0><<<grid, block, smem_prs, s>>>(A, L, residual, n, n - n0, M[b]);
+          adj2d_vel_tma<0><<<grid, block, smem_vel, s>>>(A, n - n0, M[b]);
+        }
+        adj2d_merge<<<grid, block, 0, s>>>(A);
+        FW_CUDA(h, cudaGetLastError());
+        FW_CUDA(h, cudaEventRecord(rev[b], s));
+      }
+      return FW_OK;
+    };
+    const int st = run();
+    if (st) {
+      cudaStreamSynchronize(s);
+      if (rs) cudaStreamSynchronize(rs);
+      cleanup();
+      return st;
+    }
+    // every operation of the second stream precedes an event `stream` waited on, so the status
+    // check (a synchronisation of `stream`) also covers it
+    const int st2 = copy_gradients(h, A, grad_out, s);
+    const int st3 = st2 ? st2 : check_device_status(h, s);
+    cleanup();
+    return st3;
+  }
   bool first = true;
   for (int seg = h->adj_nckpt - 1; seg >= 0; --seg) {
     const int n0 = seg * K, n1 = std::min(n0 + K, (int)h->d.nt);
     // recompute the segment from its checkpoint, keeping every state
-    set_step_counter<<<1, 1, 0, s>>>(h->step, n0);
     if (oop) {
-      FW_CUDA(h, cudaMemcpyAsync(h->adj_store, h->adj_ckpt + state_elems * seg,
-                                 state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
-      StepArgs out = h->args;
-      for (int n = n0; n < n1; ++n) {
-        set_state_pointers(h, &out, h->adj_store + state_elems * (n - n0 + 1));
-        vel2d_tile<kTileIso, true><<<grid, block, sizeof(VelTileSmem<kTileIso>), s>>>(
-            out, MT, n - n0);
-        prs2d_tile<kTileIso, false, true><<<grid, block, sizeof(PrsTileSmem<kTileIso, false>),
-                                            s>>>(out, MT, n - n0);
-      }
-      if (seg == 0)   // leave the first segment's recomputation in the handle, as in place
-        FW_CUDA(h, cudaMemcpyAsync(h->state, h->adj_store + state_elems * (n1 - n0),
-                                   state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
+      int st = recompute_oop(seg, 0, s);
+      if (st) return st;
     } else {
+      set_step_counter<<<1, 1, 0, s>>>(h->step, n0);
       FW_CUDA(h, cudaMemcpyAsync(h->state, h->adj_ckpt + state_elems * seg,
                                  state_elems * sizeof(float), cudaMemcpyDeviceToDevice, s));
       for (int n = n0; n < n1; ++n) {
@@ -240,8 +327,8 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
       A.Sn = h->adj_store + state_elems * (n - n0);
       A.Sn1 = h->adj_store + state_elems * (n - n0 + 1);
       if (tma) {
-        adj2d_prs_tma<0><<<grid, block, smem_prs, s>>>(A, L, residual, n, n - n0, M);
-        adj2d_vel_tma<0><<<grid, block, smem_vel, s>>>(A, n - n0, M);
+        adj2d_prs_tma<0><<<grid, block, smem_prs, s>>>(A, L, residual, n, n - n0, M[0]);
+        adj2d_vel_tma<0><<<grid, block, smem_vel, s>>>(A, n - n0, M[0]);
         continue;
       }
       if (fused) {
@@ -285,13 +372,8 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     if (!f64_steps) adj2d_merge<<<grid, block, 0, s>>>(A);
     FW_CUDA(h, cudaGetLastError());
   }
-  if (grad_out) {
-    for (int q = 0; q < kNumGrad; ++q)
-      FW_CUDA(h, cudaMemcpy2DAsync(grad_out + (size_t)q * h->nx * h->ny, h->ny * sizeof(double),
-                                   A.grad[q], h->pitch * sizeof(double), h->ny * sizeof(double),
-                                   h->nx, cudaMemcpyDeviceToDevice, s));
-  }
-  return check_device_status(h, s);
+  const int st = copy_gradients(h, A, grad_out, s);
+  return st ? st : check_device_status(h, s);
 }
 
 }  // extern "C"

@@ -932,7 +932,7 @@ int fw_selftest_waits(int32_t status_out[2]) {
 int fw_destroy(fw_handle* h) {
   if (!h) return FW_OK;
   {
-    void* bufs[] = {h->adj_ckpt, h->adj_store, h->adj_lam, h->adj_grad, h->groups};
+    void* bufs[] = {h->adj_ckpt, h->adj_store, h->adj_store2, h->adj_lam, h->adj_grad, h->groups};
     for (void* b : bufs)
       if (b) cudaFree(b);
   }

@@ -108,6 +108,8 @@ struct fw_handle {
   int adj_every = 0, adj_nckpt = 0;
   float* adj_ckpt = nullptr;     // adj_nckpt states
   float* adj_store = nullptr;    // adj_every + 1 states
+  float* adj_store2 = nullptr;   // second store: the next segment is recomputed into it while
+                                 // the current one is reversed (nullptr: no overlap)
   float* adj_lam = nullptr;      // 11 adjoint fields + 4 temporaries
   double* adj_grad = nullptr;    // kNumGrad padded FP64 arrays
   size_t adj_bytes = 0;

@@ -39,7 +39,9 @@ class GradientJob:
         pitch = -(-shape[-1] // 32) * 32
         cells = shape[0] * pitch
         nt = self.problem.grid.nt
-        n_states = nt // self.checkpoint_every + self.checkpoint_every + 1
+        # checkpoints plus two stores of checkpoint_every + 1 states (the next segment is
+        # recomputed into one while the other is reversed)
+        n_states = nt // self.checkpoint_every + 2 * (self.checkpoint_every + 1)
         fwd = engine_bytes(shape, nt, self.observed.shape[1])
         return fwd + cells * 4 * (11 * n_states + 15) + cells * 8 * 24
 

@@ -214,8 +214,9 @@ FWGB_API int fw_destroy(fw_handle *h);
  * respect to the engine's coefficient maps, by the discrete adjoint of the time step. No
  * counterpart in the reference (it has no gradient computation).
  * fw_adjoint_forward: run the full forward solve from rest, keeping a checkpoint of the wavefield
- * every `checkpoint_every` steps (device memory: nt / checkpoint_every + checkpoint_every + 1
- * wavefield copies); the traces are then available from fw_read_traces. */
+ * every `checkpoint_every` steps (device memory: nt / checkpoint_every + 2 (checkpoint_every + 1)
+ * wavefield copies: the checkpoints and two state stores; FWGB_ADJ_OVERLAP=0 at this call keeps
+ * one store); the traces are then available from fw_read_traces. */
 FWGB_API int fw_adjoint_forward(fw_handle *h, void *stream, int32_t checkpoint_every);
 
 /* Reverse pass: recompute each segment from its checkpoint and run the adjoint step backwards,
@@ -223,7 +224,10 @@ FWGB_API int fw_adjoint_forward(fw_handle *h, void *stream, int32_t checkpoint_e
  * adjoint fields) into per-segment FP32 partial sums that are added into FP64 time sums at the
  * end of every segment (FWGB_ADJ_F64_STEPS=1: every step's contributions in FP64 instead).
  * Each reverse step is two launches whose operands are staged in shared memory by TMA
- * (FWGB_ADJ_TMA=0: the same arithmetic with the operands loaded by the threads).
+ * (FWGB_ADJ_TMA=0: the same arithmetic with the operands loaded by the threads). With two state
+ * stores, the next segment is recomputed into one on a second (internal) stream while the current
+ * segment is reversed from the other on `stream`; the gradient is bitwise the same as one segment
+ * after another.
  * `residual` = traces - observed, device float32 [n_out][ncoordsout]. `grad_out`: device FP64
  * [12][nx][ny] in the order dt/rho, dt*K, 1/kappau, 1/kappax, au1, bu1, au2, bu2, ax1, bx1, ax2,
  * bx2 (ghost cells zero). The wavefield left in the handle afterwards is the first segment's

@@ -157,7 +157,9 @@ def test_reverse_pass_variants_ragged(engine_lib, cuda, shape, every, ghost_src)
     inp = problem(1.0)
     observed = Oracle(problem(1.03)).run().astype(np.float32)
     out = {}
-    modes = {"default": {}, "tiled": {"FWGB_ADJ_TMA": "0"}, "copies": {"FWGB_ADJ_OOP": "0"}}
+    fields = {}
+    modes = {"default": {}, "sequential": {"FWGB_ADJ_OVERLAP": "0"},
+             "tiled": {"FWGB_ADJ_TMA": "0"}, "copies": {"FWGB_ADJ_OOP": "0"}}
     for mode, env in modes.items():
         os.environ.update(env)
         try:
@@ -168,12 +170,14 @@ def test_reverse_pass_variants_ragged(engine_lib, cuda, shape, every, ghost_src)
                 eng.adjoint_backward(res.data_ptr(), g.data_ptr())
                 torch.cuda.synchronize()
                 out[mode] = g.cpu().numpy()
+                fields[mode] = eng.get_field(0)
         finally:
             for k in env:
                 os.environ.pop(k, None)
     assert np.abs(out["copies"]).max() > 0
-    np.testing.assert_array_equal(out["default"], out["copies"])
-    np.testing.assert_array_equal(out["tiled"], out["copies"])
+    for mode in ("default", "sequential", "tiled"):
+        np.testing.assert_array_equal(out[mode], out["copies"], err_msg=mode)
+        np.testing.assert_array_equal(fields[mode], fields["copies"], err_msg=mode)
 
 
 def test_concurrent_gradients_with_different_tap_tables(engine_lib, cuda):
