@@ -185,6 +185,10 @@ class Solver:
                 icc = resident.inputs.icc
                 icc = icc.cpu().numpy() if hasattr(icc, "cpu") else np.asarray(icc)
                 nb = (resident.inputs.shape[0] - self.grid.shape[0]) // 2
+                if (tuple(n + 2 * nb for n in self.grid.shape) != tuple(resident.inputs.shape)
+                        or self.grid.nt != resident.inputs.nt):
+                    raise ValueError("a static-map run with recalculate_pml=False must use the "
+                                     "grid (shape and nt) of the resident medium")
                 if (self.source.incoords.shape != icc.shape
                         or not np.array_equal(self.source.incoords + nb, icc)):
                     raise ValueError("a static-map run with recalculate_pml=False must drive the "

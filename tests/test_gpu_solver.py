@@ -153,5 +153,10 @@ def test_static_map_sequence_keeps_the_medium_resident(engine_lib, cuda):
                    n_transition_layer=12)
         with pytest.raises(ValueError, match="source cells"):
             s.run("txrx_x", is_static_map=True, recalculate_pml=False)
+        # nor one on another grid
+        g2, m2, src2, sen2, _ = _problem(seed=6, nt=320)
+        s = Solver(work, g2, m2, src2, sen2, pml_layer_thickness_px=12, n_transition_layer=12)
+        with pytest.raises(ValueError, match="grid"):
+            s.run("txrx_y", is_static_map=True, recalculate_pml=False)
     finally:
         release_resident_media()
