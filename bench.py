@@ -24,7 +24,8 @@ e2e), ``batched`` (64 simulations: group engine vs one by one on the device, vs 
 through ``Solver.run()`` on 16 instances and through the host-side NumPy pre-processing on 8),
 ``serving_short`` (10 s of the Poisson stream at half size: continuous batching vs FIFO) and
 ``solver_config0`` (host-to-host ``Solver.run()`` of the plain 2D problem, GPU and NumPy
-pre-processing) and ``adjoint`` (gradient evaluations of the 1024^2, nt 6000 misfit through the
+pre-processing), ``solver_config1`` (the same for the plain 3D workload: host arrays of the 512^3
+medium in, 65,536 traces back, against the device-built workload's solve) and ``adjoint`` (gradient evaluations of the 1024^2, nt 6000 misfit through the
 autograd API). ``--no-extra`` (or FWGB_BENCH_EXTRA=0) leaves them out.
 
 Multi-GPU (torchrun): every rank runs an independent replica of the workload (the engine does
@@ -452,6 +453,8 @@ def collect_extras() -> dict:
                             "clocks": sv["clocks"]}
     torch.cuda.empty_cache()
     out["solver_config0"] = solver_host_to_host(engine_solve_ms=p2["ms_per_step"])
+    torch.cuda.empty_cache()
+    out["solver_config1"] = measure_solver3d(512)
     torch.cuda.empty_cache()
     ad = measure_adjoint(1024, 0, 200, steps=2, warmup=1)
     out["adjoint"] = {k: ad[k] for k in ("value", "unit", "ms_per_step", "gradient_check",
