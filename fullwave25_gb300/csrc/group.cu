@@ -20,11 +20,23 @@ struct fw_group {
   bool beta = false;
   cudaStream_t capture_stream = nullptr;
   std::map<int, cudaGraphExec_t> graphs;  // active tile count -> graph of kGroupGraphSteps steps
+  // fw_group_run: the whole run (every member from step 0 to its own nt) as one graph, rebuilt
+  // when the members, their order or the kernel shape change
+  cudaGraphExec_t run_graph = nullptr;
+  std::vector<fw_handle*> run_graph_members;
+  int run_graph_shape = -1;
 };
 
 namespace {
 
 constexpr int kGroupGraphSteps = 64;
+
+void drop_run_graph(fw_group* g) {
+  if (g->run_graph) cudaGraphExecDestroy(g->run_graph);
+  g->run_graph = nullptr;
+  g->run_graph_members.clear();
+  g->run_graph_shape = -1;
+}
 
 template <int TY, int XC, bool kStream>
 void group_launch_march_t(fw_group* g, int n_blocks, cudaStream_t s) {
@@ -130,6 +142,7 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
   if ((size_t)n > g->args_cap || tiles.size() > g->tiles_cap) {
     for (auto& kv : g->graphs) cudaGraphExecDestroy(kv.second);
     g->graphs.clear();
+    drop_run_graph(g);
     if (g->d_args) cudaFree(g->d_args);
     if (g->d_tiles) cudaFree(g->d_tiles);
     if (g->d_maps) cudaFree(g->d_maps);
@@ -161,6 +174,7 @@ int group_set(fw_group* g, fw_handle* const* handles, int32_t n) {
 int group_set_shape(fw_group* g, int k) {
   for (auto& kv : g->graphs) cudaGraphExecDestroy(kv.second);
   g->graphs.clear();
+  drop_run_graph(g);
   g->shape = k;
   std::vector<fw_handle*> m = g->members;
   return m.empty() ? FW_OK : group_set(g, m.data(), (int)m.size());
@@ -235,6 +249,43 @@ int group_advance(fw_group* g, cudaStream_t s, int n_steps) {
     for (int r = 0; r < k; ++r) g->members[r]->host_step += seg;
     done += seg;
   }
+  return FW_OK;
+}
+
+// The whole run of a freshly reset group as one CUDA graph: the same segments as group_advance
+// (members ordered by nt, the active tiles a prefix that shrinks as members finish), every step
+// captured as its two launches. Replayed by later runs while the members and shape stay the same.
+int group_run_graph(fw_group* g, cudaGraphExec_t* out) {
+  if (g->run_graph && g->run_graph_members == g->members && g->run_graph_shape == g->shape) {
+    *out = g->run_graph;
+    return FW_OK;
+  }
+  drop_run_graph(g);
+  const int n = (int)g->members.size();
+  std::vector<int> left(n);
+  for (int r = 0; r < n; ++r) left[r] = g->members[r]->d.nt;
+  cudaGraph_t graph = nullptr;
+  FW_CUDA(nullptr, cudaStreamBeginCapture(g->capture_stream, cudaStreamCaptureModeThreadLocal));
+  for (;;) {
+    int k = 0, seg = 0;
+    for (int r = 0; r < n && left[r] > 0; ++r) {
+      seg = k == 0 ? left[r] : std::min(seg, left[r]);
+      k = r + 1;
+    }
+    if (k == 0) break;
+    for (int i = 0; i < seg; ++i) group_launch_step(g, g->tiles_upto[k], g->capture_stream);
+    for (int r = 0; r < k; ++r) left[r] -= seg;
+  }
+  const cudaError_t ce = cudaStreamEndCapture(g->capture_stream, &graph);
+  if (ce != cudaSuccess) return fail(nullptr, FW_ERR_CUDA, "group run capture: %s", cudaGetErrorString(ce));
+  cudaGraphExec_t exec = nullptr;
+  const cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  if (e != cudaSuccess) return fail(nullptr, FW_ERR_CUDA, "group run graph: %s", cudaGetErrorString(e));
+  g->run_graph = exec;
+  g->run_graph_members = g->members;
+  g->run_graph_shape = g->shape;
+  *out = exec;
   return FW_OK;
 }
 
@@ -321,7 +372,20 @@ int fw_group_run(fw_group* g, void* stream) {
       if (st) return st;
     }
   }
-  return fw_group_advance(g, stream, max_nt);
+  // FWGB_GROUP_RUN_GRAPH=0: blocks of kGroupGraphSteps steps as fw_group_advance issues them
+  const char* rg = std::getenv("FWGB_GROUP_RUN_GRAPH");
+  if ((rg && std::strcmp(rg, "0") == 0) || g->members.empty()) return fw_group_advance(g, stream, max_nt);
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(static_cast<cudaStream_t>(stream), &cs) != cudaSuccess ||
+      cs != cudaStreamCaptureStatusNone)
+    return fw_group_advance(g, stream, max_nt);
+  std::vector<fw_handle*> m = g->members;
+  int st = group_set(g, m.data(), (int)m.size());   // order by steps left (all at step 0)
+  cudaGraphExec_t exec = nullptr;
+  if (st || (st = group_run_graph(g, &exec))) return st;
+  FW_CUDA(nullptr, cudaGraphLaunch(exec, static_cast<cudaStream_t>(stream)));
+  for (fw_handle* h : g->members) h->host_step = h->d.nt;
+  return FW_OK;
 }
 
 int fw_group_block_tile(const fw_group* g, int32_t tile[3]) {
@@ -335,6 +399,7 @@ int fw_group_block_tile(const fw_group* g, int32_t tile[3]) {
 int fw_group_destroy(fw_group* g) {
   if (!g) return FW_OK;
   for (auto& kv : g->graphs) cudaGraphExecDestroy(kv.second);
+  drop_run_graph(g);
   if (g->capture_stream) cudaStreamDestroy(g->capture_stream);
   if (g->d_args) cudaFree(g->d_args);
   if (g->d_tiles) cudaFree(g->d_tiles);

@@ -248,7 +248,10 @@ typedef struct fw_group fw_group;
 FWGB_API int fw_group_create(fw_handle *const *handles, int32_t n, fw_group **out);
 
 /* Reset every member and run each for its own nt steps (asynchronous on stream); afterwards
- * read each member's traces with fw_read_traces. Errors: fw_last_error(NULL). */
+ * read each member's traces with fw_read_traces. The whole run is captured once into one CUDA
+ * graph (every step's two launches over the shrinking prefix of active members) and replayed by
+ * later runs while the members and the kernel shape stay the same (FWGB_GROUP_RUN_GRAPH=0: blocks
+ * of 64-step graphs as fw_group_advance issues them). Errors: fw_last_error(NULL). */
 FWGB_API int fw_group_run(fw_group *g, void *stream);
 
 /* Replace the member list (members may be at different steps; continuous batching admits new

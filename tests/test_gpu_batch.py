@@ -33,6 +33,36 @@ def test_group_equals_individual_runs(engine_lib, cuda, instances):
         e.close()
 
 
+def test_whole_run_graph_equals_stepwise_blocks(engine_lib, cuda, instances):
+    """fw_group_run replays the whole run (every member to its own nt) as one captured graph;
+    with FWGB_GROUP_RUN_GRAPH=0 the same run is issued as blocks of 64-step graphs. Traces are
+    bitwise equal, on repeated runs (the graph is reused) and after the member set changes (the
+    graph is rebuilt)."""
+    import os
+
+    from fullwave25_gb300.engine import EngineGroup
+
+    engines = [d.make_engine() for d in instances]
+    os.environ["FWGB_GROUP_RUN_GRAPH"] = "0"
+    try:
+        with EngineGroup(engines) as grp:
+            grp.run()
+            blocks = grp.traces()
+    finally:
+        os.environ.pop("FWGB_GROUP_RUN_GRAPH", None)
+    with EngineGroup(engines) as grp:
+        for _ in range(2):
+            grp.run()
+            for a, t in zip(blocks, grp.traces()):
+                np.testing.assert_array_equal(a, t)
+        grp.set_members(engines[1:4])
+        grp.run()
+        for a, t in zip(blocks[1:4], grp.traces()):
+            np.testing.assert_array_equal(a, t)
+    for e in engines:
+        e.close()
+
+
 def test_group_member_matches_oracle(engine_lib, cuda, instances):
     from fdtd_oracle_c import run_oracle_c
     from fullwave25_gb300.engine import EngineGroup
