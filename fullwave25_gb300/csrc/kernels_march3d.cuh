@@ -27,6 +27,11 @@ constexpr int kXSlot = 416, kYSlot = kYW * kYH, kZSlot = kZW * kZH;  // vx slot 
 static_assert(kXSlot >= kXW * kXH && (kXSlot * 4) % 128 == 0, "vx slot");
 static_assert((kYSlot * 4) % 128 == 0 && (kZSlot * 4) % 128 == 0 && (kPSlot * 4) % 128 == 0, "slots");
 
+// The plane loops below run in unrolled groups of 16 planes starting at multiples of 16 from the
+// block's first plane, so a plane's ring slot and mbarrier phase follow from its position u in the
+// group alone: (it + k) % kRing == (u + k) % kRing and ((it + 2) / kRing) & 1 == ((u + 2) / kRing) & 1.
+static_assert(16 % kRing == 0 && (16 / kRing) % 2 == 0, "ring slots and phases repeat every 16 planes");
+
 struct MarchMaps {
   CUtensorMap p, vx, vy, vz;
 };
@@ -73,7 +78,6 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
   for (int u = 0; u < 16; ++u) {
     const int x = x0 + u;
     if (x >= xe) break;  // uniform over the block
-    const int it = x - xb;
     const int64_t c = (int64_t)x * sx + col;
     // point-wise operands of this plane: issued before the block barrier and the TMA wait so
     // their HBM latency overlaps them
@@ -82,19 +86,19 @@ vel3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_p) {
     const float qn = (active && x + 9 < g.nx) ? __ldg(p + (int64_t)(x + 9) * sx + col) : 0.f;
     __syncthreads();  // the slot of plane x-2 is no longer read
     if (tid == 0 && x + 1 < xe) {
-      const int s = (it + 3) % kRing;
+      const int s = (u + 3) % kRing;
       fence_proxy_async_smem();
       mbar_arrive_expect_tx(&bar[s], kBytes);
       tma_load_3d(ring[s], &tm_p, &bar[s], z0 - 8, y0 - 8, x + 2);
     }
-    if (it == 0) {
+    if (u == 0 && x0 == xb) {
       mbar_wait_bounded(&bar[0], 0, status);
       mbar_wait_bounded(&bar[1], 0, status);
     }
-    mbar_wait_bounded(&bar[(it + 2) % kRing], ((it + 2) / kRing) & 1, status);
-    const float* Pm = ring[it % kRing];
-    const float* P0 = ring[(it + 1) % kRing];
-    const float* P1 = ring[(it + 2) % kRing];
+    mbar_wait_bounded(&bar[(u + 2) % kRing], ((u + 2) / kRing) & 1, status);
+    const float* Pm = ring[u % kRing];
+    const float* P0 = ring[(u + 1) % kRing];
+    const float* P1 = ring[(u + 2) % kRing];
     if (active) {
       float cm[8], co;
       load_taps(A.m.taps, cv.dc, cm, co);
@@ -167,7 +171,6 @@ prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
   for (int u = 0; u < 16; ++u) {
     const int x = x0 + u;
     if (x >= xe) break;  // uniform over the block
-    const int it = x - xb;
     const int64_t c = (int64_t)x * sx + col;
     CP cp;
     if (active) cp.load(A, c);
@@ -175,21 +178,21 @@ prs3d_march(const StepArgs A, const __grid_constant__ CUtensorMap tm_vx,
     __syncthreads();
     if (tid == 0 && x + 1 < xe) {
       fence_proxy_async_smem();
-      issue((it + 3) % kRing, x + 2);
+      issue((u + 3) % kRing, x + 2);
     }
-    if (it == 0) {
+    if (u == 0 && x0 == xb) {
       mbar_wait_bounded(&bar[0], 0, status);
       mbar_wait_bounded(&bar[1], 0, status);
     }
-    mbar_wait_bounded(&bar[(it + 2) % kRing], ((it + 2) / kRing) & 1, status);
-    const float* Xm = rx[it % kRing];
-    const float* X0 = rx[(it + 1) % kRing];
-    const float* Ym = ry[it % kRing];
-    const float* Y0 = ry[(it + 1) % kRing];
-    const float* Y1 = ry[(it + 2) % kRing];
-    const float* Zm = rz[it % kRing];
-    const float* Z0 = rz[(it + 1) % kRing];
-    const float* Z1 = rz[(it + 2) % kRing];
+    mbar_wait_bounded(&bar[(u + 2) % kRing], ((u + 2) / kRing) & 1, status);
+    const float* Xm = rx[u % kRing];
+    const float* X0 = rx[(u + 1) % kRing];
+    const float* Ym = ry[u % kRing];
+    const float* Y0 = ry[(u + 1) % kRing];
+    const float* Y1 = ry[(u + 2) % kRing];
+    const float* Zm = rz[u % kRing];
+    const float* Z0 = rz[(u + 1) % kRing];
+    const float* Z1 = rz[(u + 2) % kRing];
     if (active) {
       float cm[8], co;
       load_taps(A.m.taps, cp.dc, cm, co);
