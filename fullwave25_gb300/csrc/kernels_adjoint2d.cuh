@@ -480,7 +480,7 @@ static __global__ void set_step_counter(int* step, int value) { *step = value; }
 // Every operand of a block's 32 (y) x 8 (x) tile is brought into shared memory at block start by
 // one thread: TMA boxes over the adjoint-field stack, the coefficient-map stack, the two stored
 // states and the tap-index map, and a bulk copy of the tap table, all completing on one mbarrier
-// (bounded wait). A block thus has its whole input (about 42 KB) in flight at once instead of a
+// (bounded wait). A block thus has its whole input (about 36 KB) in flight at once instead of a
 // few dependent loads per thread, which is what limits the tiled kernels above (long-scoreboard
 // stalls at full occupancy, a fifth of the DRAM bandwidth). The arithmetic is that of
 // adj2d_prs_fused / adj2d_vel_tiled, term for term in the same order.
@@ -509,7 +509,7 @@ struct AdjMaps {
 // (i0 - 1, j0 - 8) (48 wide, 10 rows), full boxes at (i0 - 8, j0 - 8) (48 x 24). Box starts
 // along y are multiples of 4 floats (16 bytes): j0 = 8 + 32 blockIdx.x.
 constexpr int kHXW = 40, kHXR = 24, kHYW = 48, kHYR = 10, kHFW = 48, kHFR = 24;
-constexpr int kPrsPW = 25, kVelPW = 26;    // point-wise planes of each kernel
+constexpr int kPrsPW = 21, kVelPW = 22;    // point-wise planes of each kernel
 
 struct AdjPrsSmem {
   float gx[kHXR][kHXW];                 // lam_g_x
@@ -518,7 +518,7 @@ struct AdjPrsSmem {
   float vy[kHYR][kHYW];                 // v_y of S_{n+1}
   uint16_t dc[kHFR][kHFW];
   // point-wise: 0 lam_p | 1-4 lam_phi | 5-10 dt_k inv_kx ax1 bx1 ax2 bx2 | 11-14 phi of S_n |
-  // 15-18 phi of S_{n+1} | 19-24 gradient partials of the pressure maps
+  // 15-20 gradient partials of the pressure maps (phi of S_{n+1} is recomputed, not staged)
   float pw[kPrsPW][kD2TX][kD2TY];
   float lp[kD2TX][kD2TY];
   uint64_t bar;
@@ -529,7 +529,7 @@ struct AdjVelSmem {
   float p[kHFR][kHFW];                  // p of S_n
   uint16_t dc[kHFR][kHFW];
   // point-wise: 0-1 lam_v | 2-5 lam_psi | 6-11 rdt_rho inv_ku au1 bu1 au2 bu2 | 12-15 psi of
-  // S_n | 16-19 psi of S_{n+1} | 20-25 gradient partials of the velocity maps
+  // S_n | 16-21 gradient partials of the velocity maps (psi of S_{n+1} is recomputed)
   float pw[kVelPW][kD2TX][kD2TY];
   uint64_t bar;
 };
@@ -577,7 +577,7 @@ __device__ __forceinline__ bool adj_tma_begin(SmemT& S, const unsigned char* bas
 
 // Reverse step, launch 1 (adj2d_prs_fused with TMA-staged operands). `slot` = store slot of S_n.
 template <int kUnused = 0>
-__global__ void __launch_bounds__(256, 4) adj2d_prs_tma(const AdjArgs A, const Lists L,
+__global__ void __launch_bounds__(256, 5) adj2d_prs_tma(const AdjArgs A, const Lists L,
                                                         const float* residual, int n, int slot,
                                                         const __grid_constant__ AdjMaps M) {
   extern __shared__ __align__(128) unsigned char adj_smem[];
@@ -598,8 +598,7 @@ __global__ void __launch_bounds__(256, 4) adj2d_prs_tma(const AdjArgs A, const L
     tma_load_3d(S.pw[1], &M.lam4, &S.bar, j0, i0, kAdjLamPhi);
     tma_load_3d(S.pw[5], &M.maps6, &S.bar, j0, i0, kAdjMapPrs);
     tma_load_4d(S.pw[11], &M.st4, &S.bar, j0, i0, kStPhi, slot);
-    tma_load_4d(S.pw[15], &M.st4, &S.bar, j0, i0, kStPhi, slot + 1);
-    tma_load_3d(S.pw[19], &M.lam6, &S.bar, j0, i0, kAdjFields + kAdjMapPrs);
+    tma_load_3d(S.pw[15], &M.lam6, &S.bar, j0, i0, kAdjFields + kAdjMapPrs);
     bulk_load(taps, A.m.taps, tap_bytes, &S.bar);
   }
   __syncthreads();   // barrier initialised before anyone polls it
@@ -696,7 +695,9 @@ __global__ void __launch_bounds__(256, 4) adj2d_prs_tma(const AdjArgs A, const L
                        (S.vy[ty][tx + 8] - S.vy[ty][tx + 7]), d);
     }
     d = d * g.inv_h[a];
-    const float n1 = P(15 + 2 * a), n2 = P(16 + 2 * a);
+    // phi of S_{n+1}: the forward update of the memory variables (CellPrsT), bit for bit
+    const float n1 = fmaf(bxm[0], P(11 + 2 * a), axm[0] * d);
+    const float n2 = fmaf(bxm[1], P(12 + 2 * a), axm[1] * d);
     div += fmaf(d, ikx, n1) + n2;
     float lam_d = -k * ikx * lp;
 #pragma unroll
@@ -711,17 +712,17 @@ __global__ void __launch_bounds__(256, 4) adj2d_prs_tma(const AdjArgs A, const L
     A.lam_d[a][c] = lam_d;
   }
   g_dtk -= div * lp;
-  A.g32[kGDtK][c] = P(19) + g_dtk;
-  A.g32[kGInvKx][c] = P(20) + g_ikx;
-  A.g32[kGAx1][c] = P(21) + g_ax[0];
-  A.g32[kGBx1][c] = P(22) + g_bx[0];
-  A.g32[kGAx2][c] = P(23) + g_ax[1];
-  A.g32[kGBx2][c] = P(24) + g_bx[1];
+  A.g32[kGDtK][c] = P(15) + g_dtk;
+  A.g32[kGInvKx][c] = P(16) + g_ikx;
+  A.g32[kGAx1][c] = P(17) + g_ax[0];
+  A.g32[kGBx1][c] = P(18) + g_bx[0];
+  A.g32[kGAx2][c] = P(19) + g_ax[1];
+  A.g32[kGBx2][c] = P(20) + g_bx[1];
 }
 
 // Reverse step, launch 2 (adj2d_vel_tiled with TMA-staged operands).
 template <int kUnused = 0>
-__global__ void __launch_bounds__(256, 4) adj2d_vel_tma(const AdjArgs A, int slot,
+__global__ void __launch_bounds__(256, 5) adj2d_vel_tma(const AdjArgs A, int slot,
                                                         const __grid_constant__ AdjMaps M) {
   extern __shared__ __align__(128) unsigned char adj_smem[];
   AdjVelSmem& S = *reinterpret_cast<AdjVelSmem*>(adj_smem);
@@ -739,8 +740,7 @@ __global__ void __launch_bounds__(256, 4) adj2d_vel_tma(const AdjArgs A, int slo
     tma_load_3d(S.pw[0], &M.lam6, &S.bar, j0, i0, kAdjLamV);
     tma_load_3d(S.pw[6], &M.maps6, &S.bar, j0, i0, kAdjMapVel);
     tma_load_4d(S.pw[12], &M.st4, &S.bar, j0, i0, kStPsi, slot);
-    tma_load_4d(S.pw[16], &M.st4, &S.bar, j0, i0, kStPsi, slot + 1);
-    tma_load_3d(S.pw[20], &M.lam6, &S.bar, j0, i0, kAdjFields + kAdjMapVel);
+    tma_load_3d(S.pw[16], &M.lam6, &S.bar, j0, i0, kAdjFields + kAdjMapVel);
     bulk_load(taps, A.m.taps, tap_bytes, &S.bar);
   }
   __syncthreads();
@@ -804,7 +804,9 @@ __global__ void __launch_bounds__(256, 4) adj2d_vel_tma(const AdjArgs A, int slo
                         (S.p[ty + 7][tx + 9] - S.p[ty + 7][tx + 8]), gr);
     }
     gr = gr * g.inv_h[a];
-    const float p1 = P(16 + 2 * a), p2 = P(17 + 2 * a);
+    // psi of S_{n+1}: the forward update of the memory variables (CellVelT), bit for bit
+    const float p1 = fmaf(bum[0], P(12 + 2 * a), aum[0] * gr);
+    const float p2 = fmaf(bum[1], P(13 + 2 * a), aum[1] * gr);
     float lam_g = -r * iku * lv;
 #pragma unroll
     for (int nu = 0; nu < 2; ++nu) {
@@ -819,12 +821,12 @@ __global__ void __launch_bounds__(256, 4) adj2d_vel_tma(const AdjArgs A, int slo
     A.lam_v[a][c] = lv;
     A.lam_g[a][c] = lam_g;
   }
-  A.g32[kGRdtRho][c] = P(20) + g_r;
-  A.g32[kGInvKu][c] = P(21) + g_iku;
-  A.g32[kGAu1][c] = P(22) + g_au[0];
-  A.g32[kGBu1][c] = P(23) + g_bu[0];
-  A.g32[kGAu2][c] = P(24) + g_au[1];
-  A.g32[kGBu2][c] = P(25) + g_bu[1];
+  A.g32[kGRdtRho][c] = P(16) + g_r;
+  A.g32[kGInvKu][c] = P(17) + g_iku;
+  A.g32[kGAu1][c] = P(18) + g_au[0];
+  A.g32[kGBu1][c] = P(19) + g_bu[0];
+  A.g32[kGAu2][c] = P(20) + g_au[1];
+  A.g32[kGBu2][c] = P(21) + g_bu[1];
 }
 
 }  // namespace fwgb

@@ -159,7 +159,7 @@ int launch_persistent_typed(fw_handle* h, cudaStream_t s, int n0, int n_steps) {
   FW_CUDA(h, cudaGetDevice(&dev));
   FW_CUDA(h, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
   int n_tiles = h->tiling.count(), n_ty = h->tiling.n[1];
-  const int max_blocks = std::min(per_sm * sms, kBarGroup * kBarMaxGroups);
+  const int max_blocks = std::min(per_sm * sms, kBarMaxBlocks);
   if (max_blocks < 1) return fail(h, FW_ERR_CUDA, "persistent kernel: no block fits an SM");
   const int per_block = (n_tiles + max_blocks - 1) / max_blocks;
   const int grid = (n_tiles + per_block - 1) / per_block;
