@@ -1,4 +1,4 @@
-"""Gradients of the sensor-trace misfit with respect to sound speed, density and alpha0 (2D).
+"""Gradients of the sensor-trace misfit with respect to sound speed, density and alpha0 (2D, 3D).
 
 Layers:
 1. :func:`map_gradients` runs the engine's checkpointed forward pass and its discrete adjoint
@@ -107,7 +107,12 @@ class FdtdMisfit:
 
 
 class AdjointProblem:
-    """2D medium -> engine inputs, differentiable in c, rho and alpha0 (gamma held fixed)."""
+    """2D or 3D medium -> engine inputs, differentiable in c, rho and alpha0 (gamma held fixed).
+
+    ``shape``: the medium's cells (depth first). The source is the whole plane (row in 2D) at
+    depth ``source_row`` firing one pulse; sensors sit on the plane at depth ``sensor_row``, every
+    ``sensor_step``-th cell along each lateral axis.
+    """
 
     def __init__(self, shape, *, nt: int, f0: float = 3e6, ppw: int = 12, cfl: float = 0.2,
                  n_pml: int = 40, n_transition: int = 40, c_ref=None, device=None,
@@ -150,7 +155,7 @@ class AdjointProblem:
     def build(self, c, rho, a0, gam) -> DeviceInputs:
         """Engine inputs (maps keep the autograd graph of c, rho, a0)."""
         torch = _torch()
-        nb = self.nb
+        nb, nd = self.nb, len(self.shape)
         p = self._relaxation(a0, gam)
         for op in ("x1", "x2"):  # mechanism sort by time constant (fullwave/medium.py:121-209)
             t1 = p[f"d_{op}_nu1"] / p[f"kappa_{op}"] + p[f"alpha_{op}_nu1"]
@@ -171,25 +176,29 @@ class AdjointProblem:
                 maps[f"bpml{ax}{nu}"] = fw2[f"b_pml_{ax}{nu}"]
         cref = extend_edge(self.c_ref if self.c_ref is not None else c.detach(), nb).detach()
         cmin, cmax = float(cref.min()), float(cref.max())
-        dmap = coefficients.d_map(np.array([cmin, cmax]), self.grid.dt, self.grid.dx, is_3d=False)
+        dmap = coefficients.d_map(np.array([cmin, cmax]), self.grid.dt, self.grid.dx,
+                                  is_3d=nd == 3)
         dcmap = (torch.round(cref + 1e-9) - round(cmin + 1e-9)).to(torch.int32).contiguous()
-        nx, ny = self.shape
         sig = _pulse(self.grid, self.p0)
-        cols = np.arange(ny)
-        icc = np.stack([np.full(ny, self.source_row), cols], axis=1) + nb
-        scols = cols[::self.sensor_step]
-        outc = np.stack([np.full(scols.size, self.sensor_row), scols], axis=1) + nb
+
+        def plane(row, step):   # (row, lateral...) coordinates of a depth plane, C order
+            lat = np.meshgrid(*[np.arange(0, n, step) for n in self.shape[1:]], indexing="ij")
+            lat = [a.reshape(-1) for a in lat]
+            return np.stack([np.full(lat[0].size, row)] + lat, axis=1) + nb
+
+        icc = plane(self.source_row, 1)
+        outc = plane(self.sensor_row, self.sensor_step)
         dev = c.device
         i32 = lambda a: torch.as_tensor(np.ascontiguousarray(a, dtype=np.int32), device=dev)  # noqa: E731
         fmaps = {k: v.detach().to(torch.float32).contiguous() for k, v in maps.items()}
         fmaps["c"] = ce.detach().to(torch.float32).contiguous()
         fmaps["beta"] = torch.zeros_like(fmaps["rho"])
-        d = DeviceInputs(shape=(nx + 2 * nb, ny + 2 * nb), nt=self.grid.nt,
-                         spacing=(self.grid.dx, self.grid.dy), dt=self.grid.dt, c0=self.grid.c0,
-                         mod_t=1, d=coefficients.d_matrix(self.grid.cfl, is_3d=False), dmap=dmap,
-                         dcmap=dcmap, maps=fmaps, icc=i32(icc),
-                         icmat=torch.as_tensor(np.tile(sig, (ny, 1)), device=dev),
-                         outc=i32(outc), icczero=i32(np.zeros((0, 2))))
+        d = DeviceInputs(shape=tuple(n + 2 * nb for n in self.shape), nt=self.grid.nt,
+                         spacing=(self.grid.dx,) * nd, dt=self.grid.dt, c0=self.grid.c0,
+                         mod_t=1, d=coefficients.d_matrix(self.grid.cfl, is_3d=nd == 3),
+                         dmap=dmap, dcmap=dcmap, maps=fmaps, icc=i32(icc),
+                         icmat=torch.as_tensor(np.tile(sig, (len(icc), 1)), device=dev),
+                         outc=i32(outc), icczero=i32(np.zeros((0, nd))))
         d.diff_maps = maps
         return d
 

@@ -1,10 +1,24 @@
-// Host side of the discrete adjoint (2D): checkpointed forward pass and the reverse pass with
-// per-segment recomputation (the C ABI's fw_adjoint_forward / fw_adjoint_backward).
+// Host side of the discrete adjoint (2D and 3D): checkpointed forward pass and the reverse pass
+// with per-segment recomputation (the C ABI's fw_adjoint_forward / fw_adjoint_backward).
 #include "engine_host.cuh"
+#include "kernels_adjoint3d.cuh"
 
 using namespace fwgbh;
 
 namespace {
+
+// Adjoint-field allocation of an ND handle, per padded cell array: lam_p, lam_v (ND),
+// lam_psi (2 ND), lam_phi (2 ND), lam_d (ND), lam_g (ND), then the FP32 gradient partials.
+// In 2D this is the layout the TMA reverse-step kernels address by constant field indices.
+struct AdjLayout {
+  int lam_v, lam_psi, lam_phi, lam_d, lam_g, fields, stack;
+  explicit AdjLayout(int nd)
+      : lam_v(1), lam_psi(1 + nd), lam_phi(1 + 3 * nd), lam_d(1 + 5 * nd), lam_g(1 + 6 * nd),
+        fields(1 + 7 * nd), stack(1 + 7 * nd + kNumGrad) {}
+};
+static_assert(1 + 2 == kAdjLamPsi && 1 + 6 == kAdjLamPhi && 1 + 10 == kAdjLamD &&
+                  1 + 12 == kAdjLamG && 1 + 14 == kAdjFields,
+              "2D adjoint-field layout of the TMA kernels");
 
 static_assert(kAdjMapVel == kMRdtRho && kAdjMapPrs == kMDtK, "map runs of the adjoint kernels");
 
@@ -64,13 +78,16 @@ int prepare_adjoint_kernels(fw_handle* h, int dev, int smem_optin) {
   return FW_OK;
 }
 
-// The FP64 gradient sums of the 12 coefficient maps into the caller's dense [12][nx][ny] buffer.
+// The FP64 gradient sums of the 12 coefficient maps into the caller's dense
+// [12][nx][ny] (2D) or [12][nx][ny][nz] (3D) buffer: rows of the last axis, unpadded.
 int copy_gradients(fw_handle* h, const AdjArgs& A, double* grad_out, cudaStream_t s) {
   if (!grad_out) return FW_OK;
+  const size_t width = h->ndim == 3 ? (size_t)h->nz : (size_t)h->ny;
+  const size_t rows = h->ndim == 3 ? (size_t)h->nx * h->ny : (size_t)h->nx;
   for (int q = 0; q < kNumGrad; ++q)
-    FW_CUDA(h, cudaMemcpy2DAsync(grad_out + (size_t)q * h->nx * h->ny, h->ny * sizeof(double),
-                                 A.grad[q], h->pitch * sizeof(double), h->ny * sizeof(double),
-                                 h->nx, cudaMemcpyDeviceToDevice, s));
+    FW_CUDA(h, cudaMemcpy2DAsync(grad_out + (size_t)q * rows * width, width * sizeof(double),
+                                 A.grad[q], h->pitch * sizeof(double), width * sizeof(double),
+                                 rows, cudaMemcpyDeviceToDevice, s));
   return FW_OK;
 }
 
@@ -92,11 +109,12 @@ extern "C" {
 
 int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
-  if (h->ndim != 2) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint is implemented for 2D grids");
   if (h->has_beta) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs beta = 0 everywhere");
   if (h->aniso || h->exp)
     return fail(h, FW_ERR_UNSUPPORTED, "the adjoint covers the isotropic relaxation engine");
   if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called first");
+  if (h->args.l.rec_group)   // the misfit is defined on individual sensor traces
+    return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs individual sensor traces: clear the sensor groups");
   if (checkpoint_every < 1) return fail(h, FW_ERR_ARGUMENT, "checkpoint_every must be >= 1");
   const size_t state_elems = (size_t)h->ncells_padded * n_state(h->ndim);
   const int nckpt = (h->d.nt + checkpoint_every - 1) / checkpoint_every;
@@ -104,12 +122,13 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
     release_adjoint(h);
     const size_t b_ckpt = state_elems * std::max(nckpt, 1) * sizeof(float);
     const size_t b_store = state_elems * (checkpoint_every + 1) * sizeof(float);
-    // 15 adjoint fields and temporaries, then the FP32 per-segment gradient partials
-    const size_t b_lam = (size_t)h->ncells_padded * kAdjStack * sizeof(float);
+    // adjoint fields and temporaries (15 in 2D, 22 in 3D), then the FP32 segment partials
+    const size_t b_lam = (size_t)h->ncells_padded * AdjLayout(h->ndim).stack * sizeof(float);
     const size_t b_grad = (size_t)h->ncells_padded * kNumGrad * sizeof(double);
     // FWGB_ADJ_OVERLAP=0: one state store, segments recomputed and reversed one after another
+    // (always so in 3D, whose recomputation runs in place on the handle's own state)
     const char* ov = std::getenv("FWGB_ADJ_OVERLAP");
-    const bool two = !(ov && std::strcmp(ov, "0") == 0);
+    const bool two = h->ndim == 2 && !(ov && std::strcmp(ov, "0") == 0);
     cudaError_t e = cudaMalloc(&h->adj_ckpt, b_ckpt);
     if (e == cudaSuccess) e = cudaMalloc(&h->adj_store, b_store);
     if (e == cudaSuccess && two) e = cudaMalloc(&h->adj_store2, b_store);
@@ -146,28 +165,31 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   if (!h->adj_ckpt || h->host_step != h->d.nt)
     return fail(h, FW_ERR_STATE, "fw_adjoint_forward must run (to nt) before fw_adjoint_backward");
   if (!residual && h->d.ncoordsout) return fail(h, FW_ERR_ARGUMENT, "residual is NULL");
+  if (h->args.l.rec_group)
+    return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs individual sensor traces: clear the sensor groups");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int64_t fs = h->ncells_padded;
   const size_t state_elems = (size_t)fs * n_state(h->ndim);
-  FW_CUDA(h, cudaMemsetAsync(h->adj_lam, 0, (size_t)fs * kAdjStack * sizeof(float), s));
+  const AdjLayout lay(h->ndim);
+  FW_CUDA(h, cudaMemsetAsync(h->adj_lam, 0, (size_t)fs * lay.stack * sizeof(float), s));
   FW_CUDA(h, cudaMemsetAsync(h->adj_grad, 0, (size_t)fs * kNumGrad * sizeof(double), s));
   AdjArgs A{};
   A.g = h->args.g;
   A.m = h->args.m;
   A.fs = fs;
   A.lam_p = h->adj_lam;
-  for (int a = 0; a < 2; ++a) {
-    A.lam_v[a] = h->adj_lam + (kAdjLamV + a) * fs;
+  for (int a = 0; a < h->ndim; ++a) {
+    A.lam_v[a] = h->adj_lam + (lay.lam_v + a) * fs;
     for (int nu = 0; nu < 2; ++nu) {
-      A.lam_psi[a][nu] = h->adj_lam + (kAdjLamPsi + 2 * a + nu) * fs;
-      A.lam_phi[a][nu] = h->adj_lam + (kAdjLamPhi + 2 * a + nu) * fs;
+      A.lam_psi[a][nu] = h->adj_lam + (lay.lam_psi + 2 * a + nu) * fs;
+      A.lam_phi[a][nu] = h->adj_lam + (lay.lam_phi + 2 * a + nu) * fs;
     }
-    A.lam_d[a] = h->adj_lam + (kAdjLamD + a) * fs;
-    A.lam_g[a] = h->adj_lam + (kAdjLamG + a) * fs;
+    A.lam_d[a] = h->adj_lam + (lay.lam_d + a) * fs;
+    A.lam_g[a] = h->adj_lam + (lay.lam_g + a) * fs;
   }
   for (int q = 0; q < kNumGrad; ++q) {
     A.grad[q] = h->adj_grad + (size_t)q * fs;
-    A.g32[q] = h->adj_lam + (size_t)(kAdjFields + kGradSlot[q]) * fs;
+    A.g32[q] = h->adj_lam + (size_t)(lay.fields + kGradSlot[q]) * fs;
   }
   A.ndmap = h->d.ndmap;
   A.status = h->step + 1;
@@ -191,14 +213,14 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   FW_CUDA(h, cudaGetDevice(&dev));
   FW_CUDA(h, cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t smem_prs = adj_prs_tma_smem(h->d.ndmap), smem_vel = adj_vel_tma_smem(h->d.ndmap);
-  const bool tma = fused && !f64_steps && !(tenv && std::strcmp(tenv, "0") == 0) &&
+  const bool tma = h->ndim == 2 && fused && !f64_steps && !(tenv && std::strcmp(tenv, "0") == 0) &&
                    std::max(smem_prs, smem_vel) <= (size_t)smem_optin;
   // Recomputation: out of place from one stored state into the next (the TMA tile step kernels
   // reading slot n and writing slot n + 1), unless pressure is written in the ghost layer (it
   // persists there in place) or FWGB_ADJ_OOP=0: then a copy of the state into the store before
   // each in-place step.
   const char* oenv = std::getenv("FWGB_ADJ_OOP");
-  const bool oop = !h->ghost_writes && !(oenv && std::strcmp(oenv, "0") == 0);
+  const bool oop = h->ndim == 2 && !h->ghost_writes && !(oenv && std::strcmp(oenv, "0") == 0);
   // Overlap (default when a second store exists, with out-of-place recomputation and the TMA
   // reverse step): segment k-1 is recomputed on a second stream into the other store while
   // segment k is reversed on `stream`; events order each store's reuse. Same kernels, same
@@ -228,6 +250,10 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   }
   const dim3 block(32, 8), grid((unsigned)((h->ny - 2 * kGhost + 31) / 32),
                                 (unsigned)((h->nx - 2 * kGhost + 7) / 8));
+  // 3D: one block per 32 (z) x 8 (y) cells of an x plane
+  const dim3 block3(kA3TZ, kA3TY),
+      grid3((unsigned)((h->nz - 2 * kGhost + kA3TZ - 1) / kA3TZ),
+            (unsigned)((h->ny - 2 * kGhost + kA3TY - 1) / kA3TY), (unsigned)(h->nx - 2 * kGhost));
   const int K = h->adj_every;
   // recompute segment seg from its checkpoint into store b, keeping every state (out of place)
   auto recompute_oop = [&](int seg, int b, cudaStream_t rs) -> int {
@@ -326,6 +352,30 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     for (int n = n1 - 1; n >= n0; --n) {
       A.Sn = h->adj_store + state_elems * (n - n0);
       A.Sn1 = h->adj_store + state_elems * (n - n0 + 1);
+      if (h->ndim == 3) {
+        if (!first) {
+          if (smem_taps) adj3d_assemble<true><<<grid3, block3, sm, s>>>(A);
+          else adj3d_assemble<false><<<grid3, block3, 0, s>>>(A);
+        }
+        first = false;
+        if (counts[2]) adj2d_io<<<(counts[2] + 255) / 256, 256, 0, s>>>(A, L, residual, n, 0, 0, counts[2]);
+        if (counts[0] || counts[1])
+          adj2d_zero<<<(std::max(counts[0], counts[1]) + 255) / 256, 256, 0, s>>>(A, L, n, counts[0], counts[1]);
+        if (f64_steps && smem_taps) {
+          adj3d_prs<true, true><<<grid3, block3, sm, s>>>(A);
+          adj3d_vel<true, true><<<grid3, block3, sm, s>>>(A);
+        } else if (f64_steps) {
+          adj3d_prs<true, false><<<grid3, block3, 0, s>>>(A);
+          adj3d_vel<true, false><<<grid3, block3, 0, s>>>(A);
+        } else if (smem_taps) {
+          adj3d_prs<false, true><<<grid3, block3, sm, s>>>(A);
+          adj3d_vel<false, true><<<grid3, block3, sm, s>>>(A);
+        } else {
+          adj3d_prs<false, false><<<grid3, block3, 0, s>>>(A);
+          adj3d_vel<false, false><<<grid3, block3, 0, s>>>(A);
+        }
+        continue;
+      }
       if (tma) {
         adj2d_prs_tma<0><<<grid, block, smem_prs, s>>>(A, L, residual, n, n - n0, M[0]);
         adj2d_vel_tma<0><<<grid, block, smem_vel, s>>>(A, n - n0, M[0]);
@@ -369,7 +419,10 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
         adj2d_vel<false, false><<<grid, block, 0, s>>>(A);
       }
     }
-    if (!f64_steps) adj2d_merge<<<grid, block, 0, s>>>(A);
+    if (!f64_steps) {
+      if (h->ndim == 3) adj3d_merge<<<grid3, block3, 0, s>>>(A);
+      else adj2d_merge<<<grid, block, 0, s>>>(A);
+    }
     FW_CUDA(h, cudaGetLastError());
   }
   const int st = copy_gradients(h, A, grad_out, s);

@@ -27,29 +27,32 @@ enum AdjGrad {
 struct AdjArgs {
   Grid g;
   Maps m;
-  const float* Sn;      // stored state before step n: 11 padded fields (state order)
+  const float* Sn;      // stored state before step n: 11 (2D) / 16 (3D) padded fields, state order
   const float* Sn1;     // stored state after step n
   int64_t fs;           // field stride (padded cells)
-  float* lam_p;
-  float* lam_v[2];
-  float* lam_psi[2][2];
-  float* lam_phi[2][2];
-  float* lam_d[2];
-  float* lam_g[2];
+  float* lam_p;         // per derivative axis (2 in 2D, 3 in 3D):
+  float* lam_v[3];
+  float* lam_psi[3][2];
+  float* lam_phi[3][2];
+  float* lam_d[3];
+  float* lam_g[3];
   int ndmap;                 // tap sets in m.taps
   double* grad[kNumGrad];    // FP64 time sums
   float* g32[kNumGrad];      // FP32 partial sums of the current segment (segmented mode)
   int* status;               // device status word (bounded waits, alignment)
 };
 
-// state field indices (2D): p, vx, vy, psi[a][nu] = 3 + 2a + nu, phi[a][nu] = 7 + 2a + nu
+// stored-state field indices in ND dimensions: p, v[ND], psi[a][nu] = 1 + ND + 2a + nu,
+// phi[a][nu] = 1 + 3 ND + 2a + nu (2D: psi 3 + 2a + nu, phi 7 + 2a + nu)
 __device__ __forceinline__ const float* S_p(const float* S, int64_t) { return S; }
 __device__ __forceinline__ const float* S_v(const float* S, int64_t fs, int a) { return S + (1 + a) * fs; }
-__device__ __forceinline__ const float* S_psi(const float* S, int64_t fs, int a, int nu) {
-  return S + (3 + 2 * a + nu) * fs;
+template <int ND>
+__device__ __forceinline__ const float* S_psiN(const float* S, int64_t fs, int a, int nu) {
+  return S + (1 + ND + 2 * a + nu) * fs;
 }
-__device__ __forceinline__ const float* S_phi(const float* S, int64_t fs, int a, int nu) {
-  return S + (7 + 2 * a + nu) * fs;
+template <int ND>
+__device__ __forceinline__ const float* S_phiN(const float* S, int64_t fs, int a, int nu) {
+  return S + (1 + 3 * ND + 2 * a + nu) * fs;
 }
 
 // Tap table access: from a shared-memory copy of the table (kS, when it fits) or through the
@@ -198,34 +201,32 @@ static __global__ void adj2d_zero(const AdjArgs A, const Lists L, int n, int n_s
 // pipe is the bottleneck then); otherwise contributions are formed in FP32 (the precision of the
 // adjoint fields themselves) and summed per checkpoint segment in FP32 partials, which
 // adj2d_merge adds into the FP64 time sums at the end of every segment.
-// Pressure adjoint of body cell c, given its assembled lam_p.
-template <bool kF64, bool kS>
-__device__ __forceinline__ void adj_prs_cell(const AdjArgs& A, const TapSrc<kS>& T, int64_t c,
-                                             const float lp) {
+// Pressure adjoint of body cell c (ND axes), given its assembled lam_p and the divergence
+// components d[a] = D'_a v^{n+1/2} at c.
+template <bool kF64, int ND>
+__device__ __forceinline__ void adj_prs_point(const AdjArgs& A, int64_t c, const float lp,
+                                              const float (&d)[ND]) {
   using acc_t = typename std::conditional<kF64, double, float>::type;
-  const Grid& g = A.g;
   const int64_t fs = A.fs;
   const float k = __ldg(A.m.dt_k + c), ikx = __ldg(A.m.inv_kx[0] + c);
   const float ax[2] = {__ldg(A.m.ax[0][0] + c), __ldg(A.m.ax[0][1] + c)};
   const float bx[2] = {__ldg(A.m.bx[0][0] + c), __ldg(A.m.bx[0][1] + c)};
   acc_t g_dtk = 0, g_ikx = 0, g_ax[2] = {0, 0}, g_bx[2] = {0, 0};
   float div = 0.f;
-  const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
 #pragma unroll
-  for (int a = 0; a < 2; ++a) {
-    const float d = div_at(A.m, T, S_v(A.Sn1, fs, a), c, se[a], sf[a], g.inv_h[a]);
-    const float n1 = __ldg(S_phi(A.Sn1, fs, a, 0) + c), n2 = __ldg(S_phi(A.Sn1, fs, a, 1) + c);
-    div += fmaf(d, ikx, n1) + n2;
+  for (int a = 0; a < ND; ++a) {
+    const float n1 = __ldg(S_phiN<ND>(A.Sn1, fs, a, 0) + c), n2 = __ldg(S_phiN<ND>(A.Sn1, fs, a, 1) + c);
+    div += fmaf(d[a], ikx, n1) + n2;
     float lam_d = -k * ikx * lp;
 #pragma unroll
     for (int nu = 0; nu < 2; ++nu) {
       const float L = A.lam_phi[a][nu][c] - k * lp;
       lam_d = fmaf(ax[nu], L, lam_d);
-      g_ax[nu] += (acc_t)L * d;
-      g_bx[nu] += (acc_t)L * __ldg(S_phi(A.Sn, fs, a, nu) + c);
+      g_ax[nu] += (acc_t)L * d[a];
+      g_bx[nu] += (acc_t)L * __ldg(S_phiN<ND>(A.Sn, fs, a, nu) + c);
       A.lam_phi[a][nu][c] = bx[nu] * L;
     }
-    g_ikx -= (acc_t)k * lp * d;
+    g_ikx -= (acc_t)k * lp * d[a];
     A.lam_d[a][c] = lam_d;
   }
   g_dtk -= (acc_t)div * lp;
@@ -246,6 +247,16 @@ __device__ __forceinline__ void adj_prs_cell(const AdjArgs& A, const TapSrc<kS>&
   }
 }
 
+// Pressure adjoint of 2D body cell c, given its assembled lam_p.
+template <bool kF64, bool kS>
+__device__ __forceinline__ void adj_prs_cell(const AdjArgs& A, const TapSrc<kS>& T, int64_t c,
+                                             const float lp) {
+  const Grid& g = A.g;
+  const float d[2] = {div_at(A.m, T, S_v(A.Sn1, A.fs, 0), c, g.sx, 1, g.inv_h[0]),
+                      div_at(A.m, T, S_v(A.Sn1, A.fs, 1), c, 1, g.sx, g.inv_h[1])};
+  adj_prs_point<kF64, 2>(A, c, lp, d);
+}
+
 template <bool kF64, bool kS>
 __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
   extern __shared__ float s_taps[];
@@ -255,34 +266,32 @@ __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
   adj_prs_cell<kF64, kS>(A, T, c, A.lam_p[c]);
 }
 
-// Velocity adjoint of body cell c, given (D'_a^T lam_d_a)(c) for both axes.
-template <bool kF64, bool kS>
-__device__ __forceinline__ void adj_vel_cell(const AdjArgs& A, const TapSrc<kS>& T, int64_t c,
-                                             const float (&dT)[2]) {
+// Velocity adjoint of body cell c (ND axes), given (D'_a^T lam_d_a)(c) and the pressure
+// gradient components gr[a] = D_a p^n at c.
+template <bool kF64, int ND>
+__device__ __forceinline__ void adj_vel_point(const AdjArgs& A, int64_t c, const float (&dT)[ND],
+                                              const float (&gr)[ND]) {
   using acc_t = typename std::conditional<kF64, double, float>::type;
-  const Grid& g = A.g;
   const int64_t fs = A.fs;
   const float r = __ldg(A.m.rdt_rho + c), iku = __ldg(A.m.inv_ku[0] + c);
   const float au[2] = {__ldg(A.m.au[0][0] + c), __ldg(A.m.au[0][1] + c)};
   const float bu[2] = {__ldg(A.m.bu[0][0] + c), __ldg(A.m.bu[0][1] + c)};
   acc_t g_r = 0, g_iku = 0, g_au[2] = {0, 0}, g_bu[2] = {0, 0};
-  const int64_t se[2] = {g.sx, 1}, sf[2] = {1, g.sx};
 #pragma unroll
-  for (int a = 0; a < 2; ++a) {
+  for (int a = 0; a < ND; ++a) {
     const float lv = A.lam_v[a][c] + dT[a];
-    const float gr = grad_at(A.m, T, S_p(A.Sn, fs), c, se[a], sf[a], g.inv_h[a]);
-    const float p1 = __ldg(S_psi(A.Sn1, fs, a, 0) + c), p2 = __ldg(S_psi(A.Sn1, fs, a, 1) + c);
+    const float p1 = __ldg(S_psiN<ND>(A.Sn1, fs, a, 0) + c), p2 = __ldg(S_psiN<ND>(A.Sn1, fs, a, 1) + c);
     float lam_g = -r * iku * lv;
 #pragma unroll
     for (int nu = 0; nu < 2; ++nu) {
       const float M = A.lam_psi[a][nu][c] - r * lv;
       lam_g = fmaf(au[nu], M, lam_g);
-      g_au[nu] += (acc_t)M * gr;
-      g_bu[nu] += (acc_t)M * __ldg(S_psi(A.Sn, fs, a, nu) + c);
+      g_au[nu] += (acc_t)M * gr[a];
+      g_bu[nu] += (acc_t)M * __ldg(S_psiN<ND>(A.Sn, fs, a, nu) + c);
       A.lam_psi[a][nu][c] = bu[nu] * M;
     }
-    g_r -= (acc_t)lv * (fmaf(gr, iku, p1) + p2);
-    g_iku -= (acc_t)r * gr * lv;
+    g_r -= (acc_t)lv * (fmaf(gr[a], iku, p1) + p2);
+    g_iku -= (acc_t)r * gr[a] * lv;
     A.lam_v[a][c] = lv;
     A.lam_g[a][c] = lam_g;
   }
@@ -301,6 +310,16 @@ __device__ __forceinline__ void adj_vel_cell(const AdjArgs& A, const TapSrc<kS>&
     A.g32[kGBu1][c] += g_bu[0];
     A.g32[kGBu2][c] += g_bu[1];
   }
+}
+
+// Velocity adjoint of 2D body cell c, given (D'_a^T lam_d_a)(c) for both axes.
+template <bool kF64, bool kS>
+__device__ __forceinline__ void adj_vel_cell(const AdjArgs& A, const TapSrc<kS>& T, int64_t c,
+                                             const float (&dT)[2]) {
+  const Grid& g = A.g;
+  const float gr[2] = {grad_at(A.m, T, S_p(A.Sn, A.fs), c, g.sx, 1, g.inv_h[0]),
+                       grad_at(A.m, T, S_p(A.Sn, A.fs), c, 1, g.sx, g.inv_h[1])};
+  adj_vel_point<kF64, 2>(A, c, dT, gr);
 }
 
 template <bool kF64, bool kS>

@@ -330,7 +330,7 @@ class Engine:
 
     def adjoint_backward(self, residual_ptr: int, grad_ptr: int, stream: int | None = None) -> None:
         """``residual_ptr``: device float32 [n_out, ncoordsout]; ``grad_ptr``: device float64
-        [12, nx, ny] (order of ``ADJOINT_MAPS``)."""
+        [12, *shape] (order of ``ADJOINT_MAPS``)."""
         self._call("fw_adjoint_backward", C.c_void_p(stream or 0),
                    C.cast(C.c_void_p(residual_ptr), _FP),
                    C.cast(C.c_void_p(grad_ptr), C.POINTER(C.c_double)))

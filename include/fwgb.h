@@ -210,27 +210,29 @@ FWGB_API int fw_launches_per_step(const fw_handle *h, int32_t *n);
 /* Release all device memory of the handle. */
 FWGB_API int fw_destroy(fw_handle *h);
 
-/* Gradient of the sensor-trace misfit J = 1/2 sum ||traces - observed||^2 (2D, beta = 0), with
- * respect to the engine's coefficient maps, by the discrete adjoint of the time step. No
- * counterpart in the reference (it has no gradient computation).
+/* Gradient of the sensor-trace misfit J = 1/2 sum ||traces - observed||^2 (2D and 3D isotropic
+ * relaxation engine, beta = 0, individual sensor traces: no sensor groups), with respect to the
+ * engine's coefficient maps, by the discrete adjoint of the time step. No counterpart in the
+ * reference (it has no gradient computation).
  * fw_adjoint_forward: run the full forward solve from rest, keeping a checkpoint of the wavefield
  * every `checkpoint_every` steps (device memory: nt / checkpoint_every + 2 (checkpoint_every + 1)
- * wavefield copies: the checkpoints and two state stores; FWGB_ADJ_OVERLAP=0 at this call keeps
- * one store); the traces are then available from fw_read_traces. */
+ * wavefield copies: the checkpoints and two state stores; one store in 3D, or with
+ * FWGB_ADJ_OVERLAP=0 at this call); the traces are then available from fw_read_traces. */
 FWGB_API int fw_adjoint_forward(fw_handle *h, void *stream, int32_t checkpoint_every);
 
 /* Reverse pass: recompute each segment from its checkpoint and run the adjoint step backwards,
  * accumulating the gradient: each step's contributions are formed in FP32 (the precision of the
  * adjoint fields) into per-segment FP32 partial sums that are added into FP64 time sums at the
  * end of every segment (FWGB_ADJ_F64_STEPS=1: every step's contributions in FP64 instead).
- * Each reverse step is two launches whose operands are staged in shared memory by TMA
+ * 2D: each reverse step is two launches whose operands are staged in shared memory by TMA
  * (FWGB_ADJ_TMA=0: the same arithmetic with the operands loaded by the threads). With two state
  * stores, the next segment is recomputed into one on a second (internal) stream while the current
  * segment is reversed from the other on `stream`; the gradient is bitwise the same as one segment
- * after another.
+ * after another. 3D: the segment is recomputed in place (state copies into the store), then each
+ * reverse step is four launches with the operands loaded by the threads.
  * `residual` = traces - observed, device float32 [n_out][ncoordsout]. `grad_out`: device FP64
- * [12][nx][ny] in the order dt/rho, dt*K, 1/kappau, 1/kappax, au1, bu1, au2, bu2, ax1, bx1, ax2,
- * bx2 (ghost cells zero). The wavefield left in the handle afterwards is the first segment's
+ * [12][nx][ny] (3D: [12][nx][ny][nz]) in the order dt/rho, dt*K, 1/kappau, 1/kappax, au1, bu1,
+ * au2, bu2, ax1, bx1, ax2, bx2 (ghost cells zero). The wavefield left in the handle afterwards is the first segment's
  * recomputation. Returns after the stream has finished the pass (FW_ERR_DEVICE if a kernel
  * reported a timed-out wait). */
 FWGB_API int fw_adjoint_backward(fw_handle *h, void *stream, const float *residual,
