@@ -25,6 +25,10 @@ struct fw_group {
   cudaGraphExec_t run_graph = nullptr;
   std::vector<fw_handle*> run_graph_members;
   int run_graph_shape = -1;
+  // persistent run (FWGB_GROUP_PERSISTENT=1): member nt (run order), tiles_upto, barrier words,
+  // the launch's status word and its 64-bit work-ticket counter
+  int* d_persist = nullptr;
+  size_t persist_cap = 0;   // ints
 };
 
 namespace {
@@ -289,6 +293,70 @@ int group_run_graph(fw_group* g, cudaGraphExec_t* out) {
   return FW_OK;
 }
 
+// The whole run of a freshly reset group as one persistent cooperative launch of the streaming
+// row-march bodies (step2d_group_persistent): grid = every block that fits on the device at once
+// (at most kBarMaxBlocks), each walking the work list with a grid stride.
+template <int TY, int XC, bool kBeta>
+int group_run_persistent_t(fw_group* g, cudaStream_t s, int* d_nt, int* d_upto, unsigned* d_bar,
+                           int max_nt) {
+  auto kern = step2d_group_persistent<TY, XC, kBeta, kMRdtRho, kMDtK>;
+  int per_sm = 0, dev = 0, sms = 0;
+  FW_CUDA(nullptr, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TY, 0));
+  FW_CUDA(nullptr, cudaGetDevice(&dev));
+  FW_CUDA(nullptr, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+  const int n = (int)g->members.size();
+  const int grid = std::min({per_sm * sms, kBarMaxBlocks, g->tiles_upto[n]});
+  if (grid < 1) return fail(nullptr, FW_ERR_CUDA, "persistent group kernel: no block fits an SM");
+  const StepArgs* a = g->d_args;
+  const March2Maps* m = g->d_maps;
+  const int4* w = g->d_tiles;
+  void* args[] = {&a, &m, &w, &d_nt, &d_upto, const_cast<int*>(&n), &max_nt, &d_bar};
+  FW_CUDA(nullptr, cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(grid),
+                                               dim3(TY), args, 0, s));
+  return FW_OK;
+}
+
+int group_run_persistent(fw_group* g, cudaStream_t s) {
+  const int n = (int)g->members.size();
+  // ints: member nt, tiles_upto, barrier words, status word, pad, 64-bit ticket counter
+  const size_t need = (size_t)n + (n + 1) + kBarWords + 4 + 1;
+  if (need > g->persist_cap) {
+    if (g->d_persist) cudaFree(g->d_persist);
+    g->d_persist = nullptr;
+    g->persist_cap = 0;
+    FW_CUDA(nullptr, cudaMalloc(&g->d_persist, need * sizeof(int)));
+    g->persist_cap = need;
+  }
+  std::vector<int> host(n + n + 1, 0);
+  int max_nt = 0;
+  for (int r = 0; r < n; ++r) {
+    host[r] = (int)g->members[r]->d.nt;
+    max_nt = std::max(max_nt, host[r]);
+  }
+  for (int r = 0; r <= n; ++r) host[n + r] = g->tiles_upto[r];
+  int* d_nt = g->d_persist;
+  int* d_upto = d_nt + n;
+  // barrier words on an 8-byte boundary: the ticket counter after them is 64-bit
+  unsigned* d_bar = reinterpret_cast<unsigned*>(d_upto + n + 1 + ((2 * n + 1) & 1));
+  FW_CUDA(nullptr, cudaMemcpyAsync(d_nt, host.data(), host.size() * sizeof(int),
+                                   cudaMemcpyHostToDevice, s));
+  FW_CUDA(nullptr, cudaMemsetAsync(d_bar, 0, (kBarWords + 4) * sizeof(unsigned), s));
+  FW_CUDA(nullptr, cudaStreamSynchronize(s));   // the host vector goes out of scope
+  switch (g->shape * 2 + (g->beta ? 1 : 0)) {
+    case 2: return group_run_persistent_t<64, 16, false>(g, s, d_nt, d_upto, d_bar, max_nt);
+    case 3: return group_run_persistent_t<64, 16, true>(g, s, d_nt, d_upto, d_bar, max_nt);
+    case 4: return group_run_persistent_t<64, 32, false>(g, s, d_nt, d_upto, d_bar, max_nt);
+    case 5: return group_run_persistent_t<64, 32, true>(g, s, d_nt, d_upto, d_bar, max_nt);
+    case 6: return group_run_persistent_t<128, 16, false>(g, s, d_nt, d_upto, d_bar, max_nt);
+    case 7: return group_run_persistent_t<128, 16, true>(g, s, d_nt, d_upto, d_bar, max_nt);
+    case 8: return group_run_persistent_t<128, 32, false>(g, s, d_nt, d_upto, d_bar, max_nt);
+    case 9: return group_run_persistent_t<128, 32, true>(g, s, d_nt, d_upto, d_bar, max_nt);
+    case 10: return group_run_persistent_t<128, 64, false>(g, s, d_nt, d_upto, d_bar, max_nt);
+    case 11: return group_run_persistent_t<128, 64, true>(g, s, d_nt, d_upto, d_bar, max_nt);
+    default: return fail(nullptr, FW_ERR_UNSUPPORTED, "persistent group run: row-march shapes only");
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -381,8 +449,17 @@ int fw_group_run(fw_group* g, void* stream) {
     return fw_group_advance(g, stream, max_nt);
   std::vector<fw_handle*> m = g->members;
   int st = group_set(g, m.data(), (int)m.size());   // order by steps left (all at step 0)
+  if (st) return st;
+  // FWGB_GROUP_PERSISTENT=1: the whole run as one persistent cooperative launch (row-march
+  // shapes with streamed operands) instead of one graph of per-step launches
+  const char* pe = std::getenv("FWGB_GROUP_PERSISTENT");
+  if (pe && std::strcmp(pe, "1") == 0 && g->shape >= 1 && g->shape <= 5 && g->stream) {
+    if ((st = group_run_persistent(g, static_cast<cudaStream_t>(stream)))) return st;
+    for (fw_handle* h : g->members) h->host_step = h->d.nt;
+    return FW_OK;
+  }
   cudaGraphExec_t exec = nullptr;
-  if (st || (st = group_run_graph(g, &exec))) return st;
+  if ((st = group_run_graph(g, &exec))) return st;
   FW_CUDA(nullptr, cudaGraphLaunch(exec, static_cast<cudaStream_t>(stream)));
   for (fw_handle* h : g->members) h->host_step = h->d.nt;
   return FW_OK;
@@ -404,6 +481,7 @@ int fw_group_destroy(fw_group* g) {
   if (g->d_args) cudaFree(g->d_args);
   if (g->d_tiles) cudaFree(g->d_tiles);
   if (g->d_maps) cudaFree(g->d_maps);
+  if (g->d_persist) cudaFree(g->d_persist);
   delete g;
   return FW_OK;
 }

@@ -15,6 +15,7 @@
 #pragma once
 #include "engine_common.cuh"
 #include "kernels_direct.cuh"
+#include "kernels_persistent2d.cuh"
 #include "tma.cuh"
 
 namespace fwgb {
@@ -46,6 +47,14 @@ constexpr int kMarch2Maps = sizeof(March2Maps) / sizeof(CUtensorMap);   // 10
 constexpr int kV2StateF = 6, kV2MapF = 6, kP2PhiF = 4;
 constexpr int kState2V0 = 1, kState2Phi0 = 7;
 
+// Column-queue load: the read-only path, or (kPersist: the field changes inside the launch) a load
+// that bypasses L1 and reads the coherent L2.
+template <bool kPersist>
+__device__ __forceinline__ float ld_col(const float* q) {
+  if constexpr (kPersist) return __ldcg(q);
+  else return __ldg(q);
+}
+
 __device__ __forceinline__ void tma_load_3d_row(void* dst, const CUtensorMap* map, uint64_t* bar,
                                                 int y, int x, int f) {
   tma_load_3d(dst, map, bar, y, x, f);
@@ -57,17 +66,46 @@ __device__ __forceinline__ void tma_load_3d_row(void* dst, const CUtensorMap* ma
 // kStream (isotropic engine): the point-wise operands of a row come by TMA too — state, maps and
 // tap index of row x+1 are in flight (two-stage ring) while row x is computed; the cell update
 // is CellVelT's / CellPrsT's, so results stay bit-identical.
-template <int TY, int XC, class CV, bool kStream = false, int kMapSlotVel = 0>
-__device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const March2Maps* tm,
-                                                 int by, int bx) {
+// kPersist: the body runs many times inside one launch (the persistent group kernel), where p and
+// v change between calls: the column queues load from L2 instead of the read-only path,
+// the ring is refilled only after a proxy fence (its slots were read by the previous call), and
+// the mbarriers are invalidated at the end so the next call can initialise them again.
+// Shared memory of one row-march body (the kernels declare it; the persistent group kernel
+// overlays the velocity and pressure bodies' in a union).
+template <int TY, bool kStream>
+struct VelMarchSmem {
+  alignas(128) float ring[kRing2][Row2<TY>::kWideSlot];
+  alignas(128) float pst[kStream ? 2 : 1][kStream ? kV2StateF : 1][kStream ? TY : 1];
+  alignas(128) float pmp[kStream ? 2 : 1][kStream ? kV2MapF : 1][kStream ? TY : 1];
+  alignas(128) uint16_t pdc[kStream ? 2 : 1][kStream ? TY : 1];
+  alignas(8) uint64_t bar[kRing2];
+  alignas(8) uint64_t pbar[2];
+};
+template <int TY, bool kStream, bool kBeta>
+struct PrsMarchSmem {
+  static constexpr int kMapF = kV2MapF + (kBeta ? 1 : 0);
+  alignas(128) float rx[kRing2][Row2<TY>::kNarrowSlot];
+  alignas(128) float ry[kRing2][Row2<TY>::kWideSlot];
+  alignas(128) float ppp[kStream ? 2 : 1][kStream ? TY : 1];
+  alignas(128) float pph[kStream ? 2 : 1][kStream ? kP2PhiF : 1][kStream ? TY : 1];
+  alignas(128) float pmp[kStream ? 2 : 1][kStream ? kMapF : 1][kStream ? TY : 1];
+  alignas(128) uint16_t pdc[kStream ? 2 : 1][kStream ? TY : 1];
+  alignas(8) uint64_t bar[kRing2];
+  alignas(8) uint64_t pbar[2];
+};
+
+template <int TY, int XC, class CV, bool kStream = false, int kMapSlotVel = 0,
+          bool kPersist = false>
+__device__ __forceinline__ void vel2d_march_body(VelMarchSmem<TY, kStream>& S, const StepArgs& A,
+                                                 const March2Maps* tm, int by, int bx) {
   using R = Row2<TY>;
   const CUtensorMap* tm_p = &tm->p;
-  __shared__ alignas(128) float ring[kRing2][R::kWideSlot];
-  __shared__ alignas(8) uint64_t bar[kRing2];
-  __shared__ alignas(128) float pst[kStream ? 2 : 1][kStream ? kV2StateF : 1][kStream ? TY : 1];
-  __shared__ alignas(128) float pmp[kStream ? 2 : 1][kStream ? kV2MapF : 1][kStream ? TY : 1];
-  __shared__ alignas(128) uint16_t pdc[kStream ? 2 : 1][kStream ? TY : 1];
-  __shared__ alignas(8) uint64_t pbar[2];
+  auto& ring = S.ring;
+  auto& bar = S.bar;
+  auto& pst = S.pst;
+  auto& pmp = S.pmp;
+  auto& pdc = S.pdc;
+  auto& pbar = S.pbar;
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tj = threadIdx.x;
@@ -94,6 +132,7 @@ __device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const March2
     }
   };
   if (tj == 0) {
+    if constexpr (kPersist) fence_proxy_async_smem();
     for (int s = 0; s < 3; ++s) {
       mbar_arrive_expect_tx(&bar[s], kBytes);
       tma_load_2d(ring[s], tm_p, &bar[s], y0 - 8, xb - 1 + s);
@@ -104,7 +143,8 @@ __device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const March2
   const float* __restrict__ p = A.f.p;
   float q[16];  // q[t] = p[x - 7 + t]
 #pragma unroll
-  for (int t = 0; t < 16; ++t) q[t] = active ? __ldg(p + (int64_t)(xb - 7 + t) * sx + j) : 0.f;
+  for (int t = 0; t < 16; ++t)
+    q[t] = active ? ld_col<kPersist>(p + (int64_t)(xb - 7 + t) * sx + j) : 0.f;
   const int si = tj + 8;
   for (int x = xb; x < xe; ++x) {
     const int it = x - xb;
@@ -113,7 +153,7 @@ __device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const March2
     if constexpr (!kStream) {
       if (active) cv.load(A, c);
     }
-    const float qn = (active && x + 9 < g.nx) ? __ldg(p + (int64_t)(x + 9) * sx + j) : 0.f;
+    const float qn = (active && x + 9 < g.nx) ? ld_col<kPersist>(p + (int64_t)(x + 9) * sx + j) : 0.f;
     __syncthreads();  // the halo slot of row x-2 and the point-wise slot of row x-1 are free
     if (tj == 0 && x + 1 < xe) {
       const int s = (it + 3) % kRing2;
@@ -168,25 +208,34 @@ __device__ __forceinline__ void vel2d_march_body(const StepArgs& A, const March2
     for (int t = 0; t < 15; ++t) q[t] = q[t + 1];
     q[15] = qn;
   }
+  if constexpr (kPersist) {
+    __syncthreads();   // every wait on the ring is over
+    if (tj == 0) {
+      for (int s = 0; s < kRing2; ++s) mbar_inval(&bar[s]);
+      if constexpr (kStream) for (int s = 0; s < 2; ++s) mbar_inval(&pbar[s]);
+    }
+  }
 }
 
+// `n`: the time step being completed (-1: read the simulation's device step counter).
 template <int TY, int XC, class CP, bool kStream = false, bool kBeta = false,
-          int kMapSlotPrs = 0>
-__device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const March2Maps* tm,
-                                                 int by, int bx) {
+          int kMapSlotPrs = 0, bool kPersist = false>
+__device__ __forceinline__ void prs2d_march_body(PrsMarchSmem<TY, kStream, kBeta>& S,
+                                                 const StepArgs& A, const March2Maps* tm,
+                                                 int by, int bx, int n = -1) {
   static_assert(TY % kD2TY == 0 && XC % kD2TX == 0, "a march block must own whole list tiles");
   using R = Row2<TY>;
-  constexpr int kMapF = kV2MapF + (kBeta ? 1 : 0);
+  constexpr int kMapF = PrsMarchSmem<TY, kStream, kBeta>::kMapF;
   const CUtensorMap* tm_vx = &tm->vx;
   const CUtensorMap* tm_vy = &tm->vy;
-  __shared__ alignas(128) float rx[kRing2][R::kNarrowSlot];
-  __shared__ alignas(128) float ry[kRing2][R::kWideSlot];
-  __shared__ alignas(8) uint64_t bar[kRing2];
-  __shared__ alignas(128) float ppp[kStream ? 2 : 1][kStream ? TY : 1];
-  __shared__ alignas(128) float pph[kStream ? 2 : 1][kStream ? kP2PhiF : 1][kStream ? TY : 1];
-  __shared__ alignas(128) float pmp[kStream ? 2 : 1][kStream ? kMapF : 1][kStream ? TY : 1];
-  __shared__ alignas(128) uint16_t pdc[kStream ? 2 : 1][kStream ? TY : 1];
-  __shared__ alignas(8) uint64_t pbar[2];
+  auto& rx = S.rx;
+  auto& ry = S.ry;
+  auto& bar = S.bar;
+  auto& ppp = S.ppp;
+  auto& pph = S.pph;
+  auto& pmp = S.pmp;
+  auto& pdc = S.pdc;
+  auto& pbar = S.pbar;
   const Grid& g = A.g;
   int* status = A.step + 1;
   const int tj = threadIdx.x;
@@ -219,6 +268,7 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const March2
     }
   };
   if (tj == 0) {
+    if constexpr (kPersist) fence_proxy_async_smem();
     for (int s = 0; s < 3; ++s) issue(s, xb - 1 + s);
     issue_pw(0, xb);
   }
@@ -227,7 +277,8 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const March2
   float* p = A.f.p;
   float r[16];  // r[t] = vx[x - 8 + t]
 #pragma unroll
-  for (int t = 0; t < 16; ++t) r[t] = active ? __ldg(vx + (int64_t)(xb - 8 + t) * sx + j) : 0.f;
+  for (int t = 0; t < 16; ++t)
+    r[t] = active ? ld_col<kPersist>(vx + (int64_t)(xb - 8 + t) * sx + j) : 0.f;
   const int xi = tj + 4, yi = tj + 8;
   for (int x = xb; x < xe; ++x) {
     const int it = x - xb;
@@ -236,7 +287,7 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const March2
     if constexpr (!kStream) {
       if (active) cp.load(A, c);
     }
-    const float rn = active ? __ldg(vx + (int64_t)(x + 8) * sx + j) : 0.f;
+    const float rn = active ? ld_col<kPersist>(vx + (int64_t)(x + 8) * sx + j) : 0.f;
     __syncthreads();
     if (tj == 0 && x + 1 < xe) {
       fence_proxy_async_smem();
@@ -292,28 +343,37 @@ __device__ __forceinline__ void prs2d_march_body(const StepArgs& A, const March2
     for (int t = 0; t < 15; ++t) r[t] = r[t + 1];
     r[15] = rn;
   }
+  if constexpr (kPersist) {
+    __syncthreads();   // every wait on the ring is over
+    if (tj == 0) {
+      for (int s = 0; s < kRing2; ++s) mbar_inval(&bar[s]);
+      if constexpr (kStream) for (int s = 0; s < 2; ++s) mbar_inval(&pbar[s]);
+    }
+  }
   // the block's list tiles: rows [tx0, tx0 + XC / kD2TX) x columns [ty0, ty0 + TY / kD2TY)
   const int n_tx = (g.nx - 2 * kGhost + kD2TX - 1) / kD2TX;
   const int n_ty = (g.ny - 2 * kGhost + kD2TY - 1) / kD2TY;
   const int tx0 = bx * (XC / kD2TX), ty0 = by * (TY / kD2TY);
   span_epilogue(A, p, tx0, min(tx0 + XC / kD2TX, n_tx), ty0, min(ty0 + TY / kD2TY, n_ty), n_ty,
-                tj, TY);
+                tj, TY, n);
 }
 
 // Single simulation: grid (y blocks, x chunks); the tensor maps travel as one kernel parameter.
 template <int TY, int XC, class CV, bool kStream = false, int kMapSlotVel = 0>
 __global__ void __launch_bounds__(TY, 1024 / TY)
 vel2d_march(const StepArgs A, const __grid_constant__ March2Maps tm) {
+  __shared__ VelMarchSmem<TY, kStream> S;
   pdl_entry();
   if (blockIdx.x == 0 && blockIdx.y == 0 && threadIdx.x == 0) *A.step += 1;
-  vel2d_march_body<TY, XC, CV, kStream, kMapSlotVel>(A, &tm, blockIdx.x, blockIdx.y);
+  vel2d_march_body<TY, XC, CV, kStream, kMapSlotVel>(S, A, &tm, blockIdx.x, blockIdx.y);
 }
 
 template <int TY, int XC, class CP, bool kStream = false, bool kBeta = false, int kMapSlotPrs = 0>
 __global__ void __launch_bounds__(TY, 1024 / TY)
 prs2d_march(const StepArgs A, const __grid_constant__ March2Maps tm) {
+  __shared__ PrsMarchSmem<TY, kStream, kBeta> S;
   pdl_entry();
-  prs2d_march_body<TY, XC, CP, kStream, kBeta, kMapSlotPrs>(A, &tm, blockIdx.x, blockIdx.y);
+  prs2d_march_body<TY, XC, CP, kStream, kBeta, kMapSlotPrs>(S, A, &tm, blockIdx.x, blockIdx.y);
 }
 
 // Group (batched) kernels: block b works on work[b] = {simulation, y block, x chunk, 1 if the
@@ -333,11 +393,12 @@ __global__ void __launch_bounds__(TY, 1024 / TY)
 vel2d_march_group(const StepArgs* __restrict__ sims, const March2Maps* __restrict__ maps,
                   const int4* __restrict__ work) {
   __shared__ alignas(16) StepArgs A;
+  __shared__ VelMarchSmem<TY, kStream> S;
   pdl_entry();
   const int4 t = work[blockIdx.x];
   stage_args(A, sims[t.x]);
   if (t.w && threadIdx.x == 0) *A.step += 1;
-  vel2d_march_body<TY, XC, CellVelT<2, false>, kStream, kMapSlotVel>(A, maps + t.x, t.y, t.z);
+  vel2d_march_body<TY, XC, CellVelT<2, false>, kStream, kMapSlotVel>(S, A, maps + t.x, t.y, t.z);
 }
 
 template <int TY, int XC, bool kBeta, bool kStream = false, int kMapSlotPrs = 0>
@@ -345,11 +406,84 @@ __global__ void __launch_bounds__(TY, 1024 / TY)
 prs2d_march_group(const StepArgs* __restrict__ sims, const March2Maps* __restrict__ maps,
                   const int4* __restrict__ work) {
   __shared__ alignas(16) StepArgs A;
+  __shared__ PrsMarchSmem<TY, kStream, kBeta> S;
   pdl_entry();
   const int4 t = work[blockIdx.x];
   stage_args(A, sims[t.x]);
   prs2d_march_body<TY, XC, CellPrsT<2, kBeta, false>, kStream, kBeta, kMapSlotPrs>(
-      A, maps + t.x, t.y, t.z);
+      S, A, maps + t.x, t.y, t.z);
+}
+
+// Persistent group kernel: the whole run of a group in one cooperative launch (all blocks
+// co-resident). Members are ordered by nt (descending), so at step n the active members are a
+// prefix and their work items the first tiles_upto[k] entries of the work list. Per step:
+//   velocity bodies of the active items | grid barrier |
+//   pressure bodies (+ epilogue) of the active items | grid barrier
+// Blocks claim items from one 64-bit ticket counter (zeroed before the launch): in a phase with
+// `items` items every block draws tickets until one falls past the phase's items, so each phase
+// consumes exactly items + gridDim.x tickets and every block knows where the next phase starts.
+// with the same bodies, and so the same results bit for bit, as the per-step group launches. A
+// barrier that gives up (bounded wait) stops the launch and marks every member's status word.
+// Between phases every thread fences its global writes against the async proxy, and the thread
+// that issues a block's TMA loads fences again after the barrier: the loads read rows written by
+// other blocks inside the same launch.
+template <int TY, int XC, bool kBeta, int kMapSlotVel, int kMapSlotPrs>
+__global__ void __launch_bounds__(TY, 1024 / TY)
+step2d_group_persistent(const StepArgs* __restrict__ sims, const March2Maps* __restrict__ maps,
+                        const int4* __restrict__ work, const int* __restrict__ member_nt,
+                        const int* __restrict__ tiles_upto, int n_members, int max_nt,
+                        unsigned* bar) {
+  __shared__ alignas(16) StepArgs A;
+  __shared__ union Rings {
+    VelMarchSmem<TY, true> v;
+    PrsMarchSmem<TY, true, kBeta> p;
+  } S;
+  __shared__ long long s_item;
+  int* gstatus = reinterpret_cast<int*>(bar + kBarWords);
+  unsigned long long* tickets = reinterpret_cast<unsigned long long*>(bar + kBarWords + 2);
+  unsigned long long base = 0;   // first ticket of the current phase
+  // next item of the phase, or -1 (every thread of the block gets the same answer)
+  auto claim = [&](int items) -> int {
+    __syncthreads();   // the previous item is done with A and s_item
+    if (threadIdx.x == 0) {
+      const unsigned long long t = atomicAdd(tickets, 1ull) - base;
+      s_item = t < (unsigned long long)items ? (long long)t : -1;
+    }
+    __syncthreads();
+    return (int)s_item;
+  };
+  auto phase_end = [&]() -> bool {
+    fence_proxy_async_global();
+    if (!grid_barrier(bar, gstatus, gridDim.x)) {
+      if (blockIdx.x == 0)
+        for (int r = threadIdx.x; r < n_members; r += blockDim.x) atomicOr(sims[r].step + 1, 4);
+      return false;
+    }
+    if (threadIdx.x == 0) fence_proxy_async_global();
+    return true;
+  };
+  for (int n = 0; n < max_nt; ++n) {
+    int k = 0;
+    while (k < n_members && member_nt[k] > n) ++k;
+    const int items = tiles_upto[k];
+    for (int w; (w = claim(items)) >= 0;) {
+      const int4 t = work[w];
+      stage_args(A, sims[t.x]);
+      if (t.w && threadIdx.x == 0) *A.step += 1;
+      vel2d_march_body<TY, XC, CellVelT<2, false>, true, kMapSlotVel, true>(S.v, A, maps + t.x,
+                                                                            t.y, t.z);
+    }
+    base += (unsigned long long)items + gridDim.x;
+    if (!phase_end()) return;
+    for (int w; (w = claim(items)) >= 0;) {
+      const int4 t = work[w];
+      stage_args(A, sims[t.x]);
+      prs2d_march_body<TY, XC, CellPrsT<2, kBeta, false>, true, kBeta, kMapSlotPrs, true>(
+          S.p, A, maps + t.x, t.y, t.z, n);
+    }
+    base += (unsigned long long)items + gridDim.x;
+    if (!phase_end()) return;
+  }
 }
 
 }  // namespace fwgb

@@ -253,7 +253,9 @@ FWGB_API int fw_group_create(fw_handle *const *handles, int32_t n, fw_group **ou
  * read each member's traces with fw_read_traces. The whole run is captured once into one CUDA
  * graph (every step's two launches over the shrinking prefix of active members) and replayed by
  * later runs while the members and the kernel shape stay the same (FWGB_GROUP_RUN_GRAPH=0: blocks
- * of 64-step graphs as fw_group_advance issues them). Errors: fw_last_error(NULL). */
+ * of 64-step graphs as fw_group_advance issues them; FWGB_GROUP_PERSISTENT=1: the whole run as
+ * one persistent cooperative launch with grid barriers between the phases, row-march shapes,
+ * bitwise the same traces). Errors: fw_last_error(NULL). */
 FWGB_API int fw_group_run(fw_group *g, void *stream);
 
 /* Replace the member list (members may be at different steps; continuous batching admits new

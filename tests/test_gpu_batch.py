@@ -132,6 +132,37 @@ def test_group_every_kernel_shape_equals_alone(engine_lib, cuda, instances, shap
         e.close()
 
 
+@pytest.mark.parametrize("shape", [1, 2, 3, 4, 5])
+def test_persistent_group_run_equals_alone(engine_lib, cuda, instances, shape):
+    """FWGB_GROUP_PERSISTENT=1: the whole run of the group as one persistent cooperative launch
+    (grid barriers between the phases, members leaving the work list at their own nt), with a
+    beta/air member mixed in: bitwise equal to solo runs, on a repeated run and after the member
+    set changes."""
+    import os
+
+    from fullwave25_gb300.engine import Engine
+    from golden_io import load_case_inputs
+
+    engines = [d.make_engine() for d in instances[:4]]
+    engines.append(Engine(load_case_inputs("2d_air_beta"), validate=False))
+    alone = [e.run() for e in engines]
+    with _group(engines, FWGB_SHAPE2D=shape) as grp:
+        os.environ["FWGB_GROUP_PERSISTENT"] = "1"
+        try:
+            for _ in range(2):
+                grp.run()
+                for a, t in zip(alone, grp.traces()):
+                    np.testing.assert_array_equal(a, t)
+            grp.set_members(engines[1:3])
+            grp.run()
+            for a, t in zip(alone[1:3], grp.traces()):
+                np.testing.assert_array_equal(a, t)
+        finally:
+            os.environ.pop("FWGB_GROUP_PERSISTENT", None)
+    for e in engines:
+        e.close()
+
+
 def test_group_register_loads_equal_streaming(engine_lib, cuda, instances):
     engines = [d.make_engine() for d in instances[:4]]
     alone = [e.run() for e in engines]
