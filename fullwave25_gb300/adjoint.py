@@ -46,7 +46,9 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
     ``observed``: CUDA float32 tensor ``[n_out, ncoordsout]``. ``stream``: a torch CUDA stream
     (None: the current one); all work is ordered on it and only it is synchronised, so gradient
     evaluations on other streams overlap. Returns ``(J, traces, grads)`` with ``grads[name]`` a
-    float64 CUDA tensor of the grid shape for every name in ``RAW_MAPS``.
+    float64 CUDA tensor of the grid shape for every name in ``RAW_MAPS``, or, for the
+    exponential-attenuation engine (inputs with an ``a_exp`` map), for ``rho``, ``K`` and
+    ``a_exp``.
     """
     torch = _torch()
     inp = engine.inputs
@@ -62,8 +64,14 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
         g = torch.zeros((len(ADJOINT_MAPS),) + tuple(inp.shape), dtype=torch.float64, device=dev)
         engine.adjoint_backward(residual.data_ptr(), g.data_ptr(), raw)
         gm = dict(zip(ADJOINT_MAPS, g))
-        m = {k: inp.maps[k].double() for k in ("rho", "K", "kappau", "kappax")}
         dt = float(np.float32(inp.dt))
+        if "a_exp" in inp.maps:   # exponential engine: a_exp sits in the au1 slot
+            rho = inp.maps["rho"].double()
+            grads = {"rho": gm["rdt_rho"] * (-dt / rho ** 2), "K": gm["dt_k"] * dt,
+                     "a_exp": gm["au1"]}
+            ts.synchronize()
+            return J, traces, grads
+        m = {k: inp.maps[k].double() for k in ("rho", "K", "kappau", "kappax")}
         grads = {
             "rho": gm["rdt_rho"] * (-dt / m["rho"] ** 2),
             "K": gm["dt_k"] * dt,

@@ -110,8 +110,9 @@ extern "C" {
 int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   if (h->has_beta) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs beta = 0 everywhere");
-  if (h->aniso || h->exp)
-    return fail(h, FW_ERR_UNSUPPORTED, "the adjoint covers the isotropic relaxation engine");
+  if (h->aniso)
+    return fail(h, FW_ERR_UNSUPPORTED,
+                "the adjoint covers the isotropic relaxation and exponential-attenuation engines");
   if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called first");
   if (h->args.l.rec_group)   // the misfit is defined on individual sensor traces
     return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs individual sensor traces: clear the sensor groups");
@@ -213,14 +214,16 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   FW_CUDA(h, cudaGetDevice(&dev));
   FW_CUDA(h, cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t smem_prs = adj_prs_tma_smem(h->d.ndmap), smem_vel = adj_vel_tma_smem(h->d.ndmap);
-  const bool tma = h->ndim == 2 && fused && !f64_steps && !(tenv && std::strcmp(tenv, "0") == 0) &&
+  const bool tma = h->ndim == 2 && !h->exp && fused && !f64_steps &&
+                   !(tenv && std::strcmp(tenv, "0") == 0) &&
                    std::max(smem_prs, smem_vel) <= (size_t)smem_optin;
   // Recomputation: out of place from one stored state into the next (the TMA tile step kernels
   // reading slot n and writing slot n + 1), unless pressure is written in the ghost layer (it
   // persists there in place) or FWGB_ADJ_OOP=0: then a copy of the state into the store before
   // each in-place step.
   const char* oenv = std::getenv("FWGB_ADJ_OOP");
-  const bool oop = h->ndim == 2 && !h->ghost_writes && !(oenv && std::strcmp(oenv, "0") == 0);
+  const bool oop = h->ndim == 2 && !h->exp && !h->ghost_writes &&
+                   !(oenv && std::strcmp(oenv, "0") == 0);
   // Overlap (default when a second store exists, with out-of-place recomputation and the TMA
   // reverse step): segment k-1 is recomputed on a second stream into the other store while
   // segment k is reversed on `stream`; events order each store's reuse. Same kernels, same
@@ -352,6 +355,33 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     for (int n = n1 - 1; n >= n0; --n) {
       A.Sn = h->adj_store + state_elems * (n - n0);
       A.Sn1 = h->adj_store + state_elems * (n - n0 + 1);
+      if (h->exp) {   // exponential-attenuation engine, 2D or 3D: thread-load kernels
+        const bool d3 = h->ndim == 3;
+        const dim3 gx = d3 ? grid3 : grid, bx = d3 ? block3 : block;
+        const size_t shm = smem_taps ? sm : 0;
+        if (!first) {
+          if (d3 && smem_taps) adj3d_assemble<true><<<gx, bx, shm, s>>>(A);
+          else if (d3) adj3d_assemble<false><<<gx, bx, 0, s>>>(A);
+          else if (smem_taps) adj2d_assemble<true><<<gx, bx, shm, s>>>(A);
+          else adj2d_assemble<false><<<gx, bx, 0, s>>>(A);
+        }
+        first = false;
+        if (counts[2]) adj2d_io<<<(counts[2] + 255) / 256, 256, 0, s>>>(A, L, residual, n, 0, 0, counts[2]);
+        if (counts[0] || counts[1])
+          adj2d_zero<<<(std::max(counts[0], counts[1]) + 255) / 256, 256, 0, s>>>(A, L, n, counts[0], counts[1]);
+        const int v = (d3 ? 4 : 0) + (f64_steps ? 2 : 0) + (smem_taps ? 1 : 0);
+        switch (v) {
+          case 0: adjx_prs<2, false, false><<<gx, bx, 0, s>>>(A); adjx_vel<2, false, false><<<gx, bx, 0, s>>>(A); break;
+          case 1: adjx_prs<2, false, true><<<gx, bx, shm, s>>>(A); adjx_vel<2, false, true><<<gx, bx, shm, s>>>(A); break;
+          case 2: adjx_prs<2, true, false><<<gx, bx, 0, s>>>(A); adjx_vel<2, true, false><<<gx, bx, 0, s>>>(A); break;
+          case 3: adjx_prs<2, true, true><<<gx, bx, shm, s>>>(A); adjx_vel<2, true, true><<<gx, bx, shm, s>>>(A); break;
+          case 4: adjx_prs<3, false, false><<<gx, bx, 0, s>>>(A); adjx_vel<3, false, false><<<gx, bx, 0, s>>>(A); break;
+          case 5: adjx_prs<3, false, true><<<gx, bx, shm, s>>>(A); adjx_vel<3, false, true><<<gx, bx, shm, s>>>(A); break;
+          case 6: adjx_prs<3, true, false><<<gx, bx, 0, s>>>(A); adjx_vel<3, true, false><<<gx, bx, 0, s>>>(A); break;
+          default: adjx_prs<3, true, true><<<gx, bx, shm, s>>>(A); adjx_vel<3, true, true><<<gx, bx, shm, s>>>(A); break;
+        }
+        continue;
+      }
       if (h->ndim == 3) {
         if (!first) {
           if (smem_taps) adj3d_assemble<true><<<grid3, block3, sm, s>>>(A);

@@ -1,5 +1,6 @@
 // Discrete adjoint of the 3D time step (isotropic relaxation engine, beta = 0): the reverse step
-// of kernels_adjoint2d.cuh with three derivative axes. One thread per body cell (blocks of
+// of kernels_adjoint2d.cuh with three derivative axes; and, at the end, the reverse step of the
+// exponential-attenuation engine in 2D and 3D. One thread per body cell (blocks of
 // 32 (z) x 8 (y) cells of one x plane), operands through the read-only path, the tap table in
 // shared memory when it fits. Per reverse step n, in order:
 //   adj3d_assemble   lam_p += sum_a D_a^T lam_g_a           (lam_g from step n+1)
@@ -167,6 +168,86 @@ static __global__ void __launch_bounds__(256) adj3d_merge(const AdjArgs A) {
     A.grad[q][c] += (double)A.g32[q][c];
     A.g32[q][c] = 0.f;
   }
+}
+
+// ---- exponential-attenuation engine, 2D and 3D -----------------------------------------------
+// Forward step: v'_a = ae (v_a - r D_a p), p' = ae (p - k sum_a D'_a v'_a). Reverse of step n,
+// after adj2d/adj3d_assemble and adj2d_io / adj2d_zero have formed lam_p (= dJ/dp' on the body):
+//   adjx_prs: d = sum_a D'_a v'_a (S_{n+1});  lam_d = -ae k lam_p  (one field, every axis);
+//             gradients dt_k -= ae d lam_p, a_exp += lam_p (p^n - k d);  lam_p <- ae lam_p
+//   adjx_vel: lam_v_a += D'_a^T lam_d;  g_a = D_a p^n;  lam_g_a = -ae r lam_v_a;
+//             gradients rdt_rho -= ae g_a lam_v_a, a_exp += lam_v_a (v_a^n - r g_a);
+//             lam_v_a <- ae lam_v_a
+// The a_exp gradient goes to the au1 slot (the map slot the engine keeps a_exp in).
+
+template <int ND>
+__device__ __forceinline__ bool adjn_cell(const Grid& g, int64_t* c) {
+  if constexpr (ND == 2) return adj_cell(g, c);
+  else return adj3_cell(g, c);
+}
+template <int ND, bool kS>
+__device__ __forceinline__ float divn_at(const Maps& m, const TapSrc<kS>& T, const float* v,
+                                         int64_t c, const Grid& g, int a) {
+  if constexpr (ND == 2) return div_at(m, T, v, c, a == 0 ? g.sx : 1, a == 0 ? 1 : g.sx, g.inv_h[a]);
+  else return div3_at(m, T, v, c, axis3(g, a));
+}
+template <int ND, bool kS>
+__device__ __forceinline__ float gradn_at(const Maps& m, const TapSrc<kS>& T, const float* f,
+                                          int64_t c, const Grid& g, int a) {
+  if constexpr (ND == 2) return grad_at(m, T, f, c, a == 0 ? g.sx : 1, a == 0 ? 1 : g.sx, g.inv_h[a]);
+  else return grad3_at(m, T, f, c, axis3(g, a));
+}
+template <int ND, bool kS>
+__device__ __forceinline__ float divn_T_at(const Maps& m, const TapSrc<kS>& T, const float* u,
+                                           int64_t q, const Grid& g, int a) {
+  if constexpr (ND == 2) return div_T_at(m, T, u, q, a == 0 ? g.sx : 1, a == 0 ? 1 : g.sx, g.inv_h[a]);
+  else return div3_T_at(m, T, u, q, axis3(g, a));
+}
+
+template <bool kF64>
+__device__ __forceinline__ void adj_add_grad(const AdjArgs& A, int q, int64_t c, float v) {
+  if constexpr (kF64) A.grad[q][c] += (double)v;
+  else A.g32[q][c] += v;
+}
+
+template <int ND, bool kF64, bool kS>
+__global__ void __launch_bounds__(256) adjx_prs(const AdjArgs A) {
+  extern __shared__ float s_taps[];
+  const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
+  int64_t c;
+  if (!adjn_cell<ND>(A.g, &c)) return;
+  float d = 0.f;
+#pragma unroll
+  for (int a = 0; a < ND; ++a) d += divn_at<ND>(A.m, T, S_v(A.Sn1, A.fs, a), c, A.g, a);
+  const float lp = A.lam_p[c];
+  const float k = __ldg(A.m.dt_k + c), ae = __ldg(A.m.a_exp + c);
+  const float pn = __ldg(S_p(A.Sn, A.fs) + c);
+  A.lam_d[0][c] = -ae * k * lp;
+  A.lam_p[c] = ae * lp;
+  adj_add_grad<kF64>(A, kGDtK, c, -(ae * d * lp));
+  adj_add_grad<kF64>(A, kGAu1, c, lp * (pn - k * d));
+}
+
+template <int ND, bool kF64, bool kS>
+__global__ void __launch_bounds__(256) adjx_vel(const AdjArgs A) {
+  extern __shared__ float s_taps[];
+  const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
+  int64_t c;
+  if (!adjn_cell<ND>(A.g, &c)) return;
+  const float r = __ldg(A.m.rdt_rho + c), ae = __ldg(A.m.a_exp + c);
+  float g_r = 0.f, g_ae = 0.f;
+#pragma unroll
+  for (int a = 0; a < ND; ++a) {
+    const float lv = A.lam_v[a][c] + divn_T_at<ND>(A.m, T, A.lam_d[0], c, A.g, a);
+    const float g = gradn_at<ND>(A.m, T, S_p(A.Sn, A.fs), c, A.g, a);
+    const float vn = __ldg(S_v(A.Sn, A.fs, a) + c);
+    A.lam_g[a][c] = -ae * r * lv;
+    A.lam_v[a][c] = ae * lv;
+    g_r -= ae * g * lv;
+    g_ae += lv * (vn - r * g);
+  }
+  adj_add_grad<kF64>(A, kGRdtRho, c, g_r);
+  adj_add_grad<kF64>(A, kGAu1, c, g_ae);
 }
 
 }  // namespace fwgb

@@ -22,6 +22,16 @@ Reverse of step n (state S_n before it, S_{n+1} after it):
                grads: rdt_rho -= lam_v_a (iku g_a + psi_1' + psi_2');  inv_ku -= r g_a lam_v_a;
                       au_nu += M_nu g_a;  bu_nu += M_nu psi_nu(S_n)
   pressure at step start: lam_p += sum_a D_a^T lam_g_a
+
+Exponential-attenuation engine (maps ``rdt_rho``, ``dt_k``, ``a_exp``; forward
+``v' = ae (v - r D_a p)``, ``p' = ae (p - k sum_a D'_a v'_a)``), reverse of step n:
+  record, air, source as above
+  pressure:    d = sum_a D'_a v'_a (S_{n+1});  lam_d = -ae k lam_p
+               grads: dt_k -= ae d lam_p;  a_exp += lam_p (p^n - k d);  lam_p <- ae lam_p
+  velocity:    lam_v_a += D'_a^T lam_d;  g_a = D_a p^n;  lam_g_a = -ae r lam_v_a
+               grads: rdt_rho -= ae g_a lam_v_a;  a_exp += lam_v_a (v_a^n - r g_a);
+               lam_v_a <- ae lam_v_a
+  pressure at step start: lam_p += sum_a D_a^T lam_g_a
 """
 
 from __future__ import annotations
@@ -34,6 +44,7 @@ from fdtd_oracle import GHOST, Oracle, _body, _unit
 
 GRAD_KEYS = ("rdt_rho", "dt_k", "inv_ku", "inv_kx", "au1", "bu1", "au2", "bu2",
              "ax1", "bx1", "ax2", "bx2")
+EXP_GRAD_KEYS = ("rdt_rho", "dt_k", "a_exp")   # exponential-attenuation engine
 
 
 class AdjointOracle(Oracle):
@@ -95,8 +106,55 @@ class AdjointOracle(Oracle):
         states.append(copy.deepcopy(self.state))
         return out, states
 
+    def _io_adjoint(self, lam_p, residual, n):
+        """Record adjoint, air and source projections of step n on lam_p (in place)."""
+        flat = lam_p.reshape(-1)
+        if n % self.inp.mod_t == 0:
+            np.add.at(flat, self.outc, residual[n // self.inp.mod_t])
+        if self.icczero.size:
+            flat[self.icczero] = 0.0
+        if n < self.icmat.shape[1] and self.src_keep.size:
+            flat[self.icc[self.src_keep]] = 0.0
+
+    def adjoint_exponential(self, residual, states):
+        """Reverse pass of the exponential-attenuation engine: FP64 body gradients with respect
+        to ``rdt_rho``, ``dt_k`` and ``a_exp``."""
+        nd, body = self.nd, _body(self.shape)
+        bshape = tuple(k - 2 * GHOST for k in self.shape)
+        G = {k: np.zeros(bshape) for k in EXP_GRAD_KEYS}
+        lam_p = np.zeros(self.shape)
+        lam_v = [np.zeros(bshape) for _ in range(nd)]
+        lam_g = None
+        k, r, ae = self.dt_k, self.rdt_rho, self.a_exp
+        for n in range(self.inp.nt - 1, -1, -1):
+            Sn, Sn1 = states[n], states[n + 1]
+            if lam_g is not None:
+                for a in range(nd):
+                    lam_p += self.grad_T(lam_g[a], a)
+            self._io_adjoint(lam_p, residual, n)
+            lp = lam_p[body].copy()
+            d = np.zeros(bshape)
+            for a in range(nd):
+                d += self.div_component(Sn1.v[a], a)
+            lam_d = -ae * k * lp
+            G["dt_k"] -= ae * d * lp
+            G["a_exp"] += lp * (Sn.p[body] - k * d)
+            lam_p[body] = ae * lp
+            lam_g = []
+            for a in range(nd):
+                lv = lam_v[a] + self.div_T(lam_d, a)[body]
+                g = self.grad(Sn.p, a)
+                lam_g.append(-ae * r * lv)
+                G["rdt_rho"] -= ae * g * lv
+                G["a_exp"] += lv * (Sn.v[a][body] - r * g)
+                lam_v[a] = ae * lv
+        return G
+
     def adjoint(self, residual, states):
-        """Reverse pass; ``residual`` [n_out, ncoordsout]. Returns dict of FP64 body gradients."""
+        """Reverse pass; ``residual`` [n_out, ncoordsout]. Returns dict of FP64 body gradients
+        (``GRAD_KEYS``; ``EXP_GRAD_KEYS`` for the exponential-attenuation engine)."""
+        if self.a_exp is not None:
+            return self.adjoint_exponential(residual, states)
         nd, body = self.nd, _body(self.shape)
         bshape = tuple(k - 2 * GHOST for k in self.shape)
         G = {k: np.zeros(bshape) for k in GRAD_KEYS}
@@ -112,13 +170,7 @@ class AdjointOracle(Oracle):
             if lam_g is not None:
                 for a in range(nd):
                     lam_p += self.grad_T(lam_g[a], a)
-            flat = lam_p.reshape(-1)
-            if n % self.inp.mod_t == 0:
-                np.add.at(flat, self.outc, residual[n // self.inp.mod_t])
-            if self.icczero.size:
-                flat[self.icczero] = 0.0
-            if n < self.icmat.shape[1] and self.src_keep.size:
-                flat[self.icc[self.src_keep]] = 0.0
+            self._io_adjoint(lam_p, residual, n)
             lp = lam_p[body]
             # pressure step
             d = [self.div_component(Sn1.v[a], a) for a in range(nd)]
@@ -167,7 +219,7 @@ def misfit(inputs, observed, maps_override=None):
     if maps_override:
         for key, val in maps_override.items():
             attr = {"rdt_rho": "rdt_rho", "dt_k": "dt_k", "inv_ku": "inv_kappa_u",
-                    "inv_kx": "inv_kappa_x"}.get(key)
+                    "inv_kx": "inv_kappa_x", "a_exp": "a_exp"}.get(key)
             if attr:
                 setattr(o, attr, val)
             else:

@@ -3,7 +3,7 @@
 import numpy as np
 import pytest
 
-from fdtd_adjoint import GRAD_KEYS, AdjointOracle, misfit, misfit_and_gradient
+from fdtd_adjoint import EXP_GRAD_KEYS, GRAD_KEYS, AdjointOracle, misfit, misfit_and_gradient
 from fdtd_oracle import GHOST, Oracle
 from golden_io import load_case_inputs
 
@@ -63,3 +63,38 @@ def test_gradient_is_nonzero_and_finite(case):
     for k in GRAD_KEYS:
         assert np.isfinite(G[k]).all()
     assert np.abs(G["dt_k"]).max() > 0 and np.abs(G["rdt_rho"]).max() > 0
+
+
+@pytest.fixture(scope="module")
+def exp_case():
+    inp = _small("2d_exp", 70)
+    obs_inp = _small("2d_exp", 70)
+    obs_inp.maps = dict(obs_inp.maps)
+    obs_inp.maps["K"] = (obs_inp.maps["K"] * np.float32(1.02)).astype(np.float32)
+    observed = Oracle(obs_inp).run()
+    J, G, traces = misfit_and_gradient(inp, observed)
+    return inp, observed, J, G
+
+
+@pytest.mark.parametrize("key", EXP_GRAD_KEYS)
+def test_exponential_gradient_matches_central_differences(exp_case, key):
+    """The exponential-attenuation engine's adjoint (gradients with respect to dt/rho, dt*K and
+    a_exp) against central differences of the FP64 oracle, same bounds as above."""
+    inp, observed, J, G = exp_case
+    o = Oracle(inp)
+    base = getattr(o, key)
+    assert np.isfinite(G[key]).all() and np.abs(G[key]).max() > 0
+    rng = np.random.default_rng(sum(map(ord, key)))
+    cells = [(int(rng.integers(2, base.shape[0] - 2)), int(rng.integers(2, base.shape[1] - 2)))
+             for _ in range(3)]
+    for c in cells:
+        mag = abs(base[c]) if base[c] != 0 else float(np.abs(base).mean())
+        h = 1e-4 * mag
+        plus, minus = base.copy(), base.copy()
+        plus[c] += h
+        minus[c] -= h
+        fd = (misfit(inp, observed, {key: plus}) - misfit(inp, observed, {key: minus})) / (2 * h)
+        ad = G[key][c]
+        floor = 1e-10 * abs(J) / mag
+        assert abs(fd - ad) <= 1e-5 * max(abs(fd), abs(ad)) + floor, \
+            f"{key} at {c}: adjoint {ad:.6e} vs finite difference {fd:.6e}"
