@@ -24,7 +24,7 @@ import dataclasses
 import numpy as np
 
 from . import coefficients
-from .engine import ADJOINT_MAPS, Engine
+from .engine import Engine, adjoint_gradient_maps
 from .grid import Grid
 from .medium import relaxation_param_keys
 from .relaxation import default_table
@@ -46,9 +46,10 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
     ``observed``: CUDA float32 tensor ``[n_out, ncoordsout]``. ``stream``: a torch CUDA stream
     (None: the current one); all work is ordered on it and only it is synchronised, so gradient
     evaluations on other streams overlap. Returns ``(J, traces, grads)`` with ``grads[name]`` a
-    float64 CUDA tensor of the grid shape for every name in ``RAW_MAPS``, or, for the
-    exponential-attenuation engine (inputs with an ``a_exp`` map), for ``rho``, ``K`` and
-    ``a_exp``.
+    float64 CUDA tensor of the grid shape for every name in ``RAW_MAPS``; for the
+    exponential-attenuation engine (inputs with an ``a_exp`` map) for ``rho``, ``K`` and
+    ``a_exp``; for the anisotropic engine for ``rho``, ``K`` and every per-direction map
+    (``kappa{u,w,v,x,y,z}``, ``apml*``, ``bpml*``).
     """
     torch = _torch()
     inp = engine.inputs
@@ -61,10 +62,22 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
         engine.read_traces_into(0, inp.n_out, traces.data_ptr(), raw)
         residual = (traces - observed).contiguous()
         J = 0.5 * float(torch.sum(residual.double() ** 2))
-        g = torch.zeros((len(ADJOINT_MAPS),) + tuple(inp.shape), dtype=torch.float64, device=dev)
+        names = adjoint_gradient_maps(inp)
+        g = torch.zeros((len(names),) + tuple(inp.shape), dtype=torch.float64, device=dev)
         engine.adjoint_backward(residual.data_ptr(), g.data_ptr(), raw)
-        gm = dict(zip(ADJOINT_MAPS, g))
+        gm = dict(zip(names, g))
         dt = float(np.float32(inp.dt))
+        if "kappay" in inp.maps:   # anisotropic engine: per-direction map sets
+            rho = inp.maps["rho"].double()
+            grads = {"rho": gm["rdt_rho"] * (-dt / rho ** 2), "K": gm["dt_k"] * dt}
+            for n in names[2:]:
+                if n.startswith("inv_k"):
+                    kap = inp.maps[f"kappa{n[5]}"].double()
+                    grads[f"kappa{n[5]}"] = gm[n] * (-1.0 / kap ** 2)
+                else:
+                    grads[f"{n[0]}pml{n[1:]}"] = gm[n]
+            ts.synchronize()
+            return J, traces, grads
         if "a_exp" in inp.maps:   # exponential engine: a_exp sits in the au1 slot
             rho = inp.maps["rho"].double()
             grads = {"rho": gm["rdt_rho"] * (-dt / rho ** 2), "K": gm["dt_k"] * dt,

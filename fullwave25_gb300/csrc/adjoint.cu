@@ -7,14 +7,18 @@ using namespace fwgbh;
 
 namespace {
 
+// Gradient maps of a handle: 12 (isotropic relaxation and exponential engines: the AdjGrad
+// order), or 2 + 10 ND (anisotropic engine: one relaxation map set per derivative axis).
+int n_grad_maps(const fw_handle* h) { return h->aniso ? 2 + 10 * h->ndim : kNumGrad; }
+
 // Adjoint-field allocation of an ND handle, per padded cell array: lam_p, lam_v (ND),
 // lam_psi (2 ND), lam_phi (2 ND), lam_d (ND), lam_g (ND), then the FP32 gradient partials.
 // In 2D this is the layout the TMA reverse-step kernels address by constant field indices.
 struct AdjLayout {
   int lam_v, lam_psi, lam_phi, lam_d, lam_g, fields, stack;
-  explicit AdjLayout(int nd)
+  AdjLayout(int nd, int n_grad)
       : lam_v(1), lam_psi(1 + nd), lam_phi(1 + 3 * nd), lam_d(1 + 5 * nd), lam_g(1 + 6 * nd),
-        fields(1 + 7 * nd), stack(1 + 7 * nd + kNumGrad) {}
+        fields(1 + 7 * nd), stack(1 + 7 * nd + n_grad) {}
 };
 static_assert(1 + 2 == kAdjLamPsi && 1 + 6 == kAdjLamPhi && 1 + 10 == kAdjLamD &&
                   1 + 12 == kAdjLamG && 1 + 14 == kAdjFields,
@@ -78,13 +82,13 @@ int prepare_adjoint_kernels(fw_handle* h, int dev, int smem_optin) {
   return FW_OK;
 }
 
-// The FP64 gradient sums of the 12 coefficient maps into the caller's dense
-// [12][nx][ny] (2D) or [12][nx][ny][nz] (3D) buffer: rows of the last axis, unpadded.
+// The FP64 gradient sums of the coefficient maps into the caller's dense
+// [n][nx][ny] (2D) or [n][nx][ny][nz] (3D) buffer: rows of the last axis, unpadded.
 int copy_gradients(fw_handle* h, const AdjArgs& A, double* grad_out, cudaStream_t s) {
   if (!grad_out) return FW_OK;
   const size_t width = h->ndim == 3 ? (size_t)h->nz : (size_t)h->ny;
   const size_t rows = h->ndim == 3 ? (size_t)h->nx * h->ny : (size_t)h->nx;
-  for (int q = 0; q < kNumGrad; ++q)
+  for (int q = 0; q < A.n_grad; ++q)
     FW_CUDA(h, cudaMemcpy2DAsync(grad_out + (size_t)q * rows * width, width * sizeof(double),
                                  A.grad[q], h->pitch * sizeof(double), width * sizeof(double),
                                  rows, cudaMemcpyDeviceToDevice, s));
@@ -110,9 +114,6 @@ extern "C" {
 int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   if (h->has_beta) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs beta = 0 everywhere");
-  if (h->aniso)
-    return fail(h, FW_ERR_UNSUPPORTED,
-                "the adjoint covers the isotropic relaxation and exponential-attenuation engines");
   if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called first");
   if (h->args.l.rec_group)   // the misfit is defined on individual sensor traces
     return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs individual sensor traces: clear the sensor groups");
@@ -124,8 +125,9 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
     const size_t b_ckpt = state_elems * std::max(nckpt, 1) * sizeof(float);
     const size_t b_store = state_elems * (checkpoint_every + 1) * sizeof(float);
     // adjoint fields and temporaries (15 in 2D, 22 in 3D), then the FP32 segment partials
-    const size_t b_lam = (size_t)h->ncells_padded * AdjLayout(h->ndim).stack * sizeof(float);
-    const size_t b_grad = (size_t)h->ncells_padded * kNumGrad * sizeof(double);
+    const size_t b_lam = (size_t)h->ncells_padded * AdjLayout(h->ndim, n_grad_maps(h)).stack *
+                         sizeof(float);
+    const size_t b_grad = (size_t)h->ncells_padded * n_grad_maps(h) * sizeof(double);
     // FWGB_ADJ_OVERLAP=0: one state store, segments recomputed and reversed one after another
     // (always so in 3D, whose recomputation runs in place on the handle's own state)
     const char* ov = std::getenv("FWGB_ADJ_OVERLAP");
@@ -171,9 +173,10 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const int64_t fs = h->ncells_padded;
   const size_t state_elems = (size_t)fs * n_state(h->ndim);
-  const AdjLayout lay(h->ndim);
+  const int n_grad = n_grad_maps(h);
+  const AdjLayout lay(h->ndim, n_grad);
   FW_CUDA(h, cudaMemsetAsync(h->adj_lam, 0, (size_t)fs * lay.stack * sizeof(float), s));
-  FW_CUDA(h, cudaMemsetAsync(h->adj_grad, 0, (size_t)fs * kNumGrad * sizeof(double), s));
+  FW_CUDA(h, cudaMemsetAsync(h->adj_grad, 0, (size_t)fs * n_grad * sizeof(double), s));
   AdjArgs A{};
   A.g = h->args.g;
   A.m = h->args.m;
@@ -188,9 +191,10 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     A.lam_d[a] = h->adj_lam + (lay.lam_d + a) * fs;
     A.lam_g[a] = h->adj_lam + (lay.lam_g + a) * fs;
   }
-  for (int q = 0; q < kNumGrad; ++q) {
+  A.n_grad = n_grad;
+  for (int q = 0; q < n_grad; ++q) {
     A.grad[q] = h->adj_grad + (size_t)q * fs;
-    A.g32[q] = h->adj_lam + (size_t)(lay.fields + kGradSlot[q]) * fs;
+    A.g32[q] = h->adj_lam + (size_t)(lay.fields + (h->aniso ? q : kGradSlot[q])) * fs;
   }
   A.ndmap = h->d.ndmap;
   A.status = h->step + 1;
@@ -214,7 +218,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   FW_CUDA(h, cudaGetDevice(&dev));
   FW_CUDA(h, cudaDeviceGetAttribute(&smem_optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
   const size_t smem_prs = adj_prs_tma_smem(h->d.ndmap), smem_vel = adj_vel_tma_smem(h->d.ndmap);
-  const bool tma = h->ndim == 2 && !h->exp && fused && !f64_steps &&
+  const bool tma = h->ndim == 2 && !h->exp && !h->aniso && fused && !f64_steps &&
                    !(tenv && std::strcmp(tenv, "0") == 0) &&
                    std::max(smem_prs, smem_vel) <= (size_t)smem_optin;
   // Recomputation: out of place from one stored state into the next (the TMA tile step kernels
@@ -222,7 +226,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   // persists there in place) or FWGB_ADJ_OOP=0: then a copy of the state into the store before
   // each in-place step.
   const char* oenv = std::getenv("FWGB_ADJ_OOP");
-  const bool oop = h->ndim == 2 && !h->exp && !h->ghost_writes &&
+  const bool oop = h->ndim == 2 && !h->exp && !h->aniso && !h->ghost_writes &&
                    !(oenv && std::strcmp(oenv, "0") == 0);
   // Overlap (default when a second store exists, with out-of-place recomputation and the TMA
   // reverse step): segment k-1 is recomputed on a second stream into the other store while
@@ -355,7 +359,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     for (int n = n1 - 1; n >= n0; --n) {
       A.Sn = h->adj_store + state_elems * (n - n0);
       A.Sn1 = h->adj_store + state_elems * (n - n0 + 1);
-      if (h->exp) {   // exponential-attenuation engine, 2D or 3D: thread-load kernels
+      if (h->exp || h->aniso) {   // exponential or anisotropic engine, 2D or 3D: thread loads
         const bool d3 = h->ndim == 3;
         const dim3 gx = d3 ? grid3 : grid, bx = d3 ? block3 : block;
         const size_t shm = smem_taps ? sm : 0;
@@ -370,6 +374,19 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
         if (counts[0] || counts[1])
           adj2d_zero<<<(std::max(counts[0], counts[1]) + 255) / 256, 256, 0, s>>>(A, L, n, counts[0], counts[1]);
         const int v = (d3 ? 4 : 0) + (f64_steps ? 2 : 0) + (smem_taps ? 1 : 0);
+        if (h->aniso) {
+          switch (v) {
+            case 0: adja_prs<2, false, false><<<gx, bx, 0, s>>>(A); adja_vel<2, false, false><<<gx, bx, 0, s>>>(A); break;
+            case 1: adja_prs<2, false, true><<<gx, bx, shm, s>>>(A); adja_vel<2, false, true><<<gx, bx, shm, s>>>(A); break;
+            case 2: adja_prs<2, true, false><<<gx, bx, 0, s>>>(A); adja_vel<2, true, false><<<gx, bx, 0, s>>>(A); break;
+            case 3: adja_prs<2, true, true><<<gx, bx, shm, s>>>(A); adja_vel<2, true, true><<<gx, bx, shm, s>>>(A); break;
+            case 4: adja_prs<3, false, false><<<gx, bx, 0, s>>>(A); adja_vel<3, false, false><<<gx, bx, 0, s>>>(A); break;
+            case 5: adja_prs<3, false, true><<<gx, bx, shm, s>>>(A); adja_vel<3, false, true><<<gx, bx, shm, s>>>(A); break;
+            case 6: adja_prs<3, true, false><<<gx, bx, 0, s>>>(A); adja_vel<3, true, false><<<gx, bx, 0, s>>>(A); break;
+            default: adja_prs<3, true, true><<<gx, bx, shm, s>>>(A); adja_vel<3, true, true><<<gx, bx, shm, s>>>(A); break;
+          }
+          continue;
+        }
         switch (v) {
           case 0: adjx_prs<2, false, false><<<gx, bx, 0, s>>>(A); adjx_vel<2, false, false><<<gx, bx, 0, s>>>(A); break;
           case 1: adjx_prs<2, false, true><<<gx, bx, shm, s>>>(A); adjx_vel<2, false, true><<<gx, bx, shm, s>>>(A); break;

@@ -23,6 +23,10 @@ enum AdjGrad {
   kGRdtRho = 0, kGDtK, kGInvKu, kGInvKx, kGAu1, kGBu1, kGAu2, kGBu2, kGAx1, kGBx1, kGAx2, kGBx2,
   kNumGrad
 };
+// The anisotropic engine has one map set per derivative axis: 2 + 10 ND gradient maps (dt/rho,
+// dt*K, then per axis 1/kappa, a1, b1, a2, b2 of the pressure-gradient maps, then the same of the
+// velocity-divergence maps), at most 32 in 3D.
+constexpr int kMaxGrad = 32;
 
 struct AdjArgs {
   Grid g;
@@ -37,8 +41,9 @@ struct AdjArgs {
   float* lam_d[3];
   float* lam_g[3];
   int ndmap;                 // tap sets in m.taps
-  double* grad[kNumGrad];    // FP64 time sums
-  float* g32[kNumGrad];      // FP32 partial sums of the current segment (segmented mode)
+  double* grad[kMaxGrad];    // FP64 time sums (kNumGrad maps; anisotropic engine: 2 + 10 ND)
+  float* g32[kMaxGrad];      // FP32 partial sums of the current segment (segmented mode)
+  int n_grad;                // gradient maps in use
   int* status;               // device status word (bounded waits, alignment)
 };
 
@@ -486,8 +491,7 @@ __global__ void __launch_bounds__(256) adj2d_vel_tiled(const AdjArgs A) {
 static __global__ void __launch_bounds__(256) adj2d_merge(const AdjArgs A) {
   int64_t c;
   if (!adj_cell(A.g, &c)) return;
-#pragma unroll
-  for (int q = 0; q < kNumGrad; ++q) {
+  for (int q = 0; q < A.n_grad; ++q) {
     A.grad[q][c] += (double)A.g32[q][c];
     A.g32[q][c] = 0.f;
   }

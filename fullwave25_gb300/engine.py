@@ -53,9 +53,25 @@ class FwFields(C.Structure):
                 ("on_device", C.c_int32)]
 
 
-# order of the gradient arrays returned by fw_adjoint_backward
+# order of the gradient arrays returned by fw_adjoint_backward (isotropic relaxation engine; the
+# exponential engine fills dt/rho, dt*K and a_exp in the au1 slot)
 ADJOINT_MAPS = ("rdt_rho", "dt_k", "inv_ku", "inv_kx", "au1", "bu1", "au2", "bu2",
                 "ax1", "bx1", "ax2", "bx2")
+
+
+def adjoint_gradient_maps(inputs) -> tuple:
+    """Engine-map names of ``fw_adjoint_backward``'s gradient arrays, in output order:
+    ``ADJOINT_MAPS`` (12), or for the anisotropic engine 2 + 10 ndim: dt/rho, dt*K, then per
+    derivative axis 1/kappa, a1, b1, a2, b2 of the pressure-gradient maps (u, w, v), then the
+    same of the velocity-divergence maps (x, y, z)."""
+    if "kappay" not in inputs.maps:
+        return ADJOINT_MAPS
+    names = ["rdt_rho", "dt_k"]
+    for letters in ("uwv", "xyz"):
+        for a in range(len(inputs.shape)):
+            g = letters[a]
+            names += [f"inv_k{g}", f"a{g}1", f"b{g}1", f"a{g}2", f"b{g}2"]
+    return tuple(names)
 
 
 ANISO_FIELDS = tuple(f"{k}{ax}{nu}" if k != "kappa" else f"kappa{ax}"
@@ -330,7 +346,7 @@ class Engine:
 
     def adjoint_backward(self, residual_ptr: int, grad_ptr: int, stream: int | None = None) -> None:
         """``residual_ptr``: device float32 [n_out, ncoordsout]; ``grad_ptr``: device float64
-        [12, *shape] (order of ``ADJOINT_MAPS``)."""
+        [n, *shape], n and order as ``adjoint_gradient_maps(inputs)``."""
         self._call("fw_adjoint_backward", C.c_void_p(stream or 0),
                    C.cast(C.c_void_p(residual_ptr), _FP),
                    C.cast(C.c_void_p(grad_ptr), C.POINTER(C.c_double)))

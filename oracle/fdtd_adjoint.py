@@ -45,6 +45,19 @@ from fdtd_oracle import GHOST, Oracle, _body, _unit
 GRAD_KEYS = ("rdt_rho", "dt_k", "inv_ku", "inv_kx", "au1", "bu1", "au2", "bu2",
              "ax1", "bx1", "ax2", "bx2")
 EXP_GRAD_KEYS = ("rdt_rho", "dt_k", "a_exp")   # exponential-attenuation engine
+GRAD_LETTERS = ("uwv", "xyz")   # per-axis map letters: pressure gradient, velocity divergence
+
+
+def aniso_grad_keys(nd):
+    """Gradient keys of the anisotropic engine: dt/rho, dt*K, then per derivative axis the five
+    pressure-gradient maps (1/kappa, a1, b1, a2, b2 of u / w / v), then per axis the five
+    velocity-divergence maps (of x / y / z) -- the order of the engine's gradient output."""
+    keys = ["rdt_rho", "dt_k"]
+    for letters in GRAD_LETTERS:
+        for a in range(nd):
+            g = letters[a]
+            keys += [f"inv_k{g}", f"a{g}1", f"b{g}1", f"a{g}2", f"b{g}2"]
+    return tuple(keys)
 
 
 class AdjointOracle(Oracle):
@@ -152,19 +165,25 @@ class AdjointOracle(Oracle):
 
     def adjoint(self, residual, states):
         """Reverse pass; ``residual`` [n_out, ncoordsout]. Returns dict of FP64 body gradients
-        (``GRAD_KEYS``; ``EXP_GRAD_KEYS`` for the exponential-attenuation engine)."""
+        (``GRAD_KEYS``; ``EXP_GRAD_KEYS`` for the exponential-attenuation engine,
+        ``aniso_grad_keys(nd)`` for the anisotropic one, whose maps differ per axis)."""
         if self.a_exp is not None:
             return self.adjoint_exponential(residual, states)
         nd, body = self.nd, _body(self.shape)
         bshape = tuple(k - 2 * GHOST for k in self.shape)
-        G = {k: np.zeros(bshape) for k in GRAD_KEYS}
+        aniso = self.axis_u[0] is not None
+        G = {k: np.zeros(bshape) for k in (aniso_grad_keys(nd) if aniso else GRAD_KEYS)}
+        # per derivative axis: (1/kappa, (a1, a2), (b1, b2)) and the map letter of the keys
+        U = [self.axis_u[a] or (self.inv_kappa_u, self.au, self.bu) for a in range(nd)]
+        X = [self.axis_x[a] or (self.inv_kappa_x, self.ax, self.bx) for a in range(nd)]
+        gu = [GRAD_LETTERS[0][a] if aniso else "u" for a in range(nd)]
+        gx = [GRAD_LETTERS[1][a] if aniso else "x" for a in range(nd)]
         lam_p = np.zeros(self.shape)
         lam_v = [np.zeros(bshape) for _ in range(nd)]
         lam_psi = [[np.zeros(bshape), np.zeros(bshape)] for _ in range(nd)]
         lam_phi = [[np.zeros(bshape), np.zeros(bshape)] for _ in range(nd)]
         lam_g = None
         k, r = self.dt_k, self.rdt_rho
-        ikx, iku = self.inv_kappa_x, self.inv_kappa_u
         for n in range(self.inp.nt - 1, -1, -1):
             Sn, Sn1 = states[n], states[n + 1]
             if lam_g is not None:
@@ -176,30 +195,32 @@ class AdjointOracle(Oracle):
             d = [self.div_component(Sn1.v[a], a) for a in range(nd)]
             div = np.zeros(bshape)
             for a in range(nd):
-                div += d[a] * ikx + Sn1.phi[a][0][body] + Sn1.phi[a][1][body]
+                div += d[a] * X[a][0] + Sn1.phi[a][0][body] + Sn1.phi[a][1][body]
             G["dt_k"] -= div * lp
             lam_d = []
             for a in range(nd):
+                ikx, ax, bx = X[a]
                 L = [lam_phi[a][nu] - k * lp for nu in range(2)]
-                lam_d.append(self.ax[0] * L[0] + self.ax[1] * L[1] - k * ikx * lp)
-                G["inv_kx"] -= k * lp * d[a]
+                lam_d.append(ax[0] * L[0] + ax[1] * L[1] - k * ikx * lp)
+                G[f"inv_k{gx[a]}"] -= k * lp * d[a]
                 for nu in range(2):
-                    G[f"ax{nu + 1}"] += L[nu] * d[a]
-                    G[f"bx{nu + 1}"] += L[nu] * Sn.phi[a][nu][body]
-                    lam_phi[a][nu] = self.bx[nu] * L[nu]
+                    G[f"a{gx[a]}{nu + 1}"] += L[nu] * d[a]
+                    G[f"b{gx[a]}{nu + 1}"] += L[nu] * Sn.phi[a][nu][body]
+                    lam_phi[a][nu] = bx[nu] * L[nu]
             # velocity step
             lam_g = []
             for a in range(nd):
+                iku, au, bu = U[a]
                 lv = lam_v[a] + self.div_T(lam_d[a], a)[body]
                 g = self.grad(Sn.p, a)
                 M = [lam_psi[a][nu] - r * lv for nu in range(2)]
-                lam_g.append(self.au[0] * M[0] + self.au[1] * M[1] - r * iku * lv)
+                lam_g.append(au[0] * M[0] + au[1] * M[1] - r * iku * lv)
                 G["rdt_rho"] -= lv * (iku * g + Sn1.psi[a][0][body] + Sn1.psi[a][1][body])
-                G["inv_ku"] -= r * g * lv
+                G[f"inv_k{gu[a]}"] -= r * g * lv
                 for nu in range(2):
-                    G[f"au{nu + 1}"] += M[nu] * g
-                    G[f"bu{nu + 1}"] += M[nu] * Sn.psi[a][nu][body]
-                    lam_psi[a][nu] = self.bu[nu] * M[nu]
+                    G[f"a{gu[a]}{nu + 1}"] += M[nu] * g
+                    G[f"b{gu[a]}{nu + 1}"] += M[nu] * Sn.psi[a][nu][body]
+                    lam_psi[a][nu] = bu[nu] * M[nu]
                 lam_v[a] = lv
         return G
 
@@ -218,8 +239,22 @@ def misfit(inputs, observed, maps_override=None):
     o = Oracle(inputs)
     if maps_override:
         for key, val in maps_override.items():
-            attr = {"rdt_rho": "rdt_rho", "dt_k": "dt_k", "inv_ku": "inv_kappa_u",
-                    "inv_kx": "inv_kappa_x", "a_exp": "a_exp"}.get(key)
+            attr = {"rdt_rho": "rdt_rho", "dt_k": "dt_k", "a_exp": "a_exp"}.get(key)
+            if o.axis_u[0] is not None and not attr:   # anisotropic: per-axis map sets
+                letter = key[5] if key.startswith("inv_k") else key[1]
+                side = 0 if letter in GRAD_LETTERS[0] else 1
+                a = GRAD_LETTERS[side].index(letter)
+                axes = o.axis_u if side == 0 else o.axis_x
+                ik, aa, bb = axes[a]
+                if key.startswith("inv_k"):
+                    ik = val
+                else:
+                    pair = list(aa if key[0] == "a" else bb)
+                    pair[int(key[2]) - 1] = val
+                    aa, bb = (tuple(pair), bb) if key[0] == "a" else (aa, tuple(pair))
+                axes[a] = (ik, aa, bb)
+                continue
+            attr = attr or {"inv_ku": "inv_kappa_u", "inv_kx": "inv_kappa_x"}.get(key)
             if attr:
                 setattr(o, attr, val)
             else:

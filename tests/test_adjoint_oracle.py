@@ -3,7 +3,8 @@
 import numpy as np
 import pytest
 
-from fdtd_adjoint import EXP_GRAD_KEYS, GRAD_KEYS, AdjointOracle, misfit, misfit_and_gradient
+from fdtd_adjoint import (EXP_GRAD_KEYS, GRAD_KEYS, GRAD_LETTERS, AdjointOracle, aniso_grad_keys,
+                          misfit, misfit_and_gradient)
 from fdtd_oracle import GHOST, Oracle
 from golden_io import load_case_inputs
 
@@ -87,6 +88,51 @@ def test_exponential_gradient_matches_central_differences(exp_case, key):
     rng = np.random.default_rng(sum(map(ord, key)))
     cells = [(int(rng.integers(2, base.shape[0] - 2)), int(rng.integers(2, base.shape[1] - 2)))
              for _ in range(3)]
+    for c in cells:
+        mag = abs(base[c]) if base[c] != 0 else float(np.abs(base).mean())
+        h = 1e-4 * mag
+        plus, minus = base.copy(), base.copy()
+        plus[c] += h
+        minus[c] -= h
+        fd = (misfit(inp, observed, {key: plus}) - misfit(inp, observed, {key: minus})) / (2 * h)
+        ad = G[key][c]
+        floor = 1e-10 * abs(J) / mag
+        assert abs(fd - ad) <= 1e-5 * max(abs(fd), abs(ad)) + floor, \
+            f"{key} at {c}: adjoint {ad:.6e} vs finite difference {fd:.6e}"
+
+
+@pytest.fixture(scope="module")
+def aniso_case():
+    inp = _small("2d_aniso", 70)
+    obs_inp = _small("2d_aniso", 70)
+    obs_inp.maps = dict(obs_inp.maps)
+    obs_inp.maps["K"] = (obs_inp.maps["K"] * np.float32(1.02)).astype(np.float32)
+    observed = Oracle(obs_inp).run()
+    J, G, traces = misfit_and_gradient(inp, observed)
+    return inp, observed, J, G
+
+
+def _aniso_base(o, key):
+    if key in ("rdt_rho", "dt_k"):
+        return getattr(o, key)
+    letter = key[5] if key.startswith("inv_k") else key[1]
+    side = 0 if letter in GRAD_LETTERS[0] else 1
+    ik, aa, bb = (o.axis_u if side == 0 else o.axis_x)[GRAD_LETTERS[side].index(letter)]
+    if key.startswith("inv_k"):
+        return ik
+    return (aa if key[0] == "a" else bb)[int(key[2]) - 1]
+
+
+@pytest.mark.parametrize("key", aniso_grad_keys(2))
+def test_anisotropic_gradient_matches_central_differences(aniso_case, key):
+    """The anisotropic engine's adjoint (one map set per derivative axis: 22 gradients in 2D)
+    against central differences of the FP64 oracle, same bounds as above."""
+    inp, observed, J, G = aniso_case
+    base = _aniso_base(Oracle(inp), key)
+    assert np.isfinite(G[key]).all() and np.abs(G[key]).max() > 0
+    rng = np.random.default_rng(sum(map(ord, key)))
+    cells = [(int(rng.integers(2, base.shape[0] - 2)), int(rng.integers(2, base.shape[1] - 2)))
+             for _ in range(2)]
     for c in cells:
         mag = abs(base[c]) if base[c] != 0 else float(np.abs(base).mean())
         h = 1e-4 * mag
