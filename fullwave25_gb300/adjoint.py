@@ -46,7 +46,8 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
     ``observed``: CUDA float32 tensor ``[n_out, ncoordsout]``. ``stream``: a torch CUDA stream
     (None: the current one); all work is ordered on it and only it is synchronised, so gradient
     evaluations on other streams overlap. Returns ``(J, traces, grads)`` with ``grads[name]`` a
-    float64 CUDA tensor of the grid shape for every name in ``RAW_MAPS``; for the
+    float64 CUDA tensor of the grid shape for every name in ``RAW_MAPS`` (and ``beta`` when the
+    beta map is not zero everywhere); for the
     exponential-attenuation engine (inputs with an ``a_exp`` map) for ``rho``, ``K`` and
     ``a_exp``; for the anisotropic engine for ``rho``, ``K`` and every per-direction map
     (``kappa{u,w,v,x,y,z}``, ``apml*``, ``bpml*``).
@@ -67,6 +68,7 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
         engine.adjoint_backward(residual.data_ptr(), g.data_ptr(), raw)
         gm = dict(zip(names, g))
         dt = float(np.float32(inp.dt))
+        extra = {"beta": gm["beta2dt"] * (2.0 * dt)} if "beta2dt" in gm else {}
         if "kappay" in inp.maps:   # anisotropic engine: per-direction map sets
             rho = inp.maps["rho"].double()
             grads = {"rho": gm["rdt_rho"] * (-dt / rho ** 2), "K": gm["dt_k"] * dt}
@@ -74,14 +76,15 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
                 if n.startswith("inv_k"):
                     kap = inp.maps[f"kappa{n[5]}"].double()
                     grads[f"kappa{n[5]}"] = gm[n] * (-1.0 / kap ** 2)
-                else:
+                elif n != "beta2dt":
                     grads[f"{n[0]}pml{n[1:]}"] = gm[n]
+            grads.update(extra)
             ts.synchronize()
             return J, traces, grads
         if "a_exp" in inp.maps:   # exponential engine: a_exp sits in the au1 slot
             rho = inp.maps["rho"].double()
             grads = {"rho": gm["rdt_rho"] * (-dt / rho ** 2), "K": gm["dt_k"] * dt,
-                     "a_exp": gm["au1"]}
+                     "a_exp": gm["au1"], **extra}
             ts.synchronize()
             return J, traces, grads
         m = {k: inp.maps[k].double() for k in ("rho", "K", "kappau", "kappax")}
@@ -95,6 +98,7 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
             for ax in ("u", "x"):
                 grads[f"apml{ax}{nu}"] = gm[f"a{ax}{nu}"]
                 grads[f"bpml{ax}{nu}"] = gm[f"b{ax}{nu}"]
+        grads.update(extra)
     ts.synchronize()
     return J, traces, grads
 

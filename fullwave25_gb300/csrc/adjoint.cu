@@ -8,8 +8,43 @@ using namespace fwgbh;
 namespace {
 
 // Gradient maps of a handle: 12 (isotropic relaxation and exponential engines: the AdjGrad
-// order), or 2 + 10 ND (anisotropic engine: one relaxation map set per derivative axis).
-int n_grad_maps(const fw_handle* h) { return h->aniso ? 2 + 10 * h->ndim : kNumGrad; }
+// order), or 2 + 10 ND (anisotropic engine: one relaxation map set per derivative axis); then
+// one more, 2 dt beta, when beta is not zero everywhere.
+int n_grad_base(const fw_handle* h) { return h->aniso ? 2 + 10 * h->ndim : kNumGrad; }
+int n_grad_maps(const fw_handle* h) { return n_grad_base(h) + (h->has_beta ? 1 : 0); }
+
+// The reverse step's launches after lam_p is assembled, for the kernels with thread-loaded
+// operands: every engine (isotropic and anisotropic relaxation, exponential attenuation), 2D
+// and 3D, linear or nonlinear.
+template <int ND, bool kF64, bool kS, bool kBeta>
+void launch_reverse_thread(const fw_handle* h, const AdjArgs& A, dim3 g, dim3 b, size_t shm,
+                           cudaStream_t s) {
+  if (h->exp) {
+    adjx_prs<ND, kF64, kS, kBeta><<<g, b, shm, s>>>(A);
+    adjx_vel<ND, kF64, kS><<<g, b, shm, s>>>(A);
+  } else if (h->aniso) {
+    adja_prs<ND, kF64, kS, kBeta><<<g, b, shm, s>>>(A);
+    adja_vel<ND, kF64, kS><<<g, b, shm, s>>>(A);
+  } else if constexpr (ND == 3) {
+    adj3d_prs<kF64, kS, kBeta><<<g, b, shm, s>>>(A);
+    adj3d_vel<kF64, kS><<<g, b, shm, s>>>(A);
+  } else {
+    adj2d_prs<kF64, kS, kBeta><<<g, b, shm, s>>>(A);
+    adj2d_vel<kF64, kS><<<g, b, shm, s>>>(A);
+  }
+}
+
+template <int ND, bool kF64>
+void launch_reverse_thread_nd(const fw_handle* h, const AdjArgs& A, bool smem_taps, dim3 g,
+                              dim3 b, size_t shm, cudaStream_t s) {
+  const int v = (smem_taps ? 2 : 0) + (h->has_beta ? 1 : 0);
+  switch (v) {
+    case 0: launch_reverse_thread<ND, kF64, false, false>(h, A, g, b, 0, s); break;
+    case 1: launch_reverse_thread<ND, kF64, false, true>(h, A, g, b, 0, s); break;
+    case 2: launch_reverse_thread<ND, kF64, true, false>(h, A, g, b, shm, s); break;
+    default: launch_reverse_thread<ND, kF64, true, true>(h, A, g, b, shm, s); break;
+  }
+}
 
 // Adjoint-field allocation of an ND handle, per padded cell array: lam_p, lam_v (ND),
 // lam_psi (2 ND), lam_phi (2 ND), lam_d (ND), lam_g (ND), then the FP32 gradient partials.
@@ -113,7 +148,6 @@ extern "C" {
 
 int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
-  if (h->has_beta) return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs beta = 0 everywhere");
   if (!h->fields_set) return fail(h, FW_ERR_STATE, "fw_set_fields must be called first");
   if (h->args.l.rec_group)   // the misfit is defined on individual sensor traces
     return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs individual sensor traces: clear the sensor groups");
@@ -192,9 +226,13 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     A.lam_g[a] = h->adj_lam + (lay.lam_g + a) * fs;
   }
   A.n_grad = n_grad;
+  A.beta_slot = h->has_beta ? n_grad_base(h) : -1;
   for (int q = 0; q < n_grad; ++q) {
     A.grad[q] = h->adj_grad + (size_t)q * fs;
-    A.g32[q] = h->adj_lam + (size_t)(lay.fields + (h->aniso ? q : kGradSlot[q])) * fs;
+    // isotropic maps: partials in coefficient-map order (the TMA kernels read runs of six);
+    // 2 dt beta after them (its map slot, kMBeta2dt, is 12)
+    const int slot = h->aniso || q >= kNumGrad ? q : kGradSlot[q];
+    A.g32[q] = h->adj_lam + (size_t)(lay.fields + slot) * fs;
   }
   A.ndmap = h->d.ndmap;
   A.status = h->step + 1;
@@ -205,7 +243,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   // FWGB_ADJ_FUSED=0: the five-launch reverse step (assemble, record, projections, pressure,
   // velocity) instead of the two tiled launches
   const char* fenv = std::getenv("FWGB_ADJ_FUSED");
-  const bool fused = !(fenv && std::strcmp(fenv, "0") == 0);
+  const bool fused = !(fenv && std::strcmp(fenv, "0") == 0) && !h->has_beta;
   const size_t sm = smem_taps ? tap_bytes : 0;
   // FWGB_ADJ_F64_STEPS=1: form and add every step's contributions in FP64 (slow on GB300's FP64
   // pipe; kept to validate the default segmented FP32-partial / FP64-total accumulation)
@@ -226,7 +264,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   // persists there in place) or FWGB_ADJ_OOP=0: then a copy of the state into the store before
   // each in-place step.
   const char* oenv = std::getenv("FWGB_ADJ_OOP");
-  const bool oop = h->ndim == 2 && !h->exp && !h->aniso && !h->ghost_writes &&
+  const bool oop = h->ndim == 2 && !h->exp && !h->aniso && !h->has_beta && !h->ghost_writes &&
                    !(oenv && std::strcmp(oenv, "0") == 0);
   // Overlap (default when a second store exists, with out-of-place recomputation and the TMA
   // reverse step): segment k-1 is recomputed on a second stream into the other store while
@@ -359,7 +397,7 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
     for (int n = n1 - 1; n >= n0; --n) {
       A.Sn = h->adj_store + state_elems * (n - n0);
       A.Sn1 = h->adj_store + state_elems * (n - n0 + 1);
-      if (h->exp || h->aniso) {   // exponential or anisotropic engine, 2D or 3D: thread loads
+      if (h->ndim == 3 || h->exp || h->aniso || !fused) {   // thread-load kernels, any engine
         const bool d3 = h->ndim == 3;
         const dim3 gx = d3 ? grid3 : grid, bx = d3 ? block3 : block;
         const size_t shm = smem_taps ? sm : 0;
@@ -373,54 +411,10 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
         if (counts[2]) adj2d_io<<<(counts[2] + 255) / 256, 256, 0, s>>>(A, L, residual, n, 0, 0, counts[2]);
         if (counts[0] || counts[1])
           adj2d_zero<<<(std::max(counts[0], counts[1]) + 255) / 256, 256, 0, s>>>(A, L, n, counts[0], counts[1]);
-        const int v = (d3 ? 4 : 0) + (f64_steps ? 2 : 0) + (smem_taps ? 1 : 0);
-        if (h->aniso) {
-          switch (v) {
-            case 0: adja_prs<2, false, false><<<gx, bx, 0, s>>>(A); adja_vel<2, false, false><<<gx, bx, 0, s>>>(A); break;
-            case 1: adja_prs<2, false, true><<<gx, bx, shm, s>>>(A); adja_vel<2, false, true><<<gx, bx, shm, s>>>(A); break;
-            case 2: adja_prs<2, true, false><<<gx, bx, 0, s>>>(A); adja_vel<2, true, false><<<gx, bx, 0, s>>>(A); break;
-            case 3: adja_prs<2, true, true><<<gx, bx, shm, s>>>(A); adja_vel<2, true, true><<<gx, bx, shm, s>>>(A); break;
-            case 4: adja_prs<3, false, false><<<gx, bx, 0, s>>>(A); adja_vel<3, false, false><<<gx, bx, 0, s>>>(A); break;
-            case 5: adja_prs<3, false, true><<<gx, bx, shm, s>>>(A); adja_vel<3, false, true><<<gx, bx, shm, s>>>(A); break;
-            case 6: adja_prs<3, true, false><<<gx, bx, 0, s>>>(A); adja_vel<3, true, false><<<gx, bx, 0, s>>>(A); break;
-            default: adja_prs<3, true, true><<<gx, bx, shm, s>>>(A); adja_vel<3, true, true><<<gx, bx, shm, s>>>(A); break;
-          }
-          continue;
-        }
-        switch (v) {
-          case 0: adjx_prs<2, false, false><<<gx, bx, 0, s>>>(A); adjx_vel<2, false, false><<<gx, bx, 0, s>>>(A); break;
-          case 1: adjx_prs<2, false, true><<<gx, bx, shm, s>>>(A); adjx_vel<2, false, true><<<gx, bx, shm, s>>>(A); break;
-          case 2: adjx_prs<2, true, false><<<gx, bx, 0, s>>>(A); adjx_vel<2, true, false><<<gx, bx, 0, s>>>(A); break;
-          case 3: adjx_prs<2, true, true><<<gx, bx, shm, s>>>(A); adjx_vel<2, true, true><<<gx, bx, shm, s>>>(A); break;
-          case 4: adjx_prs<3, false, false><<<gx, bx, 0, s>>>(A); adjx_vel<3, false, false><<<gx, bx, 0, s>>>(A); break;
-          case 5: adjx_prs<3, false, true><<<gx, bx, shm, s>>>(A); adjx_vel<3, false, true><<<gx, bx, shm, s>>>(A); break;
-          case 6: adjx_prs<3, true, false><<<gx, bx, 0, s>>>(A); adjx_vel<3, true, false><<<gx, bx, 0, s>>>(A); break;
-          default: adjx_prs<3, true, true><<<gx, bx, shm, s>>>(A); adjx_vel<3, true, true><<<gx, bx, shm, s>>>(A); break;
-        }
-        continue;
-      }
-      if (h->ndim == 3) {
-        if (!first) {
-          if (smem_taps) adj3d_assemble<true><<<grid3, block3, sm, s>>>(A);
-          else adj3d_assemble<false><<<grid3, block3, 0, s>>>(A);
-        }
-        first = false;
-        if (counts[2]) adj2d_io<<<(counts[2] + 255) / 256, 256, 0, s>>>(A, L, residual, n, 0, 0, counts[2]);
-        if (counts[0] || counts[1])
-          adj2d_zero<<<(std::max(counts[0], counts[1]) + 255) / 256, 256, 0, s>>>(A, L, n, counts[0], counts[1]);
-        if (f64_steps && smem_taps) {
-          adj3d_prs<true, true><<<grid3, block3, sm, s>>>(A);
-          adj3d_vel<true, true><<<grid3, block3, sm, s>>>(A);
-        } else if (f64_steps) {
-          adj3d_prs<true, false><<<grid3, block3, 0, s>>>(A);
-          adj3d_vel<true, false><<<grid3, block3, 0, s>>>(A);
-        } else if (smem_taps) {
-          adj3d_prs<false, true><<<grid3, block3, sm, s>>>(A);
-          adj3d_vel<false, true><<<grid3, block3, sm, s>>>(A);
-        } else {
-          adj3d_prs<false, false><<<grid3, block3, 0, s>>>(A);
-          adj3d_vel<false, false><<<grid3, block3, 0, s>>>(A);
-        }
+        if (d3 && f64_steps) launch_reverse_thread_nd<3, true>(h, A, smem_taps, gx, bx, shm, s);
+        else if (d3) launch_reverse_thread_nd<3, false>(h, A, smem_taps, gx, bx, shm, s);
+        else if (f64_steps) launch_reverse_thread_nd<2, true>(h, A, smem_taps, gx, bx, shm, s);
+        else launch_reverse_thread_nd<2, false>(h, A, smem_taps, gx, bx, shm, s);
         continue;
       }
       if (tma) {
@@ -428,42 +422,19 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
         adj2d_vel_tma<0><<<grid, block, smem_vel, s>>>(A, n - n0, M[0]);
         continue;
       }
-      if (fused) {
-        if (f64_steps && smem_taps) {
-          adj2d_prs_fused<true, true><<<grid, block, sm, s>>>(A, L, residual, n);
-          adj2d_vel_tiled<true, true><<<grid, block, sm, s>>>(A);
-        } else if (f64_steps) {
-          adj2d_prs_fused<true, false><<<grid, block, 0, s>>>(A, L, residual, n);
-          adj2d_vel_tiled<true, false><<<grid, block, 0, s>>>(A);
-        } else if (smem_taps) {
-          adj2d_prs_fused<false, true><<<grid, block, sm, s>>>(A, L, residual, n);
-          adj2d_vel_tiled<false, true><<<grid, block, sm, s>>>(A);
-        } else {
-          adj2d_prs_fused<false, false><<<grid, block, 0, s>>>(A, L, residual, n);
-          adj2d_vel_tiled<false, false><<<grid, block, 0, s>>>(A);
-        }
-        continue;
-      }
-      if (!first) {
-        if (smem_taps) adj2d_assemble<true><<<grid, block, sm, s>>>(A);
-        else adj2d_assemble<false><<<grid, block, 0, s>>>(A);
-      }
-      first = false;
-      if (counts[2]) adj2d_io<<<(counts[2] + 255) / 256, 256, 0, s>>>(A, L, residual, n, 0, 0, counts[2]);
-      if (counts[0] || counts[1])
-        adj2d_zero<<<(std::max(counts[0], counts[1]) + 255) / 256, 256, 0, s>>>(A, L, n, counts[0], counts[1]);
+      // 2D isotropic linear engine, tiled thread-load form (FWGB_ADJ_TMA=0)
       if (f64_steps && smem_taps) {
-        adj2d_prs<true, true><<<grid, block, sm, s>>>(A);
-        adj2d_vel<true, true><<<grid, block, sm, s>>>(A);
+        adj2d_prs_fused<true, true><<<grid, block, sm, s>>>(A, L, residual, n);
+        adj2d_vel_tiled<true, true><<<grid, block, sm, s>>>(A);
       } else if (f64_steps) {
-        adj2d_prs<true, false><<<grid, block, 0, s>>>(A);
-        adj2d_vel<true, false><<<grid, block, 0, s>>>(A);
+        adj2d_prs_fused<true, false><<<grid, block, 0, s>>>(A, L, residual, n);
+        adj2d_vel_tiled<true, false><<<grid, block, 0, s>>>(A);
       } else if (smem_taps) {
-        adj2d_prs<false, true><<<grid, block, sm, s>>>(A);
-        adj2d_vel<false, true><<<grid, block, sm, s>>>(A);
+        adj2d_prs_fused<false, true><<<grid, block, sm, s>>>(A, L, residual, n);
+        adj2d_vel_tiled<false, true><<<grid, block, sm, s>>>(A);
       } else {
-        adj2d_prs<false, false><<<grid, block, 0, s>>>(A);
-        adj2d_vel<false, false><<<grid, block, 0, s>>>(A);
+        adj2d_prs_fused<false, false><<<grid, block, 0, s>>>(A, L, residual, n);
+        adj2d_vel_tiled<false, false><<<grid, block, 0, s>>>(A);
       }
     }
     if (!f64_steps) {

@@ -1,5 +1,7 @@
-// Discrete adjoint of the 2D time step (beta = 0), for gradients of the sensor-trace misfit
-// J = 1/2 sum_n || p^{n+1}[outc] - d_n ||^2 with respect to the engine's coefficient maps.
+// Discrete adjoint of the 2D time step, for gradients of the sensor-trace misfit
+// J = 1/2 sum_n || p^{n+1}[outc] - d_n ||^2 with respect to the engine's coefficient maps. The
+// steps below are those of the linear isotropic engine (beta = 0); the nonlinear term is the
+// kBeta variant of the pressure adjoint (adj_prs_point).
 //
 // Reverse of step n uses the stored forward states S_n (before the step) and S_{n+1} (after):
 //   assemble  lam_p += sum_a D_a^T lam_g_a                      (from step n+1's velocity adjoint)
@@ -26,7 +28,7 @@ enum AdjGrad {
 // The anisotropic engine has one map set per derivative axis: 2 + 10 ND gradient maps (dt/rho,
 // dt*K, then per axis 1/kappa, a1, b1, a2, b2 of the pressure-gradient maps, then the same of the
 // velocity-divergence maps), at most 32 in 3D.
-constexpr int kMaxGrad = 32;
+constexpr int kMaxGrad = 33;
 
 struct AdjArgs {
   Grid g;
@@ -41,9 +43,11 @@ struct AdjArgs {
   float* lam_d[3];
   float* lam_g[3];
   int ndmap;                 // tap sets in m.taps
-  double* grad[kMaxGrad];    // FP64 time sums (kNumGrad maps; anisotropic engine: 2 + 10 ND)
+  double* grad[kMaxGrad];    // FP64 time sums (kNumGrad maps; anisotropic engine: 2 + 10 ND;
+                             // plus one for 2 dt beta when beta is not zero)
   float* g32[kMaxGrad];      // FP32 partial sums of the current segment (segmented mode)
   int n_grad;                // gradient maps in use
+  int beta_slot;             // gradient map of 2 dt beta (the last one), or -1
   int* status;               // device status word (bounded waits, alignment)
 };
 
@@ -207,13 +211,18 @@ static __global__ void adj2d_zero(const AdjArgs A, const Lists L, int n, int n_s
 // adjoint fields themselves) and summed per checkpoint segment in FP32 partials, which
 // adj2d_merge adds into the FP64 time sums at the end of every segment.
 // Pressure adjoint of body cell c (ND axes), given its assembled lam_p and the divergence
-// components d[a] = D'_a v^{n+1/2} at c.
-template <bool kF64, int ND>
+// components d[a] = D'_a v^{n+1/2} at c. kBeta (nonlinear engine): the forward update is
+// p' = p - (dt K + 2 dt beta p) div, so the coefficient of div is that sum at p = p^n, lam_p
+// passes to p^n times (1 - 2 dt beta div), and 2 dt beta gets the gradient -p^n div lam_p.
+template <bool kF64, int ND, bool kBeta = false>
 __device__ __forceinline__ void adj_prs_point(const AdjArgs& A, int64_t c, const float lp,
                                               const float (&d)[ND]) {
   using acc_t = typename std::conditional<kF64, double, float>::type;
   const int64_t fs = A.fs;
-  const float k = __ldg(A.m.dt_k + c), ikx = __ldg(A.m.inv_kx[0] + c);
+  const float dtk = __ldg(A.m.dt_k + c), ikx = __ldg(A.m.inv_kx[0] + c);
+  const float b2dt = kBeta ? __ldg(A.m.beta2dt + c) : 0.f;
+  const float pn = kBeta ? __ldg(S_p(A.Sn, fs) + c) : 0.f;
+  const float k = kBeta ? fmaf(b2dt, pn, dtk) : dtk;   // the forward's coefficient of div
   const float ax[2] = {__ldg(A.m.ax[0][0] + c), __ldg(A.m.ax[0][1] + c)};
   const float bx[2] = {__ldg(A.m.bx[0][0] + c), __ldg(A.m.bx[0][1] + c)};
   acc_t g_dtk = 0, g_ikx = 0, g_ax[2] = {0, 0}, g_bx[2] = {0, 0};
@@ -235,6 +244,11 @@ __device__ __forceinline__ void adj_prs_point(const AdjArgs& A, int64_t c, const
     A.lam_d[a][c] = lam_d;
   }
   g_dtk -= (acc_t)div * lp;
+  if constexpr (kBeta) {
+    A.lam_p[c] = lp - b2dt * div * lp;
+    if constexpr (kF64) A.grad[A.beta_slot][c] -= (double)pn * div * lp;
+    else A.g32[A.beta_slot][c] -= pn * div * lp;
+  }
   if constexpr (kF64) {
     A.grad[kGDtK][c] += g_dtk;
     A.grad[kGInvKx][c] += g_ikx;
@@ -253,22 +267,22 @@ __device__ __forceinline__ void adj_prs_point(const AdjArgs& A, int64_t c, const
 }
 
 // Pressure adjoint of 2D body cell c, given its assembled lam_p.
-template <bool kF64, bool kS>
+template <bool kF64, bool kS, bool kBeta = false>
 __device__ __forceinline__ void adj_prs_cell(const AdjArgs& A, const TapSrc<kS>& T, int64_t c,
                                              const float lp) {
   const Grid& g = A.g;
   const float d[2] = {div_at(A.m, T, S_v(A.Sn1, A.fs, 0), c, g.sx, 1, g.inv_h[0]),
                       div_at(A.m, T, S_v(A.Sn1, A.fs, 1), c, 1, g.sx, g.inv_h[1])};
-  adj_prs_point<kF64, 2>(A, c, lp, d);
+  adj_prs_point<kF64, 2, kBeta>(A, c, lp, d);
 }
 
-template <bool kF64, bool kS>
+template <bool kF64, bool kS, bool kBeta = false>
 __global__ void __launch_bounds__(256) adj2d_prs(const AdjArgs A) {
   extern __shared__ float s_taps[];
   const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
   int64_t c;
   if (!adj_cell(A.g, &c)) return;
-  adj_prs_cell<kF64, kS>(A, T, c, A.lam_p[c]);
+  adj_prs_cell<kF64, kS, kBeta>(A, T, c, A.lam_p[c]);
 }
 
 // Velocity adjoint of body cell c (ND axes), given (D'_a^T lam_d_a)(c) and the pressure

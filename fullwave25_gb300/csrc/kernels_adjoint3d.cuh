@@ -1,6 +1,7 @@
-// Discrete adjoint of the 3D time step (isotropic relaxation engine, beta = 0): the reverse step
-// of kernels_adjoint2d.cuh with three derivative axes; and, at the end, the reverse step of the
-// exponential-attenuation engine in 2D and 3D. One thread per body cell (blocks of
+// Discrete adjoint of the 3D time step (isotropic relaxation engine): the reverse step of
+// kernels_adjoint2d.cuh with three derivative axes; and, further down, the reverse steps of the
+// exponential-attenuation and anisotropic relaxation engines in 2D and 3D. Every pressure
+// adjoint has a kBeta variant for the nonlinear term. One thread per body cell (blocks of
 // 32 (z) x 8 (y) cells of one x plane), operands through the read-only path, the tap table in
 // shared memory when it fits. Per reverse step n, in order:
 //   adj3d_assemble   lam_p += sum_a D_a^T lam_g_a           (lam_g from step n+1)
@@ -131,7 +132,7 @@ __global__ void __launch_bounds__(256) adj3d_assemble(const AdjArgs A) {
   A.lam_p[q] += add;
 }
 
-template <bool kF64, bool kS>
+template <bool kF64, bool kS, bool kBeta = false>
 __global__ void __launch_bounds__(256) adj3d_prs(const AdjArgs A) {
   extern __shared__ float s_taps[];
   const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
@@ -140,7 +141,7 @@ __global__ void __launch_bounds__(256) adj3d_prs(const AdjArgs A) {
   float d[3];
 #pragma unroll
   for (int a = 0; a < 3; ++a) d[a] = div3_at(A.m, T, S_v(A.Sn1, A.fs, a), c, axis3(A.g, a));
-  adj_prs_point<kF64, 3>(A, c, A.lam_p[c], d);
+  adj_prs_point<kF64, 3, kBeta>(A, c, A.lam_p[c], d);
 }
 
 template <bool kF64, bool kS>
@@ -174,6 +175,8 @@ static __global__ void __launch_bounds__(256) adj3d_merge(const AdjArgs A) {
 // after adj2d/adj3d_assemble and adj2d_io / adj2d_zero have formed lam_p (= dJ/dp' on the body):
 //   adjx_prs: d = sum_a D'_a v'_a (S_{n+1});  lam_d = -ae k lam_p  (one field, every axis);
 //             gradients dt_k -= ae d lam_p, a_exp += lam_p (p^n - k d);  lam_p <- ae lam_p
+//             (kBeta: k = dt K + 2 dt beta p^n, lam_p <- ae (1 - 2 dt beta d) lam_p and
+//             2 dt beta -= ae p^n d lam_p)
 //   adjx_vel: lam_v_a += D'_a^T lam_d;  g_a = D_a p^n;  lam_g_a = -ae r lam_v_a;
 //             gradients rdt_rho -= ae g_a lam_v_a, a_exp += lam_v_a (v_a^n - r g_a);
 //             lam_v_a <- ae lam_v_a
@@ -211,7 +214,7 @@ __device__ __forceinline__ void adj_add_grad(const AdjArgs& A, int q, int64_t c,
   else A.g32[q][c] += v;
 }
 
-template <int ND, bool kF64, bool kS>
+template <int ND, bool kF64, bool kS, bool kBeta = false>
 __global__ void __launch_bounds__(256) adjx_prs(const AdjArgs A) {
   extern __shared__ float s_taps[];
   const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
@@ -221,12 +224,15 @@ __global__ void __launch_bounds__(256) adjx_prs(const AdjArgs A) {
 #pragma unroll
   for (int a = 0; a < ND; ++a) d += divn_at<ND>(A.m, T, S_v(A.Sn1, A.fs, a), c, A.g, a);
   const float lp = A.lam_p[c];
-  const float k = __ldg(A.m.dt_k + c), ae = __ldg(A.m.a_exp + c);
+  const float dtk = __ldg(A.m.dt_k + c), ae = __ldg(A.m.a_exp + c);
   const float pn = __ldg(S_p(A.Sn, A.fs) + c);
+  const float b2dt = kBeta ? __ldg(A.m.beta2dt + c) : 0.f;
+  const float k = kBeta ? fmaf(b2dt, pn, dtk) : dtk;
   A.lam_d[0][c] = -ae * k * lp;
-  A.lam_p[c] = ae * lp;
+  A.lam_p[c] = kBeta ? ae * (lp - b2dt * d * lp) : ae * lp;
   adj_add_grad<kF64>(A, kGDtK, c, -(ae * d * lp));
   adj_add_grad<kF64>(A, kGAu1, c, lp * (pn - k * d));
+  if constexpr (kBeta) adj_add_grad<kF64>(A, A.beta_slot, c, -(ae * pn * d * lp));
 }
 
 template <int ND, bool kF64, bool kS>
@@ -257,11 +263,14 @@ __global__ void __launch_bounds__(256) adjx_vel(const AdjArgs A) {
 // Gradient slots: 0 dt/rho, 1 dt*K, 2 + 5 a + j the pressure-gradient maps of axis a, 2 + 5 ND
 // + 5 a + j the velocity-divergence maps, j = 1/kappa, a1, b1, a2, b2.
 
-template <bool kF64, int ND>
+template <bool kF64, int ND, bool kBeta = false>
 __device__ __forceinline__ void adja_prs_point(const AdjArgs& A, int64_t c, const float lp,
                                                const float (&d)[ND]) {
   const int64_t fs = A.fs;
-  const float k = __ldg(A.m.dt_k + c);
+  const float dtk = __ldg(A.m.dt_k + c);
+  const float b2dt = kBeta ? __ldg(A.m.beta2dt + c) : 0.f;
+  const float pn = kBeta ? __ldg(S_p(A.Sn, fs) + c) : 0.f;
+  const float k = kBeta ? fmaf(b2dt, pn, dtk) : dtk;   // the forward's coefficient of div
   float div = 0.f;
 #pragma unroll
   for (int a = 0; a < ND; ++a) {
@@ -289,6 +298,10 @@ __device__ __forceinline__ void adja_prs_point(const AdjArgs& A, int64_t c, cons
     adj_add_grad<kF64>(A, q + 4, c, g_bx[1]);
   }
   adj_add_grad<kF64>(A, kGDtK, c, -(div * lp));
+  if constexpr (kBeta) {
+    A.lam_p[c] = lp - b2dt * div * lp;
+    adj_add_grad<kF64>(A, A.beta_slot, c, -(pn * div * lp));
+  }
 }
 
 template <bool kF64, int ND>
@@ -327,7 +340,7 @@ __device__ __forceinline__ void adja_vel_point(const AdjArgs& A, int64_t c, cons
   adj_add_grad<kF64>(A, kGRdtRho, c, g_r);
 }
 
-template <int ND, bool kF64, bool kS>
+template <int ND, bool kF64, bool kS, bool kBeta = false>
 __global__ void __launch_bounds__(256) adja_prs(const AdjArgs A) {
   extern __shared__ float s_taps[];
   const TapSrc<kS> T = stage_taps<kS>(A, s_taps);
@@ -336,7 +349,7 @@ __global__ void __launch_bounds__(256) adja_prs(const AdjArgs A) {
   float d[ND];
 #pragma unroll
   for (int a = 0; a < ND; ++a) d[a] = divn_at<ND>(A.m, T, S_v(A.Sn1, A.fs, a), c, A.g, a);
-  adja_prs_point<kF64, ND>(A, c, A.lam_p[c], d);
+  adja_prs_point<kF64, ND, kBeta>(A, c, A.lam_p[c], d);
 }
 
 template <int ND, bool kF64, bool kS>

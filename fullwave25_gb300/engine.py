@@ -63,15 +63,18 @@ def adjoint_gradient_maps(inputs) -> tuple:
     """Engine-map names of ``fw_adjoint_backward``'s gradient arrays, in output order:
     ``ADJOINT_MAPS`` (12), or for the anisotropic engine 2 + 10 ndim: dt/rho, dt*K, then per
     derivative axis 1/kappa, a1, b1, a2, b2 of the pressure-gradient maps (u, w, v), then the
-    same of the velocity-divergence maps (x, y, z)."""
+    same of the velocity-divergence maps (x, y, z); followed by ``beta2dt`` (2 dt beta) when the
+    beta map is not zero everywhere."""
+    beta = inputs.maps.get("beta")
+    tail = ("beta2dt",) if beta is not None and bool((beta != 0).any()) else ()
     if "kappay" not in inputs.maps:
-        return ADJOINT_MAPS
+        return ADJOINT_MAPS + tail
     names = ["rdt_rho", "dt_k"]
     for letters in ("uwv", "xyz"):
         for a in range(len(inputs.shape)):
             g = letters[a]
             names += [f"inv_k{g}", f"a{g}1", f"b{g}1", f"a{g}2", f"b{g}2"]
-    return tuple(names)
+    return tuple(names) + tail
 
 
 ANISO_FIELDS = tuple(f"{k}{ax}{nu}" if k != "kappa" else f"kappa{ax}"

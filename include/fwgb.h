@@ -211,9 +211,10 @@ FWGB_API int fw_launches_per_step(const fw_handle *h, int32_t *n);
 FWGB_API int fw_destroy(fw_handle *h);
 
 /* Gradient of the sensor-trace misfit J = 1/2 sum ||traces - observed||^2 (2D and 3D; isotropic
- * or anisotropic relaxation, or exponential-attenuation engine; beta = 0; individual sensor
- * traces: no sensor groups), with respect to the engine's coefficient maps, by the discrete
- * adjoint of the time step. No counterpart in the reference (it has no gradient computation).
+ * or anisotropic relaxation, or exponential-attenuation engine; linear or with beta; individual
+ * sensor traces: no sensor groups), with respect to the engine's coefficient maps, by the
+ * discrete adjoint of the time step. No counterpart in the reference (it has no gradient
+ * computation).
  * fw_adjoint_forward: run the full forward solve from rest, keeping a checkpoint of the wavefield
  * every `checkpoint_every` steps (device memory: nt / checkpoint_every + 2 (checkpoint_every + 1)
  * wavefield copies: the checkpoints and two state stores; one store in 3D, or with
@@ -236,7 +237,9 @@ FWGB_API int fw_adjoint_forward(fw_handle *h, void *stream, int32_t checkpoint_e
  * dt*K and, in the au1 slot, a_exp, and leaves the other slots zero; the anisotropic engine
  * returns [2 + 10 ndim][...]: dt/rho, dt*K, then for each derivative axis 1/kappa, a1, b1, a2, b2
  * of its pressure-gradient maps (u, w, v), then the same of its velocity-divergence maps
- * (x, y, z). Those two engines' reverse step is four thread-load launches in 2D and 3D. The wavefield left in the handle afterwards is the first segment's
+ * (x, y, z). When beta is not zero everywhere one more array follows: the gradient with
+ * respect to 2 dt beta. Those engines' reverse step, and any reverse step with beta, is four
+ * thread-load launches in 2D and 3D. The wavefield left in the handle afterwards is the first segment's
  * recomputation. Returns after the stream has finished the pass (FW_ERR_DEVICE if a kernel
  * reported a timed-out wait). */
 FWGB_API int fw_adjoint_backward(fw_handle *h, void *stream, const float *residual,

@@ -1,4 +1,4 @@
-"""FP64 NumPy adjoint of the oracle's time loop (2D and 3D, beta = 0).
+"""FP64 NumPy adjoint of the oracle's time loop (2D and 3D).
 
 TEST INFRASTRUCTURE ONLY: the reference adjoint that the GPU adjoint is checked against, itself
 checked against central finite differences of the FP64 oracle (tests/test_adjoint_oracle.py).
@@ -22,6 +22,10 @@ Reverse of step n (state S_n before it, S_{n+1} after it):
                grads: rdt_rho -= lam_v_a (iku g_a + psi_1' + psi_2');  inv_ku -= r g_a lam_v_a;
                       au_nu += M_nu g_a;  bu_nu += M_nu psi_nu(S_n)
   pressure at step start: lam_p += sum_a D_a^T lam_g_a
+
+Nonlinear term (beta != 0): the pressure update is p' = p - (k + b p) div with b = 2 dt beta, so
+k above becomes k + b p^n, lam_p passes to p^n times (1 - b div), and b gets the gradient
+-p^n div lam_p (``beta2dt``).
 
 Exponential-attenuation engine (maps ``rdt_rho``, ``dt_k``, ``a_exp``; forward
 ``v' = ae (v - r D_a p)``, ``p' = ae (p - k sum_a D'_a v'_a)``), reverse of step n:
@@ -109,8 +113,6 @@ class AdjointOracle(Oracle):
 
     def forward_storing(self):
         """Run nT steps; returns (traces, states) with states[n] = state before step n."""
-        if self.has_beta:
-            raise NotImplementedError("the adjoint covers beta = 0")
         states = []
         out = np.zeros((self.inp.n_out, self.outc.size))
         for _ in range(self.inp.nt):
@@ -134,11 +136,12 @@ class AdjointOracle(Oracle):
         to ``rdt_rho``, ``dt_k`` and ``a_exp``."""
         nd, body = self.nd, _body(self.shape)
         bshape = tuple(k - 2 * GHOST for k in self.shape)
-        G = {k: np.zeros(bshape) for k in EXP_GRAD_KEYS}
+        keys = EXP_GRAD_KEYS + (("beta2dt",) if self.has_beta else ())
+        G = {k: np.zeros(bshape) for k in keys}
         lam_p = np.zeros(self.shape)
         lam_v = [np.zeros(bshape) for _ in range(nd)]
         lam_g = None
-        k, r, ae = self.dt_k, self.rdt_rho, self.a_exp
+        dtk, r, ae = self.dt_k, self.rdt_rho, self.a_exp
         for n in range(self.inp.nt - 1, -1, -1):
             Sn, Sn1 = states[n], states[n + 1]
             if lam_g is not None:
@@ -149,10 +152,16 @@ class AdjointOracle(Oracle):
             d = np.zeros(bshape)
             for a in range(nd):
                 d += self.div_component(Sn1.v[a], a)
+            pn = Sn.p[body]
+            k = dtk + self.beta2dt * pn if self.has_beta else dtk
             lam_d = -ae * k * lp
             G["dt_k"] -= ae * d * lp
-            G["a_exp"] += lp * (Sn.p[body] - k * d)
-            lam_p[body] = ae * lp
+            G["a_exp"] += lp * (pn - k * d)
+            if self.has_beta:
+                G["beta2dt"] -= ae * pn * d * lp
+                lam_p[body] = ae * (1.0 - self.beta2dt * d) * lp
+            else:
+                lam_p[body] = ae * lp
             lam_g = []
             for a in range(nd):
                 lv = lam_v[a] + self.div_T(lam_d, a)[body]
@@ -172,7 +181,8 @@ class AdjointOracle(Oracle):
         nd, body = self.nd, _body(self.shape)
         bshape = tuple(k - 2 * GHOST for k in self.shape)
         aniso = self.axis_u[0] is not None
-        G = {k: np.zeros(bshape) for k in (aniso_grad_keys(nd) if aniso else GRAD_KEYS)}
+        keys = (aniso_grad_keys(nd) if aniso else GRAD_KEYS) + (("beta2dt",) if self.has_beta else ())
+        G = {k: np.zeros(bshape) for k in keys}
         # per derivative axis: (1/kappa, (a1, a2), (b1, b2)) and the map letter of the keys
         U = [self.axis_u[a] or (self.inv_kappa_u, self.au, self.bu) for a in range(nd)]
         X = [self.axis_x[a] or (self.inv_kappa_x, self.ax, self.bx) for a in range(nd)]
@@ -183,20 +193,25 @@ class AdjointOracle(Oracle):
         lam_psi = [[np.zeros(bshape), np.zeros(bshape)] for _ in range(nd)]
         lam_phi = [[np.zeros(bshape), np.zeros(bshape)] for _ in range(nd)]
         lam_g = None
-        k, r = self.dt_k, self.rdt_rho
+        dtk, r = self.dt_k, self.rdt_rho
         for n in range(self.inp.nt - 1, -1, -1):
             Sn, Sn1 = states[n], states[n + 1]
             if lam_g is not None:
                 for a in range(nd):
                     lam_p += self.grad_T(lam_g[a], a)
             self._io_adjoint(lam_p, residual, n)
-            lp = lam_p[body]
+            lp = lam_p[body].copy()
+            pn = Sn.p[body]
+            k = dtk + self.beta2dt * pn if self.has_beta else dtk   # coefficient of div
             # pressure step
             d = [self.div_component(Sn1.v[a], a) for a in range(nd)]
             div = np.zeros(bshape)
             for a in range(nd):
                 div += d[a] * X[a][0] + Sn1.phi[a][0][body] + Sn1.phi[a][1][body]
             G["dt_k"] -= div * lp
+            if self.has_beta:
+                G["beta2dt"] -= pn * div * lp
+                lam_p[body] = (1.0 - self.beta2dt * div) * lp
             lam_d = []
             for a in range(nd):
                 ikx, ax, bx = X[a]
@@ -239,7 +254,8 @@ def misfit(inputs, observed, maps_override=None):
     o = Oracle(inputs)
     if maps_override:
         for key, val in maps_override.items():
-            attr = {"rdt_rho": "rdt_rho", "dt_k": "dt_k", "a_exp": "a_exp"}.get(key)
+            attr = {"rdt_rho": "rdt_rho", "dt_k": "dt_k", "a_exp": "a_exp",
+                    "beta2dt": "beta2dt"}.get(key)
             if o.axis_u[0] is not None and not attr:   # anisotropic: per-axis map sets
                 letter = key[5] if key.startswith("inv_k") else key[1]
                 side = 0 if letter in GRAD_LETTERS[0] else 1
@@ -257,6 +273,8 @@ def misfit(inputs, observed, maps_override=None):
             attr = attr or {"inv_ku": "inv_kappa_u", "inv_kx": "inv_kappa_x"}.get(key)
             if attr:
                 setattr(o, attr, val)
+                if key == "beta2dt":
+                    o.has_beta = True
             else:
                 kind, nu = key[:2], int(key[2]) - 1
                 tup = list(getattr(o, kind))

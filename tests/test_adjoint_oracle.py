@@ -144,3 +144,50 @@ def test_anisotropic_gradient_matches_central_differences(aniso_case, key):
         floor = 1e-10 * abs(J) / mag
         assert abs(fd - ad) <= 1e-5 * max(abs(fd), abs(ad)) + floor, \
             f"{key} at {c}: adjoint {ad:.6e} vs finite difference {fd:.6e}"
+
+
+def _beta_case(name, nt, beta=None):
+    inp = _small(name, nt)
+    if beta is not None:   # a nonlinear variant of a linear golden case
+        inp.maps = dict(inp.maps)
+        inp.maps["beta"] = np.full(inp.shape, beta, dtype=np.float32)
+    obs_inp = _small(name, nt)
+    obs_inp.maps = dict(inp.maps)
+    obs_inp.maps["K"] = (obs_inp.maps["K"] * np.float32(1.02)).astype(np.float32)
+    observed = Oracle(obs_inp).run()
+    J, G, traces = misfit_and_gradient(inp, observed)
+    return inp, observed, J, G
+
+
+@pytest.fixture(scope="module")
+def beta_cases():
+    return {"relaxation": _beta_case("2d_air_beta", 70),
+            "exponential": _beta_case("2d_exp", 70, beta=8.0)}
+
+
+@pytest.mark.parametrize("engine,key", [("relaxation", k) for k in GRAD_KEYS + ("beta2dt",)] +
+                         [("exponential", k) for k in EXP_GRAD_KEYS + ("beta2dt",)])
+def test_nonlinear_gradient_matches_central_differences(beta_cases, engine, key):
+    """The adjoint of the nonlinear engines (beta != 0: the coefficient of the divergence is
+    dt K + 2 dt beta p, so the pressure adjoint is linearised around the stored forward states)
+    against central differences of the FP64 oracle, including the gradient with respect to
+    2 dt beta; the relaxation case also has air cells and a recording interval above 1."""
+    inp, observed, J, G = beta_cases[engine]
+    o = Oracle(inp)
+    assert o.has_beta
+    base = _base_map(o, key) if engine == "relaxation" and key != "beta2dt" else getattr(o, key)
+    assert np.isfinite(G[key]).all() and np.abs(G[key]).max() > 0
+    rng = np.random.default_rng(sum(map(ord, key)) + len(engine))
+    cells = [(int(rng.integers(2, base.shape[0] - 2)), int(rng.integers(2, base.shape[1] - 2)))
+             for _ in range(2)]
+    for c in cells:
+        mag = abs(base[c]) if base[c] != 0 else float(np.abs(base).mean())
+        h = 1e-4 * mag
+        plus, minus = base.copy(), base.copy()
+        plus[c] += h
+        minus[c] -= h
+        fd = (misfit(inp, observed, {key: plus}) - misfit(inp, observed, {key: minus})) / (2 * h)
+        ad = G[key][c]
+        floor = 1e-10 * abs(J) / mag
+        assert abs(fd - ad) <= 1e-5 * max(abs(fd), abs(ad)) + floor, \
+            f"{engine} {key} at {c}: adjoint {ad:.6e} vs finite difference {fd:.6e}"

@@ -275,13 +275,10 @@ def test_physical_gradients_match_finite_differences(engine_lib, cuda, problem):
     assert checked == 24
 
 
-def test_adjoint_rejects_beta_and_sensor_groups(engine_lib, cuda):
-    """The misfit is defined on individual sensor traces of the linear (beta = 0) engine."""
+def test_adjoint_rejects_sensor_groups(engine_lib, cuda):
+    """The misfit is defined on individual sensor traces."""
     from fullwave25_gb300.engine import Engine, EngineError
 
-    with Engine(load_case_inputs("2d_air_beta")) as e:
-        with pytest.raises(EngineError, match="FW_ERR_UNSUPPORTED"):
-            e.adjoint_forward(10)
     inp = _small("2d_small", 40)
     with Engine(inp) as e:
         n = inp.outc.shape[0]
