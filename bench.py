@@ -977,6 +977,66 @@ def measure_adjoint(n=1024, nt=0, every=200, steps=3, warmup=3):
     return line
 
 
+def measure_adjoint3d(edge=160, nt=600, every=60, steps=3, warmup=3, physics="isotropic"):
+    """The 3D discrete adjoint through the engine's C ABI on a block of the plain 3D medium
+    (``edge``^3 + PML 16 + transition 16): per evaluation one ``fw_adjoint_forward`` (forward
+    solve with checkpoints) and one ``fw_adjoint_backward`` (recomputation + reverse pass) of the
+    misfit against traces scaled by 0.9, each timed with CUDA events."""
+    import torch
+
+    from fullwave25_gb300.engine import Engine, adjoint_gradient_maps
+    from fullwave25_gb300.workloads3d import plain_3d_device_inputs
+
+    torch.cuda.set_device(0)
+    d = plain_3d_device_inputs(shape=(edge,) * 3, nt=nt, n_pml=16, n_transition=16,
+                               sensor_plane=min(256, edge // 2), element_height=8,
+                               physics=physics)
+    cells = int(np.prod(d.shape))
+    names = adjoint_gradient_maps(d)
+    s = torch.cuda.current_stream()
+    fw, bw = [], []
+    with Engine(d, validate=False) as eng:
+        for i in range(warmup + steps):
+            e0, e1, e2, e3 = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+            e0.record(s)
+            eng.adjoint_forward(every, s.cuda_stream)
+            e1.record(s)
+            tr = torch.empty((d.n_out, d.outc.shape[0]), device="cuda")
+            eng.read_traces_into(0, d.n_out, tr.data_ptr(), s.cuda_stream)
+            res = (0.1 * tr).contiguous()
+            g = torch.zeros((len(names),) + tuple(d.shape), dtype=torch.float64, device="cuda")
+            e2.record(s)
+            eng.adjoint_backward(res.data_ptr(), g.data_ptr(), s.cuda_stream)
+            e3.record(s)
+            torch.cuda.synchronize()
+            if i >= warmup:
+                fw.append(e0.elapsed_time(e1))
+                bw.append(e2.elapsed_time(e3))
+        dev_gb = eng.device_bytes / 1e9
+    ms = float(np.mean(fw) + np.mean(bw))
+    return {"metric": "gradient evaluations/s (3D adjoint)", "value": 1e3 / ms, "unit": "grad/s",
+            "n_gpus": 1, "steps": steps, "warmup": warmup, "ms_per_step": ms,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 wavefields, f64 gradient accumulation", "data": "synthetic",
+            "config": {"workload": f"3D adjoint ({physics}), plain 3D medium {edge}^3 + PML 16 + "
+                                   f"transition 16 ({d.shape[0]}^3 = {cells / 1e6:.1f} M cells), "
+                                   f"nt {nt}, checkpoints every {every} steps, "
+                                   f"{d.outc.shape[0]} sensors",
+                       "gradient_maps": len(names)},
+            "forward_ms": float(np.mean(fw)), "backward_ms": float(np.mean(bw)),
+            "forward_gcell_updates_per_s": cells * nt / float(np.mean(fw)) / 1e6,
+            "backward_gcell_steps_per_s": cells * nt / float(np.mean(bw)) / 1e6,
+            "device_gb": dev_gb, "gradient_finite": bool(torch.isfinite(g).all()),
+            "gradient_nonzero": bool((g != 0).any())}
+
+
+def run_adjoint3d(args):
+    line = measure_adjoint3d(args.grid or 160, args.nt or 600, args.checkpoint_every
+                             if args.checkpoint_every != 200 else 60, args.steps, args.warmup,
+                             args.physics)
+    print(json.dumps(line), flush=True)
+
+
 def plain_3d_problem(edge=512, seed=0, nt=3000, f0=2e6, ppw=10, cfl=0.2, element_height=32,
                      sensor_plane=256):
     """The plain 3D workload as a user of the reference API holds it: host arrays of the
@@ -1092,10 +1152,11 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--workload", default=os.environ.get("FWGB_WORKLOAD", "plain3d"),
-                    choices=["plain2d", "plain3d", "batch2d", "serve2d", "adjoint2d", "solver3d"])
+                    choices=["plain2d", "plain3d", "batch2d", "serve2d", "adjoint2d", "adjoint3d",
+                             "solver3d"])
     ap.add_argument("--physics", default="isotropic", choices=["isotropic", "aniso", "exp"],
-                    help="plain2d/plain3d: cell physics (relaxation engine, anisotropic "
-                         "relaxation, exponential attenuation)")
+                    help="plain2d/plain3d/adjoint3d: cell physics (relaxation engine, "
+                         "anisotropic relaxation, exponential attenuation)")
     ap.add_argument("--rate", type=float, default=20.0, help="serve2d: arrivals per second")
     ap.add_argument("--duration", type=float, default=10.0, help="serve2d: stream length [s]")
     ap.add_argument("--scale", type=float, default=0.5, help="serve2d: instance size scale")
@@ -1116,11 +1177,14 @@ def main():
                     help="plain3d: leave out the secondary workloads of the default line")
     ap.add_argument("--grid", type=int, default=0,
                     help="3D workload edge in cells (default 512; smaller for profiling); "
-                         "adjoint2d: grid edge (default 1024)")
+                         "adjoint2d: grid edge (default 1024); adjoint3d: medium edge "
+                         "(default 160)")
     ap.add_argument("--nt", type=int, default=0,
-                    help="adjoint2d: time steps (default 6000 at 1024, scaled with the grid)")
+                    help="adjoint2d: time steps (default 6000 at 1024, scaled with the grid); "
+                         "adjoint3d: default 600")
     ap.add_argument("--checkpoint-every", type=int, default=200,
-                    help="adjoint2d: steps between wavefield checkpoints")
+                    help="adjoint2d: steps between wavefield checkpoints (adjoint3d: 60 unless "
+                         "given)")
     args = ap.parse_args()
     if args.warmup < 3:
         print("warning: fewer than 3 warm-up steps requested; using 3", file=sys.stderr)
@@ -1133,6 +1197,8 @@ def main():
         run_serve(args)
     elif args.workload == "adjoint2d":
         run_adjoint(args)
+    elif args.workload == "adjoint3d":
+        run_adjoint3d(args)
     elif args.workload == "solver3d":
         run_solver3d(args)
     else:

@@ -1,7 +1,7 @@
 // Host side of the discrete adjoint (2D and 3D): checkpointed forward pass and the reverse pass
 // with per-segment recomputation (the C ABI's fw_adjoint_forward / fw_adjoint_backward).
 #include "engine_host.cuh"
-#include "kernels_adjoint3d.cuh"
+#include "kernels_adjoint_nd.cuh"
 
 using namespace fwgbh;
 

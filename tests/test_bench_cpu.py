@@ -45,16 +45,18 @@ def test_workload_entry_points_pass_their_arguments(monkeypatch):
             return {"value": 1.0, "config": {}, "host_to_host_s": 1.0}
         return f
 
-    for name in ("measure_adjoint", "measure_batch", "measure_serve", "measure_solver3d"):
+    for name in ("measure_adjoint", "measure_adjoint3d", "measure_batch", "measure_serve",
+                 "measure_solver3d"):
         monkeypatch.setattr(bench, name, recorder(name))
     monkeypatch.setattr(torch.cuda, "set_device", lambda *a: None)
     argv = ["bench.py", "--steps", "4", "--warmup", "5", "--grid", "96", "--nt", "70",
             "--checkpoint-every", "10", "--batch", "7", "--host-sample", "2", "--solver-sample", "3",
             "--rate", "5", "--duration", "2", "--scale", "0.25"]
-    for workload in ("adjoint2d", "batch2d", "serve2d", "solver3d"):
+    for workload in ("adjoint2d", "adjoint3d", "batch2d", "serve2d", "solver3d"):
         monkeypatch.setattr(sys, "argv", argv + ["--workload", workload])
         bench.main()
     assert calls["measure_adjoint"][0] == (96, 70, 10, 4, 5)
+    assert calls["measure_adjoint3d"][0] == (96, 70, 10, 4, 5, "isotropic")
     assert calls["measure_batch"][0] == (7, 4, 5, 2, 3)
     assert calls["measure_serve"][0][:3] == (5.0, 2.0, 0.25)
     assert calls["measure_solver3d"][0] == (96,)
