@@ -304,13 +304,13 @@ int group_run_persistent_t(fw_group* g, cudaStream_t s, int* d_nt, int* d_upto, 
   FW_CUDA(nullptr, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, TY, 0));
   FW_CUDA(nullptr, cudaGetDevice(&dev));
   FW_CUDA(nullptr, cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-  const int n = (int)g->members.size();
+  int n = (int)g->members.size();
   const int grid = std::min({per_sm * sms, kBarMaxBlocks, g->tiles_upto[n]});
   if (grid < 1) return fail(nullptr, FW_ERR_CUDA, "persistent group kernel: no block fits an SM");
   const StepArgs* a = g->d_args;
   const March2Maps* m = g->d_maps;
   const int4* w = g->d_tiles;
-  void* args[] = {&a, &m, &w, &d_nt, &d_upto, const_cast<int*>(&n), &max_nt, &d_bar};
+  void* args[] = {&a, &m, &w, &d_nt, &d_upto, &n, &max_nt, &d_bar};
   FW_CUDA(nullptr, cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(kern), dim3(grid),
                                                dim3(TY), args, 0, s));
   return FW_OK;
