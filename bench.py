@@ -21,7 +21,7 @@ The default line (plain3d, one GPU) also carries ``extra``: secondary workloads 
 same run, each with its own CUDA-event timing and its own check against the FP64 oracle or the
 one-by-one path: ``plain2d`` (full solves, rel-L2 of a full solve against the FP64 C oracle,
 e2e), ``batched`` (64 simulations: group engine vs one by one on the device, vs one by one
-through ``Solver.run()`` on 16 instances and through the host-side NumPy pre-processing on 8),
+through ``Solver.run()`` and through the host-side NumPy pre-processing on 16 instances each),
 ``serving_short`` (10 s of the Poisson stream at half size: continuous batching vs FIFO) and
 ``solver_config0`` (host-to-host ``Solver.run()`` of the plain 2D problem, GPU and NumPy
 pre-processing), ``solver_config1`` (the same for the plain 3D workload: host arrays of the 512^3
@@ -435,7 +435,7 @@ def collect_extras() -> dict:
                           roofline={k: p2["roofline"][k] for k in ("achieved", "peak", "frac",
                                                                    "unit")})
     torch.cuda.empty_cache()
-    b = measure_batch(64, steps=1, warmup=1, host_sample=8, solver_sample=16)
+    b = measure_batch(64, steps=1, warmup=1, host_sample=16, solver_sample=16)
     out["batched"] = {k: b[k] for k in ("value", "unit", "ms_per_step", "sims_per_s", "e2e",
                                         "one_by_one_host_api", "one_by_one_solver_run",
                                         "one_by_one_latency_ms", "batched_latency_ms", "parity",
@@ -1167,7 +1167,7 @@ def main():
     ap.add_argument("--grad-frac", type=float, default=0.2,
                     help="serve2d: fraction of gradient requests")
     ap.add_argument("--batch", type=int, default=64, help="simulations per rank (batch2d)")
-    ap.add_argument("--host-sample", type=int, default=8,
+    ap.add_argument("--host-sample", type=int, default=16,
                     help="batch2d / serve2d: instances (forward requests) also run one by one "
                          "through the host-side API")
     ap.add_argument("--solver-sample", type=int, default=16,
