@@ -69,12 +69,16 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
         gm = dict(zip(names, g))
         dt = float(np.float32(inp.dt))
         extra = {"beta": gm["beta2dt"] * (2.0 * dt)} if "beta2dt" in gm else {}
+
+        def dmap(k):   # an input map as a float64 tensor on the device (numpy or torch inputs)
+            return torch.as_tensor(inp.maps[k], device=dev).double()
+
         if "kappay" in inp.maps:   # anisotropic engine: per-direction map sets
-            rho = inp.maps["rho"].double()
+            rho = dmap("rho")
             grads = {"rho": gm["rdt_rho"] * (-dt / rho ** 2), "K": gm["dt_k"] * dt}
             for n in names[2:]:
                 if n.startswith("inv_k"):
-                    kap = inp.maps[f"kappa{n[5]}"].double()
+                    kap = dmap(f"kappa{n[5]}")
                     grads[f"kappa{n[5]}"] = gm[n] * (-1.0 / kap ** 2)
                 elif n != "beta2dt":
                     grads[f"{n[0]}pml{n[1:]}"] = gm[n]
@@ -82,12 +86,12 @@ def map_gradients(engine: Engine, observed, checkpoint_every: int = 200, stream=
             ts.synchronize()
             return J, traces, grads
         if "a_exp" in inp.maps:   # exponential engine: a_exp sits in the au1 slot
-            rho = inp.maps["rho"].double()
+            rho = dmap("rho")
             grads = {"rho": gm["rdt_rho"] * (-dt / rho ** 2), "K": gm["dt_k"] * dt,
                      "a_exp": gm["au1"], **extra}
             ts.synchronize()
             return J, traces, grads
-        m = {k: inp.maps[k].double() for k in ("rho", "K", "kappau", "kappax")}
+        m = {k: dmap(k) for k in ("rho", "K", "kappau", "kappax")}
         grads = {
             "rho": gm["rdt_rho"] * (-dt / m["rho"] ** 2),
             "K": gm["dt_k"] * dt,
