@@ -3,8 +3,8 @@ time sums across segments) against the FP64 NumPy adjoint, against the all-FP64 
 mode, and against central finite differences of the FP64 oracle.
 
 Tolerances: engine-map gradients within 1e-3 relative L2 of the FP64 adjoint; physical-map
-gradients (c, rho, alpha0) within 2e-2 of central differences (h = 1e-3 relative, tap sets
-held fixed) at 16 random cells, relative to the larger of the two values plus 1e-3 of the
+gradients (c, rho, alpha0) within 5e-3 of central differences (h = 1e-3 relative, tap sets
+held fixed) at 16 random cells, relative to the larger of the two values plus 1e-6 of the
 field's largest gradient.
 """
 
@@ -269,7 +269,9 @@ def test_physical_gradients_match_finite_differences(engine_lib, cuda, problem):
             minus[k][cell] -= h
             fd = (J64(*plus) - J64(*minus)) / (2 * h)
             ad = float(grads[name][cell])
-            assert abs(fd - ad) <= 2e-2 * max(abs(fd), abs(ad)) + 1e-3 * gmax, \
+            # measured: c within 2e-5, alpha0 within 5e-6, rho within 1.8e-3 (relative); cells
+            # whose gradient is ~1e-9 of the field's largest sit at the FP64 differences' noise
+            assert abs(fd - ad) <= 5e-3 * max(abs(fd), abs(ad)) + 1e-6 * gmax, \
                 f"d J / d {name} at {cell}: adjoint {ad:.6e}, finite difference {fd:.6e}"
             checked += 1
     assert checked == 24
