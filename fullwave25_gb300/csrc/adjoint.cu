@@ -139,7 +139,7 @@ void release_adjoint(fw_handle* h) {
   h->adj_grad = nullptr;
   h->bytes -= h->adj_bytes;
   h->adj_bytes = 0;
-  h->adj_every = h->adj_nckpt = 0;
+  h->adj_every = h->adj_nckpt = h->adj_ngrad = 0;
 }
 
 }  // namespace
@@ -154,7 +154,9 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
   if (checkpoint_every < 1) return fail(h, FW_ERR_ARGUMENT, "checkpoint_every must be >= 1");
   const size_t state_elems = (size_t)h->ncells_padded * n_state(h->ndim);
   const int nckpt = (h->d.nt + checkpoint_every - 1) / checkpoint_every;
-  if (checkpoint_every != h->adj_every || nckpt != h->adj_nckpt) {
+  // (re)allocate when the checkpointing or the number of gradient maps (beta set or cleared by
+  // fw_set_fields since the last call) changes
+  if (checkpoint_every != h->adj_every || nckpt != h->adj_nckpt || n_grad_maps(h) != h->adj_ngrad) {
     release_adjoint(h);
     const size_t b_ckpt = state_elems * std::max(nckpt, 1) * sizeof(float);
     const size_t b_store = state_elems * (checkpoint_every + 1) * sizeof(float);
@@ -184,6 +186,7 @@ int fw_adjoint_forward(fw_handle* h, void* stream, int32_t checkpoint_every) {
     h->bytes += h->adj_bytes;
     h->adj_every = checkpoint_every;
     h->adj_nckpt = nckpt;
+    h->adj_ngrad = n_grad_maps(h);
   }
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   int st = fw_reset(h, stream);
@@ -201,6 +204,8 @@ int fw_adjoint_backward(fw_handle* h, void* stream, const float* residual, doubl
   if (!h) return fail(nullptr, FW_ERR_ARGUMENT, "handle is NULL");
   if (!h->adj_ckpt || h->host_step != h->d.nt)
     return fail(h, FW_ERR_STATE, "fw_adjoint_forward must run (to nt) before fw_adjoint_backward");
+  if (n_grad_maps(h) != h->adj_ngrad)
+    return fail(h, FW_ERR_STATE, "the fields changed since fw_adjoint_forward: run it again");
   if (!residual && h->d.ncoordsout) return fail(h, FW_ERR_ARGUMENT, "residual is NULL");
   if (h->args.l.rec_group)
     return fail(h, FW_ERR_UNSUPPORTED, "the adjoint needs individual sensor traces: clear the sensor groups");

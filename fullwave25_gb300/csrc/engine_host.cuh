@@ -104,14 +104,15 @@ struct fw_handle {
   bool stream3d = false;       // 3D isotropic: point-wise operands staged by TMA too
   int ps3d = 2;                // stages of the point-wise ring of the streaming kernels
   int march_xc = fwgbh::kMarchXC;     // x planes per block of the 3D march (streaming: kStreamXC)
-  // adjoint (2D): checkpoints every adj_every steps, per-segment state store, adjoint fields
-  int adj_every = 0, adj_nckpt = 0;
+  // adjoint: checkpoints every adj_every steps, per-segment state store, adjoint fields and
+  // gradient maps (adj_ngrad of them: the allocation depends on the engine and on beta)
+  int adj_every = 0, adj_nckpt = 0, adj_ngrad = 0;
   float* adj_ckpt = nullptr;     // adj_nckpt states
   float* adj_store = nullptr;    // adj_every + 1 states
   float* adj_store2 = nullptr;   // second store: the next segment is recomputed into it while
                                  // the current one is reversed (nullptr: no overlap)
-  float* adj_lam = nullptr;      // 11 adjoint fields + 4 temporaries
-  double* adj_grad = nullptr;    // kNumGrad padded FP64 arrays
+  float* adj_lam = nullptr;      // adjoint fields and temporaries, then FP32 gradient partials
+  double* adj_grad = nullptr;    // adj_ngrad padded FP64 arrays
   size_t adj_bytes = 0;
 };
 

@@ -57,3 +57,29 @@ def test_nonlinear_map_gradients_match_fp64_adjoint(engine_lib, cuda, name, nt, 
         assert np.abs(ref).max() > 0, key
         err = np.linalg.norm(g[i][body] - ref) / np.linalg.norm(ref)
         assert err < 1e-3, f"{name} {key}: rel-L2 {err:.3e}"
+
+
+def test_beta_set_between_adjoint_calls(engine_lib, cuda):
+    """Setting a nonzero beta after fw_adjoint_forward adds a gradient map: the backward pass
+    refuses the stale forward pass (FW_ERR_STATE) instead of writing past its buffers, and a new
+    forward pass reallocates them for the extra map."""
+    torch = cuda
+    from fullwave25_gb300.engine import Engine, EngineError, adjoint_gradient_maps
+
+    lin = _case("2d_small", 40)
+    nonlin = _case("2d_small", 40, beta=6.0)
+    observed = Oracle(nonlin).run().astype(np.float32)
+    with Engine(lin) as eng:
+        eng.adjoint_forward(15)
+        eng.set_fields(nonlin)
+        res = torch.zeros(observed.shape, dtype=torch.float32, device="cuda")
+        g = torch.zeros((13,) + tuple(lin.shape), dtype=torch.float64, device="cuda")
+        with pytest.raises(EngineError, match="FW_ERR_STATE"):
+            eng.adjoint_backward(res.data_ptr(), g.data_ptr())
+        names = adjoint_gradient_maps(nonlin)
+        assert len(names) == 13
+        eng.adjoint_forward(15)
+        res = torch.as_tensor(eng.read_traces() - observed * 1.01, device="cuda").contiguous()
+        eng.adjoint_backward(res.data_ptr(), g.data_ptr())
+        torch.cuda.synchronize()
+    assert np.isfinite(g.cpu().numpy()).all() and g[12].abs().max() > 0
