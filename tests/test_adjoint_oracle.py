@@ -191,3 +191,58 @@ def test_nonlinear_gradient_matches_central_differences(beta_cases, engine, key)
         floor = 1e-10 * abs(J) / mag
         assert abs(fd - ad) <= 1e-5 * max(abs(fd), abs(ad)) + floor, \
             f"{engine} {key} at {c}: adjoint {ad:.6e} vs finite difference {fd:.6e}"
+
+
+@pytest.mark.parametrize("name,beta,keys", [
+    ("3d_small", None, ("rdt_rho", "dt_k", "inv_ku", "bx2")),
+    ("3d_aniso", 6.0, ("inv_kv", "az1", "bw2", "beta2dt")),
+    ("3d_exp", 8.0, ("rdt_rho", "dt_k", "a_exp", "beta2dt")),
+])
+def test_3d_gradients_match_central_differences(name, beta, keys):
+    """The FP64 adjoint in 3D (isotropic, anisotropic with beta, exponential with beta) against
+    central differences of the FP64 oracle on a short run of the golden 3D cases."""
+    inp = _small(name, 16)
+    if beta is not None:
+        inp.maps = dict(inp.maps)
+        inp.maps["beta"] = np.full(inp.shape, beta, dtype=np.float32)
+    obs_inp = _small(name, 16)
+    obs_inp.maps = dict(inp.maps)
+    obs_inp.maps["K"] = (obs_inp.maps["K"] * np.float32(1.02)).astype(np.float32)
+    observed = Oracle(obs_inp).run()
+    J, G, _ = misfit_and_gradient(inp, observed)
+    o = Oracle(inp)
+    for key in keys:
+        if key in ("rdt_rho", "dt_k", "a_exp", "beta2dt"):
+            base = getattr(o, key)
+        elif o.axis_u[0] is not None:
+            base = _aniso_base(o, key)
+        else:
+            base = _base_map(o, key)
+        assert np.abs(G[key]).max() > 0, key
+        # the cell where this gradient is largest: well above the differences' rounding
+        c = np.unravel_index(int(np.argmax(np.abs(G[key]))), G[key].shape)
+        mag = abs(base[c]) if base[c] != 0 else float(np.abs(base).mean())
+        h = 1e-4 * mag
+        plus, minus = base.copy(), base.copy()
+        plus[c] += h
+        minus[c] -= h
+        fd = (misfit(inp, observed, {key: plus}) - misfit(inp, observed, {key: minus})) / (2 * h)
+        ad = G[key][c]
+        assert abs(fd - ad) <= 1e-5 * max(abs(fd), abs(ad)) + 1e-10 * abs(J) / mag, \
+            f"{name} {key} at {c}: adjoint {ad:.6e} vs finite difference {fd:.6e}"
+
+
+def test_gradient_map_names_follow_the_oracle_keys():
+    """``engine.adjoint_gradient_maps`` (the order of fw_adjoint_backward's output arrays) names
+    the same maps, in the same order, as the FP64 adjoint's keys, for every engine."""
+    import sys
+    from pathlib import Path
+
+    sys.path.insert(0, str(Path(__file__).resolve().parents[1]))
+    from fullwave25_gb300.engine import ADJOINT_MAPS, adjoint_gradient_maps
+
+    assert adjoint_gradient_maps(load_case_inputs("2d_small")) == GRAD_KEYS == ADJOINT_MAPS
+    assert adjoint_gradient_maps(load_case_inputs("2d_air_beta")) == GRAD_KEYS + ("beta2dt",)
+    for name, nd in (("2d_aniso", 2), ("3d_aniso", 3)):
+        assert adjoint_gradient_maps(load_case_inputs(name)) == aniso_grad_keys(nd)
+    assert len(aniso_grad_keys(3)) == 32
